@@ -1,0 +1,264 @@
+"""flutas_gb300: GB300-native pressure-projection path of FluTAS.
+
+Python front end over the C ABI in ``include/flutas_gb300.h``
+(``libflutas_gb300.so``, built in-tree by ``flutas_gb300.build``).  The
+functions keep the names and argument meaning of the Fortran routines they
+replace (src/initsolver.f90, src/solver_cpu.f90, src/fillps.f90,
+src/correc.f90, src/bound.f90, src/chkdiv.f90, src/source.f90) and raise
+``FlutasError`` where the C call returns a negative status.
+
+Array arguments are either numpy arrays (host memory: the library copies them
+to the device and back inside the call) or CUDA tensors / any object with a
+``data_ptr()`` method (device memory: used in place).  3-D fields use the
+Fortran memory order, i.e. a C-contiguous array of shape (nz+2h, ny+2h, nx+2h).
+
+There is no CPU fallback: if the CUDA library is missing, importing the
+compute functions raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libflutas_gb300.so")
+
+FLUTAS_OK = 0
+FLUTAS_EINVAL = -1
+FLUTAS_EUNSUPPORTED = -2
+FLUTAS_ECUDA = -3
+FLUTAS_ENOMEM = -4
+FLUTAS_EITER = -5
+FLUTAS_ENONFINITE = -6
+FLUTAS_EBUSY = -7
+
+EXPORTED = [
+    "flutas_gb300_initsolver", "flutas_gb300_solver", "flutas_gb300_fillps", "flutas_gb300_correc",
+    "flutas_gb300_boundp", "flutas_gb300_updt_rhs_b", "flutas_gb300_chkdiv",
+    "flutas_gb300_pres_tw_src", "flutas_gb300_fftend", "flutas_gb300_last_error",
+    "flutas_gb300_plan_set_stream", "flutas_gb300_solve_mixed", "flutas_gb300_projection",
+    "flutas_gb300_plan_info",
+]
+
+
+class FlutasError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FlutasError(FLUTAS_ECUDA, f"CUDA extension missing: {p} (run flutas_gb300.build.build())")
+    L = C.CDLL(p)
+    vp, dp, ip = C.c_void_p, C.c_double, C.c_int
+    L.flutas_gb300_initsolver.argtypes = [vp, vp, ip, vp, vp, C.c_char_p, vp, C.c_char_p, vp, vp, vp,
+                                          vp, vp, vp, vp, vp, vp]
+    L.flutas_gb300_solver.argtypes = [vp, vp, dp, vp, vp, vp, vp, C.c_char_p, C.c_char_p, vp]
+    L.flutas_gb300_fillps.argtypes = [ip] * 5 + [dp] * 3 + [vp, dp, dp, vp, vp, vp, vp]
+    L.flutas_gb300_correc.argtypes = [ip] * 5 + [dp] * 3 + [vp, dp, dp, vp, vp, vp, vp, vp]
+    L.flutas_gb300_boundp.argtypes = [C.c_char_p, vp, vp, ip, ip, vp, vp, vp, vp, vp]
+    L.flutas_gb300_updt_rhs_b.argtypes = [ip] * 3 + [C.c_char_p, C.c_char_p, ip, vp, vp, vp, vp]
+    L.flutas_gb300_chkdiv.argtypes = [ip] * 3 + [dp] * 3 + [ip] * 2 + [vp, vp, vp, vp, vp, vp]
+    L.flutas_gb300_pres_tw_src.argtypes = [ip] * 3 + [dp] * 3 + [ip] * 2 + [vp, dp, dp, dp, vp, vp,
+                                                                             vp, vp, vp, vp]
+    L.flutas_gb300_fftend.argtypes = [vp]
+    L.flutas_gb300_last_error.argtypes = [C.c_char_p, ip]
+    L.flutas_gb300_plan_set_stream.argtypes = [vp, vp, ip]
+    L.flutas_gb300_solve_mixed.argtypes = [vp, vp, dp, ip, vp, vp]
+    L.flutas_gb300_projection.argtypes = [vp, ip, dp, dp, vp, vp, vp, dp, dp, vp, vp, vp, vp, ip, dp,
+                                          ip]
+    L.flutas_gb300_plan_info.argtypes = [vp, vp, vp, vp]
+    for name in EXPORTED:
+        getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(512)
+    load().flutas_gb300_last_error(buf, 512)
+    return buf.value.decode(errors="replace")
+
+
+def _check(rc: int, allow=()):
+    if rc != FLUTAS_OK and rc not in allow:
+        raise FlutasError(rc, last_error())
+    return rc
+
+
+def _ptr(a):
+    """Address of an array argument (numpy host array or device tensor)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        if hasattr(a, "is_contiguous") and not a.is_contiguous():
+            raise ValueError("device tensor must be contiguous")
+        return a.data_ptr()
+    if isinstance(a, np.ndarray):
+        if not a.flags.c_contiguous or a.dtype != np.float64:
+            raise ValueError("numpy arrays must be C-contiguous float64")
+        return a.ctypes.data
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def _d3(v):
+    return (C.c_double * 3)(*[float(x) for x in v])
+
+
+def _d6(v):
+    return (C.c_double * 6)(*[float(x) for x in v])
+
+
+def _i3(v):
+    return (C.c_int * 3)(*[int(x) for x in v])
+
+
+def _chars(s, n):
+    s = "".join(s) if not isinstance(s, (str, bytes)) else s
+    s = s.encode() if isinstance(s, str) else s
+    if len(s) != n:
+        raise ValueError(f"expected {n} BC characters, got {s!r}")
+    return s
+
+
+class Plan:
+    """The plan held in arrplan(1,1), plus every host output of initsolver.
+
+    Mirrors ``initsolver(n,dims,dims_z,dli,nh_d,dzci,dzfi,cbc,bc,c_or_f,
+    lambdaxy,a,b,c,arrplan,normfft,rhsbx,rhsby,rhsbz)`` (src/initsolver.f90:21).
+    """
+
+    def __init__(self, n, dli, nh_d, dzci, dzfi, cbc, bc, c_or_f="ccc"):
+        L = load()
+        self.n = [int(x) for x in n]
+        nx, ny, nz = self.n
+        self.nh_d = int(nh_d)
+        self.dli = [float(x) for x in dli]
+        self.cbc = _chars(cbc, 6).decode()
+        self.bc = [float(x) for x in bc]
+        self.c_or_f = _chars(c_or_f, 3).decode()
+        self.dzci = np.ascontiguousarray(dzci, dtype=np.float64)
+        self.dzfi = np.ascontiguousarray(dzfi, dtype=np.float64)
+        if self.dzci.size != nz + 2 * self.nh_d or self.dzfi.size != nz + 2 * self.nh_d:
+            raise ValueError("dzci/dzfi must have nz+2*nh_d entries")
+        self.lambdaxy = np.empty((ny, nx))
+        self.a, self.b, self.c = np.empty(nz), np.empty(nz), np.empty(nz)
+        self.rhsbx = np.empty((2, nz, ny))
+        self.rhsby = np.empty((2, nz, nx))
+        self.rhsbz = np.empty((2, ny, nx))
+        self.arrplan = (C.c_void_p * 4)()
+        nf = C.c_double()
+        _check(L.flutas_gb300_initsolver(
+            C.cast(_i3(self.n), C.c_void_p), C.cast(_d3(self.dli), C.c_void_p), self.nh_d,
+            self.dzci.ctypes.data, self.dzfi.ctypes.data, self.cbc.encode(),
+            C.cast(_d6(self.bc), C.c_void_p), self.c_or_f.encode(), self.lambdaxy.ctypes.data,
+            self.a.ctypes.data, self.b.ctypes.data, self.c.ctypes.data,
+            C.cast(self.arrplan, C.c_void_p), C.addressof(nf), self.rhsbx.ctypes.data,
+            self.rhsby.ctypes.data, self.rhsbz.ctypes.data))
+        self.normfft = nf.value
+        self.handle = self.arrplan[0]
+
+    # -- the reference-facing calls -------------------------------------------------
+    def solver(self, p):
+        """solver(n,arrplan,normfft,lambdaxy,a,b,c,bcz,c_or_f,p), in place (FP64)."""
+        L = load()
+        _check(L.flutas_gb300_solver(
+            C.cast(_i3(self.n), C.c_void_p), C.cast(self.arrplan, C.c_void_p), self.normfft,
+            self.lambdaxy.ctypes.data, self.a.ctypes.data, self.b.ctypes.data, self.c.ctypes.data,
+            self.cbc[4:6].encode(), self.c_or_f.encode(), _ptr(p)))
+        return p
+
+    def solve_mixed(self, p, tol=1e-10, max_iter=8, allow_unconverged=False):
+        """FP32-bulk solve with FP64 residual refinement; returns (relres, nsolves)."""
+        L = load()
+        rr, it = C.c_double(), C.c_int()
+        _check(L.flutas_gb300_solve_mixed(self.handle, _ptr(p), float(tol), int(max_iter),
+                                          C.addressof(rr), C.addressof(it)),
+               allow=(FLUTAS_EITER,) if allow_unconverged else ())
+        return rr.value, it.value
+
+    def projection(self, nh_u, dxi, dyi, dzci, dzfi, bcpre, dt, rho0, u, v, w, p, precision=0,
+                   tol=1e-10, max_iter=8):
+        L = load()
+        _check(L.flutas_gb300_projection(self.handle, int(nh_u), float(dxi), float(dyi), _ptr(dzci),
+                                         _ptr(dzfi), C.cast(_d6(bcpre), C.c_void_p), float(dt),
+                                         float(rho0), _ptr(u), _ptr(v), _ptr(w), _ptr(p),
+                                         int(precision), float(tol), int(max_iter)))
+
+    def set_stream(self, stream_handle: int | None, synchronous: bool = True):
+        _check(load().flutas_gb300_plan_set_stream(self.handle, stream_handle or None,
+                                                   1 if synchronous else 0))
+
+    def info(self):
+        b, p64, p32 = C.c_size_t(), C.c_int(), C.c_int()
+        _check(load().flutas_gb300_plan_info(self.handle, C.addressof(b), C.addressof(p64),
+                                             C.addressof(p32)))
+        return {"device_bytes": b.value, "xy_path_fp64": p64.value, "xy_path_fp32": p32.value}
+
+    def fftend(self):
+        if self.arrplan[0]:
+            _check(load().flutas_gb300_fftend(C.cast(self.arrplan, C.c_void_p)))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if _lib is not None and self.arrplan[0]:
+                _lib.flutas_gb300_fftend(C.cast(self.arrplan, C.c_void_p))
+        except Exception:
+            pass
+
+
+def initsolver(n, dli, nh_d, dzci, dzfi, cbc, bc, c_or_f="ccc") -> Plan:
+    return Plan(n, dli, nh_d, dzci, dzfi, cbc, bc, c_or_f)
+
+
+def fillps(n, nh_d, nh_u, dxi, dyi, dzi, dzfi, dti, rho0, u, v, w, p):
+    _check(load().flutas_gb300_fillps(int(n[0]), int(n[1]), int(n[2]), int(nh_d), int(nh_u), float(dxi),
+                                      float(dyi), float(dzi), _ptr(dzfi), float(dti), float(rho0),
+                                      _ptr(u), _ptr(v), _ptr(w), _ptr(p)))
+
+
+def correc(n, nh_d, nh_u, dxi, dyi, dzi, dzci, dt, rho0, p, u, v, w, rho=None):
+    _check(load().flutas_gb300_correc(int(n[0]), int(n[1]), int(n[2]), int(nh_d), int(nh_u), float(dxi),
+                                      float(dyi), float(dzi), _ptr(dzci), float(dt), float(rho0),
+                                      _ptr(p), _ptr(u), _ptr(v), _ptr(w), _ptr(rho)))
+
+
+def boundp(cbc, n, bc, nh_d, dl, dzc, dzf, p, nh_p=1):
+    halo = (C.c_int * 3)(1, 1, 1)
+    _check(load().flutas_gb300_boundp(_chars(cbc, 6), C.cast(_i3(n), C.c_void_p),
+                                      C.cast(_d6(bc), C.c_void_p), int(nh_d), int(nh_p),
+                                      C.cast(halo, C.c_void_p), C.cast(_d3(dl), C.c_void_p),
+                                      _ptr(dzc), _ptr(dzf), _ptr(p)))
+
+
+def updt_rhs_b(n, c_or_f, cbc, rhsbx, rhsby, rhsbz, p, nh_p=1):
+    _check(load().flutas_gb300_updt_rhs_b(int(n[0]), int(n[1]), int(n[2]), _chars(c_or_f, 3),
+                                          _chars(cbc, 6), int(nh_p), _ptr(rhsbx), _ptr(rhsby),
+                                          _ptr(rhsbz), _ptr(p)))
+
+
+def chkdiv(n, dxi, dyi, dzi, nh_d, nh_u, dzfi, u, v, w):
+    tot, mx = C.c_double(), C.c_double()
+    _check(load().flutas_gb300_chkdiv(int(n[0]), int(n[1]), int(n[2]), float(dxi), float(dyi), float(dzi),
+                                      int(nh_d), int(nh_u), _ptr(dzfi), _ptr(u), _ptr(v), _ptr(w),
+                                      C.addressof(tot), C.addressof(mx)))
+    return tot.value, mx.value
+
+
+def pres_tw_src(n, dxi, dyi, dzi, nh_d, nh_u, dzci, rho0i, f_t12, f_t12_o, p, pold, rho, u, v, w):
+    _check(load().flutas_gb300_pres_tw_src(int(n[0]), int(n[1]), int(n[2]), float(dxi), float(dyi),
+                                           float(dzi), int(nh_d), int(nh_u), _ptr(dzci), float(rho0i),
+                                           float(f_t12), float(f_t12_o), _ptr(p), _ptr(pold), _ptr(rho),
+                                           _ptr(u), _ptr(v), _ptr(w)))

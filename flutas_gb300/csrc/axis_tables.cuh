@@ -1,0 +1,50 @@
+// axis_tables.cuh -- host construction of the per-axis twiddle tables and
+// radix plan (shared by the library and the CPU emulator used in tests).
+#pragma once
+#include <cmath>
+#include <vector>
+
+#include "fft_engine.cuh"
+
+namespace fg {
+
+// Fills ap (except the W/Q device pointers) and the host tables.
+// Returns 0, or -1 if the size is not supported (odd n for ND/DN, prime > 13).
+template <typename T>
+inline int fill_axis_tables(int n, int pair, AxisPlan *ap, std::vector<C2<T>> &W, std::vector<C2<T>> &Q) {
+  *ap = AxisPlan{};
+  ap->n = n;
+  ap->pair = pair;
+  const bool pr = pair <= BC_DD;
+  if (!pr && (n % 2)) return -1;
+  ap->N = pr ? n : n / 2;
+  const int ns = ap->N == 1 ? 0 : make_radix_plan(ap->N, ap->radix);
+  if (ns < 0) return -1;
+  ap->nst = ns;
+  const long double PI = 3.141592653589793238462643383279502884L;
+  W.assign(ap->N, mk<T>(0, 0));
+  Q.assign(n, mk<T>(0, 0));
+  for (int t = 0; t < ap->N; t++) {
+    const long double a = 2.0L * PI * t / ap->N;
+    W[t] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+  }
+  if (pr) {
+    for (int k = 0; k < n; k++) {
+      const long double a = PI * k / (2.0L * n);
+      Q[k] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+    }
+  } else {
+    const int h = n / 2;
+    for (int j = 0; j < h; j++) {
+      const long double a = PI * (4.0L * j + 1.0L) / (4.0L * n);
+      Q[j] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+    }
+    for (int k = 0; k < h; k++) {
+      const long double a = PI * k / (long double)n;
+      Q[h + k] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+    }
+  }
+  return 0;
+}
+
+}  // namespace fg

@@ -1,0 +1,71 @@
+// emu.cu -- CPU execution of the transform passes of fft_engine.cuh.
+//
+// Test infrastructure: the pre/stage/post passes are __host__ __device__ and
+// contain no barrier, so running each pass with (tid = 0, nth = 1) on the CPU
+// executes exactly the arithmetic and indexing the kernels run on the GPU.
+// Built as a host-only shared library (libflutas_emu.so) for the CPU tests.
+#include <cstring>
+#include <vector>
+
+#include "axis_tables.cuh"
+#include "fft_engine.cuh"
+
+using namespace fg;
+
+namespace {
+
+template <typename T> struct HostStore {
+  T *out;
+  long ls, es;
+  void pair(int c, int t, T v0, T v1) {
+    out[(2L * c) * ls + t * es] = v0;
+    out[(2L * c + 1) * ls + t * es] = v1;
+  }
+  void single(int c, int t, T v) { out[(long)c * ls + t * es] = v; }
+};
+
+template <typename T>
+int run_lines(int pair, int n, int M, int backward, int cols, const double *in, double *out) {
+  AxisPlan ap;
+  std::vector<C2<T>> W, Q;
+  if (fill_axis_tables<T>(n, pair, &ap, W, Q) != 0) return -2;
+  ap.W = W.data();
+  ap.Q = Q.data();
+  const long ls = cols ? 1 : n, es = cols ? M : 1;
+  std::vector<T> R((size_t)M * n), O((size_t)M * n, (T)0);
+  for (long i = 0; i < (long)M * n; i++) R[i] = (T)in[i];
+  const int B = cbatch(pair, M);
+  std::vector<C2<T>> c1((size_t)B * ap.N + 1), c2((size_t)B * ap.N + 1);
+  if (backward) pre_bwd<T>(ap, R.data(), ls, es, M, c1.data(), B, 0, 1);
+  else pre_fwd<T>(ap, R.data(), ls, es, M, c1.data(), B, 0, 1);
+  C2<T> *cur = c1.data(), *nxt = c2.data();
+  const bool inv = fft_inverse(pair, backward != 0);
+  int Ns = 1;
+  for (int s = 0; s < ap.nst; s++) {
+    if (inv) stage_dispatch<T, true>(ap.radix[s], cur, nxt, ap.N, B, B, Ns, W.data(), 0, 1);
+    else stage_dispatch<T, false>(ap.radix[s], cur, nxt, ap.N, B, B, Ns, W.data(), 0, 1);
+    Ns *= ap.radix[s];
+    C2<T> *t = cur; cur = nxt; nxt = t;
+  }
+  HostStore<T> st{O.data(), ls, es};
+  if (backward) post_bwd<T>(ap, cur, B, M, st, 0, 1);
+  else post_fwd<T>(ap, cur, B, M, st, 0, 1);
+  for (long i = 0; i < (long)M * n; i++) out[i] = (double)O[i];
+  return 0;
+}
+
+}  // namespace
+
+// Applies the r2r transform of BC pair `pair` (0 PP,1 NN,2 DD,3 ND,4 DN),
+// forward or backward, to M lines of length n.  cols = 0: line l at
+// in[l*n + t]; cols = 1: in[t*M + l] (the y-pass layout).  dbl selects FP64.
+extern "C" __attribute__((visibility("default"))) int fg_emu_lines(int dbl, int pair, int n, int M, int backward,
+                                                                   int cols, const double *in, double *out) {
+  if (n < 1 || M < 1 || pair < 0 || pair > 4) return -1;
+  return dbl ? run_lines<double>(pair, n, M, backward, cols, in, out)
+             : run_lines<float>(pair, n, M, backward, cols, in, out);
+}
+
+extern "C" __attribute__((visibility("default"))) int fg_emu_radix_plan(int N, int *radix) {
+  return make_radix_plan(N, radix);
+}

@@ -1,0 +1,1062 @@
+// flutas_gb300.cu -- host side of the C ABI (include/flutas_gb300.h).
+//
+// Owns the plan (the GPU counterpart of FluTAS's arrplan + the initsolver
+// outputs), stages host-pointer arguments through device mirrors, and issues
+// the sm_103a kernels of kernels.cuh.  Reference routines are cited at each
+// entry point.
+#include "../../include/flutas_gb300.h"
+#include "axis_tables.cuh"
+#include "kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+using namespace fg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      return fail(FLUTAS_ECUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                                      \
+  } while (0)
+
+#define TRY(expr)             \
+  do {                        \
+    int rc_ = (expr);         \
+    if (rc_ != 0) return rc_; \
+  } while (0)
+
+bool bc_ok(char c) { return c == 'P' || c == 'N' || c == 'D'; }
+
+int pair_code(char b0, char b1) {
+  if (b0 == 'P' && b1 == 'P') return BC_PP;
+  if (b0 == 'N' && b1 == 'N') return BC_NN;
+  if (b0 == 'D' && b1 == 'D') return BC_DD;
+  if (b0 == 'N' && b1 == 'D') return BC_ND;
+  if (b0 == 'D' && b1 == 'N') return BC_DN;
+  return -1;
+}
+
+// ------------------------------------------------------------ device buffers
+struct DBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t b) {
+    if (b <= bytes) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return fail(FLUTAS_ENOMEM, "cudaMalloc(%zu) failed: %s", b, cudaGetErrorString(e));
+    }
+    bytes = b;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T> T *as() const { return (T *)p; }
+};
+
+bool is_device_ptr(const void *ptr) {
+  if (!ptr) return false;
+  cudaPointerAttributes at;
+  cudaError_t e = cudaPointerGetAttributes(&at, ptr);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// A field argument: device pointers are used in place, host pointers are
+// copied to a mirror before the kernels and back after (if written).
+struct Staged {
+  double *d = nullptr;
+  const void *host = nullptr;
+  size_t bytes = 0;
+  bool out = false;
+};
+
+struct Mirrors {
+  std::vector<DBuf> bufs;
+  int used = 0;
+  void reset() { used = 0; }
+  int get(size_t bytes, void **out) {
+    if (used == (int)bufs.size()) bufs.emplace_back();
+    TRY(bufs[used].ensure(bytes));
+    *out = bufs[used].p;
+    used++;
+    return 0;
+  }
+  void release() {
+    for (auto &b : bufs) b.release();
+    bufs.clear();
+    used = 0;
+  }
+};
+
+int stage_in(Mirrors &m, const void *user, size_t bytes, bool in, bool out, cudaStream_t st, Staged *s) {
+  s->host = nullptr;
+  s->bytes = bytes;
+  s->out = out;
+  if (!user) return fail(FLUTAS_EINVAL, "null array argument");
+  if (is_device_ptr(user)) {
+    s->d = (double *)user;
+    return 0;
+  }
+  void *d = nullptr;
+  TRY(m.get(bytes, &d));
+  s->d = (double *)d;
+  s->host = user;
+  if (in) CK(cudaMemcpyAsync(d, user, bytes, cudaMemcpyHostToDevice, st));
+  return 0;
+}
+
+int stage_out(const Staged &s, cudaStream_t st) {
+  if (s.host && s.out) CK(cudaMemcpyAsync((void *)s.host, s.d, s.bytes, cudaMemcpyDeviceToHost, st));
+  return 0;
+}
+
+int num_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+int max_smem_optin() {
+  static int v = 0;
+  if (!v) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  return v;
+}
+
+template <typename K> int grid_for(K kernel, int threads, size_t smem, long work_items) {
+  CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+  if (per_sm < 1) return fail(FLUTAS_EUNSUPPORTED, "kernel does not fit on an SM (smem %zu)", smem);
+  long g = (long)per_sm * num_sms();
+  if (work_items < g) g = work_items;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+// ------------------------------------------------------------ axis tables
+struct AxisTables {
+  DBuf W, Q;
+  AxisPlan ap{};
+  bool ok = false;
+};
+
+template <typename T>
+int build_axis(int n, int pair, AxisTables *t) {
+  AxisPlan ap{};
+  std::vector<C2<T>> W, Q;
+  if (fill_axis_tables<T>(n, pair, &ap, W, Q) != 0) {
+    if (pair > BC_DD && (n % 2))
+      return fail(FLUTAS_EUNSUPPORTED, "ND/DN transforms need an even number of cells (n=%d)", n);
+    return fail(FLUTAS_EUNSUPPORTED, "transform length %d has a prime factor above 13", n);
+  }
+  TRY(t->W.ensure(sizeof(C2<T>) * W.size()));
+  TRY(t->Q.ensure(sizeof(C2<T>) * Q.size()));
+  CK(cudaMemcpy(t->W.p, W.data(), sizeof(C2<T>) * W.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(t->Q.p, Q.data(), sizeof(C2<T>) * Q.size(), cudaMemcpyHostToDevice));
+  ap.W = t->W.p;
+  ap.Q = t->Q.p;
+  t->ap = ap;
+  t->ok = true;
+  return 0;
+}
+
+// ----------------------------------------------------- block reduction helper
+__device__ __forceinline__ void block_add(double v, double *acc) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(acc, v);
+}
+
+}  // namespace
+
+// ===========================================================================
+// Plan
+// ===========================================================================
+struct flutas_plan {
+  static constexpr unsigned MAGIC = 0xF1A7A5u;
+  unsigned magic = MAGIC;
+  int dev = 0;
+  int n[3];
+  char cbc[6];
+  char c_or_f[3];
+  double dli[3];
+  double bc[6];
+  int nh_d;
+  double normfft;
+  int nn;  // nz - q
+  std::vector<double> lam_h, a_h, b_h, c_h, dzci_h, dzfi_h;
+  const void *host_lam = nullptr, *host_a = nullptr, *host_b = nullptr, *host_c = nullptr;
+  DBuf lam, a, b, c, dzci, dzfi, rhsb[3];
+  AxisTables tx64, ty64, tx32, ty32;
+  DBuf S64, S32, fbuf, phi, nrm;
+  Mirrors mir;
+  cudaStream_t stream = 0;
+  bool sync = true;
+  int path64 = 0, path32 = 0;  // 0 separate passes, 1 fused plane kernel
+  bool pin_zero_mode = false;  // singular (lam == 0, z in N/N or P/P) column
+};
+
+namespace {
+
+int check_plan(void *p, flutas_plan **out) {
+  flutas_plan *pl = (flutas_plan *)p;
+  if (!pl || pl->magic != flutas_plan::MAGIC) return fail(FLUTAS_EINVAL, "invalid plan handle");
+  *out = pl;
+  return 0;
+}
+
+template <typename T> size_t plane_smem(int nx, int ny) {
+  return align_up<T>(sizeof(T) * (size_t)ny * xpitch(nx)) + sizeof(T) * (size_t)nx * ny;
+}
+
+// --------------------------------------------------------------------------
+// forward (x,y) transform of one field into S, reading through functor In.
+// --------------------------------------------------------------------------
+template <typename T, typename In>
+int fwd_xy(flutas_plan *pl, const In &in, T *S, const AxisTables &tx, const AxisTables &ty, int path) {
+  Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
+  cudaStream_t st = pl->stream;
+  if (path == 1) {
+    const size_t sm = plane_smem<T>(g.nx, g.ny);
+    int grid = grid_for(k_xyfwd_plane<T, In>, 512, sm, g.nz);
+    if (grid < 0) return grid;
+    k_xyfwd_plane<T, In><<<grid, 512, sm, st>>>(tx.ap, ty.ap, in, S, g);
+    CK(cudaGetLastError());
+    return 0;
+  }
+  // x pass
+  {
+    const int P = xpitch(g.nx);
+    int M = (int)((64 * 1024) / (sizeof(T) * (size_t)(P + g.nx)));
+    M = (M / 2) * 2;
+    if (M < 2) M = 2;
+    const size_t sm = align_up<T>(sizeof(T) * (size_t)M * P) + sizeof(T) * (size_t)M * g.nx;
+    const long rows = (long)g.ny * g.nz;
+    int grid = grid_for(k_xfwd<T, In>, 256, sm, (rows + M - 1) / M);
+    if (grid < 0) return grid;
+    k_xfwd<T, In><<<grid, 256, sm, st>>>(tx.ap, in, S, g, M);
+    CK(cudaGetLastError());
+  }
+  // y pass
+  {
+    int W = (int)((64 * 1024) / (2 * sizeof(T) * (size_t)g.ny));
+    W = (W / 2) * 2;
+    if (W > g.nx + (g.nx & 1)) W = g.nx + (g.nx & 1);
+    if (W < 2) W = 2;
+    const size_t sm = align_up<T>(sizeof(T) * (size_t)W * g.ny) + sizeof(T) * (size_t)W * g.ny;
+    const long tiles = (long)((g.nx + W - 1) / W) * g.nz;
+    int grid = grid_for(k_ypass<T, false>, 256, sm, tiles);
+    if (grid < 0) return grid;
+    k_ypass<T, false><<<grid, 256, sm, st>>>(ty.ap, S, g, W);
+    CK(cudaGetLastError());
+  }
+  return 0;
+}
+
+template <typename T, typename Out>
+int inv_xy(flutas_plan *pl, const T *S, const Out &out, const AxisTables &tx, const AxisTables &ty, int path) {
+  Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
+  cudaStream_t st = pl->stream;
+  if (path == 1) {
+    const size_t sm = plane_smem<T>(g.nx, g.ny);
+    int grid = grid_for(k_xyinv_plane<T, Out>, 512, sm, g.nz);
+    if (grid < 0) return grid;
+    k_xyinv_plane<T, Out><<<grid, 512, sm, st>>>(tx.ap, ty.ap, S, out, g);
+    CK(cudaGetLastError());
+    return 0;
+  }
+  {
+    int W = (int)((64 * 1024) / (2 * sizeof(T) * (size_t)g.ny));
+    W = (W / 2) * 2;
+    if (W > g.nx + (g.nx & 1)) W = g.nx + (g.nx & 1);
+    if (W < 2) W = 2;
+    const size_t sm = align_up<T>(sizeof(T) * (size_t)W * g.ny) + sizeof(T) * (size_t)W * g.ny;
+    const long tiles = (long)((g.nx + W - 1) / W) * g.nz;
+    int grid = grid_for(k_ypass<T, true>, 256, sm, tiles);
+    if (grid < 0) return grid;
+    k_ypass<T, true><<<grid, 256, sm, st>>>(ty.ap, (T *)S, g, W);
+    CK(cudaGetLastError());
+  }
+  {
+    const int P = xpitch(g.nx);
+    int M = (int)((64 * 1024) / (sizeof(T) * (size_t)(P + g.nx)));
+    M = (M / 2) * 2;
+    if (M < 2) M = 2;
+    const size_t sm = align_up<T>(sizeof(T) * (size_t)M * P) + sizeof(T) * (size_t)M * g.nx;
+    const long rows = (long)g.ny * g.nz;
+    int grid = grid_for(k_xinv<T, Out>, 256, sm, (rows + M - 1) / M);
+    if (grid < 0) return grid;
+    k_xinv<T, Out><<<grid, 256, sm, st>>>(tx.ap, S, out, g, M);
+    CK(cudaGetLastError());
+  }
+  return 0;
+}
+
+template <typename T>
+int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const double *b, const double *c, bool pin) {
+  ZArgs za;
+  za.a = a; za.b = b; za.c = c; za.lam = lam;
+  za.nq = pl->n[0] * pl->n[1];
+  za.nz = pl->n[2];
+  za.nn = pl->nn;
+  za.periodic = (pl->cbc[4] == 'P' && pl->cbc[5] == 'P') ? 1 : 0;
+  za.pin = pin ? 1 : 0;
+  int TC = sizeof(T) == 8 ? 32 : 64;
+  const size_t sm = sizeof(T) * (size_t)(za.periodic ? 3 : 2) * za.nz * TC;
+  if ((int)sm > max_smem_optin()) {
+    TC = 32;
+  }
+  const size_t sm2 = sizeof(T) * (size_t)(za.periodic ? 3 : 2) * za.nz * TC;
+  if ((int)sm2 > max_smem_optin()) return fail(FLUTAS_EUNSUPPORTED, "nz=%d too large for the z kernel", za.nz);
+  int grid = grid_for(k_zsolve<T>, TC, sm2, ((long)za.nq + TC - 1) / TC);
+  if (grid < 0) return grid;
+  k_zsolve<T><<<grid, TC, sm2, pl->stream>>>(za, S);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// In-functors with side effects / norms for the mixed path ------------------
+struct InHaloCopyNorm {  // value = p interior; also fbuf = value; accumulates value^2
+  const double *p;
+  double *fbuf;
+  Geo g;
+  __device__ double operator()(int i0, int j0, int k0) const {
+    const long id = g.pidx(i0 + 1, j0 + 1, k0 + 1);
+    const double v = p[id];
+    fbuf[id] = v;
+    return v;
+  }
+};
+
+}  // namespace
+
+// norm kernels (sum of squares of the interior of a halo-1 array) -----------
+__global__ void k_sumsq_halo(const double *f, Geo g, double *acc) {
+  const long N = (long)g.nx * g.ny * g.nz;
+  double s = 0.0;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
+    const double v = f[g.pidx(i, j, k)];
+    s += v * v;
+  }
+  block_add(s, acc);
+}
+
+// residual sum of squares (FP64), r = f - A x
+__global__ void k_ressq(InResidual r, double *acc) {
+  const Geo &g = r.g;
+  const long N = (long)g.nx * g.ny * g.nz;
+  double s = 0.0;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
+    const int i0 = (int)(t % g.nx), j0 = (int)((t / g.nx) % g.ny), k0 = (int)(t / ((long)g.nx * g.ny));
+    const double v = r(i0, j0, k0);
+    s += v * v;
+  }
+  block_add(s, acc);
+}
+
+__global__ void k_copy_interior(const double *src, double *dst, Geo g) {
+  const long N = (long)g.nx * g.ny * g.nz;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
+    dst[g.pidx(i, j, k)] = src[g.pidx(i, j, k)];
+  }
+}
+
+__global__ void k_add_interior(const double *src, double *dst, Geo g) {
+  const long N = (long)g.nx * g.ny * g.nz;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
+    dst[g.pidx(i, j, k)] += src[g.pidx(i, j, k)];
+  }
+}
+
+namespace {
+
+int stream_grid(long n, int threads = 256) {
+  long g = (n + threads - 1) / threads;
+  long cap = (long)num_sms() * 8;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+int finish(flutas_plan *pl) {
+  if (pl->sync) CK(cudaStreamSynchronize(pl->stream));
+  return 0;
+}
+
+// FP64 solve on a device halo array (the plan's own stream).
+int solve_fp64_dev(flutas_plan *pl, double *p, const double *lam, const double *a, const double *b, const double *c) {
+  Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
+  TRY(pl->S64.ensure(sizeof(double) * (size_t)g.nx * g.ny * g.nz));
+  double *S = pl->S64.as<double>();
+  TRY(fwd_xy<double>(pl, InHalo{p, g}, S, pl->tx64, pl->ty64, pl->path64));
+  TRY(zsolve<double>(pl, S, lam, a, b, c, pl->pin_zero_mode));
+  TRY(inv_xy<double>(pl, S, OutHalo{p, pl->normfft, g}, pl->tx64, pl->ty64, pl->path64));
+  return 0;
+}
+
+// Mixed solve on a device halo array p (RHS in, solution out).
+int solve_mixed_dev(flutas_plan *pl, double *p, double tol, int max_iter, double *relres, int *iters) {
+  Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
+  const size_t halo_bytes = sizeof(double) * (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+  TRY(pl->S32.ensure(sizeof(float) * (size_t)g.nx * g.ny * g.nz));
+  TRY(pl->fbuf.ensure(halo_bytes));
+  TRY(pl->nrm.ensure(sizeof(double) * 4));
+  float *S = pl->S32.as<float>();
+  double *f = pl->fbuf.as<double>();
+  double *nrm = pl->nrm.as<double>();
+  cudaStream_t st = pl->stream;
+  const double *lam = pl->lam.as<double>(), *a = pl->a.as<double>(), *b = pl->b.as<double>(), *c = pl->c.as<double>();
+  CK(cudaMemsetAsync(nrm, 0, sizeof(double) * 4, st));
+  // ||f||^2 and the first FP32 solve (fbuf <- f copy fused into the load)
+  k_sumsq_halo<<<stream_grid((long)g.nx * g.ny * g.nz), 256, 0, st>>>(p, g, nrm + 0);
+  CK(cudaGetLastError());
+  TRY(fwd_xy<float>(pl, InHaloCopyNorm{p, f, g}, S, pl->tx32, pl->ty32, pl->path32));
+  TRY(zsolve<float>(pl, S, lam, a, b, c, true));
+  TRY(inv_xy<float>(pl, S, OutHalo{p, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
+  InResidual R;
+  R.f = f; R.x = p;
+  R.dzci = pl->dzci.as<double>() + (pl->nh_d - 1);
+  R.dzfi = pl->dzfi.as<double>() + (pl->nh_d - 1);
+  R.dxi2 = pl->dli[0] * pl->dli[0];
+  R.dyi2 = pl->dli[1] * pl->dli[1];
+  memcpy(R.bc, pl->cbc, 6);
+  R.g = g;
+  int it = 1;
+  double fn2 = 0.0, rn2 = 0.0, rel = 0.0;
+  for (;;) {
+    CK(cudaMemsetAsync(nrm + 1, 0, sizeof(double), st));
+    k_ressq<<<stream_grid((long)g.nx * g.ny * g.nz), 256, 0, st>>>(R, nrm + 1);
+    CK(cudaGetLastError());
+    double h[2];
+    CK(cudaMemcpyAsync(h, nrm, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    fn2 = h[0];
+    rn2 = h[1];
+    if (!std::isfinite(rn2) || !std::isfinite(fn2))
+      return fail(FLUTAS_ENONFINITE, "non-finite residual in mixed solve");
+    rel = fn2 > 0 ? std::sqrt(rn2 / fn2) : std::sqrt(rn2);
+    if (rel <= tol || it >= max_iter) break;
+    // correction: e = A^-1 r in FP32, p += e (FP64)
+    TRY(fwd_xy<float>(pl, R, S, pl->tx32, pl->ty32, pl->path32));
+    TRY(zsolve<float>(pl, S, lam, a, b, c, true));
+    TRY(inv_xy<float>(pl, S, OutHaloAdd{p, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
+    it++;
+  }
+  if (relres) *relres = rel;
+  if (iters) *iters = it;
+  if (rel > tol) return fail(FLUTAS_EITER, "mixed solve reached %d solves at relative residual %.3e > %.3e", it, rel, tol);
+  return 0;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int flutas_gb300_last_error(char *buf, int len) {
+  if (!buf || len <= 0) return FLUTAS_EINVAL;
+  snprintf(buf, (size_t)len, "%s", g_err.c_str());
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const double *dzci,
+                            const double *dzfi, const char cbc[6], const double bc[6],
+                            const char c_or_f[3], double *lambdaxy, double *a, double *b, double *c,
+                            void **arrplan, double *normfft, double *rhsbx, double *rhsby,
+                            double *rhsbz) {
+  // src/initsolver.f90:21-120
+  if (!n || !dli || !dzci || !dzfi || !cbc || !bc || !c_or_f || !lambdaxy || !a || !b || !c || !arrplan ||
+      !normfft || !rhsbx || !rhsby || !rhsbz)
+    return fail(FLUTAS_EINVAL, "initsolver: null argument");
+  const int nx = n[0], ny = n[1], nz = n[2];
+  if (nx < 2 || ny < 2 || nz < 3 || nh_d < 1) return fail(FLUTAS_EINVAL, "initsolver: bad sizes n=(%d,%d,%d) nh_d=%d", nx, ny, nz, nh_d);
+  for (int i = 0; i < 6; i++)
+    if (!bc_ok(cbc[i])) return fail(FLUTAS_EINVAL, "initsolver: bad BC character '%c'", cbc[i]);
+  for (int d = 0; d < 3; d++) {
+    if ((cbc[2 * d] == 'P') != (cbc[2 * d + 1] == 'P'))
+      return fail(FLUTAS_EINVAL, "initsolver: periodic BC must be set on both ends (axis %d)", d + 1);
+  }
+  if (c_or_f[0] != 'c' || c_or_f[1] != 'c' || c_or_f[2] != 'c')
+    return fail(FLUTAS_EUNSUPPORTED, "initsolver: only cell-centred ('ccc') pressure is implemented on the GPU");
+  int px = pair_code(cbc[0], cbc[1]), py = pair_code(cbc[2], cbc[3]);
+  if (px < 0 || py < 0) return fail(FLUTAS_EINVAL, "initsolver: bad BC pair");
+  flutas_plan *pl = new flutas_plan();
+  int rc = 0;
+  auto bail = [&](int r) { pl->magic = 0; delete pl; return r; };
+  cudaGetDevice(&pl->dev);
+  memcpy(pl->n, n, sizeof(int) * 3);
+  memcpy(pl->cbc, cbc, 6);
+  memcpy(pl->c_or_f, c_or_f, 3);
+  memcpy(pl->dli, dli, sizeof(double) * 3);
+  memcpy(pl->bc, bc, sizeof(double) * 6);
+  pl->nh_d = nh_d;
+  // eigenvalues (initsolver.f90:122-186), CPU natural order, times dli^2 (61-64)
+  const double pi = 3.141592653589793238462643383279502884;
+  auto eig = [&](int nn, int pair, double *lam) {
+    for (int l = 1; l <= nn; l++) {
+      double s;
+      switch (pair) {
+        case BC_PP: s = std::sin((1.0 * (l - 1)) * pi / (1.0 * nn)); break;
+        case BC_NN: s = std::sin((1.0 * (l - 1)) * pi / (2.0 * nn)); break;
+        case BC_DD: s = std::sin((1.0 * (l - 0)) * pi / (2.0 * nn)); break;
+        default: s = std::sin((1.0 * (2 * l - 1)) * pi / (4.0 * nn)); break;
+      }
+      lam[l - 1] = -4.0 * s * s;
+    }
+  };
+  std::vector<double> lx(nx), ly(ny);
+  eig(nx, px, lx.data());
+  eig(ny, py, ly.data());
+  for (int i = 0; i < nx; i++) lx[i] = lx[i] * (dli[0] * dli[0]);
+  for (int j = 0; j < ny; j++) ly[j] = ly[j] * (dli[1] * dli[1]);
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) lambdaxy[i + (long)nx * j] = lx[i] + ly[j];
+  // tridmatrix (initsolver.f90:188-246), cell-centred
+  auto DZCI = [&](int k) { return dzci[k - 1 + nh_d]; };
+  auto DZFI = [&](int k) { return dzfi[k - 1 + nh_d]; };
+  for (int k = 1; k <= nz; k++) {
+    a[k - 1] = DZFI(k) * DZCI(k - 1);
+    c[k - 1] = DZFI(k) * DZCI(k);
+  }
+  for (int k = 0; k < nz; k++) b[k] = -(a[k] + c[k]);
+  auto fac = [](char ch) { return ch == 'D' ? -1.0 : (ch == 'N' ? 1.0 : 0.0); };
+  b[0] = b[0] + fac(cbc[4]) * a[0];
+  b[nz - 1] = b[nz - 1] + fac(cbc[5]) * c[nz - 1];
+  // bc_rhs (initsolver.f90:248-298), cell-centred
+  auto bc_rhs = [&](const char *cb, int n1, int n2, const double *bv, const double dlc[2], const double dlf[2], double *rhs) {
+    double factor[2];
+    for (int ib = 0; ib < 2; ib++) {
+      double sgn = ib == 0 ? 1.0 : -1.0;
+      if (cb[ib] == 'P') factor[ib] = 0.0;
+      else if (cb[ib] == 'D') factor[ib] = -2.0 * bv[ib];
+      else factor[ib] = sgn * dlc[ib] * bv[ib];
+    }
+    for (int ib = 0; ib < 2; ib++) {
+      double v = factor[ib] / dlc[ib] / dlf[ib];
+      for (long t = 0; t < (long)n1 * n2; t++) rhs[(long)ib * n1 * n2 + t] = v;
+    }
+  };
+  {
+    double dl0[2] = {1.0 / dli[0], 1.0 / dli[0]}, dl1[2] = {1.0 / dli[1], 1.0 / dli[1]};
+    double dlc[2] = {1.0 / DZCI(0), 1.0 / DZCI(nz)}, dlf[2] = {1.0 / DZFI(1), 1.0 / DZFI(nz)};
+    bc_rhs(cbc + 0, ny, nz, bc + 0, dl0, dl0, rhsbx);
+    bc_rhs(cbc + 2, nx, nz, bc + 2, dl1, dl1, rhsby);
+    bc_rhs(cbc + 4, nx, ny, bc + 4, dlc, dlf, rhsbz);
+  }
+  // fftini normalisation (fft.f90:71-150)
+  double nf = 1.0;
+  nf *= (px == BC_PP ? 1.0 : 2.0) * nx;
+  nf *= (py == BC_PP ? 1.0 : 2.0) * ny;
+  pl->normfft = 1.0 / nf;
+  *normfft = pl->normfft;
+  pl->nn = nz;  // cell-centred: q = 0 (solver_cpu.f90:71-72)
+  pl->pin_zero_mode = false;  // FP64 path follows dgtsv_homebrewed's z == 0 test
+  // host copies + device copies
+  pl->lam_h.assign(lambdaxy, lambdaxy + (long)nx * ny);
+  pl->a_h.assign(a, a + nz);
+  pl->b_h.assign(b, b + nz);
+  pl->c_h.assign(c, c + nz);
+  pl->dzci_h.assign(dzci, dzci + nz + 2 * nh_d);
+  pl->dzfi_h.assign(dzfi, dzfi + nz + 2 * nh_d);
+  pl->host_lam = lambdaxy; pl->host_a = a; pl->host_b = b; pl->host_c = c;
+  auto up = [&](DBuf &d, const double *h, size_t cnt) -> int {
+    TRY(d.ensure(sizeof(double) * cnt));
+    CK(cudaMemcpy(d.p, h, sizeof(double) * cnt, cudaMemcpyHostToDevice));
+    return 0;
+  };
+  if ((rc = up(pl->lam, lambdaxy, (size_t)nx * ny))) return bail(rc);
+  if ((rc = up(pl->a, a, nz)) || (rc = up(pl->b, b, nz)) || (rc = up(pl->c, c, nz))) return bail(rc);
+  if ((rc = up(pl->dzci, dzci, nz + 2 * nh_d)) || (rc = up(pl->dzfi, dzfi, nz + 2 * nh_d))) return bail(rc);
+  if ((rc = up(pl->rhsb[0], rhsbx, 2 * (size_t)ny * nz)) || (rc = up(pl->rhsb[1], rhsby, 2 * (size_t)nx * nz)) ||
+      (rc = up(pl->rhsb[2], rhsbz, 2 * (size_t)nx * ny)))
+    return bail(rc);
+  if ((rc = build_axis<double>(nx, px, &pl->tx64)) || (rc = build_axis<double>(ny, py, &pl->ty64)) ||
+      (rc = build_axis<float>(nx, px, &pl->tx32)) || (rc = build_axis<float>(ny, py, &pl->ty32)))
+    return bail(rc);
+  const int smax = max_smem_optin();
+  pl->path64 = (nx % 2 == 0 && ny % 2 == 0 && (int)plane_smem<double>(nx, ny) <= smax) ? 1 : 0;
+  pl->path32 = (nx % 2 == 0 && ny % 2 == 0 && (int)plane_smem<float>(nx, ny) <= smax) ? 1 : 0;
+  arrplan[0] = pl;
+  arrplan[1] = arrplan[2] = arrplan[3] = nullptr;
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_fftend(void **arrplan) {
+  if (!arrplan) return fail(FLUTAS_EINVAL, "fftend: null arrplan");
+  flutas_plan *pl;
+  TRY(check_plan(arrplan[0], &pl));
+  cudaStreamSynchronize(pl->stream);
+  DBuf *bufs[] = {&pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
+                  &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W, &pl->tx32.Q, &pl->ty32.W,
+                  &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->nrm};
+  for (DBuf *d : bufs) d->release();
+  pl->mir.release();
+  pl->magic = 0;
+  delete pl;
+  arrplan[0] = nullptr;
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_plan_set_stream(void *plan, void *stream, int synchronous) {
+  flutas_plan *pl;
+  TRY(check_plan(plan, &pl));
+  pl->stream = (cudaStream_t)stream;
+  pl->sync = synchronous != 0;
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_plan_info(void *plan, size_t *device_bytes, int *xy_path_fp64, int *xy_path_fp32) {
+  flutas_plan *pl;
+  TRY(check_plan(plan, &pl));
+  if (device_bytes) {
+    size_t s = 0;
+    const DBuf *bufs[] = {&pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1],
+                          &pl->rhsb[2], &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W,
+                          &pl->tx32.Q, &pl->ty32.W, &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->nrm};
+    for (const DBuf *d : bufs) s += d->bytes;
+    for (const DBuf &d : pl->mir.bufs) s += d.bytes;
+    *device_bytes = s;
+  }
+  if (xy_path_fp64) *xy_path_fp64 = pl->path64;
+  if (xy_path_fp32) *xy_path_fp32 = pl->path32;
+  return FLUTAS_OK;
+}
+
+// src/solver_cpu.f90:20-115 (behaviour), src/solver_gpu.f90:31 (GPU form)
+int flutas_gb300_solver(const int n[3], void *const *arrplan, double normfft, const double *lambdaxy,
+                        const double *a, const double *b, const double *c, const char bcz[2],
+                        const char c_or_f[3], double *p) {
+  if (!n || !arrplan || !bcz || !c_or_f || !p) return fail(FLUTAS_EINVAL, "solver: null argument");
+  flutas_plan *pl;
+  TRY(check_plan(arrplan[0], &pl));
+  if (n[0] != pl->n[0] || n[1] != pl->n[1] || n[2] != pl->n[2])
+    return fail(FLUTAS_EINVAL, "solver: n=(%d,%d,%d) differs from the plan's (%d,%d,%d)", n[0], n[1], n[2], pl->n[0], pl->n[1], pl->n[2]);
+  if (bcz[0] != pl->cbc[4] || bcz[1] != pl->cbc[5])
+    return fail(FLUTAS_EINVAL, "solver: bcz differs from the plan's z BCs");
+  if (c_or_f[0] != 'c' || c_or_f[1] != 'c' || c_or_f[2] != 'c')
+    return fail(FLUTAS_EUNSUPPORTED, "solver: only cell-centred ('ccc') is implemented on the GPU");
+  (void)normfft;  // the plan's normfft (identical to initsolver's output) is used
+  // coefficient arrays: device pointers are used as given; host arrays must be
+  // the ones initsolver filled (their device copies live in the plan)
+  auto pick = [&](const double *user, const void *hostinit, const DBuf &dev, size_t cnt, const double **out) -> int {
+    if (!user || user == hostinit) { *out = dev.as<double>(); return 0; }
+    if (is_device_ptr(user)) { *out = user; return 0; }
+    // a different host array: refresh the plan's device copy
+    CK(cudaMemcpyAsync(dev.p, user, sizeof(double) * cnt, cudaMemcpyHostToDevice, pl->stream));
+    *out = dev.as<double>();
+    return 0;
+  };
+  const double *dl, *da, *db, *dc;
+  TRY(pick(lambdaxy, pl->host_lam, pl->lam, (size_t)pl->n[0] * pl->n[1], &dl));
+  TRY(pick(a, pl->host_a, pl->a, pl->n[2], &da));
+  TRY(pick(b, pl->host_b, pl->b, pl->n[2], &db));
+  TRY(pick(c, pl->host_c, pl->c, pl->n[2], &dc));
+  pl->mir.reset();
+  Staged sp;
+  const size_t pbytes = sizeof(double) * (size_t)(pl->n[0] + 2) * (pl->n[1] + 2) * (pl->n[2] + 2);
+  TRY(stage_in(pl->mir, p, pbytes, true, true, pl->stream, &sp));
+  TRY(solve_fp64_dev(pl, sp.d, dl, da, db, dc));
+  TRY(stage_out(sp, pl->stream));
+  if (sp.host) CK(cudaStreamSynchronize(pl->stream));
+  return finish(pl);
+}
+
+int flutas_gb300_solve_mixed(void *plan, double *p, double tol, int max_iter, double *relres, int *iters) {
+  flutas_plan *pl;
+  TRY(check_plan(plan, &pl));
+  if (!p) return fail(FLUTAS_EINVAL, "solve_mixed: null p");
+  if (!(tol > 0.0) || max_iter < 1) return fail(FLUTAS_EINVAL, "solve_mixed: need tol > 0 and max_iter >= 1");
+  pl->mir.reset();
+  Staged sp;
+  const size_t pbytes = sizeof(double) * (size_t)(pl->n[0] + 2) * (pl->n[1] + 2) * (pl->n[2] + 2);
+  TRY(stage_in(pl->mir, p, pbytes, true, true, pl->stream, &sp));
+  int rc = solve_mixed_dev(pl, sp.d, tol, max_iter, relres, iters);
+  if (rc != 0 && rc != FLUTAS_EITER) return rc;
+  TRY(stage_out(sp, pl->stream));
+  CK(cudaStreamSynchronize(pl->stream));
+  return rc;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Plan-less stencil entry points: a process-wide context (mirrors + stream 0)
+// ===========================================================================
+namespace {
+std::mutex g_ctx_mu;
+Mirrors g_ctx_mir;
+DBuf g_ctx_small[4];
+}  // namespace
+
+extern "C" {
+
+int flutas_gb300_fillps(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, double dyi, double dzi,
+                        const double *dzfi, double dti, double rho0, const double *u, const double *v,
+                        const double *w, double *p) {
+  // src/fillps.f90:16-69
+  (void)dzi;
+  if (nx < 1 || ny < 1 || nz < 1 || nh_u < 1 || nh_d < 1) return fail(FLUTAS_EINVAL, "fillps: bad sizes");
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  g_ctx_mir.reset();
+  cudaStream_t st = 0;
+  const size_t ub = sizeof(double) * (size_t)(nx + 2 * nh_u) * (ny + 2 * nh_u) * (nz + 2 * nh_u);
+  const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+  Staged su, sv, sw, sp, sz;
+  TRY(stage_in(g_ctx_mir, u, ub, true, false, st, &su));
+  TRY(stage_in(g_ctx_mir, v, ub, true, false, st, &sv));
+  TRY(stage_in(g_ctx_mir, w, ub, true, false, st, &sw));
+  TRY(stage_in(g_ctx_mir, dzfi, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sz));
+  TRY(stage_in(g_ctx_mir, p, pb, true, true, st, &sp));
+  InFillps in;
+  in.u = su.d; in.v = sv.d; in.w = sw.d;
+  in.dzfi = sz.d + (nh_d - 1);
+  in.dti = dti; in.dtidxi = dti * dxi; in.dtidyi = dti * dyi; in.rho0 = rho0;
+  in.rhsbx = in.rhsby = in.rhsbz = nullptr;
+  in.q1 = in.q2 = in.q3 = 0;
+  in.g = Geo{nx, ny, nz, nh_u};
+  k_fillps<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(in, sp.d);
+  CK(cudaGetLastError());
+  TRY(stage_out(sp, st));
+  CK(cudaStreamSynchronize(st));
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_correc(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, double dyi, double dzi,
+                        const double *dzci, double dt, double rho0, const double *p, double *u, double *v,
+                        double *w, const double *rho) {
+  // src/correc.f90:16-81 (constant-coefficient branch 57-60)
+  (void)dzi;
+  (void)rho;
+  if (nx < 1 || ny < 1 || nz < 1 || nh_u < 1 || nh_d < 1) return fail(FLUTAS_EINVAL, "correc: bad sizes");
+  if (rho0 == 0.0) return fail(FLUTAS_EINVAL, "correc: rho0 == 0");
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  g_ctx_mir.reset();
+  cudaStream_t st = 0;
+  const size_t ub = sizeof(double) * (size_t)(nx + 2 * nh_u) * (ny + 2 * nh_u) * (nz + 2 * nh_u);
+  const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+  Staged su, sv, sw, sp, sz;
+  TRY(stage_in(g_ctx_mir, u, ub, true, true, st, &su));
+  TRY(stage_in(g_ctx_mir, v, ub, true, true, st, &sv));
+  TRY(stage_in(g_ctx_mir, w, ub, true, true, st, &sw));
+  TRY(stage_in(g_ctx_mir, dzci, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sz));
+  TRY(stage_in(g_ctx_mir, p, pb, true, false, st, &sp));
+  CorrecArgs ca;
+  ca.p = sp.d; ca.dzci = sz.d + (nh_d - 1);
+  ca.u = su.d; ca.v = sv.d; ca.w = sw.d;
+  ca.factori = dt * dxi; ca.factorj = dt * dyi; ca.dt = dt; ca.rho0i = 1.0 / rho0;
+  ca.g = Geo{nx, ny, nz, nh_u};
+  k_correc<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(ca);
+  CK(cudaGetLastError());
+  TRY(stage_out(su, st));
+  TRY(stage_out(sv, st));
+  TRY(stage_out(sw, st));
+  CK(cudaStreamSynchronize(st));
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_boundp(const char cbc[6], const int n[3], const double bc[6], int nh_d, int nh_p,
+                        const int halo[3], const double dl[3], const double *dzc, const double *dzf, double *p) {
+  // src/bound.f90:146-225 boundp, set_bc 227-646 (centred, nh_p = 1)
+  (void)halo;
+  (void)dzf;
+  if (!cbc || !n || !bc || !dl || !dzc || !p) return fail(FLUTAS_EINVAL, "boundp: null argument");
+  if (nh_p != 1) return fail(FLUTAS_EUNSUPPORTED, "boundp: nh_p must be 1");
+  for (int i = 0; i < 6; i++)
+    if (!bc_ok(cbc[i])) return fail(FLUTAS_EINVAL, "boundp: bad BC character");
+  const int nx = n[0], ny = n[1], nz = n[2];
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  g_ctx_mir.reset();
+  cudaStream_t st = 0;
+  const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+  Staged sp;
+  TRY(stage_in(g_ctx_mir, p, pb, true, true, st, &sp));
+  // dzc may live on the device: read the two spacings we need
+  double dzc0, dzcn;
+  if (is_device_ptr(dzc)) {
+    CK(cudaMemcpy(&dzc0, dzc + (0 - 1 + nh_d), sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&dzcn, dzc + (nz - 1 + nh_d), sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    dzc0 = dzc[0 - 1 + nh_d];
+    dzcn = dzc[nz - 1 + nh_d];
+  }
+  const double dr[3][2] = {{dl[0], dl[0]}, {dl[1], dl[1]}, {dzc0, dzcn}};
+  for (int d = 0; d < 3; d++) {
+    BoundArgs ba;
+    ba.p = sp.d;
+    ba.g = Geo{nx, ny, nz, 1};
+    ba.idir = d + 1;
+    ba.ctype0 = cbc[2 * d];
+    ba.ctype1 = cbc[2 * d + 1];
+    auto fs = [&](char ct, int ib, double rv, double drv, double *f, double *s) {
+      if (ct == 'D') { *f = 2.0 * rv; *s = -1.0; }
+      else if (ct == 'N') { *f = ib == 0 ? -drv * rv : drv * rv; *s = 1.0; }
+      else { *f = 0.0; *s = 0.0; }
+    };
+    fs(ba.ctype0, 0, bc[2 * d], dr[d][0], &ba.f0, &ba.s0);
+    fs(ba.ctype1, 1, bc[2 * d + 1], dr[d][1], &ba.f1, &ba.s1);
+    long cnt = d == 0 ? (long)(ny + 2) * (nz + 2) : (d == 1 ? (long)(nx + 2) * (nz + 2) : (long)(nx + 2) * (ny + 2));
+    k_boundp_dir<<<stream_grid(cnt), 256, 0, st>>>(ba);
+    CK(cudaGetLastError());
+  }
+  TRY(stage_out(sp, st));
+  CK(cudaStreamSynchronize(st));
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_chkdiv(int nx, int ny, int nz, double dxi, double dyi, double dzi, int nh_d, int nh_u,
+                        const double *dzfi, const double *u, const double *v, const double *w, double *divtot,
+                        double *divmax) {
+  // src/chkdiv.f90:18-69
+  (void)dzi;
+  if (!divtot || !divmax) return fail(FLUTAS_EINVAL, "chkdiv: null output");
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  g_ctx_mir.reset();
+  cudaStream_t st = 0;
+  const size_t ub = sizeof(double) * (size_t)(nx + 2 * nh_u) * (ny + 2 * nh_u) * (nz + 2 * nh_u);
+  Staged su, sv, sw, sz;
+  TRY(stage_in(g_ctx_mir, u, ub, true, false, st, &su));
+  TRY(stage_in(g_ctx_mir, v, ub, true, false, st, &sv));
+  TRY(stage_in(g_ctx_mir, w, ub, true, false, st, &sw));
+  TRY(stage_in(g_ctx_mir, dzfi, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sz));
+  const int grid = stream_grid((long)nx * ny * nz);
+  TRY(g_ctx_small[0].ensure(sizeof(double) * 2 * grid));
+  DivArgs da;
+  da.u = su.d; da.v = sv.d; da.w = sw.d; da.dzfi = sz.d + (nh_d - 1);
+  da.dxi = dxi; da.dyi = dyi;
+  da.g = Geo{nx, ny, nz, nh_u};
+  k_chkdiv<<<grid, 256, 0, st>>>(da, g_ctx_small[0].as<double>());
+  CK(cudaGetLastError());
+  std::vector<double> part(2 * grid);
+  CK(cudaMemcpyAsync(part.data(), g_ctx_small[0].p, sizeof(double) * 2 * grid, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  double tot = 0.0, mx = 0.0;
+  for (int i = 0; i < grid; i++) {
+    tot += part[2 * i];
+    mx = std::fmax(mx, part[2 * i + 1]);
+  }
+  *divtot = tot;
+  *divmax = mx;
+  return FLUTAS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// boundp on a device halo array with the plan-less BoundArgs kernel
+int boundp_dev(double *p, const int n[3], const char cbc[6], const double bc[6], const double dl[3], double dzc0,
+               double dzcn, cudaStream_t st) {
+  const int nx = n[0], ny = n[1], nz = n[2];
+  const double dr[3][2] = {{dl[0], dl[0]}, {dl[1], dl[1]}, {dzc0, dzcn}};
+  for (int d = 0; d < 3; d++) {
+    BoundArgs ba;
+    ba.p = p;
+    ba.g = Geo{nx, ny, nz, 1};
+    ba.idir = d + 1;
+    ba.ctype0 = cbc[2 * d];
+    ba.ctype1 = cbc[2 * d + 1];
+    auto fs = [&](char ct, int ib, double rv, double drv, double *f, double *s) {
+      if (ct == 'D') { *f = 2.0 * rv; *s = -1.0; }
+      else if (ct == 'N') { *f = ib == 0 ? -drv * rv : drv * rv; *s = 1.0; }
+      else { *f = 0.0; *s = 0.0; }
+    };
+    fs(ba.ctype0, 0, bc[2 * d], dr[d][0], &ba.f0, &ba.s0);
+    fs(ba.ctype1, 1, bc[2 * d + 1], dr[d][1], &ba.f1, &ba.s1);
+    long cnt = d == 0 ? (long)(ny + 2) * (nz + 2) : (d == 1 ? (long)(nx + 2) * (nz + 2) : (long)(nx + 2) * (ny + 2));
+    k_boundp_dir<<<stream_grid(cnt), 256, 0, st>>>(ba);
+    CK(cudaGetLastError());
+  }
+  return 0;
+}
+
+int updt_rhs_b_dev(double *p, Geo g, const double *rx, const double *ry, const double *rz, int q1, int q2, int q3,
+                   cudaStream_t st) {
+  const double *r[3] = {rx, ry, rz};
+  const int q[3] = {q1, q2, q3};
+  const long cnt[3] = {(long)g.ny * g.nz, (long)g.nx * g.nz, (long)g.nx * g.ny};
+  for (int d = 0; d < 3; d++) {
+    RhsbArgs ra{p, r[d], g, d + 1, q[d]};
+    k_updt_rhs_b_dir<<<stream_grid(cnt[d]), 256, 0, st>>>(ra);
+    CK(cudaGetLastError());
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int flutas_gb300_updt_rhs_b(int nx, int ny, int nz, const char c_or_f[3], const char cbc[6], int nh_p,
+                            const double *rhsbx, const double *rhsby, const double *rhsbz, double *p) {
+  // src/bound.f90:829-944 (single domain: every face is a physical boundary)
+  if (!c_or_f || !cbc) return fail(FLUTAS_EINVAL, "updt_rhs_b: null argument");
+  if (nh_p != 1) return fail(FLUTAS_EUNSUPPORTED, "updt_rhs_b: nh_p must be 1");
+  const int q1 = (c_or_f[0] == 'f' && cbc[1] == 'D'), q2 = (c_or_f[1] == 'f' && cbc[3] == 'D'),
+            q3 = (c_or_f[2] == 'f' && cbc[5] == 'D');
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  g_ctx_mir.reset();
+  cudaStream_t st = 0;
+  const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+  Staged sp, sx, sy, sz;
+  TRY(stage_in(g_ctx_mir, p, pb, true, true, st, &sp));
+  TRY(stage_in(g_ctx_mir, rhsbx, sizeof(double) * 2 * (size_t)ny * nz, true, false, st, &sx));
+  TRY(stage_in(g_ctx_mir, rhsby, sizeof(double) * 2 * (size_t)nx * nz, true, false, st, &sy));
+  TRY(stage_in(g_ctx_mir, rhsbz, sizeof(double) * 2 * (size_t)nx * ny, true, false, st, &sz));
+  TRY(updt_rhs_b_dev(sp.d, Geo{nx, ny, nz, 1}, sx.d, sy.d, sz.d, q1, q2, q3, st));
+  TRY(stage_out(sp, st));
+  CK(cudaStreamSynchronize(st));
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, double dzi, int nh_d, int nh_u,
+                             const double *dzci, double rho0i, double f_t12, double f_t12_o, const double *p,
+                             const double *pold, const double *rho, double *u, double *v, double *w) {
+  // src/source.f90:247-309, constant-coefficient branch (289-295)
+  (void)dzi;
+  if (f_t12_o == 0.0) return fail(FLUTAS_EINVAL, "pres_tw_src: f_t12_o == 0");
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  g_ctx_mir.reset();
+  cudaStream_t st = 0;
+  const size_t ub = sizeof(double) * (size_t)(nx + 2 * nh_u) * (ny + 2 * nh_u) * (nz + 2 * nh_u);
+  const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+  Staged su, sv, sw, sp, so, sr, sz;
+  TRY(stage_in(g_ctx_mir, u, ub, true, true, st, &su));
+  TRY(stage_in(g_ctx_mir, v, ub, true, true, st, &sv));
+  TRY(stage_in(g_ctx_mir, w, ub, true, true, st, &sw));
+  TRY(stage_in(g_ctx_mir, p, pb, true, false, st, &sp));
+  TRY(stage_in(g_ctx_mir, pold, pb, true, false, st, &so));
+  TRY(stage_in(g_ctx_mir, rho, pb, true, false, st, &sr));
+  TRY(stage_in(g_ctx_mir, dzci, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sz));
+  PresTwArgs a;
+  a.p = sp.d; a.pold = so.d; a.rho = sr.d; a.dzci = sz.d + (nh_d - 1);
+  a.u = su.d; a.v = sv.d; a.w = sw.d;
+  a.dxi = dxi; a.dyi = dyi; a.rho0i = rho0i; a.f_t12 = f_t12;
+  a.f1 = 1.0 + (f_t12 / f_t12_o);
+  a.f2 = (f_t12 / f_t12_o);
+  a.g = Geo{nx, ny, nz, nh_u};
+  k_pres_tw_src<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(a);
+  CK(cudaGetLastError());
+  TRY(stage_out(su, st));
+  TRY(stage_out(sv, st));
+  TRY(stage_out(sw, st));
+  CK(cudaStreamSynchronize(st));
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_projection(void *plan, int nh_u, double dxi, double dyi, const double *dzci, const double *dzfi,
+                            const double bcpre[6], double dt, double rho0, double *u, double *v, double *w,
+                            double *p, int precision, double tol, int max_iter) {
+  // fillps -> updt_rhs_b -> solver -> boundp -> correc -> p = pold + p -> boundp
+  // (src/apps/single_phase/main__single_phase.f90:705-747,
+  //  src/apps/two_phase_inc_isot/main__two_phase_inc_isot.f90:655-716)
+  flutas_plan *pl;
+  TRY(check_plan(plan, &pl));
+  if (!dzci || !dzfi || !bcpre || !u || !v || !w || !p) return fail(FLUTAS_EINVAL, "projection: null argument");
+  if (nh_u < 1 || dt == 0.0 || rho0 == 0.0) return fail(FLUTAS_EINVAL, "projection: bad nh_u/dt/rho0");
+  if (precision == 1 && (!(tol > 0.0) || max_iter < 1)) return fail(FLUTAS_EINVAL, "projection: need tol > 0, max_iter >= 1");
+  const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2], nh_d = pl->nh_d;
+  Geo g{nx, ny, nz, nh_u};
+  cudaStream_t st = pl->stream;
+  pl->mir.reset();
+  const size_t ub = sizeof(double) * (size_t)(nx + 2 * nh_u) * (ny + 2 * nh_u) * (nz + 2 * nh_u);
+  const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+  Staged su, sv, sw, sp, sci, sfi;
+  TRY(stage_in(pl->mir, u, ub, true, true, st, &su));
+  TRY(stage_in(pl->mir, v, ub, true, true, st, &sv));
+  TRY(stage_in(pl->mir, w, ub, true, true, st, &sw));
+  TRY(stage_in(pl->mir, p, pb, true, true, st, &sp));
+  TRY(stage_in(pl->mir, dzci, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sci));
+  TRY(stage_in(pl->mir, dzfi, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sfi));
+  TRY(pl->phi.ensure(pb));
+  double *phi = pl->phi.as<double>();
+  InFillps in;
+  in.u = su.d; in.v = sv.d; in.w = sw.d;
+  in.dzfi = sfi.d + (nh_d - 1);
+  in.dti = 1.0 / dt; in.dtidxi = in.dti * dxi; in.dtidyi = in.dti * dyi; in.rho0 = rho0;
+  in.rhsbx = pl->rhsb[0].as<double>(); in.rhsby = pl->rhsb[1].as<double>(); in.rhsbz = pl->rhsb[2].as<double>();
+  in.q1 = in.q2 = in.q3 = 0;
+  in.g = g;
+  const Geo gp{nx, ny, nz, 1};
+  int rc = 0;
+  if (precision == 0) {
+    TRY(pl->S64.ensure(sizeof(double) * (size_t)nx * ny * nz));
+    double *S = pl->S64.as<double>();
+    TRY(fwd_xy<double>(pl, in, S, pl->tx64, pl->ty64, pl->path64));
+    TRY(zsolve<double>(pl, S, pl->lam.as<double>(), pl->a.as<double>(), pl->b.as<double>(), pl->c.as<double>(),
+                       pl->pin_zero_mode));
+    TRY(inv_xy<double>(pl, S, OutHalo{phi, pl->normfft, gp}, pl->tx64, pl->ty64, pl->path64));
+  } else {
+    k_fillps<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(in, phi);
+    CK(cudaGetLastError());
+    rc = solve_mixed_dev(pl, phi, tol, max_iter, nullptr, nullptr);
+    if (rc != 0 && rc != FLUTAS_EITER) return rc;
+  }
+  const double dl[3] = {1.0 / dxi, 1.0 / dyi, 0.0};
+  const double dzc0 = 1.0 / pl->dzci_h[0 - 1 + nh_d], dzcn = 1.0 / pl->dzci_h[nz - 1 + nh_d];
+  TRY(boundp_dev(phi, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
+  CorrecAddArgs ca;
+  ca.phi = phi; ca.dzci = sci.d + (nh_d - 1);
+  ca.u = su.d; ca.v = sv.d; ca.w = sw.d; ca.p = sp.d;
+  ca.factori = dt * dxi; ca.factorj = dt * dyi; ca.dt = dt; ca.rho0i = 1.0 / rho0;
+  ca.g = g;
+  k_correc_padd<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(ca);
+  CK(cudaGetLastError());
+  TRY(boundp_dev(sp.d, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
+  TRY(stage_out(su, st));
+  TRY(stage_out(sv, st));
+  TRY(stage_out(sw, st));
+  TRY(stage_out(sp, st));
+  if (su.host || sp.host) CK(cudaStreamSynchronize(st));
+  TRY(finish(pl));
+  return rc;
+}
+
+}  // extern "C"

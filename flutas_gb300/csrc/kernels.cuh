@@ -1,0 +1,668 @@
+// kernels.cuh -- sm_103a kernels of the FluTAS pressure-projection path.
+//
+//   x / y transform passes  : src/solver_cpu.f90:59,65,83,89 (FFTW r2r along x, y)
+//   z tridiagonal solve      : src/solver_cpu.f90:71-77, gaussel 117-145,
+//                              gaussel_periodic 147-185, dgtsv_homebrewed 187-223
+//   fillps                   : src/fillps.f90:50-57
+//   correc                   : src/correc.f90:57-60
+//   boundp / set_bc          : src/bound.f90:146-646 (nh_p = 1, single domain)
+//   updt_rhs_b               : src/bound.f90:829-944
+//   chkdiv                   : src/chkdiv.f90:37-63
+//   pres_tw_src              : src/source.f90:247-309 (constant-coefficient branch)
+//
+// Layouts (Fortran column-major, x fastest):
+//   p-like fields  (0:nx+1, 0:ny+1, 0:nz+1)        double
+//   velocities     (1-h:nx+h, 1-h:ny+h, 1-h:nz+h)   double, h = nh_u
+//   spectral S     (nx, ny, nz) no halo             T (double or float)
+#pragma once
+#include "fft_engine.cuh"
+
+namespace fg {
+
+// ------------------------------------------------------------------ indexing
+struct Geo {
+  int nx, ny, nz;
+  int h;  // velocity halo nh_u
+  FG_HD long pidx(int i, int j, int k) const {  // Fortran (i,j,k), halo 1
+    return (long)i + (long)(nx + 2) * ((long)j + (long)(ny + 2) * (long)k);
+  }
+  FG_HD long uidx(int i, int j, int k) const {  // Fortran (i,j,k), halo h
+    return (long)(i - 1 + h) + (long)(nx + 2 * h) * ((long)(j - 1 + h) + (long)(ny + 2 * h) * (long)(k - 1 + h));
+  }
+  FG_HD long sidx(int i0, int j0, int k0) const {  // 0-based, no halo
+    return (long)i0 + (long)nx * ((long)j0 + (long)ny * (long)k0);
+  }
+};
+
+// ------------------------------------------------------- forward input modes
+// All take 0-based interior coordinates (i0,j0,k0) and return the RHS value.
+struct InHalo {  // p(1:nx,1:ny,1:nz) of a halo-1 array
+  const double *p;
+  Geo g;
+  __device__ double operator()(int i0, int j0, int k0) const { return p[g.pidx(i0 + 1, j0 + 1, k0 + 1)]; }
+};
+
+struct InPlain {  // contiguous (nx,ny,nz) FP64 array
+  const double *f;
+  Geo g;
+  __device__ double operator()(int i0, int j0, int k0) const { return f[g.sidx(i0, j0, k0)]; }
+};
+
+// fillps (src/fillps.f90:50-57) + optional updt_rhs_b (src/bound.f90:829-944)
+struct InFillps {
+  const double *u, *v, *w, *dzfi;  // dzfi is (1-nh_d:), already offset so dzfi[k] = dzfi(k)
+  double dti, dtidxi, dtidyi, rho0;
+  const double *rhsbx, *rhsby, *rhsbz;  // nullable
+  int q1, q2, q3;
+  Geo g;
+  __device__ double operator()(int i0, int j0, int k0) const {
+    const int i = i0 + 1, j = j0 + 1, k = k0 + 1;
+    double val = ((w[g.uidx(i, j, k)] - w[g.uidx(i, j, k - 1)]) * dti * dzfi[k] +
+                  (v[g.uidx(i, j, k)] - v[g.uidx(i, j - 1, k)]) * dtidyi +
+                  (u[g.uidx(i, j, k)] - u[g.uidx(i - 1, j, k)]) * dtidxi);
+    val = val * rho0;
+    if (rhsbx) {
+      const int nx = g.nx, ny = g.ny, nz = g.nz;
+      if (i == 1) val += rhsbx[(j - 1) + (long)ny * (k - 1)];
+      if (i == nx - q1) val += rhsbx[(j - 1) + (long)ny * (k - 1) + (long)ny * nz];
+      if (j == 1) val += rhsby[(i - 1) + (long)nx * (k - 1)];
+      if (j == ny - q2) val += rhsby[(i - 1) + (long)nx * (k - 1) + (long)nx * nz];
+      if (k == 1) val += rhsbz[(i - 1) + (long)nx * (j - 1)];
+      if (k == nz - q3) val += rhsbz[(i - 1) + (long)nx * (j - 1) + (long)nx * ny];
+    }
+    return val;
+  }
+};
+
+// FP64 residual r = f - A x of the cell-centred 7-point operator that the
+// solver inverts (ghost rules of src/initsolver.f90:188-246 tridmatrix and the
+// x/y eigenvalues: P wrap, N p0=p1, D p0=-p1).  f and x are halo-1 arrays.
+struct InResidual {
+  const double *f, *x;
+  const double *dzci, *dzfi;  // offset so that dzci[k] = dzci(k)
+  double dxi2, dyi2;
+  char bc[6];
+  Geo g;
+  __device__ double ghost(char b, double pc, double pw) const { return b == 'P' ? pw : (b == 'N' ? pc : -pc); }
+  __device__ double operator()(int i0, int j0, int k0) const {
+    const int i = i0 + 1, j = j0 + 1, k = k0 + 1, nx = g.nx, ny = g.ny, nz = g.nz;
+    const double pc = x[g.pidx(i, j, k)];
+    const double pw = i > 1 ? x[g.pidx(i - 1, j, k)] : ghost(bc[0], pc, x[g.pidx(nx, j, k)]);
+    const double pe = i < nx ? x[g.pidx(i + 1, j, k)] : ghost(bc[1], pc, x[g.pidx(1, j, k)]);
+    const double ps = j > 1 ? x[g.pidx(i, j - 1, k)] : ghost(bc[2], pc, x[g.pidx(i, ny, k)]);
+    const double pn = j < ny ? x[g.pidx(i, j + 1, k)] : ghost(bc[3], pc, x[g.pidx(i, 1, k)]);
+    const double pb = k > 1 ? x[g.pidx(i, j, k - 1)] : ghost(bc[4], pc, x[g.pidx(i, j, nz)]);
+    const double pt = k < nz ? x[g.pidx(i, j, k + 1)] : ghost(bc[5], pc, x[g.pidx(i, j, 1)]);
+    const double ax = ((pe - pc) - (pc - pw)) * dxi2;
+    const double ay = ((pn - pc) - (pc - ps)) * dyi2;
+    const double az = ((pt - pc) * dzci[k] - (pc - pb) * dzci[k - 1]) * dzfi[k];
+    return f[g.pidx(i, j, k)] - (ax + ay + az);
+  }
+};
+
+// ------------------------------------------------------ inverse output modes
+struct OutHalo {  // p(i,j,k) = v * scale
+  double *p;
+  double scale;
+  Geo g;
+  __device__ void operator()(int i0, int j0, int k0, double v) const { p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = v * scale; }
+};
+struct OutHaloAdd {  // p(i,j,k) += v * scale  (iterative-refinement update, FP64)
+  double *p;
+  double scale;
+  Geo g;
+  __device__ void operator()(int i0, int j0, int k0, double v) const { p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] += v * scale; }
+};
+
+// ---------------------------------------------------------------- smem sizes
+template <typename T> FG_HD size_t align_up(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Row-batch geometry for the x pass: M rows (even) of length nx, pitch P.
+FG_HD int xpitch(int nx) { return nx + 1; }
+
+// ===========================================================================
+// x pass (forward): rows -> spectral rows.  One CTA handles M rows at a time.
+// ===========================================================================
+template <typename T>
+struct StoreRowsS {  // store into S rows: line l of this batch -> global row row0+l
+  T *S;
+  long row0, rows;
+  int nx;
+  __device__ void pair(int c, int t, T v0, T v1) {
+    const long r0 = row0 + 2 * c;
+    if (r0 < rows) S[r0 * nx + t] = v0;
+    if (r0 + 1 < rows) S[(r0 + 1) * nx + t] = v1;
+  }
+  __device__ void single(int c, int t, T v) {
+    const long r = row0 + c;
+    if (r < rows) S[r * nx + t] = v;
+  }
+};
+
+template <typename T, typename In>
+__global__ void __launch_bounds__(256) k_xfwd(AxisPlan ax, In in, T *S, Geo g, int M) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nx = g.nx, P = xpitch(nx);
+  T *A = (T *)smem_raw;
+  C2<T> *C1 = (C2<T> *)(smem_raw + align_up<T>(sizeof(T) * (size_t)M * P));
+  C2<T> *C2b = (C2<T> *)A;  // ping-pong partner aliases the input rows
+  const long rows = (long)g.ny * g.nz;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int B = cbatch(ax.pair, M);
+  for (long row0 = (long)blockIdx.x * M; row0 < rows; row0 += (long)gridDim.x * M) {
+    for (int idx = tid; idx < M * nx; idx += nth) {
+      const int m = idx / nx, x = idx % nx;
+      const long r = row0 + m;
+      T v = (T)0;
+      if (r < rows) v = (T)in(x, (int)(r % g.ny), (int)(r / g.ny));
+      A[m * P + x] = v;
+    }
+    __syncthreads();
+    pre_fwd<T>(ax, A, P, 1, M, C1, B, tid, nth);
+    __syncthreads();
+    C2<T> *cur = C1, *nxt = C2b;
+    int Ns = 1;
+    for (int s = 0; s < ax.nst; s++) {
+      stage_dispatch<T, false>(ax.radix[s], cur, nxt, ax.N, B, B, Ns, (const C2<T> *)ax.W, tid, nth);
+      Ns *= ax.radix[s];
+      C2<T> *t = cur; cur = nxt; nxt = t;
+      __syncthreads();
+    }
+    StoreRowsS<T> st{S, row0, rows, nx};
+    post_fwd<T>(ax, cur, B, M, st, tid, nth);
+    __syncthreads();
+  }
+}
+
+// x pass (inverse): spectral rows -> output functor, times normfft
+template <typename T, typename Out>
+struct StoreRowsOut {
+  Out out;
+  long row0, rows;
+  int ny;
+  __device__ void put(long r, int t, T v) {
+    if (r < rows) out(t, (int)(r % ny), (int)(r / ny), (double)v);
+  }
+  __device__ void pair(int c, int t, T v0, T v1) { put(row0 + 2 * c, t, v0); put(row0 + 2 * c + 1, t, v1); }
+  __device__ void single(int c, int t, T v) { put(row0 + c, t, v); }
+};
+
+template <typename T, typename Out>
+__global__ void __launch_bounds__(256) k_xinv(AxisPlan ax, const T *S, Out out, Geo g, int M) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nx = g.nx, P = xpitch(nx);
+  T *A = (T *)smem_raw;
+  C2<T> *C1 = (C2<T> *)(smem_raw + align_up<T>(sizeof(T) * (size_t)M * P));
+  C2<T> *C2b = (C2<T> *)A;
+  const long rows = (long)g.ny * g.nz;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int B = cbatch(ax.pair, M);
+  const bool inv = fft_inverse(ax.pair, true);
+  for (long row0 = (long)blockIdx.x * M; row0 < rows; row0 += (long)gridDim.x * M) {
+    for (int idx = tid; idx < M * nx; idx += nth) {
+      const int m = idx / nx, x = idx % nx;
+      const long r = row0 + m;
+      A[m * P + x] = r < rows ? S[r * nx + x] : (T)0;
+    }
+    __syncthreads();
+    pre_bwd<T>(ax, A, P, 1, M, C1, B, tid, nth);
+    __syncthreads();
+    C2<T> *cur = C1, *nxt = C2b;
+    int Ns = 1;
+    for (int s = 0; s < ax.nst; s++) {
+      if (inv) stage_dispatch<T, true>(ax.radix[s], cur, nxt, ax.N, B, B, Ns, (const C2<T> *)ax.W, tid, nth);
+      else stage_dispatch<T, false>(ax.radix[s], cur, nxt, ax.N, B, B, Ns, (const C2<T> *)ax.W, tid, nth);
+      Ns *= ax.radix[s];
+      C2<T> *t = cur; cur = nxt; nxt = t;
+      __syncthreads();
+    }
+    StoreRowsOut<T, Out> st{out, row0, rows, g.ny};
+    post_bwd<T>(ax, cur, B, M, st, tid, nth);
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// y pass: a tile of W columns (all ny rows) of one z-plane.  S -> S.
+// ===========================================================================
+template <typename T>
+struct StoreColsS {  // line l of the tile = column x0+l; position t = row y
+  T *S;
+  long plane_off;
+  int nx, x0, W;
+  __device__ void pair(int c, int t, T v0, T v1) {
+    const int x = x0 + 2 * c;
+    T *dst = S + plane_off + (long)t * nx + x;
+    if (2 * c + 1 < W) { dst[0] = v0; dst[1] = v1; }
+    else if (2 * c < W) dst[0] = v0;
+  }
+  __device__ void single(int c, int t, T v) {
+    if (c < W) S[plane_off + (long)t * nx + x0 + c] = v;
+  }
+};
+
+template <typename T, bool BACKWARD>
+__global__ void __launch_bounds__(256) k_ypass(AxisPlan ay, T *S, Geo g, int W) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ny = g.ny, nx = g.nx;
+  T *A = (T *)smem_raw;  // ny rows x W
+  C2<T> *C1 = (C2<T> *)(smem_raw + align_up<T>(sizeof(T) * (size_t)W * ny));
+  C2<T> *C2b = (C2<T> *)A;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int tiles_x = (nx + W - 1) / W;
+  const long ntiles = (long)tiles_x * g.nz;
+  const int B = cbatch(ay.pair, W);
+  const bool inv = fft_inverse(ay.pair, BACKWARD);
+  for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int tx = (int)(tile % tiles_x), k = (int)(tile / tiles_x);
+    const int x0 = tx * W, Wv = min(W, nx - x0);
+    const long off = (long)k * nx * ny;
+    for (int idx = tid; idx < W * ny; idx += nth) {
+      const int y = idx / W, xx = idx % W;
+      A[idx] = xx < Wv ? S[off + (long)y * nx + x0 + xx] : (T)0;
+    }
+    __syncthreads();
+    if (BACKWARD) pre_bwd<T>(ay, A, 1, W, W, C1, B, tid, nth);
+    else pre_fwd<T>(ay, A, 1, W, W, C1, B, tid, nth);
+    __syncthreads();
+    C2<T> *cur = C1, *nxt = C2b;
+    int Ns = 1;
+    for (int s = 0; s < ay.nst; s++) {
+      if (inv) stage_dispatch<T, true>(ay.radix[s], cur, nxt, ay.N, B, B, Ns, (const C2<T> *)ay.W, tid, nth);
+      else stage_dispatch<T, false>(ay.radix[s], cur, nxt, ay.N, B, B, Ns, (const C2<T> *)ay.W, tid, nth);
+      Ns *= ay.radix[s];
+      C2<T> *t = cur; cur = nxt; nxt = t;
+      __syncthreads();
+    }
+    StoreColsS<T> st{S, off, nx, x0, Wv};
+    if (BACKWARD) post_bwd<T>(ay, cur, B, W, st, tid, nth);
+    else post_fwd<T>(ay, cur, B, W, st, tid, nth);
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// Fused x+y plane pass (one CTA owns a whole z-plane in shared memory).
+// Forward: In -> x transform -> y transform -> S.
+// Inverse: S -> y^-1 -> x^-1 -> Out.
+// Shared memory: two buffers of nx*ny reals (plus row padding of the first).
+// ===========================================================================
+template <typename T>
+struct StorePlaneReal {  // write real plane (row-major y*pitch + x)
+  T *R;
+  int pitch, rowbase;  // line l = row rowbase + l for x lines
+  __device__ void pair(int c, int t, T v0, T v1) {
+    R[(long)(2 * c) * pitch + t] = v0;
+    R[(long)(2 * c + 1) * pitch + t] = v1;
+  }
+  __device__ void single(int c, int t, T v) { R[(long)c * pitch + t] = v; }
+};
+template <typename T>
+struct StorePlaneRealCols {  // columns as lines: line l = column l, position t = row
+  T *R;
+  int pitch;
+  __device__ void pair(int c, int t, T v0, T v1) {
+    R[(long)t * pitch + 2 * c] = v0;
+    R[(long)t * pitch + 2 * c + 1] = v1;
+  }
+  __device__ void single(int c, int t, T v) { R[(long)t * pitch + c] = v; }
+};
+
+template <typename T, bool INV>
+__device__ __forceinline__ C2<T> *run_stages(const AxisPlan &ap, C2<T> *cur, C2<T> *nxt, int B, int tid, int nth) {
+  int Ns = 1;
+  for (int s = 0; s < ap.nst; s++) {
+    stage_dispatch<T, INV>(ap.radix[s], cur, nxt, ap.N, B, B, Ns, (const C2<T> *)ap.W, tid, nth);
+    Ns *= ap.radix[s];
+    C2<T> *t = cur; cur = nxt; nxt = t;
+    __syncthreads();
+  }
+  return cur;
+}
+
+template <typename T, typename In>
+__global__ void __launch_bounds__(512) k_xyfwd_plane(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nx = g.nx, ny = g.ny, P = xpitch(nx);
+  T *A = (T *)smem_raw;  // ny x P
+  T *Bu = (T *)(smem_raw + align_up<T>(sizeof(T) * (size_t)ny * P));  // nx*ny reals
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int k = blockIdx.x; k < g.nz; k += gridDim.x) {
+    for (int idx = tid; idx < nx * ny; idx += nth) {
+      const int y = idx / nx, x = idx % nx;
+      A[y * P + x] = (T)in(x, y, k);
+    }
+    __syncthreads();
+    // ---- x transform: lines = rows of A
+    const int Bx = cbatch(ax.pair, ny);
+    pre_fwd<T>(ax, A, P, 1, ny, (C2<T> *)Bu, Bx, tid, nth);
+    __syncthreads();
+    C2<T> *fin = run_stages<T, false>(ax, (C2<T> *)Bu, (C2<T> *)A, Bx, tid, nth);
+    T *G = (fin == (C2<T> *)Bu) ? A : Bu;   // free buffer for the real x-spectrum
+    const int gp = (G == A) ? P : nx;
+    StorePlaneReal<T> sx{G, gp, 0};
+    post_fwd<T>(ax, fin, Bx, ny, sx, tid, nth);
+    __syncthreads();
+    // ---- y transform: lines = columns of G
+    const int By = cbatch(ay.pair, nx);
+    C2<T> *F = (C2<T> *)(G == A ? Bu : A);
+    pre_fwd<T>(ay, G, 1, gp, nx, F, By, tid, nth);
+    __syncthreads();
+    C2<T> *fy = run_stages<T, false>(ay, F, (C2<T> *)G, By, tid, nth);
+    StoreColsS<T> st{S, (long)k * nx * ny, nx, 0, nx};
+    post_fwd<T>(ay, fy, By, nx, st, tid, nth);
+    __syncthreads();
+  }
+}
+
+template <typename T, typename Out>
+__global__ void __launch_bounds__(512) k_xyinv_plane(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nx = g.nx, ny = g.ny, P = xpitch(nx);
+  T *A = (T *)smem_raw;
+  T *Bu = (T *)(smem_raw + align_up<T>(sizeof(T) * (size_t)ny * P));
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const bool invx = fft_inverse(ax.pair, true), invy = fft_inverse(ay.pair, true);
+  for (int k = blockIdx.x; k < g.nz; k += gridDim.x) {
+    const T *Sp = S + (long)k * nx * ny;
+    for (int idx = tid; idx < nx * ny; idx += nth) {
+      const int y = idx / nx, x = idx % nx;
+      A[y * P + x] = Sp[idx];
+    }
+    __syncthreads();
+    // ---- y^-1: lines = columns of A
+    const int By = cbatch(ay.pair, nx);
+    pre_bwd<T>(ay, A, 1, P, nx, (C2<T> *)Bu, By, tid, nth);
+    __syncthreads();
+    C2<T> *fy = invy ? run_stages<T, true>(ay, (C2<T> *)Bu, (C2<T> *)A, By, tid, nth)
+                     : run_stages<T, false>(ay, (C2<T> *)Bu, (C2<T> *)A, By, tid, nth);
+    T *G = (fy == (C2<T> *)Bu) ? A : Bu;
+    const int gp = (G == A) ? P : nx;
+    StorePlaneRealCols<T> sy{G, gp};
+    post_bwd<T>(ay, fy, By, nx, sy, tid, nth);
+    __syncthreads();
+    // ---- x^-1: lines = rows of G
+    const int Bx = cbatch(ax.pair, ny);
+    C2<T> *F = (C2<T> *)(G == A ? Bu : A);
+    pre_bwd<T>(ax, G, gp, 1, ny, F, Bx, tid, nth);
+    __syncthreads();
+    C2<T> *fx = invx ? run_stages<T, true>(ax, F, (C2<T> *)G, Bx, tid, nth)
+                     : run_stages<T, false>(ax, F, (C2<T> *)G, Bx, tid, nth);
+    StoreRowsOut<T, Out> st{out, (long)k * ny, (long)(k + 1) * ny, ny};
+    post_bwd<T>(ax, fx, Bx, ny, st, tid, nth);
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// z solve: Thomas per (kx,ky) column (src/solver_cpu.f90:117-223).
+// A CTA stages TC consecutive columns (all nz levels) in shared memory.
+// Columns are indexed q = kx + nx*ky; element (q,k) at S[q + nx*ny*k].
+// ===========================================================================
+struct ZArgs {
+  const double *a, *b, *c;   // tridmatrix coefficients (nz)
+  const double *lam;         // lambdaxy (nx*ny)
+  int nq;                    // nx*ny columns
+  int nz;                    // full nz
+  int nn;                    // nz - q   (solver_cpu.f90:71-72)
+  int periodic;              // bcz == 'PP'
+  int pin;                   // 1: the singular (lam == 0) column of an N/P z problem is pinned
+};
+
+// Thomas on a column in shared memory (stride ts), in place; d scratch (stride ts).
+// T is the arithmetic type.  Follows dgtsv_homebrewed step by step.
+template <typename T, typename St>
+__device__ __forceinline__ void thomas_col(int n, const double *a, const double *b, const double *c,
+                                           double lam, St *p, St *d, int ts, bool pin_last) {
+  T z = (T)1 / (T)(b[0] + lam);
+  d[0] = (St)((T)c[0] * z);
+  p[0] = (St)((T)p[0] * z);
+  for (int l = 1; l < n - 1; l++) {
+    z = (T)1 / ((T)(b[l] + lam) - (T)a[l] * (T)d[(l - 1) * ts]);
+    d[l * ts] = (St)((T)c[l] * z);
+    p[l * ts] = (St)(((T)p[l * ts] - (T)a[l] * (T)p[(l - 1) * ts]) * z);
+  }
+  T zl = (T)(b[n - 1] + lam) - (T)a[n - 1] * (T)d[(n - 2) * ts];
+  if (zl != (T)0 && !pin_last) p[(n - 1) * ts] = (St)(((T)p[(n - 1) * ts] - (T)a[n - 1] * (T)p[(n - 2) * ts]) / zl);
+  else p[(n - 1) * ts] = (St)0;
+  for (int l = n - 2; l >= 0; l--) p[l * ts] = (St)((T)p[l * ts] - (T)d[l * ts] * (T)p[(l + 1) * ts]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_zsolve(ZArgs za, T *S) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int TC = blockDim.x, nz = za.nz, tid = threadIdx.x;
+  T *col = (T *)smem_raw;        // nz x TC
+  T *dd = col + (long)nz * TC;   // nz x TC
+  T *p2 = dd + (long)nz * TC;    // nz x TC (periodic only)
+  const long plane = za.nq;
+  for (long q0 = (long)blockIdx.x * TC; q0 < za.nq; q0 += (long)gridDim.x * TC) {
+    const int tcv = (int)min((long)TC, za.nq - q0);
+    for (int idx = tid; idx < nz * TC; idx += TC) {
+      const int k = idx / TC, t = idx % TC;
+      if (t < tcv) col[idx] = S[q0 + t + plane * k];
+    }
+    __syncthreads();
+    if (tid < tcv) {
+      const long q = q0 + tid;
+      const double lam = za.lam[q];
+      T *pc = col + tid, *dc = dd + tid;
+      const int n = za.nn;
+      if (!za.periodic) {
+        const bool pin = za.pin && lam == 0.0;
+        thomas_col<T, T>(n, za.a, za.b, za.c, lam, pc, dc, TC, pin);
+      } else {
+        // gaussel_periodic (solver_cpu.f90:147-185)
+        T *p2c = p2 + tid;
+        for (int k = 0; k < n; k++) p2c[k * TC] = (T)0;
+        p2c[0] = (T)(-za.a[0]);
+        p2c[(n - 2) * TC] = (T)(-za.c[n - 2]);
+        thomas_col<T, T>(n - 1, za.a, za.b, za.c, lam, pc, dc, TC, false);
+        thomas_col<T, T>(n - 1, za.a, za.b, za.c, lam, p2c, dc, TC, false);
+        const T num = (T)pc[(n - 1) * TC] - (T)za.c[n - 1] * (T)pc[0] - (T)za.a[n - 1] * (T)pc[(n - 2) * TC];
+        const T den = (T)(za.b[n - 1] + lam) + (T)za.c[n - 1] * (T)p2c[0] + (T)za.a[n - 1] * (T)p2c[(n - 2) * TC];
+        const bool pin = (za.pin && lam == 0.0) || den == (T)0;
+        const T pn = pin ? (T)0 : num / den;
+        pc[(n - 1) * TC] = pn;
+        for (int k = 0; k < n - 1; k++) pc[k * TC] = (T)pc[k * TC] + (T)p2c[k * TC] * pn;
+      }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < nz * TC; idx += TC) {
+      const int k = idx / TC, t = idx % TC;
+      if (t < tcv) S[q0 + t + plane * k] = col[idx];
+    }
+    __syncthreads();
+  }
+}
+
+// ===========================================================================
+// Stencil kernels (drop-in entry points).  One thread per interior cell.
+// ===========================================================================
+__global__ void k_fillps(InFillps in, double *p) {
+  const Geo &g = in.g;
+  const long N = (long)g.nx * g.ny * g.nz;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
+    const int i0 = (int)(t % g.nx), j0 = (int)((t / g.nx) % g.ny), k0 = (int)(t / ((long)g.nx * g.ny));
+    p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = in(i0, j0, k0);
+  }
+}
+
+struct CorrecArgs {
+  const double *p, *dzci;  // dzci offset: dzci[k] = dzci(k)
+  double *u, *v, *w;
+  double factori, factorj, dt, rho0i;
+  Geo g;
+};
+__global__ void k_correc(CorrecArgs a) {
+  // src/correc.f90:57-60
+  const Geo &g = a.g;
+  const long N = (long)g.nx * g.ny * g.nz;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
+    const double pc = a.p[g.pidx(i, j, k)];
+    const long ui = g.uidx(i, j, k);
+    a.u[ui] = a.u[ui] - a.factori * (a.p[g.pidx(i + 1, j, k)] - pc) * a.rho0i;
+    a.v[ui] = a.v[ui] - a.factorj * (a.p[g.pidx(i, j + 1, k)] - pc) * a.rho0i;
+    a.w[ui] = a.w[ui] - a.dt * a.dzci[k] * (a.p[g.pidx(i, j, k + 1)] - pc) * a.rho0i;
+  }
+}
+
+// boundp for one direction: set_bc (src/bound.f90:227-646), centred, nh_p = 1.
+struct BoundArgs {
+  double *p;
+  Geo g;
+  int idir;           // 1,2,3
+  char ctype0, ctype1;
+  double f0, s0, f1, s1;  // ghost = f + s * inner
+};
+__global__ void k_boundp_dir(BoundArgs a) {
+  const Geo &g = a.g;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  long n1, n2;
+  if (a.idir == 1) { n1 = ny + 2; n2 = nz + 2; }
+  else if (a.idir == 2) { n1 = nx + 2; n2 = nz + 2; }
+  else { n1 = nx + 2; n2 = ny + 2; }
+  const long N = n1 * n2;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
+    const int s = (int)(t % n1), r = (int)(t / n1);
+    long lo, lo_in, hi, hi_in, lo_wrap, hi_wrap;
+    if (a.idir == 1) {
+      lo = g.pidx(0, s, r); lo_in = g.pidx(1, s, r); hi = g.pidx(nx + 1, s, r); hi_in = g.pidx(nx, s, r);
+    } else if (a.idir == 2) {
+      lo = g.pidx(s, 0, r); lo_in = g.pidx(s, 1, r); hi = g.pidx(s, ny + 1, r); hi_in = g.pidx(s, ny, r);
+    } else {
+      lo = g.pidx(s, r, 0); lo_in = g.pidx(s, r, 1); hi = g.pidx(s, r, nz + 1); hi_in = g.pidx(s, r, nz);
+    }
+    lo_wrap = hi_in; hi_wrap = lo_in;  // periodic copies: p(0)=p(n), p(n+1)=p(1)
+    double plo, phi;
+    if (a.ctype0 == 'P') plo = a.p[lo_wrap]; else plo = a.f0 + a.s0 * a.p[lo_in];
+    if (a.ctype1 == 'P') phi = a.p[hi_wrap]; else phi = a.f1 + a.s1 * a.p[hi_in];
+    a.p[lo] = plo;
+    a.p[hi] = phi;
+  }
+}
+
+// divergence check: per-block partial (sum, max) in double
+struct DivArgs {
+  const double *u, *v, *w, *dzfi;  // dzfi[k] = dzfi(k)
+  double dxi, dyi;
+  Geo g;
+};
+__global__ void k_chkdiv(DivArgs a, double *partial) {
+  const Geo &g = a.g;
+  const long N = (long)g.nx * g.ny * g.nz;
+  double tot = 0.0, mx = 0.0;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
+    const double div = (a.w[g.uidx(i, j, k)] - a.w[g.uidx(i, j, k - 1)]) * a.dzfi[k] +
+                       (a.v[g.uidx(i, j, k)] - a.v[g.uidx(i, j - 1, k)]) * a.dyi +
+                       (a.u[g.uidx(i, j, k)] - a.u[g.uidx(i - 1, j, k)]) * a.dxi;
+    tot += div;
+    mx = fmax(mx, fabs(div));
+  }
+  __shared__ double s_tot[32], s_mx[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    tot += __shfl_down_sync(0xffffffffu, tot, o);
+    mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { s_tot[wid] = tot; s_mx[wid] = mx; }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    tot = lane < nw ? s_tot[lane] : 0.0;
+    mx = lane < nw ? s_mx[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      tot += __shfl_down_sync(0xffffffffu, tot, o);
+      mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    }
+    if (lane == 0) { partial[2 * blockIdx.x] = tot; partial[2 * blockIdx.x + 1] = mx; }
+  }
+}
+
+}  // namespace fg
+
+namespace fg {
+
+// updt_rhs_b (src/bound.f90:829-944) for one direction: add rhs planes.
+struct RhsbArgs {
+  double *p;
+  const double *rhs;  // (n1, n2, 0:1)
+  Geo g;
+  int idir, q;
+};
+__global__ void k_updt_rhs_b_dir(RhsbArgs a) {
+  const Geo &g = a.g;
+  int n1, n2;
+  if (a.idir == 1) { n1 = g.ny; n2 = g.nz; }
+  else if (a.idir == 2) { n1 = g.nx; n2 = g.nz; }
+  else { n1 = g.nx; n2 = g.ny; }
+  const long N = (long)n1 * n2;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
+    const int s = (int)(t % n1) + 1, r = (int)(t / n1) + 1;
+    long lo, hi;
+    if (a.idir == 1) { lo = g.pidx(1, s, r); hi = g.pidx(g.nx - a.q, s, r); }
+    else if (a.idir == 2) { lo = g.pidx(s, 1, r); hi = g.pidx(s, g.ny - a.q, r); }
+    else { lo = g.pidx(s, r, 1); hi = g.pidx(s, r, g.nz - a.q); }
+    a.p[lo] += a.rhs[t];
+    a.p[hi] += a.rhs[t + N];
+  }
+}
+
+// pres_tw_src (src/source.f90:247-309), _CONSTANT_COEFFS_POISSON branch.
+struct PresTwArgs {
+  const double *p, *pold, *rho, *dzci;  // dzci[k] = dzci(k)
+  double *u, *v, *w;
+  double dxi, dyi, rho0i, f_t12, f1, f2;
+  Geo g;
+};
+__device__ __forceinline__ void pres_tw_cell(const PresTwArgs &a, int i, int j, int k) {
+  const Geo &g = a.g;
+  const long c0 = g.pidx(i, j, k), cx = g.pidx(i + 1, j, k), cy = g.pidx(i, j + 1, k), cz = g.pidx(i, j, k + 1);
+  const double rhoxi = 1.0 / (0.5 * (a.rho[cx] + a.rho[c0]));
+  const double rhoyi = 1.0 / (0.5 * (a.rho[cy] + a.rho[c0]));
+  const double rhozi = 1.0 / (0.5 * (a.rho[cz] + a.rho[c0]));
+  const double dzc = a.dzci[k];
+  const double q0 = a.f1 * a.p[c0] - a.f2 * a.pold[c0];
+  const long ui = g.uidx(i, j, k);
+  a.u[ui] = a.u[ui] + a.f_t12 * ((-(a.p[cx] - a.p[c0]) * a.dxi) * a.rho0i -
+                                 (rhoxi - a.rho0i) * ((a.f1 * a.p[cx] - a.f2 * a.pold[cx]) - q0) * a.dxi);
+  a.v[ui] = a.v[ui] + a.f_t12 * ((-(a.p[cy] - a.p[c0]) * a.dyi) * a.rho0i -
+                                 (rhoyi - a.rho0i) * ((a.f1 * a.p[cy] - a.f2 * a.pold[cy]) - q0) * a.dyi);
+  a.w[ui] = a.w[ui] + a.f_t12 * ((-(a.p[cz] - a.p[c0]) * dzc) * a.rho0i -
+                                 (rhozi - a.rho0i) * ((a.f1 * a.p[cz] - a.f2 * a.pold[cz]) - q0) * dzc);
+}
+__global__ void k_pres_tw_src(PresTwArgs a) {
+  const Geo &g = a.g;
+  const long N = (long)g.nx * g.ny * g.nz;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
+    pres_tw_cell(a, i, j, k);
+  }
+}
+
+// correc with the pressure increment phi, fused with p = p + phi
+// (src/correc.f90:57-60 and the update of src/apps/two_phase_inc_isot/main__two_phase_inc_isot.f90:698-714).
+struct CorrecAddArgs {
+  const double *phi, *dzci;
+  double *u, *v, *w, *p;
+  double factori, factorj, dt, rho0i;
+  Geo g;
+};
+__global__ void k_correc_padd(CorrecAddArgs a) {
+  const Geo &g = a.g;
+  const long N = (long)g.nx * g.ny * g.nz;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
+    const long pc = g.pidx(i, j, k);
+    const double ph = a.phi[pc];
+    const long ui = g.uidx(i, j, k);
+    a.u[ui] = a.u[ui] - a.factori * (a.phi[g.pidx(i + 1, j, k)] - ph) * a.rho0i;
+    a.v[ui] = a.v[ui] - a.factorj * (a.phi[g.pidx(i, j + 1, k)] - ph) * a.rho0i;
+    a.w[ui] = a.w[ui] - a.dt * a.dzci[k] * (a.phi[g.pidx(i, j, k + 1)] - ph) * a.rho0i;
+    a.p[pc] = a.p[pc] + ph;
+  }
+}
+
+}  // namespace fg

@@ -1,0 +1,145 @@
+/*
+ * flutas_gb300.h -- C ABI of the GB300-native FluTAS pressure-projection path.
+ *
+ * The entry points keep the argument lists of the Fortran routines they
+ * replace, so a FluTAS app binds them through iso_c_binding with a one-line
+ * `use` swap.  Plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Arrays are Fortran column-major (x fastest) and are passed as the address
+ *    of their first element: p(0:nx+1,0:ny+1,0:nz+1) with halo 1; velocities
+ *    u,v,w(1-nh_u:nx+nh_u, ...); z spacings dzci,dzfi(1-nh_d:nz+nh_d).
+ *  - Field pointers may be device pointers (CUDA device or managed memory:
+ *    used in place) or host pointers (pageable or pinned: copied to
+ *    library-owned device mirrors and back inside the call).
+ *  - BC characters are 'P','N','D'; cbc is the Fortran cbc(0:1,1:3) in
+ *    memory order (x-low, x-high, y-low, y-high, z-low, z-high).
+ *  - Every call returns FLUTAS_OK (0) or a negative code; the message of the
+ *    last failure on the calling thread is available from
+ *    flutas_gb300_last_error().  Nothing aborts the process, nothing traps
+ *    the device.
+ *  - Calls are synchronous (drop-in semantics) unless the plan was switched
+ *    to asynchronous mode with flutas_gb300_plan_set_stream().
+ */
+#ifndef FLUTAS_GB300_H
+#define FLUTAS_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define FLUTAS_API __attribute__((visibility("default")))
+#else
+#define FLUTAS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FLUTAS_OK 0
+#define FLUTAS_EINVAL (-1)       /* bad argument: size, BC character, null pointer */
+#define FLUTAS_EUNSUPPORTED (-2) /* combination the GPU path does not implement */
+#define FLUTAS_ECUDA (-3)        /* CUDA runtime error */
+#define FLUTAS_ENOMEM (-4)       /* device allocation failed or over the HBM budget */
+#define FLUTAS_EITER (-5)        /* iterative refinement hit its iteration limit */
+#define FLUTAS_ENONFINITE (-6)   /* NaN/Inf found in the input or the result */
+#define FLUTAS_EBUSY (-7)        /* serving queue full / request not finished */
+
+/* Replaces initsolver (src/initsolver.f90:21, with fftini src/fft.f90:24-157).
+ * Host outputs exactly as the reference: lambdaxy(nx,ny), a,b,c(nz), normfft,
+ * rhsbx(ny,nz,0:1), rhsby(nx,nz,0:1), rhsbz(nx,ny,0:1).  arrplan points at the
+ * Fortran arrplan(2,2) of type(C_PTR): element (1,1) receives the opaque plan
+ * (device-resident eigenvalues, z coefficients, twiddles and scratch); the
+ * other three are set to NULL.  dims / dims_z of the reference are 1 (one GPU). */
+FLUTAS_API int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const double *dzci,
+                            const double *dzfi, const char cbc[6], const double bc[6],
+                            const char c_or_f[3], double *lambdaxy, double *a, double *b,
+                            double *c, void **arrplan, double *normfft, double *rhsbx,
+                            double *rhsby, double *rhsbz);
+
+/* Replaces solver_cpu (src/solver_cpu.f90:20) / solver_gpu (src/solver_gpu.f90:31):
+ * FP64 fwd x/y r2r transforms, z tridiagonal solve per (kx,ky), inverse
+ * transforms, times normfft.  p(0:n+1,...) in place (interior overwritten).
+ * lambdaxy/a/b/c may be the host arrays filled by initsolver (the plan's
+ * device copies are used) or device arrays. */
+FLUTAS_API int flutas_gb300_solver(const int n[3], void *const *arrplan, double normfft,
+                        const double *lambdaxy, const double *a, const double *b, const double *c,
+                        const char bcz[2], const char c_or_f[3], double *p);
+
+/* Replaces fillps (src/fillps.f90:16): p = rho0 * dti * div(u,v,w). */
+FLUTAS_API int flutas_gb300_fillps(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, double dyi,
+                        double dzi, const double *dzfi, double dti, double rho0, const double *u,
+                        const double *v, const double *w, double *p);
+
+/* Replaces correc (src/correc.f90:16), constant-coefficient branch (57-60):
+ * u -= dt*dxi*(p(i+1)-p(i))/rho0, etc.  rho is accepted for signature
+ * compatibility and not read (the reference never builds the variable branch). */
+FLUTAS_API int flutas_gb300_correc(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, double dyi,
+                        double dzi, const double *dzci, double dt, double rho0, const double *p,
+                        double *u, double *v, double *w, const double *rho);
+
+/* Replaces boundp (src/bound.f90:146) for a single domain with nh_p = 1:
+ * ghost cells of p per set_bc (src/bound.f90:227-646), x then y then z.
+ * halo is accepted for signature compatibility (MPI halo types, unused). */
+FLUTAS_API int flutas_gb300_boundp(const char cbc[6], const int n[3], const double bc[6], int nh_d, int nh_p,
+                        const int halo[3], const double dl[3], const double *dzc,
+                        const double *dzf, double *p);
+
+/* Replaces updt_rhs_b (src/bound.f90:829): adds the inhomogeneous-BC terms
+ * rhsbx/rhsby/rhsbz (host or device) to the boundary planes of p. */
+FLUTAS_API int flutas_gb300_updt_rhs_b(int nx, int ny, int nz, const char c_or_f[3], const char cbc[6],
+                            int nh_p, const double *rhsbx, const double *rhsby,
+                            const double *rhsbz, double *p);
+
+/* Replaces chkdiv (src/chkdiv.f90:18) on one GPU: total and max |div u|. */
+FLUTAS_API int flutas_gb300_chkdiv(int nx, int ny, int nz, double dxi, double dyi, double dzi, int nh_d,
+                        int nh_u, const double *dzfi, const double *u, const double *v,
+                        const double *w, double *divtot, double *divmax);
+
+/* Replaces pres_tw_src (src/source.f90:247), constant-coefficient
+ * (Dodd-Ferrante) branch: adds the explicit pressure terms to u*,v*,w*. */
+FLUTAS_API int flutas_gb300_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, double dzi, int nh_d,
+                             int nh_u, const double *dzci, double rho0i, double f_t12,
+                             double f_t12_o, const double *p, const double *pold,
+                             const double *rho, double *u, double *v, double *w);
+
+/* Replaces fftend (src/fft.f90:159-179): frees the plan in arrplan(1,1). */
+FLUTAS_API int flutas_gb300_fftend(void **arrplan);
+
+/* Copies the message of the last failure on this thread into buf (NUL-terminated). */
+FLUTAS_API int flutas_gb300_last_error(char *buf, int len);
+
+/* ---------------------------------------------------------------------------
+ * Extensions beyond the reference interface (no Fortran counterpart).
+ * ------------------------------------------------------------------------- */
+
+/* Asynchronous mode: run the plan's work on `stream` (a cudaStream_t, or NULL
+ * for the legacy default stream) and return without synchronising. */
+FLUTAS_API int flutas_gb300_plan_set_stream(void *plan, void *stream, int synchronous);
+
+/* Mixed-precision solve: FP32 transforms and tridiagonal solves, FP64
+ * residual of the 7-point operator and FP64 update, iterated until
+ * ||f - A p||_2 / ||f||_2 <= tol or max_iter corrections.  Same in/out as
+ * flutas_gb300_solver (p holds the RHS on entry, the solution on exit).
+ * relres/iters (nullable) receive the achieved relative residual and the
+ * number of FP32 solves.  Returns FLUTAS_EITER if tol was not reached. */
+FLUTAS_API int flutas_gb300_solve_mixed(void *plan, double *p, double tol, int max_iter, double *relres,
+                             int *iters);
+
+/* Fused projection (one call for the steps of src/apps/<app>/main__<app>.f90: fillps ->
+ * updt_rhs_b -> solver -> boundp -> correc -> p = pold + p -> boundp):
+ * on exit u,v,w are projected and p holds pold + phi.  precision: 0 = FP64,
+ * 1 = mixed to tol.  dzci/dzfi: (1-nh_d:nz+nh_d).  bcpre = bc(0:1,1:3). */
+FLUTAS_API int flutas_gb300_projection(void *plan, int nh_u, double dxi, double dyi, const double *dzci,
+                            const double *dzfi, const double bcpre[6], double dt, double rho0,
+                            double *u, double *v, double *w, double *p, int precision,
+                            double tol, int max_iter);
+
+/* Plan introspection: bytes of device memory held by the plan, and which
+ * transform path it uses (0 = separate x/y passes, 1 = fused plane kernel). */
+FLUTAS_API int flutas_gb300_plan_info(void *plan, size_t *device_bytes, int *xy_path_fp64, int *xy_path_fp32);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLUTAS_GB300_H */

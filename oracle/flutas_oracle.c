@@ -1,0 +1,701 @@
+/*
+ * flutas_oracle.c -- CPU FP64 restatement of the FluTAS pressure-projection
+ * path.  TEST INFRASTRUCTURE ONLY: the checker for the CUDA path (tests,
+ * smoke(), bench.py's CPU-baseline leg).  The product library never links it.
+ *
+ * "parity unpinned" against the reference binary: the reference solver_cpu
+ * depends on FFTW 3.3.10 (getting_started/REQ.md, src/targets/target.generic-gnu:25),
+ * which is not vendored, and on gfortran, which is absent.  The r2r transforms
+ * below are written from FFTW's published definitions of R2HC/HC2R and
+ * REDFTab/RODFTab; the solver steps follow the Fortran line by line (citations
+ * at each function).  The restatement is pinned by discrete-eigenfunction
+ * known answers and an independent scipy.fft restatement (see tests/).
+ *
+ * Build: gcc -O2 -fopenmp -ffp-contract=off -shared -fPIC (oracle/Makefile).
+ * -ffp-contract=off keeps results identical on x86_64 and aarch64 hosts.
+ */
+#include "flutas_oracle.h"
+
+#include <complex.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef double _Complex cplx;
+
+/* ------------------------------------------------------------------------- */
+/* threads                                                                    */
+/* ------------------------------------------------------------------------- */
+static int g_threads = 0;
+void or_set_threads(int nthreads) { g_threads = nthreads; }
+int or_get_threads(void) {
+#ifdef _OPENMP
+  return g_threads > 0 ? g_threads : omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+#define NT or_get_threads()
+
+/* ------------------------------------------------------------------------- */
+/* Mixed-radix complex FFT (recursive decimation in time), own code.          */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  int n, nf;
+  int f[64];
+  cplx *w; /* w[t] = exp(-2 pi i t / n) */
+} cplan;
+
+#define MAX_PLANS 64
+static cplan *g_plans[MAX_PLANS];
+static int g_nplans = 0;
+
+static cplan *make_plan(int n) {
+  cplan *p = (cplan *)calloc(1, sizeof(cplan));
+  p->n = n;
+  int m = n;
+  while (m % 4 == 0) { p->f[p->nf++] = 4; m /= 4; }
+  while (m % 2 == 0) { p->f[p->nf++] = 2; m /= 2; }
+  for (int q = 3; q * q <= m; q += 2)
+    while (m % q == 0) { p->f[p->nf++] = q; m /= q; }
+  if (m > 1) p->f[p->nf++] = m;
+  p->w = (cplx *)malloc(sizeof(cplx) * (size_t)n);
+  for (int t = 0; t < n; t++) {
+    /* angle 2 pi t / n evaluated in long double, rounded once to double */
+    long double a = 2.0L * 3.141592653589793238462643383279502884L * (long double)t / (long double)n;
+    p->w[t] = (double)cosl(a) - I * (double)sinl(a);
+  }
+  return p;
+}
+
+static const cplan *get_plan(int n) {
+  const cplan *res = NULL;
+#pragma omp critical(or_plan_cache)
+  {
+    for (int i = 0; i < g_nplans; i++)
+      if (g_plans[i]->n == n) { res = g_plans[i]; break; }
+    if (!res) {
+      cplan *p = make_plan(n);
+      if (g_nplans < MAX_PLANS) g_plans[g_nplans++] = p;
+      res = p;
+    }
+  }
+  return res;
+}
+
+static inline cplx tw(const cplan *P, long e, int sign) {
+  cplx w = P->w[e % P->n];
+  return sign < 0 ? w : conj(w);
+}
+
+/* out[0..n) = DFT_n(in[0], in[is], ...), sign -1 forward, +1 backward (unnormalised). */
+static void fft_rec(const cplan *P, int n, const cplx *in, long is, cplx *out, int fi, int sign) {
+  if (n == 1) { out[0] = in[0]; return; }
+  const int p = P->f[fi], m = n / p;
+  for (int r = 0; r < p; r++) fft_rec(P, m, in + r * is, is * p, out + (long)r * m, fi + 1, sign);
+  const long s = P->n / n;       /* W_n^e = W_N^(e*s) */
+  const long sp = P->n / p;      /* W_p^e = W_N^(e*sp) */
+  if (p == 2) {
+    for (int k = 0; k < m; k++) {
+      cplx a = out[k], b = out[k + m] * tw(P, (long)k * s, sign);
+      out[k] = a + b; out[k + m] = a - b;
+    }
+    return;
+  }
+  if (p == 4) {
+    const cplx j = sign < 0 ? -I : I;
+    for (int k = 0; k < m; k++) {
+      cplx a0 = out[k];
+      cplx a1 = out[k + m] * tw(P, (long)k * s, sign);
+      cplx a2 = out[k + 2 * m] * tw(P, 2L * k * s, sign);
+      cplx a3 = out[k + 3 * m] * tw(P, 3L * k * s, sign);
+      cplx t0 = a0 + a2, t1 = a0 - a2, t2 = a1 + a3, t3 = (a1 - a3) * j;
+      out[k] = t0 + t2; out[k + m] = t1 + t3; out[k + 2 * m] = t0 - t2; out[k + 3 * m] = t1 - t3;
+    }
+    return;
+  }
+  cplx stackbuf[2 * 64];
+  cplx *t = p <= 64 ? stackbuf : (cplx *)malloc(sizeof(cplx) * 2 * (size_t)p);
+  cplx *o = t + p;
+  for (int k = 0; k < m; k++) {
+    for (int r = 0; r < p; r++) t[r] = out[(long)r * m + k] * tw(P, (long)r * k * s, sign);
+    for (int q = 0; q < p; q++) {
+      cplx acc = 0;
+      for (int r = 0; r < p; r++) acc += t[r] * tw(P, (long)((r * q) % p) * sp, sign);
+      o[q] = acc;
+    }
+    for (int q = 0; q < p; q++) out[k + (long)q * m] = o[q];
+  }
+  if (p > 64) free(t);
+}
+
+static void cfft(int n, const cplx *in, cplx *out, int sign) {
+  const cplan *P = get_plan(n);
+  fft_rec(P, n, in, 1, out, 0, sign);
+}
+
+/* ------------------------------------------------------------------------- */
+/* r2r transforms, FFTW definitions (unnormalised).                           */
+/* scratch: at least 4*(n+1) complex values.                                  */
+/* ------------------------------------------------------------------------- */
+static void r2r_line(int kind, int n, const double *x, double *y, cplx *scr) {
+  cplx *z = scr, *Z = scr + 2 * (n + 1);
+  const double pi = 3.141592653589793238462643383279502884;
+  switch (kind) {
+  case OR_R2HC: {
+    for (int j = 0; j < n; j++) z[j] = x[j];
+    cfft(n, z, Z, -1);
+    for (int k = 0; k <= n / 2; k++) y[k] = creal(Z[k]);
+    for (int k = 1; k <= (n - 1) / 2; k++) y[n - k] = cimag(Z[k]);
+  } break;
+  case OR_HC2R: {
+    z[0] = x[0];
+    for (int k = 1; k <= (n - 1) / 2; k++) { z[k] = x[k] + I * x[n - k]; z[n - k] = x[k] - I * x[n - k]; }
+    if (n % 2 == 0) z[n / 2] = x[n / 2];
+    cfft(n, z, Z, +1);
+    for (int j = 0; j < n; j++) y[j] = creal(Z[j]);
+  } break;
+  case OR_REDFT10: { /* Makhoul: even samples forward, odd samples reversed */
+    for (int j = 0; 2 * j < n; j++) z[j] = x[2 * j];
+    for (int j = 0; 2 * j + 1 < n; j++) z[n - 1 - j] = x[2 * j + 1];
+    cfft(n, z, Z, -1);
+    for (int k = 0; k < n; k++) y[k] = 2.0 * creal(cexp(-I * pi * k / (2.0 * n)) * Z[k]);
+  } break;
+  case OR_REDFT01: {
+    for (int k = 0; k < n; k++) {
+      double xnk = (k == 0) ? 0.0 : x[n - k];
+      z[k] = cexp(I * pi * k / (2.0 * n)) * (x[k] - I * xnk);
+    }
+    cfft(n, z, Z, +1);
+    for (int j = 0; 2 * j < n; j++) y[2 * j] = creal(Z[j]);
+    for (int j = 0; 2 * j + 1 < n; j++) y[2 * j + 1] = creal(Z[n - 1 - j]);
+  } break;
+  case OR_RODFT10: { /* DST-II(x)_k = DCT-II((-1)^j x_j)_{n-1-k} */
+    double *xs = (double *)calloc(2 * (size_t)n, sizeof(double)), *ys = xs + n;
+    for (int j = 0; j < n; j++) xs[j] = (j & 1) ? -x[j] : x[j];
+    r2r_line(OR_REDFT10, n, xs, ys, scr);
+    for (int k = 0; k < n; k++) y[k] = ys[n - 1 - k];
+    free(xs);
+  } break;
+  case OR_RODFT01: { /* DST-III(X)_j = (-1)^j DCT-III(X reversed)_j */
+    double *xs = (double *)calloc(2 * (size_t)n, sizeof(double)), *ys = xs + n;
+    for (int k = 0; k < n; k++) xs[k] = x[n - 1 - k];
+    r2r_line(OR_REDFT01, n, xs, ys, scr);
+    for (int j = 0; j < n; j++) y[j] = (j & 1) ? -ys[j] : ys[j];
+    free(xs);
+  } break;
+  case OR_REDFT11: { /* 2n-point DFT of x_j e^{-i pi j/(2n)} */
+    for (int j = 0; j < n; j++) z[j] = x[j] * cexp(-I * pi * j / (2.0 * n));
+    for (int j = n; j < 2 * n; j++) z[j] = 0;
+    cfft(2 * n, z, Z, -1);
+    for (int k = 0; k < n; k++) y[k] = 2.0 * creal(cexp(-I * pi * (2 * k + 1) / (4.0 * n)) * Z[k]);
+  } break;
+  case OR_RODFT11: { /* DST-IV(x)_k = DCT-IV((-1)^j x_j)_{n-1-k} */
+    double *xs = (double *)calloc(2 * (size_t)n, sizeof(double)), *ys = xs + n;
+    for (int j = 0; j < n; j++) xs[j] = (j & 1) ? -x[j] : x[j];
+    r2r_line(OR_REDFT11, n, xs, ys, scr);
+    for (int k = 0; k < n; k++) y[k] = ys[n - 1 - k];
+    free(xs);
+  } break;
+  case OR_REDFT00: { /* even extension, length 2(n-1) */
+    if (n == 1) { y[0] = x[0]; break; }
+    int N = 2 * (n - 1);
+    for (int j = 0; j < n; j++) z[j] = x[j];
+    for (int j = 1; j < n - 1; j++) z[N - j] = x[j];
+    cfft(N, z, Z, -1);
+    for (int k = 0; k < n; k++) y[k] = creal(Z[k]);
+  } break;
+  case OR_RODFT00: { /* odd extension, length 2(n+1) */
+    int N = 2 * (n + 1);
+    z[0] = 0; z[n + 1] = 0;
+    for (int j = 0; j < n; j++) { z[j + 1] = x[j]; z[N - 1 - j] = -x[j]; }
+    cfft(N, z, Z, -1);
+    for (int k = 0; k < n; k++) y[k] = -cimag(Z[k + 1]);
+  } break;
+  default: break;
+  }
+}
+
+static int kind_ok(int kind) {
+  return kind == OR_R2HC || kind == OR_HC2R || (kind >= OR_REDFT00 && kind <= OR_RODFT11);
+}
+
+int or_r2r(int kind, int n, const double *in, double *out) {
+  if (n < 1 || !kind_ok(kind)) return -1;
+  cplx *scr = (cplx *)malloc(sizeof(cplx) * 4 * (size_t)(n + 2));
+  r2r_line(kind, n, in, out, scr);
+  free(scr);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* initsolver pieces                                                          */
+/* ------------------------------------------------------------------------- */
+int or_eigenvalues(int n, char bc0, char bc1, char c_or_f, double *lambda) {
+  /* initsolver.f90:122-186 (CPU branch: natural / halfcomplex-compatible order) */
+  const double pi = 3.141592653589793238462643383279502884; /* mod_param pi = acos(-1) */
+  double s;
+  if (bc0 == 'P' && bc1 == 'P') {
+    for (int l = 1; l <= n; l++) { s = sin((1.0 * (l - 1)) * pi / (1.0 * n)); lambda[l - 1] = -4.0 * s * s; }
+  } else if (bc0 == 'N' && bc1 == 'N') {
+    if (c_or_f == 'c') {
+      for (int l = 1; l <= n; l++) { s = sin((1.0 * (l - 1)) * pi / (2.0 * n)); lambda[l - 1] = -4.0 * s * s; }
+    } else {
+      for (int l = 1; l <= n; l++) { s = sin((1.0 * (l - 1)) * pi / (2.0 * (n - 1 + 1))); lambda[l - 1] = -4.0 * s * s; }
+    }
+  } else if (bc0 == 'D' && bc1 == 'D') {
+    if (c_or_f == 'c') {
+      for (int l = 1; l <= n; l++) { s = sin((1.0 * (l - 0)) * pi / (2.0 * n)); lambda[l - 1] = -4.0 * s * s; }
+    } else {
+      /* point n is a boundary (not transformed); the reference leaves it unset, 0 here */
+      for (int l = 1; l <= n - 1; l++) { s = sin((1.0 * (l - 0)) * pi / (2.0 * (n + 1 - 1))); lambda[l - 1] = -4.0 * s * s; }
+      lambda[n - 1] = 0.0;
+    }
+  } else if ((bc0 == 'N' && bc1 == 'D') || (bc0 == 'D' && bc1 == 'N')) {
+    for (int l = 1; l <= n; l++) { s = sin((1.0 * (2 * l - 1)) * pi / (4.0 * n)); lambda[l - 1] = -4.0 * s * s; }
+  } else {
+    return -1;
+  }
+  return 0;
+}
+
+static double bcfactor_trid(char bc) { return bc == 'D' ? -1.0 : (bc == 'N' ? 1.0 : 0.0); }
+
+int or_tridmatrix(char bc0, char bc1, int n, int nh_d, const double *dzci, const double *dzfi,
+                  char c_or_f, double *a, double *b, double *c) {
+  /* initsolver.f90:188-246; dzci/dzfi are (1-nh_d:), so Fortran index k -> [k-1+nh_d] */
+#define DZCI(k) dzci[(k) - 1 + nh_d]
+#define DZFI(k) dzfi[(k) - 1 + nh_d]
+  if (c_or_f == 'c') {
+    for (int k = 1; k <= n; k++) { a[k - 1] = DZFI(k) * DZCI(k - 1); c[k - 1] = DZFI(k) * DZCI(k); }
+  } else if (c_or_f == 'f') {
+    for (int k = 1; k <= n; k++) { a[k - 1] = DZFI(k) * DZCI(k); c[k - 1] = DZFI(k + 1) * DZCI(k); }
+  } else return -1;
+#undef DZCI
+#undef DZFI
+  for (int k = 0; k < n; k++) b[k] = -(a[k] + c[k]);
+  double f0 = bcfactor_trid(bc0), f1 = bcfactor_trid(bc1);
+  if (c_or_f == 'c') {
+    b[0] = b[0] + f0 * a[0];
+    b[n - 1] = b[n - 1] + f1 * c[n - 1];
+  } else {
+    if (bc0 == 'N') b[0] = b[0] + f0 * a[0];
+    if (bc1 == 'N') b[n - 1] = b[n - 1] + f1 * c[n - 1];
+  }
+  return 0;
+}
+
+int or_find_fft(char bc0, char bc1, char c_or_f, int *kf, int *kb, double norm[2]) {
+  /* fft.f90:233-291 */
+  char s[3] = {bc0, bc1, 0};
+  if (c_or_f == 'c') {
+    if (!strcmp(s, "PP")) { *kf = OR_R2HC; *kb = OR_HC2R; norm[0] = 1; norm[1] = 0; }
+    else if (!strcmp(s, "NN")) { *kf = OR_REDFT10; *kb = OR_REDFT01; norm[0] = 2; norm[1] = 0; }
+    else if (!strcmp(s, "DD")) { *kf = OR_RODFT10; *kb = OR_RODFT01; norm[0] = 2; norm[1] = 0; }
+    else if (!strcmp(s, "ND")) { *kf = OR_REDFT11; *kb = OR_REDFT11; norm[0] = 2; norm[1] = 0; }
+    else if (!strcmp(s, "DN")) { *kf = OR_RODFT11; *kb = OR_RODFT11; norm[0] = 2; norm[1] = 0; }
+    else return -1;
+  } else if (c_or_f == 'f') {
+    if (!strcmp(s, "PP")) { *kf = OR_R2HC; *kb = OR_HC2R; norm[0] = 1; norm[1] = 0; }
+    else if (!strcmp(s, "NN")) { *kf = OR_REDFT00; *kb = OR_REDFT00; norm[0] = 2; norm[1] = -1; }
+    else if (!strcmp(s, "DD")) { *kf = OR_RODFT00; *kb = OR_RODFT00; norm[0] = 2; norm[1] = 1; }
+    else if (!strcmp(s, "ND")) { *kf = OR_REDFT10; *kb = OR_REDFT01; norm[0] = 2; norm[1] = 0; }
+    else if (!strcmp(s, "DN")) { *kf = OR_RODFT01; *kb = OR_RODFT10; norm[0] = 2; norm[1] = 0; }
+    else return -1;
+  } else return -1;
+  return 0;
+}
+
+static void bc_rhs(const char cbc[2], int n1, int n2, const double bc[2], const double dlc[2],
+                   const double dlf[2], char c_or_f, double *rhs) {
+  /* initsolver.f90:248-298; rhs is (n1, n2, 0:1) */
+  double factor[2];
+  for (int ib = 0; ib < 2; ib++) {
+    double sgn = ib == 0 ? 1.0 : -1.0;
+    if (cbc[ib] == 'P') factor[ib] = 0.0;
+    else if (cbc[ib] == 'D') factor[ib] = c_or_f == 'c' ? -2.0 * bc[ib] : -bc[ib];
+    else factor[ib] = sgn * (c_or_f == 'c' ? dlc[ib] : dlf[ib]) * bc[ib];
+  }
+  for (int ib = 0; ib < 2; ib++) {
+    double v = factor[ib] / dlc[ib] / dlf[ib];
+    for (long t = 0; t < (long)n1 * n2; t++) rhs[(long)ib * n1 * n2 + t] = v;
+  }
+}
+
+int or_initsolver(const int n[3], const double dli[3], int nh_d, const double *dzci,
+                  const double *dzfi, const char cbc[6], const double bc[6], const char c_or_f[3],
+                  double *lambdaxy, double *a, double *b, double *c, or_plan *plan, double *normfft,
+                  double *rhsbx, double *rhsby, double *rhsbz) {
+  const int nx = n[0], ny = n[1], nz = n[2];
+  double *lx = (double *)malloc(sizeof(double) * nx), *ly = (double *)malloc(sizeof(double) * ny);
+  if (or_eigenvalues(nx, cbc[0], cbc[1], c_or_f[0], lx) || or_eigenvalues(ny, cbc[2], cbc[3], c_or_f[1], ly)) {
+    free(lx); free(ly); return -1;
+  }
+  for (int i = 0; i < nx; i++) lx[i] = lx[i] * (dli[0] * dli[0]);
+  for (int j = 0; j < ny; j++) ly[j] = ly[j] * (dli[1] * dli[1]);
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) lambdaxy[i + (long)nx * j] = lx[i] + ly[j];
+  free(lx); free(ly);
+  if (or_tridmatrix(cbc[4], cbc[5], nz, nh_d, dzci, dzfi, c_or_f[2], a, b, c)) return -1;
+  /* bc_rhs: dl = 1/dli, dzc = 1/dzci, dzf = 1/dzfi */
+  double dl[3] = {1.0 / dli[0], 1.0 / dli[1], 1.0 / dli[2]};
+#define DZC(k) (1.0 / dzci[(k) - 1 + nh_d])
+#define DZF(k) (1.0 / dzfi[(k) - 1 + nh_d])
+  double dlx[2] = {dl[0], dl[0]}, dly[2] = {dl[1], dl[1]};
+  bc_rhs(cbc + 0, ny, nz, bc + 0, dlx, dlx, c_or_f[0], rhsbx);
+  bc_rhs(cbc + 2, nx, nz, bc + 2, dly, dly, c_or_f[1], rhsby);
+  if (c_or_f[2] == 'c') {
+    double dlc[2] = {DZC(0), DZC(nz)}, dlf[2] = {DZF(1), DZF(nz)};
+    bc_rhs(cbc + 4, nx, ny, bc + 4, dlc, dlf, c_or_f[2], rhsbz);
+  } else {
+    double dlc[2] = {DZC(1), DZC(nz - 1)}, dlf[2] = {DZF(1), DZF(nz)};
+    bc_rhs(cbc + 4, nx, ny, bc + 4, dlc, dlf, c_or_f[2], rhsbz);
+  }
+#undef DZC
+#undef DZF
+  /* fftini (fft.f90:24-157) */
+  double norm[2], nf = 1.0;
+  plan->n[0] = nx; plan->n[1] = ny; plan->n[2] = nz;
+  plan->ix = (cbc[0] == 'D' && cbc[1] == 'D' && c_or_f[0] == 'f') ? 1 : 0;
+  plan->iy = (cbc[2] == 'D' && cbc[3] == 'D' && c_or_f[1] == 'f') ? 1 : 0;
+  if (or_find_fft(cbc[0], cbc[1], c_or_f[0], &plan->kind_fwd[0], &plan->kind_bwd[0], norm)) return -1;
+  nf = nf * norm[0] * (nx + norm[1] - plan->ix);
+  if (or_find_fft(cbc[2], cbc[3], c_or_f[1], &plan->kind_fwd[1], &plan->kind_bwd[1], norm)) return -1;
+  nf = nf * norm[0] * (ny + norm[1] - plan->iy);
+  *normfft = 1.0 / nf;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* solver_cpu                                                                 */
+/* ------------------------------------------------------------------------- */
+static void dgtsv_homebrewed(int n, const double *a, const double *b, const double *c, double *p, double *d) {
+  /* solver_cpu.f90:187-223 (Thomas, zero-pivot pin at 209-214) */
+  double z = 1.0 / b[0];
+  d[0] = c[0] * z;
+  p[0] = p[0] * z;
+  for (int l = 1; l < n - 1; l++) {
+    z = 1.0 / (b[l] - a[l] * d[l - 1]);
+    d[l] = c[l] * z;
+    p[l] = (p[l] - a[l] * p[l - 1]) * z;
+  }
+  z = b[n - 1] - a[n - 1] * d[n - 2];
+  if (z != 0.0) p[n - 1] = (p[n - 1] - a[n - 1] * p[n - 2]) / z;
+  else p[n - 1] = 0.0;
+  for (int l = n - 2; l >= 0; l--) p[l] = p[l] - d[l] * p[l + 1];
+}
+
+static void transform_x(const or_plan *pl, int fwd, double *px) {
+  const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2], len = nx - pl->ix;
+  const int kind = fwd ? pl->kind_fwd[0] : pl->kind_bwd[0];
+#pragma omp parallel num_threads(NT)
+  {
+    cplx *scr = (cplx *)malloc(sizeof(cplx) * 4 * (size_t)(nx + 2));
+    double *line = (double *)malloc(sizeof(double) * (size_t)nx);
+#pragma omp for schedule(static)
+    for (long jk = 0; jk < (long)ny * nz; jk++) {
+      double *row = px + jk * nx;
+      r2r_line(kind, len, row, line, scr);
+      memcpy(row, line, sizeof(double) * len);
+    }
+    free(scr); free(line);
+  }
+}
+
+static void transform_y(const or_plan *pl, int fwd, double *px) {
+  const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2], len = ny - pl->iy;
+  const int kind = fwd ? pl->kind_fwd[1] : pl->kind_bwd[1];
+#pragma omp parallel num_threads(NT)
+  {
+    cplx *scr = (cplx *)malloc(sizeof(cplx) * 4 * (size_t)(ny + 2));
+    double *in = (double *)malloc(sizeof(double) * 2 * (size_t)ny), *out = in + ny;
+#pragma omp for schedule(static)
+    for (long ik = 0; ik < (long)nx * nz; ik++) {
+      long i = ik % nx, k = ik / nx;
+      double *base = px + k * (long)nx * ny + i;
+      for (int j = 0; j < len; j++) in[j] = base[(long)j * nx];
+      r2r_line(kind, len, in, out, scr);
+      for (int j = 0; j < len; j++) base[(long)j * nx] = out[j];
+    }
+    free(scr); free(in);
+  }
+}
+
+int or_solver(const or_plan *pl, double normfft, const double *lambdaxy, const double *a,
+              const double *b, const double *c, const char bcz[2], const char c_or_f[3], double *p) {
+  const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2];
+  const long NX = nx + 2, NY = ny + 2;
+  double *px = (double *)malloc(sizeof(double) * (size_t)nx * ny * nz);
+  if (!px) return -2;
+  /* px = p(1:n(1),1:n(2),1:n(3))   (solver_cpu.f90:40) */
+#pragma omp parallel for num_threads(NT) schedule(static)
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      memcpy(px + ((long)k * ny + j) * nx, p + 1 + NX * ((j + 1) + NY * (k + 1)), sizeof(double) * nx);
+  transform_x(pl, 1, px); /* fft(arrplan(1,1),px)  (59) */
+  transform_y(pl, 1, px); /* fft(arrplan(1,2),py)  (65) */
+  int q = (c_or_f[2] == 'f' && bcz[1] == 'D') ? 1 : 0; /* (71-72) */
+  const int nn = nz - q;
+  const int periodic = bcz[0] == 'P' && bcz[1] == 'P';
+  const long plane = (long)nx * ny;
+#pragma omp parallel num_threads(NT)
+  {
+    double *bb = (double *)malloc(sizeof(double) * 5 * (size_t)(nz + 1));
+    double *col = bb + (nz + 1), *d = col + (nz + 1), *p1 = d + (nz + 1), *p2 = p1 + (nz + 1);
+#pragma omp for schedule(static)
+    for (long ij = 0; ij < plane; ij++) {
+      const double lam = lambdaxy[ij];
+      double *base = px + ij;
+      if (!periodic) {
+        /* gaussel (117-145) */
+        for (int k = 0; k < nn; k++) { bb[k] = b[k] + lam; col[k] = base[k * plane]; }
+        dgtsv_homebrewed(nn, a, bb, c, col, d);
+        for (int k = 0; k < nn; k++) base[k * plane] = col[k];
+      } else {
+        /* gaussel_periodic (147-185) */
+        for (int k = 0; k < nz; k++) bb[k] = b[k] + lam;
+        for (int k = 0; k < nn - 1; k++) p1[k] = base[k * plane];
+        dgtsv_homebrewed(nn - 1, a, bb, c, p1, d);
+        for (int k = 0; k < nn; k++) p2[k] = 0.0;
+        p2[0] = -a[0];
+        p2[nn - 2] = -c[nn - 2];
+        dgtsv_homebrewed(nn - 1, a, bb, c, p2, d);
+        /* The singular zero mode makes the denominator exactly zero on uniform
+         * grids; the reference then returns Inf/NaN.  Any value is a valid
+         * null-space component, so the restatement (and the GPU path) pins it to 0. */
+        const double den = bb[nn - 1] + c[nn - 1] * p2[0] + a[nn - 1] * p2[nn - 2];
+        double pn = den != 0.0 ? (base[(nn - 1) * plane] - c[nn - 1] * p1[0] - a[nn - 1] * p1[nn - 2]) / den : 0.0;
+        base[(nn - 1) * plane] = pn;
+        for (int k = 0; k < nn - 1; k++) base[k * plane] = p1[k] + p2[k] * pn;
+      }
+    }
+    free(bb);
+  }
+  transform_y(pl, 0, px); /* fft(arrplan(2,2),py)  (83) */
+  transform_x(pl, 0, px); /* fft(arrplan(2,1),px)  (89) */
+  /* p(1:n) = px*normfft  (93) */
+#pragma omp parallel for num_threads(NT) schedule(static)
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++) {
+      double *dst = p + 1 + NX * ((j + 1) + NY * (k + 1));
+      const double *src = px + ((long)k * ny + j) * nx;
+      for (int i = 0; i < nx; i++) dst[i] = src[i] * normfft;
+    }
+  free(px);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* stencils                                                                   */
+/* ------------------------------------------------------------------------- */
+#define PIDX(i, j, k) ((long)(i) + NX * ((long)(j) + NY * (long)(k)))              /* halo 1, Fortran i -> i */
+#define UIDX(i, j, k) ((long)((i) - 1 + h) + UX * ((long)((j) - 1 + h) + UY * (long)((k) - 1 + h)))
+
+void or_fillps(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, double dyi, double dzi,
+               const double *dzfi, double dti, double rho0, const double *u, const double *v,
+               const double *w, double *p) {
+  /* fillps.f90:50-57 */
+  (void)dzi;
+  const long NX = nx + 2, NY = ny + 2, h = nh_u, UX = nx + 2 * h, UY = ny + 2 * h;
+  const double dtidxi = dti * dxi, dtidyi = dti * dyi;
+#pragma omp parallel for num_threads(NT) schedule(static)
+  for (int k = 1; k <= nz; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        double val = ((w[UIDX(i, j, k)] - w[UIDX(i, j, k - 1)]) * dti * dzfi[k - 1 + nh_d] +
+                      (v[UIDX(i, j, k)] - v[UIDX(i, j - 1, k)]) * dtidyi +
+                      (u[UIDX(i, j, k)] - u[UIDX(i - 1, j, k)]) * dtidxi);
+        p[PIDX(i, j, k)] = val * rho0;
+      }
+}
+
+void or_correc(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, double dyi, double dzi,
+               const double *dzci, double dt, double rho0, const double *p, double *u, double *v,
+               double *w) {
+  /* correc.f90:57-60 */
+  (void)dzi;
+  const long NX = nx + 2, NY = ny + 2, h = nh_u, UX = nx + 2 * h, UY = ny + 2 * h;
+  const double rho0i = 1.0 / rho0, factori = dt * dxi, factorj = dt * dyi;
+#pragma omp parallel for num_threads(NT) schedule(static)
+  for (int k = 1; k <= nz; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        u[UIDX(i, j, k)] = u[UIDX(i, j, k)] - factori * (p[PIDX(i + 1, j, k)] - p[PIDX(i, j, k)]) * rho0i;
+        v[UIDX(i, j, k)] = v[UIDX(i, j, k)] - factorj * (p[PIDX(i, j + 1, k)] - p[PIDX(i, j, k)]) * rho0i;
+        w[UIDX(i, j, k)] = w[UIDX(i, j, k)] - dt * dzci[k - 1 + nh_d] * (p[PIDX(i, j, k + 1)] - p[PIDX(i, j, k)]) * rho0i;
+      }
+}
+
+static void set_bc(int nx, int ny, int nz, char ctype, int ibound, int idir, double rvalue, double dr, double *p) {
+  /* bound.f90:227-646, centered = .true., nh_p = 1 (qq_d = 0) */
+  const long NX = nx + 2, NY = ny + 2;
+  double factor = rvalue, sgn = 0.0;
+  if (ctype == 'D') { factor = 2.0 * factor; sgn = -1.0; }
+  if (ctype == 'N') { factor = ibound == 0 ? -dr * factor : dr * factor; sgn = 1.0; }
+  if (ctype == 'P') {
+    if (idir == 1) {
+      for (int k = 0; k <= nz + 1; k++) for (int j = 0; j <= ny + 1; j++) {
+        p[PIDX(0, j, k)] = p[PIDX(nx, j, k)]; p[PIDX(nx + 1, j, k)] = p[PIDX(1, j, k)]; }
+    } else if (idir == 2) {
+      for (int k = 0; k <= nz + 1; k++) for (int i = 0; i <= nx + 1; i++) {
+        p[PIDX(i, 0, k)] = p[PIDX(i, ny, k)]; p[PIDX(i, ny + 1, k)] = p[PIDX(i, 1, k)]; }
+    } else {
+      for (int j = 0; j <= ny + 1; j++) for (int i = 0; i <= nx + 1; i++) {
+        p[PIDX(i, j, 0)] = p[PIDX(i, j, nz)]; p[PIDX(i, j, nz + 1)] = p[PIDX(i, j, 1)]; }
+    }
+    return;
+  }
+  if (idir == 1) {
+    for (int k = 0; k <= nz + 1; k++) for (int j = 0; j <= ny + 1; j++) {
+      if (ibound == 0) p[PIDX(0, j, k)] = factor + sgn * p[PIDX(1, j, k)];
+      else p[PIDX(nx + 1, j, k)] = factor + sgn * p[PIDX(nx, j, k)]; }
+  } else if (idir == 2) {
+    for (int k = 0; k <= nz + 1; k++) for (int i = 0; i <= nx + 1; i++) {
+      if (ibound == 0) p[PIDX(i, 0, k)] = factor + sgn * p[PIDX(i, 1, k)];
+      else p[PIDX(i, ny + 1, k)] = factor + sgn * p[PIDX(i, ny, k)]; }
+  } else {
+    for (int j = 0; j <= ny + 1; j++) for (int i = 0; i <= nx + 1; i++) {
+      if (ibound == 0) p[PIDX(i, j, 0)] = factor + sgn * p[PIDX(i, j, 1)];
+      else p[PIDX(i, j, nz + 1)] = factor + sgn * p[PIDX(i, j, nz)]; }
+  }
+}
+
+void or_boundp(const char cbc[6], const int n[3], const double bc[6], int nh_d, const double dl[3],
+               const double *dzc, const double *dzf, double *p) {
+  /* bound.f90:146-225 */
+  (void)dzf;
+  const int nx = n[0], ny = n[1], nz = n[2];
+  set_bc(nx, ny, nz, cbc[0], 0, 1, bc[0], dl[0], p);
+  set_bc(nx, ny, nz, cbc[1], 1, 1, bc[1], dl[0], p);
+  set_bc(nx, ny, nz, cbc[2], 0, 2, bc[2], dl[1], p);
+  set_bc(nx, ny, nz, cbc[3], 1, 2, bc[3], dl[1], p);
+  set_bc(nx, ny, nz, cbc[4], 0, 3, bc[4], dzc[0 - 1 + nh_d], p);
+  set_bc(nx, ny, nz, cbc[5], 1, 3, bc[5], dzc[nz - 1 + nh_d], p);
+}
+
+void or_updt_rhs_b(int nx, int ny, int nz, const char c_or_f[3], const char cbc[6],
+                   const double *rhsbx, const double *rhsby, const double *rhsbz, double *p) {
+  /* bound.f90:829-944 (single domain: every face is a physical boundary) */
+  const long NX = nx + 2, NY = ny + 2;
+  int q1 = (c_or_f[0] == 'f' && cbc[1] == 'D'), q2 = (c_or_f[1] == 'f' && cbc[3] == 'D'),
+      q3 = (c_or_f[2] == 'f' && cbc[5] == 'D');
+  for (int k = 1; k <= nz; k++) for (int j = 1; j <= ny; j++) {
+    p[PIDX(1, j, k)] += rhsbx[(j - 1) + (long)ny * (k - 1)];
+    p[PIDX(nx - q1, j, k)] += rhsbx[(j - 1) + (long)ny * (k - 1) + (long)ny * nz];
+  }
+  for (int k = 1; k <= nz; k++) for (int i = 1; i <= nx; i++) {
+    p[PIDX(i, 1, k)] += rhsby[(i - 1) + (long)nx * (k - 1)];
+    p[PIDX(i, ny - q2, k)] += rhsby[(i - 1) + (long)nx * (k - 1) + (long)nx * nz];
+  }
+  for (int j = 1; j <= ny; j++) for (int i = 1; i <= nx; i++) {
+    p[PIDX(i, j, 1)] += rhsbz[(i - 1) + (long)nx * (j - 1)];
+    p[PIDX(i, j, nz - q3)] += rhsbz[(i - 1) + (long)nx * (j - 1) + (long)nx * ny];
+  }
+}
+
+void or_chkdiv(int nx, int ny, int nz, double dxi, double dyi, double dzi, int nh_d, int nh_u,
+               const double *dzfi, const double *u, const double *v, const double *w, double *divtot,
+               double *divmax) {
+  /* chkdiv.f90:37-63 */
+  (void)dzi;
+  const long h = nh_u, UX = nx + 2 * h, UY = ny + 2 * h;
+  double tot = 0.0, mx = 0.0;
+#pragma omp parallel for num_threads(NT) reduction(+ : tot) reduction(max : mx) schedule(static)
+  for (int k = 1; k <= nz; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        double div = (w[UIDX(i, j, k)] - w[UIDX(i, j, k - 1)]) * dzfi[k - 1 + nh_d] +
+                     (v[UIDX(i, j, k)] - v[UIDX(i, j - 1, k)]) * dyi +
+                     (u[UIDX(i, j, k)] - u[UIDX(i - 1, j, k)]) * dxi;
+        double ad = fabs(div);
+        if (ad > mx) mx = ad;
+        tot += div;
+      }
+  *divtot = tot;
+  *divmax = mx;
+}
+
+void or_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, double dzi, int nh_d, int nh_u,
+                    const double *dzci, double rho0i, double f_t12, double f_t12_o, const double *p,
+                    const double *pold, const double *rho, double *u, double *v, double *w) {
+  /* source.f90:247-309, _CONSTANT_COEFFS_POISSON branch (289-295) */
+  (void)dzi;
+  const long NX = nx + 2, NY = ny + 2, h = nh_u, UX = nx + 2 * h, UY = ny + 2 * h;
+  const double f1 = 1.0 + (f_t12 / f_t12_o), f2 = (f_t12 / f_t12_o);
+#pragma omp parallel for num_threads(NT) schedule(static)
+  for (int k = 1; k <= nz; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        const long c0 = PIDX(i, j, k), cx = PIDX(i + 1, j, k), cy = PIDX(i, j + 1, k), cz = PIDX(i, j, k + 1);
+        double rhox = 0.5 * (rho[cx] + rho[c0]), rhoxi = 1.0 / rhox;
+        double rhoy = 0.5 * (rho[cy] + rho[c0]), rhoyi = 1.0 / rhoy;
+        double rhoz = 0.5 * (rho[cz] + rho[c0]), rhozi = 1.0 / rhoz;
+        const double dzc = dzci[k - 1 + nh_d];
+        u[UIDX(i, j, k)] = u[UIDX(i, j, k)] + f_t12 * ((-(p[cx] - p[c0]) * dxi) * rho0i -
+                           (rhoxi - rho0i) * ((f1 * p[cx] - f2 * pold[cx]) - (f1 * p[c0] - f2 * pold[c0])) * dxi);
+        v[UIDX(i, j, k)] = v[UIDX(i, j, k)] + f_t12 * ((-(p[cy] - p[c0]) * dyi) * rho0i -
+                           (rhoyi - rho0i) * ((f1 * p[cy] - f2 * pold[cy]) - (f1 * p[c0] - f2 * pold[c0])) * dyi);
+        w[UIDX(i, j, k)] = w[UIDX(i, j, k)] + f_t12 * ((-(p[cz] - p[c0]) * dzc) * rho0i -
+                           (rhozi - rho0i) * ((f1 * p[cz] - f2 * pold[cz]) - (f1 * p[c0] - f2 * pold[c0])) * dzc);
+      }
+}
+
+void or_initgrid(int two_end, int n, double gr, double lz, int nh_d, double *dzc, double *dzf, double *zc,
+                 double *zf) {
+  /* initgrid.f90:17-97; arrays are (1-nh_d:n+nh_d) -> index k-1+nh_d */
+#define A(x, k) x[(k) - 1 + nh_d]
+  for (int k = 1; k <= n; k++) {
+    double z0 = (k - 0.0) / (1.0 * n), z;
+    if (two_end) z = gr != 0.0 ? 0.5 * (1.0 + tanh((z0 - 0.5) * gr) / tanh(gr / 2.0)) : z0;
+    else z = gr != 0.0 ? 1.0 * (1.0 + tanh((z0 - 1.0) * gr) / tanh(gr / 1.0)) : z0;
+    A(zf, k) = z * lz;
+  }
+  A(zf, 0) = 0.0;
+  for (int k = 1; k <= n; k++) A(dzf, k) = A(zf, k) - A(zf, k - 1);
+  A(dzf, 0) = A(dzf, 1);
+  A(dzf, n + 1) = A(dzf, n);
+  for (int k = 0; k <= n; k++) A(dzc, k) = 0.5 * (A(dzf, k) + A(dzf, k + 1));
+  A(dzc, n + 1) = A(dzc, n);
+  A(zc, 0) = -A(dzc, 0) / 2.0;
+  A(zf, 0) = 0.0;
+  for (int k = 1; k <= n + 1; k++) { A(zc, k) = A(zc, k - 1) + A(dzc, k - 1); A(zf, k) = A(zf, k - 1) + A(dzf, k); }
+  for (int k = 1 - nh_d; k <= 0; k++) { A(dzf, k) = A(dzf, -k + 1); A(dzc, k) = A(dzc, -k); }
+  for (int k = n + 1; k <= n + nh_d; k++) { A(dzf, k) = A(dzf, 2 * n - k - 1); A(dzc, k) = A(dzc, 2 * n - k); }
+  for (int k = 0; k >= 1 - nh_d; k--) { A(zf, k) = A(zf, k + 1) - A(dzf, k); A(zc, k) = A(zf, k + 1) - A(dzc, k + 1); }
+  for (int k = n + 1; k <= n + nh_d; k++) { A(zf, k) = A(zf, k - 1) + A(dzf, k); A(zc, k) = A(zf, k - 1) + A(dzc, k - 1); }
+#undef A
+}
+
+void or_update_property(int nx, int ny, int nz, double rho1, double rho2, const double *psi, double *rho) {
+  const long tot = (long)(nx + 2) * (ny + 2) * (nz + 2);
+#pragma omp parallel for num_threads(NT) schedule(static)
+  for (long t = 0; t < tot; t++) rho[t] = psi[t] * rho1 + (1.0 - psi[t]) * rho2;
+}
+
+static inline double ghost_lo(char bc, double p1, double pn) { return bc == 'P' ? pn : (bc == 'N' ? p1 : -p1); }
+
+void or_residual(const int n[3], const char cbc[6], double dxi, double dyi, int nh_d, const double *dzci,
+                 const double *dzfi, const double *f, const double *p, double *r) {
+  const int nx = n[0], ny = n[1], nz = n[2];
+  const long NX = nx + 2, NY = ny + 2;
+  const double dxi2 = dxi * dxi, dyi2 = dyi * dyi;
+#pragma omp parallel for num_threads(NT) schedule(static)
+  for (int k = 1; k <= nz; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        const double pc = p[PIDX(i, j, k)];
+        double pw = i > 1 ? p[PIDX(i - 1, j, k)] : ghost_lo(cbc[0], pc, p[PIDX(nx, j, k)]);
+        double pe = i < nx ? p[PIDX(i + 1, j, k)] : ghost_lo(cbc[1], pc, p[PIDX(1, j, k)]);
+        double ps = j > 1 ? p[PIDX(i, j - 1, k)] : ghost_lo(cbc[2], pc, p[PIDX(i, ny, k)]);
+        double pn = j < ny ? p[PIDX(i, j + 1, k)] : ghost_lo(cbc[3], pc, p[PIDX(i, 1, k)]);
+        double pb = k > 1 ? p[PIDX(i, j, k - 1)] : ghost_lo(cbc[4], pc, p[PIDX(i, j, nz)]);
+        double pt = k < nz ? p[PIDX(i, j, k + 1)] : ghost_lo(cbc[5], pc, p[PIDX(i, j, 1)]);
+        double ax = ((pe - pc) - (pc - pw)) * dxi2;
+        double ay = ((pn - pc) - (pc - ps)) * dyi2;
+        double az = ((pt - pc) * dzci[k - 1 + nh_d] - (pc - pb) * dzci[k - 2 + nh_d]) * dzfi[k - 1 + nh_d];
+        r[PIDX(i, j, k)] = f[PIDX(i, j, k)] - (ax + ay + az);
+      }
+}

@@ -1,0 +1,79 @@
+"""CPU tests of the C-ABI boundary: the library builds for sm_103a, loads, and
+exports every symbol include/flutas_gb300.h declares; argument validation
+rejects bad input before any device work (no GPU needed for these paths).
+"""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    hdr = open(os.path.join(ROOT, "include", "flutas_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(flutas_gb300_\w+)\s*\(", hdr)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", lib.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (flutas_gb300_\w+)", out))
+    missing = [s for s in declared_symbols() if s not in exported]
+    assert not missing, missing
+    # the Python front end binds every one of them
+    assert sorted(lib.EXPORTED) == declared_symbols()
+
+
+def test_initsolver_rejects_bad_bc_without_touching_the_device(lib):
+    L = lib.load()
+    n = (C.c_int * 3)(8, 8, 8)
+    dli = (C.c_double * 3)(8.0, 8.0, 8.0)
+    dz = np.ones(10)
+    bc = (C.c_double * 6)()
+    lam = np.empty(64)
+    abc = [np.empty(8) for _ in range(3)]
+    rh = [np.empty(128) for _ in range(3)]
+    arr = (C.c_void_p * 4)()
+    nf = C.c_double()
+    for cbc, code in [(b"PPPPNX", lib.FLUTAS_EINVAL), (b"PNPPNN", lib.FLUTAS_EINVAL)]:
+        rc = L.flutas_gb300_initsolver(C.cast(n, C.c_void_p), C.cast(dli, C.c_void_p), 1, dz.ctypes.data,
+                                       dz.ctypes.data, cbc, C.cast(bc, C.c_void_p), b"ccc", lam.ctypes.data,
+                                       abc[0].ctypes.data, abc[1].ctypes.data, abc[2].ctypes.data,
+                                       C.cast(arr, C.c_void_p), C.addressof(nf), rh[0].ctypes.data,
+                                       rh[1].ctypes.data, rh[2].ctypes.data)
+        assert rc == code
+        assert lib.last_error()
+    # face-centred pressure is not implemented on the GPU: a clear error, not a fallback
+    rc = L.flutas_gb300_initsolver(C.cast(n, C.c_void_p), C.cast(dli, C.c_void_p), 1, dz.ctypes.data,
+                                   dz.ctypes.data, b"PPPPNN", C.cast(bc, C.c_void_p), b"ccf",
+                                   lam.ctypes.data, abc[0].ctypes.data, abc[1].ctypes.data,
+                                   abc[2].ctypes.data, C.cast(arr, C.c_void_p), C.addressof(nf),
+                                   rh[0].ctypes.data, rh[1].ctypes.data, rh[2].ctypes.data)
+    assert rc == lib.FLUTAS_EUNSUPPORTED
+
+
+def test_invalid_plan_handles_are_rejected(lib):
+    L = lib.load()
+    assert L.flutas_gb300_fftend(None) == lib.FLUTAS_EINVAL
+    bogus = (C.c_void_p * 4)(None, None, None, None)
+    assert L.flutas_gb300_fftend(C.cast(bogus, C.c_void_p)) == lib.FLUTAS_EINVAL
+    assert L.flutas_gb300_plan_set_stream(None, None, 1) == lib.FLUTAS_EINVAL
+    assert "invalid plan" in lib.last_error()
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    import flutas_gb300 as F
+    saved = F._lib
+    try:
+        F._lib = None
+        try:
+            F.load(str(tmp_path / "nope.so"))
+        except F.FlutasError as e:
+            assert "missing" in str(e)
+        else:
+            raise AssertionError("load() of a missing library must raise")
+    finally:
+        F._lib = saved

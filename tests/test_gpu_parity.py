@@ -1,0 +1,202 @@
+"""GPU parity tests: the CUDA path through the C ABI against the FP64 oracle.
+
+Tolerances (written here, from the target of the path):
+  FP64 solver vs oracle           relative L2 <= 1e-12 (mean-removed where the
+                                  problem is singular: x,y in {P,N}, z in N/N or P/P)
+  stencils (fillps, correc, ...)  max relative difference <= 1e-14
+  projection                      max |div u| <= 1e-11 * U / dx   (U = 1)
+  mixed precision                 relative residual <= requested tol; the error
+                                  against the FP64 oracle is asserted per case
+"""
+import numpy as np
+import pytest
+
+from conftest import (compatible_rhs, golden_cases, random_velocity, rel_l2, singular,
+                      velocity_ghosts, zgrid)
+
+pytestmark = pytest.mark.gpu
+
+
+def plan_for(lib, n, cbc, gr=0.0, dli=None, bc=None):
+    dzci, dzfi, dzc, dzf = zgrid(n[2], gr)
+    dli = dli or [n[0] * 1.0, n[1] * 1.0, n[2] * 1.0]
+    P = lib.initsolver(n, dli, 1, dzci, dzfi, cbc, bc or [0.0] * 6, "ccc")
+    return P, dzci, dzfi, dzc, dzf, dli
+
+
+@pytest.mark.parametrize("fn", golden_cases(), ids=lambda s: s.split("kat_")[-1][:-4])
+def test_gpu_known_answers_fp64(lib, fn):
+    d = np.load(fn)
+    n = [int(x) for x in d["n"]]
+    cbc = str(d["cbc"])
+    if cbc[0:2] in ("ND", "DN") and n[0] % 2 or cbc[2:4] in ("ND", "DN") and n[1] % 2:
+        pytest.skip("DCT-IV needs even n on the GPU")
+    P = lib.initsolver(n, d["dli"], 1, d["dzci"], d["dzfi"], cbc, [0] * 6, "ccc")
+    p = np.zeros((n[2] + 2, n[1] + 2, n[0] + 2))
+    p[1:-1, 1:-1, 1:-1] = d["f"]
+    P.solver(p)
+    assert rel_l2(p[1:-1, 1:-1, 1:-1], d["p"], remove_mean=singular(cbc)) <= 1e-12
+
+
+CASES = [
+    ((16, 16, 16), "PPPPNN", 0.0),
+    ((32, 32, 24), "PPPPNN", 2.0),
+    ((24, 20, 12), "NNPPND", 2.0),
+    ((20, 16, 10), "DDNNDD", 1.0),
+    ((16, 24, 9), "NDDNNN", 0.0),
+    ((48, 16, 8), "PPDDDN", 0.5),
+    ((16, 12, 16), "NNNNPP", 0.0),
+    ((18, 14, 7), "DNNDNN", 1.0),
+    ((128, 128, 12), "PPPPNN", 0.0),   # fused plane path in FP32, separate passes in FP64
+    ((256, 64, 6), "NNPPNN", 1.5),     # FP64 plane too large: separate x and y passes
+    ((176, 144, 5), "PPNNDD", 0.0),    # radices 11, 9
+]
+
+
+@pytest.mark.parametrize("n,cbc,gr", CASES, ids=[f"{c}-{n[0]}x{n[1]}x{n[2]}" for n, c, _ in CASES])
+def test_gpu_solver_matches_oracle_fp64(lib, oracle, n, cbc, gr):
+    rng = np.random.default_rng(sum(n))
+    P, dzci, dzfi, dzc, dzf, dli = plan_for(lib, n, cbc, gr)
+    S = oracle.SolverSetup(n, dli, 1, dzci, dzfi, cbc, [0] * 6, "ccc")
+    assert np.array_equal(P.lambdaxy, S.lambdaxy) and np.array_equal(P.a, S.a)
+    assert np.array_equal(P.b, S.b) and P.normfft == S.normfft
+    p = compatible_rhs(rng, n, cbc, dzf)
+    ref = p.copy()
+    S.solve(ref)
+    got = p.copy()
+    P.solver(got)
+    e = rel_l2(got[1:-1, 1:-1, 1:-1], ref[1:-1, 1:-1, 1:-1], remove_mean=singular(cbc))
+    assert e <= 1e-12, e
+    # halo untouched by the solver (like solver_cpu, which writes p(1:n) only)
+    assert np.array_equal(got[0], p[0]) and np.array_equal(got[:, :, -1], p[:, :, -1])
+
+
+def test_gpu_solver_device_pointers(lib, oracle):
+    import torch
+    n, cbc = (64, 48, 32), "PPNNNN"
+    rng = np.random.default_rng(5)
+    P, dzci, dzfi, dzc, dzf, dli = plan_for(lib, n, cbc, 1.5)
+    S = oracle.SolverSetup(n, dli, 1, dzci, dzfi, cbc, [0] * 6, "ccc")
+    p = compatible_rhs(rng, n, cbc, dzf)
+    ref = p.copy()
+    S.solve(ref)
+    pd = torch.from_numpy(p).cuda()
+    P.solver(pd)
+    got = pd.cpu().numpy()
+    assert rel_l2(got[1:-1, 1:-1, 1:-1], ref[1:-1, 1:-1, 1:-1], remove_mean=True) <= 1e-12
+
+
+def test_gpu_stencils_match_oracle(lib, oracle):
+    n = [20, 14, 12]
+    rng = np.random.default_rng(11)
+    for nh_u in (1, 3):
+        dzci, dzfi, dzc, dzf = zgrid(n[2], 1.2, nh_d=nh_u)
+        u, v, w = random_velocity(rng, n, nh_u)
+        p_ref = np.zeros((n[2] + 2, n[1] + 2, n[0] + 2))
+        p_gpu = rng.standard_normal(p_ref.shape)  # halo values must be left alone
+        p_ref[...] = p_gpu
+        oracle.fillps(n, nh_u, nh_u, 20.0, 14.0, 12.0, dzfi, 1e3, 1.7, u, v, w, p_ref)
+        lib.fillps(n, nh_u, nh_u, 20.0, 14.0, 12.0, dzfi, 1e3, 1.7, u, v, w, p_gpu)
+        assert np.abs(p_gpu - p_ref).max() <= 1e-14 * np.abs(p_ref).max()
+        # correc
+        p = rng.standard_normal(p_ref.shape)
+        uo, vo, wo = u.copy(), v.copy(), w.copy()
+        oracle.correc(n, nh_u, nh_u, 20.0, 14.0, 12.0, dzci, 1e-3, 1.3, p, uo, vo, wo)
+        lib.correc(n, nh_u, nh_u, 20.0, 14.0, 12.0, dzci, 1e-3, 1.3, p, u, v, w)
+        for a, b in ((u, uo), (v, vo), (w, wo)):
+            assert np.abs(a - b).max() <= 1e-14 * np.abs(b).max()
+        tot_o, mx_o = oracle.chkdiv(n, 20.0, 14.0, 12.0, nh_u, nh_u, dzfi, u, v, w)
+        tot_g, mx_g = lib.chkdiv(n, 20.0, 14.0, 12.0, nh_u, nh_u, dzfi, u, v, w)
+        assert mx_g == pytest.approx(mx_o, rel=1e-14)
+        assert tot_g == pytest.approx(tot_o, rel=1e-9, abs=1e-9)
+    # boundp for every BC type, non-zero BC values
+    dzci, dzfi, dzc, dzf = zgrid(n[2], 1.2)
+    for cbc in ("PPPPPP", "NNDDND", "DNNDPP", "PPNDDN"):
+        bc = [0.3, -0.2, 0.5, 0.1, -0.4, 0.7]
+        p = rng.standard_normal((n[2] + 2, n[1] + 2, n[0] + 2))
+        po = p.copy()
+        oracle.boundp(cbc, n, bc, 1, [1 / 20, 1 / 14, 1 / 12], dzc, dzf, po)
+        lib.boundp(cbc, n, bc, 1, [1 / 20, 1 / 14, 1 / 12], dzc, dzf, p)
+        assert np.abs(p - po).max() <= 1e-15 * np.abs(po).max(), cbc
+    # updt_rhs_b with inhomogeneous BCs from initsolver
+    cbc = "NNDDND"
+    S = oracle.SolverSetup(n, [20.0, 14.0, 12.0], 1, dzci, dzfi, cbc, [0.3, -0.2, 0.5, 0.1, -0.4, 0.7])
+    p = rng.standard_normal((n[2] + 2, n[1] + 2, n[0] + 2))
+    po = p.copy()
+    oracle.updt_rhs_b(n, "ccc", cbc, S.rhsbx, S.rhsby, S.rhsbz, po)
+    lib.updt_rhs_b(n, "ccc", cbc, S.rhsbx, S.rhsby, S.rhsbz, p)
+    assert np.abs(p - po).max() <= 1e-14 * np.abs(po).max()
+
+
+def test_gpu_pres_tw_src_matches_oracle(lib, oracle):
+    n = [16, 12, 10]
+    rng = np.random.default_rng(21)
+    dzci, dzfi, dzc, dzf = zgrid(n[2], 0.0)
+    u, v, w = random_velocity(rng, n, 1)
+    shp = (n[2] + 2, n[1] + 2, n[0] + 2)
+    p, pold = rng.standard_normal(shp), rng.standard_normal(shp)
+    rho = rng.uniform(1.0, 1000.0, shp)
+    uo, vo, wo = u.copy(), v.copy(), w.copy()
+    oracle.pres_tw_src(n, 16.0, 12.0, 10.0, 1, 1, dzci, 1.0, 1e-3, 2e-3, p, pold, rho, uo, vo, wo)
+    lib.pres_tw_src(n, 16.0, 12.0, 10.0, 1, 1, dzci, 1.0, 1e-3, 2e-3, p, pold, rho, u, v, w)
+    for a, b in ((u, uo), (v, vo), (w, wo)):
+        assert np.abs(a - b).max() <= 1e-14 * np.abs(b).max()
+
+
+def _projection_inputs(rng, n, cbc, nh_u=1):
+    return velocity_ghosts(*random_velocity(rng, n, nh_u), n, cbc, nh_u)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_gpu_fused_projection(lib, oracle, precision):
+    """One fused call == fillps, updt_rhs_b, solver, boundp, correc, p=pold+p, boundp of the oracle."""
+    n, cbc = [32, 32, 24], "PPPPNN"
+    rng = np.random.default_rng(31)
+    dzci, dzfi, dzc, dzf = zgrid(n[2], 0.0)
+    dxi, dyi = 32.0, 32.0
+    P = lib.initsolver(n, [dxi, dyi, 24.0], 1, dzci, dzfi, cbc, [0] * 6, "ccc")
+    S = oracle.SolverSetup(n, [dxi, dyi, 24.0], 1, dzci, dzfi, cbc, [0] * 6, "ccc")
+    u, v, w = _projection_inputs(rng, n, cbc)
+    pold = rng.standard_normal((n[2] + 2, n[1] + 2, n[0] + 2))
+    dt, rho0 = 1e-3, 1.0
+    # oracle sequence
+    uo, vo, wo = u.copy(), v.copy(), w.copy()
+    phi = np.zeros_like(pold)
+    oracle.fillps(n, 1, 1, dxi, dyi, 24.0, dzfi, 1 / dt, rho0, uo, vo, wo, phi)
+    oracle.updt_rhs_b(n, "ccc", cbc, S.rhsbx, S.rhsby, S.rhsbz, phi)
+    S.solve(phi)
+    oracle.boundp(cbc, n, [0] * 6, 1, [1 / dxi, 1 / dyi, 1.0], dzc, dzf, phi)
+    oracle.correc(n, 1, 1, dxi, dyi, 24.0, dzci, dt, rho0, phi, uo, vo, wo)
+    po = pold.copy()
+    po[1:-1, 1:-1, 1:-1] += phi[1:-1, 1:-1, 1:-1]
+    oracle.boundp(cbc, n, [0] * 6, 1, [1 / dxi, 1 / dyi, 1.0], dzc, dzf, po)
+    # GPU
+    p = pold.copy()
+    P.projection(1, dxi, dyi, dzci, dzfi, [0] * 6, dt, rho0, u, v, w, p, precision=precision, tol=1e-12,
+                 max_iter=10)
+    tol = 1e-12 if precision == 0 else 1e-9
+    for a, b in ((u, uo), (v, vo), (w, wo)):
+        assert rel_l2(a, b) <= tol
+    assert rel_l2(p[1:-1, 1:-1, 1:-1], po[1:-1, 1:-1, 1:-1], remove_mean=True) <= tol * 100
+    velocity_ghosts(u, v, w, n, cbc)
+    tot, mx = lib.chkdiv(n, dxi, dyi, 24.0, 1, 1, dzfi, u, v, w)
+    assert mx <= 1e-11 * dxi
+
+
+@pytest.mark.parametrize("n,cbc,gr", [((64, 64, 32), "PPPPNN", 0.0), ((64, 48, 32), "NNPPND", 2.0),
+                                      ((48, 80, 16), "DDNNDD", 1.0), ((32, 32, 32), "PPPPPP", 0.0)])
+@pytest.mark.parametrize("tol", [1e-6, 1e-10])
+def test_gpu_mixed_precision_refinement(lib, oracle, n, cbc, gr, tol):
+    rng = np.random.default_rng(41)
+    P, dzci, dzfi, dzc, dzf, dli = plan_for(lib, n, cbc, gr)
+    S = oracle.SolverSetup(n, dli, 1, dzci, dzfi, cbc, [0] * 6, "ccc")
+    p = compatible_rhs(rng, n, cbc, dzf)
+    f = p.copy()
+    ref = p.copy()
+    S.solve(ref)
+    relres, iters = P.solve_mixed(p, tol=tol, max_iter=10)
+    assert relres <= tol
+    r = oracle.residual(n, cbc, dli[0], dli[1], 1, dzci, dzfi, f, p)
+    assert np.linalg.norm(r) / np.linalg.norm(f[1:-1, 1:-1, 1:-1]) <= tol * 1.01
+    err = rel_l2(p[1:-1, 1:-1, 1:-1], ref[1:-1, 1:-1, 1:-1], remove_mean=singular(cbc))
+    assert err <= max(1e3 * tol, 1e-12), err
