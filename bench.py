@@ -1,0 +1,514 @@
+"""Benchmark of the GB300 pressure-projection path (one JSON line on rank 0).
+
+Workload (the two-phase projection the headline metric is quoted on):
+  256^3 cells on [0,1]^3, periodic in x and y, walls in z (pressure N/N),
+  VoF field of 64 non-overlapping spheres (radii U[0.03,0.08], tanh interface
+  of width 1.5 dx), density ratio 1000 (rho0 = min rho = 1), previous
+  pressures p^n, p^(n-1) = seeded sums of 32 Fourier modes, velocities
+  U[-1,1] with periodic / no-slip ghosts, dt = f_t12 = f_t12_o = 1e-3.
+  One step = one call of flutas_gb300_projection_df: pres_tw_src (Dodd-
+  Ferrante split) -> bounduvw -> fillps -> updt_rhs_b -> Poisson solve ->
+  boundp -> correc -> bounduvw -> p = p + phi -> boundp.  Each step projects the fields the previous
+  step left (as a time loop does), so every step solves a new RHS.
+
+value        : projections/s with the mixed-precision solve (FP32 bulk, FP64
+               residual/update) refined to relative residual <= 1e-10,
+               device-resident fields, whole job (sum over replicas).
+e2e          : same through the C ABI with pinned HOST buffers (H2D of
+               u,v,w,p,rho,pold and D2H of u,v,w,p inside every step).
+modes        : the same step refined to 1e-6, and the plain FP64 solve.
+roofline     : the kernel with the largest share of the timed region, its
+               algorithmic bytes per launch / its mean CUDA-event duration.
+cpu_baseline : the FP64 oracle restatement of solver_cpu (not FFTW) on the
+               host cores, a bounded sample of the same projection.
+
+--impl reference times that CPU restatement alone (the reference's own
+solver_cpu needs gfortran + FFTW, neither of which exists on these machines).
+Multi-GPU (torchrun): independent replicas, one per GPU, no collective on the
+data path; barrier + max over ranks for timing only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 256
+SPHERES = 64
+RHO_RATIO = 1000.0
+DT = 1e-3
+CBC = "PPPPNN"
+CBCVEL = "PPPPDD" * 3     # u, v, w: periodic x,y; no-slip walls in z (cbcvel(0:1,1:3,1:3))
+BCVEL = [0.0] * 18
+METRIC = "Poisson solves/s at <=1e-6 & <=1e-10 rel. residual, mixed vs FP64; p50/p99 latency"
+
+# algorithmic bytes per cell of each kernel (one launch covers every cell)
+BYTES_PER_CELL = {
+    "k_pres_tw_src": 72,            # R p,pold,rho,u,v,w ; W u,v,w
+    "k_fillps": 32,                 # R u,v,w ; W rhs
+    "k_sumsq_halo": 8,
+    "k_ressq": 16,                  # R f, x
+    "k_correc_padd": 72,            # R phi ; RW u,v,w ; RW p
+    "k_xfwd<f32,halocopy>": 20,     # R f(8) W f-copy(8) W S(4)
+    "k_xfwd<f32,residual>": 20,     # R f, x (16) W S (4)
+    "k_xyfwd_plane<f32,halocopy>": 20,
+    "k_xyfwd_plane<f32,residual>": 20,
+    "k_ypass_fwd<f32>": 8,
+    "k_ypass_inv<f32>": 8,
+    "k_zsolve<f32>": 8,
+    "k_xinv<f32,halo>": 12,         # R S(4) W p(8)
+    "k_xinv<f32,haloadd>": 20,      # R S(4) RW p(16)
+    "k_xyinv_plane<f32,halo>": 12,
+    "k_xyinv_plane<f32,haloadd>": 20,
+    "k_xfwd<f64,fillps>": 32,       # R u,v,w W S
+    "k_xyfwd_plane<f64,fillps>": 32,
+    "k_ypass_fwd<f64>": 16,
+    "k_ypass_inv<f64>": 16,
+    "k_zsolve<f64>": 16,
+    "k_xinv<f64,halo>": 16,
+    "k_xyinv_plane<f64,halo>": 16,
+}
+
+
+def peaks():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------- inputs
+def make_fields(n, seed, device):
+    """Seeded synthetic two-phase projection inputs (torch, float64, Fortran layout)."""
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    dx = 1.0 / n
+    xc = (torch.arange(0, n + 2, dtype=torch.float64, device=device) - 0.5) * dx  # cell centres incl. ghosts
+    Z, Y, X = torch.meshgrid(xc, xc, xc, indexing="ij")
+    # spheres: rejection-sampled non-overlapping centres, periodic in x,y, away from the walls
+    cents, radii = [], []
+    rs = 0.03 + 0.05 * torch.rand(SPHERES * 20, generator=g, dtype=torch.float64)
+    cs = torch.rand(SPHERES * 20, 3, generator=g, dtype=torch.float64)
+    for r, c in zip(rs.tolist(), cs.tolist()):
+        cz = 0.1 + 0.8 * c[2]
+        c = [c[0], c[1], cz]
+        ok = True
+        for (c2, r2) in zip(cents, radii):
+            d = [abs(c[0] - c2[0]), abs(c[1] - c2[1]), abs(c[2] - c2[2])]
+            d[0], d[1] = min(d[0], 1 - d[0]), min(d[1], 1 - d[1])
+            if math.sqrt(sum(t * t for t in d)) < r + r2 + 3 * dx:
+                ok = False
+                break
+        if ok:
+            cents.append(c)
+            radii.append(r)
+        if len(cents) == SPHERES:
+            break
+    psi = torch.zeros((n + 2,) * 3, dtype=torch.float64, device=device)
+    w_int = 1.5 * dx
+    for c, r in zip(cents, radii):
+        ddx = torch.remainder(X - c[0] + 0.5, 1.0) - 0.5
+        ddy = torch.remainder(Y - c[1] + 0.5, 1.0) - 0.5
+        dist = torch.sqrt(ddx * ddx + ddy * ddy + (Z - c[2]) ** 2)
+        psi = torch.maximum(psi, 0.5 * (1.0 + torch.tanh((r - dist) / w_int)))
+    rho = psi * RHO_RATIO + (1.0 - psi) * 1.0   # update_property (src/vof.f90:240-271)
+    # smooth previous pressures: 32 Fourier modes, periodic in x,y, Neumann in z
+    def modes():
+        k = torch.randint(0, 5, (32, 3), generator=g)
+        a = torch.randn(32, generator=g, dtype=torch.float64)
+        ph = 2 * math.pi * torch.rand(32, generator=g, dtype=torch.float64)
+        f = torch.zeros_like(X)
+        for m in range(32):
+            kx, ky, kz = (int(t) for t in k[m])
+            amp = float(a[m]) / (1.0 + kx * kx + ky * ky + kz * kz)
+            f += amp * torch.cos(2 * math.pi * (kx * X + ky * Y) + float(ph[m])) * torch.cos(math.pi * kz * Z)
+        return f
+    p = modes()
+    pold = modes()
+    # velocities U[-1,1], periodic ghosts in x,y, no-slip walls in z
+    u, v, w = (2 * torch.rand((n + 2,) * 3, generator=g, dtype=torch.float64) - 1 for _ in range(3))
+    u, v, w = u.to(device), v.to(device), w.to(device)
+    for f in (u, v, w):
+        f[:, :, 0] = f[:, :, n]
+        f[:, :, n + 1] = f[:, :, 1]
+        f[:, 0, :] = f[:, n, :]
+        f[:, n + 1, :] = f[:, 1, :]
+    w[0] = 0.0
+    w[n] = 0.0
+    u[0] = -u[1]
+    u[n + 1] = -u[n]
+    v[0] = -v[1]
+    v[n + 1] = -v[n]
+    return {k: t.contiguous() for k, t in dict(u=u, v=v, w=w, p=p, pold=pold, rho=rho).items()}
+
+
+def zgrid(n):
+    dz = np.full(n + 2, 1.0 / n)
+    return 1.0 / dz, 1.0 / dz, dz
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "50", "-i", str(self.idx)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        def rd():
+            for line in self.proc.stdout:
+                self.rows.append([x.strip() for x in line.split(",")])
+        self.thread = threading.Thread(target=rd, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for nm, val in zip(names, r[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- GPU arm
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import flutas_gb300 as F
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    F.load()
+    n = args.n
+    dzci, dzfi, dz = zgrid(n)
+    dxi = dyi = float(n)
+    P = F.initsolver([n, n, n], [dxi, dyi, float(n)], 1, dzci, dzfi, CBC, [0.0] * 6, "ccc")
+    P.set_stream(torch.cuda.current_stream().cuda_stream, synchronous=True)
+    dzci_d = torch.from_numpy(dzci).to(dev)
+    dzfi_d = torch.from_numpy(dzfi).to(dev)
+    pristine = make_fields(n, args.seed, dev)
+    torch.cuda.synchronize()
+
+    def fresh():
+        return {k: t.clone() for k, t in pristine.items()}
+
+    def step(f, precision, tol):
+        P.projection_df(1, dxi, dyi, dzci_d, dzfi_d, [0.0] * 6, DT, DT, 1.0, f["rho"], f["pold"], f["u"],
+                        f["v"], f["w"], f["p"], precision=precision, tol=tol, max_iter=12, cbcvel=CBCVEL,
+                        bcvel=BCVEL)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed(precision, tol, steps, warmup, profile=False):
+        f = fresh()
+        for _ in range(warmup):
+            step(f, precision, tol)
+        iters = []
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        barrier()
+        torch.cuda.synchronize()
+        launches0 = F.launch_count()
+        if profile:
+            F.profile_report(reset=True)
+            F.profile(True)
+        ev[0].record()
+        for i in range(steps):
+            step(f, precision, tol)
+            ev[i + 1].record()
+            if precision == 1:
+                iters.append(P.last_solve()[1])
+        torch.cuda.synchronize()
+        barrier()
+        if profile:
+            F.profile(False)
+        launches = F.launch_count() - launches0
+        lat = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+        total = ev[0].elapsed_time(ev[steps])
+        rep = F.profile_report(reset=True) if profile else None
+        return total, lat, iters, launches, rep, f
+
+    clk = ClockSampler(local_rank)
+    clk.start()
+    t_mix, lat_mix, it_mix, launches, rep, f_mix = timed(1, 1e-10, args.steps, args.warmup, profile=True)
+    t_m6, lat_m6, it_m6, _, _, _ = timed(1, 1e-6, args.steps, args.warmup)
+    t_64, lat_64, _, _, _, f_64 = timed(0, 0.0, max(3, args.steps // 4), min(args.warmup, 3))
+    clocks = clk.stop()
+
+    # accuracy of one mixed step against one FP64 step on the same input
+    fa, fb = fresh(), fresh()
+    step(fa, 1, 1e-10)
+    relres_mix = P.last_solve()[0]
+    step(fb, 0, 0.0)
+    def rel(a, b):
+        a, b = a[1:-1, 1:-1, 1:-1], b[1:-1, 1:-1, 1:-1]
+        a, b = a - a.mean(), b - b.mean()
+        return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+    err_p = rel(fa["p"] - pristine["p"], fb["p"] - pristine["p"])
+    err_u = max(float(torch.linalg.vector_norm(fa[k] - fb[k]) / torch.linalg.vector_norm(fb[k]))
+                for k in ("u", "v", "w"))
+    _, divmax = F.chkdiv([n, n, n], dxi, dyi, float(n), 1, 1, dzfi_d, fa["u"], fa["v"], fa["w"])
+
+    # e2e: pinned host buffers through the C ABI
+    host = {k: t.cpu().pin_memory() for k, t in pristine.items()}
+    hnp = {k: t.numpy() for k, t in host.items()}
+    for _ in range(min(args.warmup, 2)):
+        P.projection_df(1, dxi, dyi, dzci, dzfi, [0.0] * 6, DT, DT, 1.0, hnp["rho"], hnp["pold"], hnp["u"],
+                        hnp["v"], hnp["w"], hnp["p"], precision=1, tol=1e-10, max_iter=12, cbcvel=CBCVEL,
+                        bcvel=BCVEL)
+    e2e_steps = max(3, args.steps // 4)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        P.projection_df(1, dxi, dyi, dzci, dzfi, [0.0] * 6, DT, DT, 1.0, hnp["rho"], hnp["pold"], hnp["u"],
+                        hnp["v"], hnp["w"], hnp["p"], precision=1, tol=1e-10, max_iter=12, cbcvel=CBCVEL,
+                        bcvel=BCVEL)
+    torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) * 1e3
+    barrier()
+    field_bytes = (n + 2) ** 3 * 8
+
+    # max over ranks
+    def agg_max(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+    t_mix, t_m6, t_64, t_e2e = (agg_max(x) for x in (t_mix, t_m6, t_64, t_e2e))
+
+    res = None
+    if rank == 0:
+        ncell = n ** 3
+        steps = args.steps
+        value = world * steps / (t_mix / 1e3)
+        # roofline of the dominant kernel
+        hbm, src = peaks()
+        dom = max(rep.items(), key=lambda kv: kv[1][1]) if rep else None
+        roof = None
+        shares = {}
+        if rep:
+            tot = sum(v[1] for v in rep.values())
+            shares = {k: {"launches": v[0], "ms": round(v[1], 4), "share": round(v[1] / tot, 4)}
+                      for k, v in sorted(rep.items(), key=lambda kv: -kv[1][1])}
+            name, (cnt, ms) = dom
+            bpc = BYTES_PER_CELL.get(name)
+            if bpc:
+                achieved = bpc * ncell / (ms / cnt / 1e3) / 1e9
+                roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": hbm,
+                        "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                        "peak_source": src, "bytes_per_launch": bpc * ncell,
+                        "traffic": ncu_traffic(name, n)}
+        res = {
+            "metric": METRIC,
+            "value": round(value, 3),
+            "unit": "projections/s",
+            "n_gpus": world,
+            "steps": steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(t_mix / steps, 4),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32 bulk + f64 residual/update",
+            "data": "synthetic: seeded VoF spheres, U[-1,1] velocities, Fourier-mode pressures",
+            "config": {"workload": f"two-phase DF-split projection {n}^3, periodic x,y, walls z, "
+                                   f"density ratio {RHO_RATIO:g}, mixed precision to 1e-10",
+                       "grid": [n, n, n], "cbc": CBC, "spheres": SPHERES,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "inputs (6 FP64 fields, 0.8 GB) larger than the 129 MB L2"},
+            "latency_ms": {"p50": round(float(np.percentile(lat_mix, 50)), 4),
+                           "p99": round(float(np.percentile(lat_mix, 99)), 4)},
+            "modes": {
+                "mixed_1e-10": {"solves_per_s": round(world * steps / (t_mix / 1e3), 3),
+                                "ms_per_step": round(t_mix / steps, 4),
+                                "fp32_solves_per_step": round(float(np.mean(it_mix)), 2)},
+                "mixed_1e-6": {"solves_per_s": round(world * steps / (t_m6 / 1e3), 3),
+                               "ms_per_step": round(t_m6 / steps, 4),
+                               "p50_ms": round(float(np.percentile(lat_m6, 50)), 4),
+                               "p99_ms": round(float(np.percentile(lat_m6, 99)), 4),
+                               "fp32_solves_per_step": round(float(np.mean(it_m6)), 2)},
+                "fp64": {"solves_per_s": round(world * len(lat_64) / (t_64 / 1e3), 3),
+                         "ms_per_step": round(t_64 / len(lat_64), 4),
+                         "p50_ms": round(float(np.percentile(lat_64, 50)), 4),
+                         "p99_ms": round(float(np.percentile(lat_64, 99)), 4)},
+            },
+            "accuracy": {"mixed_relres": relres_mix, "mixed_vs_fp64_rel_l2_phi": err_p,
+                         "mixed_vs_fp64_rel_l2_u": err_u, "max_div_after": divmax,
+                         "div_bound": 1e-11 * dxi},
+            "e2e": {"value": round(world * e2e_steps / (t_e2e / 1e3), 3), "unit": "projections/s",
+                    "h2d_bytes_per_step": 6 * field_bytes, "d2h_bytes_per_step": 4 * field_bytes},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "kernels": shares,
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            res["cpu_baseline"] = cpu_baseline(n, pristine, budget_s=args.cpu_budget)
+    return res
+
+
+def ncu_traffic(kernel, n):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, scaled to n^3."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
+        e = d[kernel]
+        return round(e["dram_bytes_per_launch"] * (n ** 3) / e["cells"], 0)
+    except Exception:
+        return None
+
+
+# ----------------------------------------------------------------- CPU arm
+def oracle_projection_fields(n, fields):
+    return {k: (v.cpu().numpy().copy() if hasattr(v, "cpu") else v.copy()) for k, v in fields.items()}
+
+
+def cpu_step(O, S, n, f, dzci, dzfi, dz):
+    """One two-phase projection with the FP64 oracle (same sequence as the GPU step)."""
+    dxi = dyi = float(n)
+    nn = [n, n, n]
+    O.pres_tw_src(nn, dxi, dyi, float(n), 1, 1, dzci, 1.0, DT, DT, f["p"], f["pold"], f["rho"], f["u"], f["v"],
+                  f["w"])
+    O.bounduvw(CBCVEL, nn, BCVEL, 1, 1, [1 / dxi, 1 / dyi, 0.0], dz, dz, f["u"], f["v"], f["w"])
+    phi = np.zeros_like(f["p"])
+    O.fillps(nn, 1, 1, dxi, dyi, float(n), dzfi, 1.0 / DT, 1.0, f["u"], f["v"], f["w"], phi)
+    O.updt_rhs_b(nn, "ccc", CBC, S.rhsbx, S.rhsby, S.rhsbz, phi)
+    S.solve(phi)
+    O.boundp(CBC, nn, [0.0] * 6, 1, [1 / dxi, 1 / dyi, 0.0], dz, dz, phi)
+    O.correc(nn, 1, 1, dxi, dyi, float(n), dzci, DT, 1.0, phi, f["u"], f["v"], f["w"])
+    O.bounduvw(CBCVEL, nn, BCVEL, 1, 1, [1 / dxi, 1 / dyi, 0.0], dz, dz, f["u"], f["v"], f["w"])
+    f["p"][1:-1, 1:-1, 1:-1] += phi[1:-1, 1:-1, 1:-1]
+    O.boundp(CBC, nn, [0.0] * 6, 1, [1 / dxi, 1 / dyi, 0.0], dz, dz, f["p"])
+
+
+def cpu_setup(n):
+    from oracle import oracle as O
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+    dzci, dzfi, dz = zgrid(n)
+    S = O.SolverSetup([n, n, n], [float(n)] * 3, 1, dzci, dzfi, CBC, [0.0] * 6, "ccc")
+    return O, S, dzci, dzfi, dz
+
+
+def cpu_baseline(n, pristine, budget_s=12.0):
+    O, S, dzci, dzfi, dz = cpu_setup(n)
+    f = oracle_projection_fields(n, pristine)
+    cpu_step(O, S, n, f, dzci, dzfi, dz)  # warm-up (plans, page faults)
+    cnt, t0 = 0, time.perf_counter()
+    while True:
+        cpu_step(O, S, n, f, dzci, dzfi, dz)
+        cnt += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or cnt >= 200:
+            break
+    return {"value": round(cnt / el, 4), "unit": "projections/s", "cores": O.get_threads(), "kind": "port",
+            "sample": f"{cnt} full FP64 two-phase projections at {n}^3 (oracle restatement of "
+                      "solver_cpu with own r2r FFTs, not FFTW), after 1 warm-up"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return None
+    import torch
+    fields = make_fields(args.n, args.seed, "cpu")
+    O, S, dzci, dzfi, dz = cpu_setup(args.n)
+    f = oracle_projection_fields(args.n, fields)
+    for _ in range(args.warmup):
+        cpu_step(O, S, args.n, f, dzci, dzfi, dz)
+    lat = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        cpu_step(O, S, args.n, f, dzci, dzfi, dz)
+        lat.append((time.perf_counter() - t0) * 1e3)
+    total = sum(lat)
+    value = args.steps / (total / 1e3)
+    sample = (f"{args.steps} FP64 two-phase projections at {args.n}^3 on {O.get_threads()} host threads "
+              "(oracle restatement of solver_cpu; the reference itself needs gfortran+FFTW, absent)")
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "projections/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded VoF spheres, U[-1,1] velocities, Fourier-mode pressures",
+        "config": {"workload": f"two-phase DF-split projection {args.n}^3, periodic x,y, walls z, "
+                               f"density ratio {RHO_RATIO:g}", "grid": [args.n] * 3, "cbc": CBC},
+        "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
+                       "p99": round(float(np.percentile(lat, 99)), 3)},
+        "cpu_baseline": {"value": round(value, 4), "unit": "projections/s", "cores": O.get_threads(),
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": "projections/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        res = run_reference(args, rank)
+    else:
+        if world > 1:
+            import torch
+            torch.cuda.set_device(local_rank)
+            torch.distributed.init_process_group("nccl")
+        res = run_ours(args, rank, world, local_rank)
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -39,7 +39,9 @@ EXPORTED = [
     "flutas_gb300_boundp", "flutas_gb300_updt_rhs_b", "flutas_gb300_chkdiv",
     "flutas_gb300_pres_tw_src", "flutas_gb300_fftend", "flutas_gb300_last_error",
     "flutas_gb300_plan_set_stream", "flutas_gb300_solve_mixed", "flutas_gb300_projection",
-    "flutas_gb300_plan_info",
+    "flutas_gb300_plan_info", "flutas_gb300_launch_count", "flutas_gb300_profile",
+    "flutas_gb300_profile_report", "flutas_gb300_projection_df", "flutas_gb300_last_solve",
+    "flutas_gb300_bounduvw",
 ]
 
 
@@ -76,9 +78,16 @@ def load(path: str | None = None):
     L.flutas_gb300_last_error.argtypes = [C.c_char_p, ip]
     L.flutas_gb300_plan_set_stream.argtypes = [vp, vp, ip]
     L.flutas_gb300_solve_mixed.argtypes = [vp, vp, dp, ip, vp, vp]
-    L.flutas_gb300_projection.argtypes = [vp, ip, dp, dp, vp, vp, vp, dp, dp, vp, vp, vp, vp, ip, dp,
-                                          ip]
+    L.flutas_gb300_projection.argtypes = [vp, ip, dp, dp, vp, vp, vp, C.c_char_p, vp, dp, dp, vp, vp, vp,
+                                          vp, ip, dp, ip]
+    L.flutas_gb300_bounduvw.argtypes = [C.c_char_p, vp, vp, ip, ip, vp, vp, vp, vp, vp, vp, vp, vp]
     L.flutas_gb300_plan_info.argtypes = [vp, vp, vp, vp]
+    L.flutas_gb300_launch_count.argtypes = [vp]
+    L.flutas_gb300_projection_df.argtypes = [vp, ip, dp, dp, vp, vp, vp, C.c_char_p, vp, dp, dp, dp, vp,
+                                             vp, vp, vp, vp, vp, ip, dp, ip]
+    L.flutas_gb300_last_solve.argtypes = [vp, vp, vp]
+    L.flutas_gb300_profile.argtypes = [ip]
+    L.flutas_gb300_profile_report.argtypes = [C.c_char_p, ip, ip]
     for name in EXPORTED:
         getattr(L, name).restype = C.c_int
     _lib = L
@@ -130,6 +139,14 @@ def _chars(s, n):
     if len(s) != n:
         raise ValueError(f"expected {n} BC characters, got {s!r}")
     return s
+
+
+def _vel_bcs(cbcvel, bcvel):
+    if cbcvel is None:
+        return None, None
+    cv = _chars(cbcvel, 18)
+    bv = (C.c_double * 18)(*[float(x) for x in (bcvel if bcvel is not None else [0.0] * 18)])
+    return cv, C.cast(bv, C.c_void_p)
 
 
 class Plan:
@@ -189,12 +206,30 @@ class Plan:
         return rr.value, it.value
 
     def projection(self, nh_u, dxi, dyi, dzci, dzfi, bcpre, dt, rho0, u, v, w, p, precision=0,
-                   tol=1e-10, max_iter=8):
+                   tol=1e-10, max_iter=8, cbcvel=None, bcvel=None):
+        """fillps -> updt_rhs_b -> solve -> boundp -> correc [-> bounduvw] -> p += phi -> boundp."""
         L = load()
+        cv, bv = _vel_bcs(cbcvel, bcvel)
         _check(L.flutas_gb300_projection(self.handle, int(nh_u), float(dxi), float(dyi), _ptr(dzci),
-                                         _ptr(dzfi), C.cast(_d6(bcpre), C.c_void_p), float(dt),
+                                         _ptr(dzfi), C.cast(_d6(bcpre), C.c_void_p), cv, bv, float(dt),
                                          float(rho0), _ptr(u), _ptr(v), _ptr(w), _ptr(p),
                                          int(precision), float(tol), int(max_iter)))
+
+    def projection_df(self, nh_u, dxi, dyi, dzci, dzfi, bcpre, f_t12, f_t12_o, rho0, rho, pold, u, v, w,
+                      p, precision=0, tol=1e-10, max_iter=8, cbcvel=None, bcvel=None):
+        """pres_tw_src (Dodd-Ferrante split) [-> bounduvw] + projection, one call."""
+        L = load()
+        cv, bv = _vel_bcs(cbcvel, bcvel)
+        _check(L.flutas_gb300_projection_df(self.handle, int(nh_u), float(dxi), float(dyi), _ptr(dzci),
+                                            _ptr(dzfi), C.cast(_d6(bcpre), C.c_void_p), cv, bv, float(f_t12),
+                                            float(f_t12_o), float(rho0), _ptr(rho), _ptr(pold), _ptr(u),
+                                            _ptr(v), _ptr(w), _ptr(p), int(precision), float(tol),
+                                            int(max_iter)))
+
+    def last_solve(self):
+        rr, it = C.c_double(), C.c_int()
+        _check(load().flutas_gb300_last_solve(self.handle, C.addressof(rr), C.addressof(it)))
+        return rr.value, it.value
 
     def set_stream(self, stream_handle: int | None, synchronous: bool = True):
         _check(load().flutas_gb300_plan_set_stream(self.handle, stream_handle or None,
@@ -243,6 +278,17 @@ def boundp(cbc, n, bc, nh_d, dl, dzc, dzf, p, nh_p=1):
                                       _ptr(dzc), _ptr(dzf), _ptr(p)))
 
 
+def bounduvw(cbcvel, n, bcvel, nh_d, nh_u, dl, dzc, dzf, u, v, w):
+    """bounduvw(cbc,n,bc,nh_d,nh_u,halo,isoutflow,dl,dzc,dzf,u,v,w) without outflow."""
+    halo = (C.c_int * 3)(1, 1, 1)
+    outf = (C.c_int * 6)()
+    _check(load().flutas_gb300_bounduvw(_chars(cbcvel, 18), C.cast(_i3(n), C.c_void_p),
+                                        C.cast((C.c_double * 18)(*[float(x) for x in bcvel]), C.c_void_p),
+                                        int(nh_d), int(nh_u), C.cast(halo, C.c_void_p), C.cast(outf, C.c_void_p),
+                                        C.cast(_d3(dl), C.c_void_p), _ptr(dzc), _ptr(dzf), _ptr(u), _ptr(v),
+                                        _ptr(w)))
+
+
 def updt_rhs_b(n, c_or_f, cbc, rhsbx, rhsby, rhsbz, p, nh_p=1):
     _check(load().flutas_gb300_updt_rhs_b(int(n[0]), int(n[1]), int(n[2]), _chars(c_or_f, 3),
                                           _chars(cbc, 6), int(nh_p), _ptr(rhsbx), _ptr(rhsby),
@@ -262,3 +308,24 @@ def pres_tw_src(n, dxi, dyi, dzi, nh_d, nh_u, dzci, rho0i, f_t12, f_t12_o, p, po
                                            float(dzi), int(nh_d), int(nh_u), _ptr(dzci), float(rho0i),
                                            float(f_t12), float(f_t12_o), _ptr(p), _ptr(pold), _ptr(rho),
                                            _ptr(u), _ptr(v), _ptr(w)))
+
+
+def launch_count() -> int:
+    c = C.c_ulonglong()
+    _check(load().flutas_gb300_launch_count(C.addressof(c)))
+    return c.value
+
+
+def profile(enable: bool):
+    _check(load().flutas_gb300_profile(1 if enable else 0))
+
+
+def profile_report(reset: bool = True) -> dict:
+    """{kernel: (launches, total_ms)} of the launches recorded since the last reset."""
+    buf = C.create_string_buffer(1 << 16)
+    _check(load().flutas_gb300_profile_report(buf, 1 << 16, 1 if reset else 0))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.rsplit(" ", 2)
+        out[name] = (int(cnt), float(ms))
+    return out

@@ -14,6 +14,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -210,6 +212,53 @@ __device__ __forceinline__ void block_add(double v, double *acc) {
   if ((threadIdx.x & 31) == 0) atomicAdd(acc, v);
 }
 
+// ------------------------------------------------------ launches + profiling
+std::atomic<unsigned long long> g_launches{0};
+
+struct ProfRec {
+  const char *name;
+  cudaEvent_t a, b;
+};
+struct Profiler {
+  std::mutex mu;
+  bool on = false;
+  std::vector<ProfRec> recs;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t get() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+} g_prof;
+
+// Every kernel launch of the library goes through here: counts it and, when
+// profiling is on, brackets it with CUDA events on its own stream.
+template <typename F> int launch(const char *name, cudaStream_t st, F &&f) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  const bool prof = g_prof.on;
+  if (prof) {
+    std::lock_guard<std::mutex> lk(g_prof.mu);
+    a = g_prof.get();
+    b = g_prof.get();
+  }
+  if (prof) cudaEventRecord(a, st);
+  f();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(FLUTAS_ECUDA, "launch of %s failed: %s", name, cudaGetErrorString(e));
+  if (prof) {
+    cudaEventRecord(b, st);
+    std::lock_guard<std::mutex> lk(g_prof.mu);
+    g_prof.recs.push_back({name, a, b});
+  }
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return 0;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -237,6 +286,8 @@ struct flutas_plan {
   bool sync = true;
   int path64 = 0, path32 = 0;  // 0 separate passes, 1 fused plane kernel
   bool pin_zero_mode = false;  // singular (lam == 0, z in N/N or P/P) column
+  double last_relres = 0.0;    // relative residual / FP32 solves of the last mixed solve
+  int last_iters = 0;
 };
 
 namespace {
@@ -252,6 +303,14 @@ template <typename T> size_t plane_smem(int nx, int ny) {
   return align_up<T>(sizeof(T) * (size_t)ny * xpitch(nx)) + sizeof(T) * (size_t)nx * ny;
 }
 
+// Launch name "<base><f32|f64,tag>" per kernel, precision and functor.
+enum KId { KID_XYFWD, KID_XFWD, KID_XYINV, KID_XINV };
+template <int KID, typename T, typename F> const char *kname() {
+  static const char *base[] = {"k_xyfwd_plane", "k_xfwd", "k_xyinv_plane", "k_xinv"};
+  static const std::string s = std::string(base[KID]) + (sizeof(T) == 8 ? "<f64," : "<f32,") + F::tag + ">";
+  return s.c_str();
+}
+
 // --------------------------------------------------------------------------
 // forward (x,y) transform of one field into S, reading through functor In.
 // --------------------------------------------------------------------------
@@ -263,8 +322,7 @@ int fwd_xy(flutas_plan *pl, const In &in, T *S, const AxisTables &tx, const Axis
     const size_t sm = plane_smem<T>(g.nx, g.ny);
     int grid = grid_for(k_xyfwd_plane<T, In>, 512, sm, g.nz);
     if (grid < 0) return grid;
-    k_xyfwd_plane<T, In><<<grid, 512, sm, st>>>(tx.ap, ty.ap, in, S, g);
-    CK(cudaGetLastError());
+    TRY(launch(kname<KID_XYFWD, T, In>(), st, [&] { k_xyfwd_plane<T, In><<<grid, 512, sm, st>>>(tx.ap, ty.ap, in, S, g); }));
     return 0;
   }
   // x pass
@@ -277,8 +335,7 @@ int fwd_xy(flutas_plan *pl, const In &in, T *S, const AxisTables &tx, const Axis
     const long rows = (long)g.ny * g.nz;
     int grid = grid_for(k_xfwd<T, In>, 256, sm, (rows + M - 1) / M);
     if (grid < 0) return grid;
-    k_xfwd<T, In><<<grid, 256, sm, st>>>(tx.ap, in, S, g, M);
-    CK(cudaGetLastError());
+    TRY(launch(kname<KID_XFWD, T, In>(), st, [&] { k_xfwd<T, In><<<grid, 256, sm, st>>>(tx.ap, in, S, g, M); }));
   }
   // y pass
   {
@@ -290,8 +347,7 @@ int fwd_xy(flutas_plan *pl, const In &in, T *S, const AxisTables &tx, const Axis
     const long tiles = (long)((g.nx + W - 1) / W) * g.nz;
     int grid = grid_for(k_ypass<T, false>, 256, sm, tiles);
     if (grid < 0) return grid;
-    k_ypass<T, false><<<grid, 256, sm, st>>>(ty.ap, S, g, W);
-    CK(cudaGetLastError());
+    TRY(launch(sizeof(T) == 8 ? "k_ypass_fwd<f64>" : "k_ypass_fwd<f32>", st, [&] { k_ypass<T, false><<<grid, 256, sm, st>>>(ty.ap, S, g, W); }));
   }
   return 0;
 }
@@ -304,8 +360,7 @@ int inv_xy(flutas_plan *pl, const T *S, const Out &out, const AxisTables &tx, co
     const size_t sm = plane_smem<T>(g.nx, g.ny);
     int grid = grid_for(k_xyinv_plane<T, Out>, 512, sm, g.nz);
     if (grid < 0) return grid;
-    k_xyinv_plane<T, Out><<<grid, 512, sm, st>>>(tx.ap, ty.ap, S, out, g);
-    CK(cudaGetLastError());
+    TRY(launch(kname<KID_XYINV, T, Out>(), st, [&] { k_xyinv_plane<T, Out><<<grid, 512, sm, st>>>(tx.ap, ty.ap, S, out, g); }));
     return 0;
   }
   {
@@ -317,8 +372,7 @@ int inv_xy(flutas_plan *pl, const T *S, const Out &out, const AxisTables &tx, co
     const long tiles = (long)((g.nx + W - 1) / W) * g.nz;
     int grid = grid_for(k_ypass<T, true>, 256, sm, tiles);
     if (grid < 0) return grid;
-    k_ypass<T, true><<<grid, 256, sm, st>>>(ty.ap, (T *)S, g, W);
-    CK(cudaGetLastError());
+    TRY(launch(sizeof(T) == 8 ? "k_ypass_inv<f64>" : "k_ypass_inv<f32>", st, [&] { k_ypass<T, true><<<grid, 256, sm, st>>>(ty.ap, (T *)S, g, W); }));
   }
   {
     const int P = xpitch(g.nx);
@@ -329,8 +383,7 @@ int inv_xy(flutas_plan *pl, const T *S, const Out &out, const AxisTables &tx, co
     const long rows = (long)g.ny * g.nz;
     int grid = grid_for(k_xinv<T, Out>, 256, sm, (rows + M - 1) / M);
     if (grid < 0) return grid;
-    k_xinv<T, Out><<<grid, 256, sm, st>>>(tx.ap, S, out, g, M);
-    CK(cudaGetLastError());
+    TRY(launch(kname<KID_XINV, T, Out>(), st, [&] { k_xinv<T, Out><<<grid, 256, sm, st>>>(tx.ap, S, out, g, M); }));
   }
   return 0;
 }
@@ -343,7 +396,9 @@ int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const doub
   za.nz = pl->n[2];
   za.nn = pl->nn;
   za.periodic = (pl->cbc[4] == 'P' && pl->cbc[5] == 'P') ? 1 : 0;
-  za.pin = pin ? 1 : 0;
+  // only a singular z operator (N/N or P/P) has a null space to pin
+  const bool zsing = (pl->cbc[4] == 'N' && pl->cbc[5] == 'N') || (pl->cbc[4] == 'P' && pl->cbc[5] == 'P');
+  za.pin = (pin && zsing) ? 1 : 0;
   int TC = sizeof(T) == 8 ? 32 : 64;
   const size_t sm = sizeof(T) * (size_t)(za.periodic ? 3 : 2) * za.nz * TC;
   if ((int)sm > max_smem_optin()) {
@@ -353,13 +408,14 @@ int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const doub
   if ((int)sm2 > max_smem_optin()) return fail(FLUTAS_EUNSUPPORTED, "nz=%d too large for the z kernel", za.nz);
   int grid = grid_for(k_zsolve<T>, TC, sm2, ((long)za.nq + TC - 1) / TC);
   if (grid < 0) return grid;
-  k_zsolve<T><<<grid, TC, sm2, pl->stream>>>(za, S);
-  CK(cudaGetLastError());
+  TRY(launch(sizeof(T) == 8 ? "k_zsolve<f64>" : "k_zsolve<f32>", pl->stream,
+             [&] { k_zsolve<T><<<grid, TC, sm2, pl->stream>>>(za, S); }));
   return 0;
 }
 
 // In-functors with side effects / norms for the mixed path ------------------
-struct InHaloCopyNorm {  // value = p interior; also fbuf = value; accumulates value^2
+struct InHaloCopyNorm {  // value = p interior; also fbuf = value
+  static constexpr const char *tag = "halocopy";
   const double *p;
   double *fbuf;
   Geo g;
@@ -454,8 +510,7 @@ int solve_mixed_dev(flutas_plan *pl, double *p, double tol, int max_iter, double
   const double *lam = pl->lam.as<double>(), *a = pl->a.as<double>(), *b = pl->b.as<double>(), *c = pl->c.as<double>();
   CK(cudaMemsetAsync(nrm, 0, sizeof(double) * 4, st));
   // ||f||^2 and the first FP32 solve (fbuf <- f copy fused into the load)
-  k_sumsq_halo<<<stream_grid((long)g.nx * g.ny * g.nz), 256, 0, st>>>(p, g, nrm + 0);
-  CK(cudaGetLastError());
+  TRY(launch("k_sumsq_halo", st, [&] { k_sumsq_halo<<<stream_grid((long)g.nx * g.ny * g.nz), 256, 0, st>>>(p, g, nrm + 0); }));
   TRY(fwd_xy<float>(pl, InHaloCopyNorm{p, f, g}, S, pl->tx32, pl->ty32, pl->path32));
   TRY(zsolve<float>(pl, S, lam, a, b, c, true));
   TRY(inv_xy<float>(pl, S, OutHalo{p, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
@@ -471,8 +526,7 @@ int solve_mixed_dev(flutas_plan *pl, double *p, double tol, int max_iter, double
   double fn2 = 0.0, rn2 = 0.0, rel = 0.0;
   for (;;) {
     CK(cudaMemsetAsync(nrm + 1, 0, sizeof(double), st));
-    k_ressq<<<stream_grid((long)g.nx * g.ny * g.nz), 256, 0, st>>>(R, nrm + 1);
-    CK(cudaGetLastError());
+    TRY(launch("k_ressq", st, [&] { k_ressq<<<stream_grid((long)g.nx * g.ny * g.nz), 256, 0, st>>>(R, nrm + 1); }));
     double h[2];
     CK(cudaMemcpyAsync(h, nrm, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -718,7 +772,9 @@ int flutas_gb300_solve_mixed(void *plan, double *p, double tol, int max_iter, do
   Staged sp;
   const size_t pbytes = sizeof(double) * (size_t)(pl->n[0] + 2) * (pl->n[1] + 2) * (pl->n[2] + 2);
   TRY(stage_in(pl->mir, p, pbytes, true, true, pl->stream, &sp));
-  int rc = solve_mixed_dev(pl, sp.d, tol, max_iter, relres, iters);
+  int rc = solve_mixed_dev(pl, sp.d, tol, max_iter, &pl->last_relres, &pl->last_iters);
+  if (relres) *relres = pl->last_relres;
+  if (iters) *iters = pl->last_iters;
   if (rc != 0 && rc != FLUTAS_EITER) return rc;
   TRY(stage_out(sp, pl->stream));
   CK(cudaStreamSynchronize(pl->stream));
@@ -762,8 +818,7 @@ int flutas_gb300_fillps(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, 
   in.rhsbx = in.rhsby = in.rhsbz = nullptr;
   in.q1 = in.q2 = in.q3 = 0;
   in.g = Geo{nx, ny, nz, nh_u};
-  k_fillps<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(in, sp.d);
-  CK(cudaGetLastError());
+  TRY(launch("k_fillps", st, [&] { k_fillps<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(in, sp.d); }));
   TRY(stage_out(sp, st));
   CK(cudaStreamSynchronize(st));
   return FLUTAS_OK;
@@ -793,8 +848,7 @@ int flutas_gb300_correc(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, 
   ca.u = su.d; ca.v = sv.d; ca.w = sw.d;
   ca.factori = dt * dxi; ca.factorj = dt * dyi; ca.dt = dt; ca.rho0i = 1.0 / rho0;
   ca.g = Geo{nx, ny, nz, nh_u};
-  k_correc<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(ca);
-  CK(cudaGetLastError());
+  TRY(launch("k_correc", st, [&] { k_correc<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(ca); }));
   TRY(stage_out(su, st));
   TRY(stage_out(sv, st));
   TRY(stage_out(sw, st));
@@ -843,8 +897,7 @@ int flutas_gb300_boundp(const char cbc[6], const int n[3], const double bc[6], i
     fs(ba.ctype0, 0, bc[2 * d], dr[d][0], &ba.f0, &ba.s0);
     fs(ba.ctype1, 1, bc[2 * d + 1], dr[d][1], &ba.f1, &ba.s1);
     long cnt = d == 0 ? (long)(ny + 2) * (nz + 2) : (d == 1 ? (long)(nx + 2) * (nz + 2) : (long)(nx + 2) * (ny + 2));
-    k_boundp_dir<<<stream_grid(cnt), 256, 0, st>>>(ba);
-    CK(cudaGetLastError());
+    TRY(launch("k_boundp_dir", st, [&] { k_boundp_dir<<<stream_grid(cnt), 256, 0, st>>>(ba); }));
   }
   TRY(stage_out(sp, st));
   CK(cudaStreamSynchronize(st));
@@ -872,8 +925,7 @@ int flutas_gb300_chkdiv(int nx, int ny, int nz, double dxi, double dyi, double d
   da.u = su.d; da.v = sv.d; da.w = sw.d; da.dzfi = sz.d + (nh_d - 1);
   da.dxi = dxi; da.dyi = dyi;
   da.g = Geo{nx, ny, nz, nh_u};
-  k_chkdiv<<<grid, 256, 0, st>>>(da, g_ctx_small[0].as<double>());
-  CK(cudaGetLastError());
+  TRY(launch("k_chkdiv", st, [&] { k_chkdiv<<<grid, 256, 0, st>>>(da, g_ctx_small[0].as<double>()); }));
   std::vector<double> part(2 * grid);
   CK(cudaMemcpyAsync(part.data(), g_ctx_small[0].p, sizeof(double) * 2 * grid, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -911,8 +963,7 @@ int boundp_dev(double *p, const int n[3], const char cbc[6], const double bc[6],
     fs(ba.ctype0, 0, bc[2 * d], dr[d][0], &ba.f0, &ba.s0);
     fs(ba.ctype1, 1, bc[2 * d + 1], dr[d][1], &ba.f1, &ba.s1);
     long cnt = d == 0 ? (long)(ny + 2) * (nz + 2) : (d == 1 ? (long)(nx + 2) * (nz + 2) : (long)(nx + 2) * (ny + 2));
-    k_boundp_dir<<<stream_grid(cnt), 256, 0, st>>>(ba);
-    CK(cudaGetLastError());
+    TRY(launch("k_boundp_dir", st, [&] { k_boundp_dir<<<stream_grid(cnt), 256, 0, st>>>(ba); }));
   }
   return 0;
 }
@@ -924,8 +975,7 @@ int updt_rhs_b_dev(double *p, Geo g, const double *rx, const double *ry, const d
   const long cnt[3] = {(long)g.ny * g.nz, (long)g.nx * g.nz, (long)g.nx * g.ny};
   for (int d = 0; d < 3; d++) {
     RhsbArgs ra{p, r[d], g, d + 1, q[d]};
-    k_updt_rhs_b_dir<<<stream_grid(cnt[d]), 256, 0, st>>>(ra);
-    CK(cudaGetLastError());
+    TRY(launch("k_updt_rhs_b_dir", st, [&] { k_updt_rhs_b_dir<<<stream_grid(cnt[d]), 256, 0, st>>>(ra); }));
   }
   return 0;
 }
@@ -982,8 +1032,7 @@ int flutas_gb300_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, dou
   a.f1 = 1.0 + (f_t12 / f_t12_o);
   a.f2 = (f_t12 / f_t12_o);
   a.g = Geo{nx, ny, nz, nh_u};
-  k_pres_tw_src<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(a);
-  CK(cudaGetLastError());
+  TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(a); }));
   TRY(stage_out(su, st));
   TRY(stage_out(sv, st));
   TRY(stage_out(sw, st));
@@ -991,35 +1040,138 @@ int flutas_gb300_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, dou
   return FLUTAS_OK;
 }
 
-int flutas_gb300_projection(void *plan, int nh_u, double dxi, double dyi, const double *dzci, const double *dzfi,
-                            const double bcpre[6], double dt, double rho0, double *u, double *v, double *w,
-                            double *p, int precision, double tol, int max_iter) {
-  // fillps -> updt_rhs_b -> solver -> boundp -> correc -> p = pold + p -> boundp
-  // (src/apps/single_phase/main__single_phase.f90:705-747,
-  //  src/apps/two_phase_inc_isot/main__two_phase_inc_isot.f90:655-716)
-  flutas_plan *pl;
-  TRY(check_plan(plan, &pl));
-  if (!dzci || !dzfi || !bcpre || !u || !v || !w || !p) return fail(FLUTAS_EINVAL, "projection: null argument");
-  if (nh_u < 1 || dt == 0.0 || rho0 == 0.0) return fail(FLUTAS_EINVAL, "projection: bad nh_u/dt/rho0");
-  if (precision == 1 && (!(tol > 0.0) || max_iter < 1)) return fail(FLUTAS_EINVAL, "projection: need tol > 0, max_iter >= 1");
+}  // extern "C"
+
+namespace {
+
+int set_bc_dev(double *p, int nx, int ny, int nz, int h, char ctype, int ibound, int idir, int centered,
+               double rvalue, const double *dr, cudaStream_t st) {
+  if (h < 1 || h > 4) return fail(FLUTAS_EUNSUPPORTED, "set_bc: halo %d not in 1..4", h);
+  SetBcArgs a;
+  a.p = p; a.nx = nx; a.ny = ny; a.nz = nz; a.h = h;
+  a.idir = idir; a.ibound = ibound; a.centered = centered; a.ctype = ctype;
+  a.sgn = 0.0;
+  for (int q = 0; q < h; q++) a.factor[q] = rvalue;
+  if (ctype == 'D' && centered) { for (int q = 0; q < h; q++) a.factor[q] = 2.0 * a.factor[q]; a.sgn = -1.0; }
+  if (ctype == 'N') {
+    for (int q = 0; q < h; q++) a.factor[q] = ibound == 0 ? -dr[q] * a.factor[q] : dr[q] * a.factor[q];
+    a.sgn = 1.0;
+  }
+  const int na = idir == 1 ? ny : nx, nb = idir == 3 ? ny : nz;
+  const long cnt = (long)(na + 2 * h) * (nb + 2 * h);
+  TRY(launch("k_set_bc", st, [&] { k_set_bc<<<stream_grid(cnt), 256, 0, st>>>(a); }));
+  return 0;
+}
+
+// bounduvw (src/bound.f90:17-144), single domain, no outflow.  dzc/dzf host values.
+int bounduvw_dev(const char *cbc, const double *bc, int nx, int ny, int nz, int nh_d, int h, const double dl[3],
+                 const double *dzc_h, const double *dzf_h, double *u, double *v, double *w, cudaStream_t st) {
+  double *f[3] = {u, v, w};
+  double dr[4];
+  auto CB = [&](int ib, int d, int c) { return cbc[ib + 2 * d + 6 * c]; };
+  auto BV = [&](int ib, int d, int c) { return bc[ib + 2 * d + 6 * c]; };
+  for (int q = 0; q < h; q++) dr[q] = dl[0];
+  for (int ib = 0; ib < 2; ib++)
+    for (int c = 0; c < 3; c++) TRY(set_bc_dev(f[c], nx, ny, nz, h, CB(ib, 0, c), ib, 1, c != 0, BV(ib, 0, c), dr, st));
+  for (int q = 0; q < h; q++) dr[q] = dl[1];
+  for (int ib = 0; ib < 2; ib++)
+    for (int c = 0; c < 3; c++) TRY(set_bc_dev(f[c], nx, ny, nz, h, CB(ib, 1, c), ib, 2, c != 1, BV(ib, 1, c), dr, st));
+  for (int q = 0; q < h; q++) dr[q] = dzc_h[-q - 1 + nh_d];
+  for (int c = 0; c < 2; c++) TRY(set_bc_dev(f[c], nx, ny, nz, h, CB(0, 2, c), 0, 3, 1, BV(0, 2, c), dr, st));
+  for (int q = 0; q < h; q++) dr[q] = dzf_h[-q - 1 + nh_d];
+  TRY(set_bc_dev(w, nx, ny, nz, h, CB(0, 2, 2), 0, 3, 0, BV(0, 2, 2), dr, st));
+  for (int q = 0; q < h; q++) dr[q] = dzc_h[nz + q - 1 + nh_d];
+  for (int c = 0; c < 2; c++) TRY(set_bc_dev(f[c], nx, ny, nz, h, CB(1, 2, c), 1, 3, 1, BV(1, 2, c), dr, st));
+  for (int q = 0; q < h; q++) dr[q] = dzf_h[nz + q - 1 + nh_d];
+  TRY(set_bc_dev(w, nx, ny, nz, h, CB(1, 2, 2), 1, 3, 0, BV(1, 2, 2), dr, st));
+  return 0;
+}
+
+int check_cbcvel(const char *cbcvel) {
+  for (int i = 0; i < 18; i++)
+    if (!bc_ok(cbcvel[i])) return fail(FLUTAS_EINVAL, "bad velocity BC character '%c'", cbcvel[i]);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int flutas_gb300_bounduvw(const char cbcvel[18], const int n[3], const double bcvel[18], int nh_d, int nh_u,
+                          const int halo[3], const int isoutflow[6], const double dl[3], const double *dzc,
+                          const double *dzf, double *u, double *v, double *w) {
+  // src/bound.f90:17-144
+  (void)halo;
+  if (!cbcvel || !n || !bcvel || !dl || !dzc || !dzf) return fail(FLUTAS_EINVAL, "bounduvw: null argument");
+  TRY(check_cbcvel(cbcvel));
+  if (isoutflow)
+    for (int i = 0; i < 6; i++)
+      if (isoutflow[i]) return fail(FLUTAS_EUNSUPPORTED, "bounduvw: outflow boundaries are not implemented");
+  if (nh_u < 1 || nh_u > 4 || nh_d < nh_u) return fail(FLUTAS_EINVAL, "bounduvw: bad halo sizes");
+  const int nx = n[0], ny = n[1], nz = n[2];
+  std::vector<double> dzc_h(nz + 2 * nh_d), dzf_h(nz + 2 * nh_d);
+  const size_t zb = sizeof(double) * (nz + 2 * nh_d);
+  if (is_device_ptr(dzc)) {
+    CK(cudaMemcpy(dzc_h.data(), dzc, zb, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dzf_h.data(), dzf, zb, cudaMemcpyDeviceToHost));
+  } else {
+    memcpy(dzc_h.data(), dzc, zb);
+    memcpy(dzf_h.data(), dzf, zb);
+  }
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  g_ctx_mir.reset();
+  cudaStream_t st = 0;
+  const size_t ub = sizeof(double) * (size_t)(nx + 2 * nh_u) * (ny + 2 * nh_u) * (nz + 2 * nh_u);
+  Staged su, sv, sw;
+  TRY(stage_in(g_ctx_mir, u, ub, true, true, st, &su));
+  TRY(stage_in(g_ctx_mir, v, ub, true, true, st, &sv));
+  TRY(stage_in(g_ctx_mir, w, ub, true, true, st, &sw));
+  TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dl, dzc_h.data(), dzf_h.data(), su.d, sv.d, sw.d, st));
+  TRY(stage_out(su, st));
+  TRY(stage_out(sv, st));
+  TRY(stage_out(sw, st));
+  CK(cudaStreamSynchronize(st));
+  return FLUTAS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Body of the fused projection on staged device pointers (plan stream).
+// rho/pold non-null: the Dodd-Ferrante explicit terms of pres_tw_src
+// (src/source.f90:247-309) are added to u*,v*,w* first.
+int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const double *dzci_d, const double *dzfi_d,
+                   double dt, double rho0, double *u, double *v, double *w, double *p, int precision, double tol,
+                   int max_iter, const double *rho, const double *pold, double f_t12_o, const char *cbcvel,
+                   const double *bcvel) {
   const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2], nh_d = pl->nh_d;
   Geo g{nx, ny, nz, nh_u};
+  std::vector<double> dzc_h(nz + 2 * nh_d), dzf_h(nz + 2 * nh_d);
+  for (int k = 0; k < nz + 2 * nh_d; k++) {
+    dzc_h[k] = 1.0 / pl->dzci_h[k];
+    dzf_h[k] = 1.0 / pl->dzfi_h[k];
+  }
+  const double dlv[3] = {1.0 / dxi, 1.0 / dyi, 0.0};
   cudaStream_t st = pl->stream;
-  pl->mir.reset();
-  const size_t ub = sizeof(double) * (size_t)(nx + 2 * nh_u) * (ny + 2 * nh_u) * (nz + 2 * nh_u);
   const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
-  Staged su, sv, sw, sp, sci, sfi;
-  TRY(stage_in(pl->mir, u, ub, true, true, st, &su));
-  TRY(stage_in(pl->mir, v, ub, true, true, st, &sv));
-  TRY(stage_in(pl->mir, w, ub, true, true, st, &sw));
-  TRY(stage_in(pl->mir, p, pb, true, true, st, &sp));
-  TRY(stage_in(pl->mir, dzci, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sci));
-  TRY(stage_in(pl->mir, dzfi, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sfi));
+  if (rho) {
+    PresTwArgs a;
+    a.p = p; a.pold = pold; a.rho = rho; a.dzci = dzci_d + (nh_d - 1);
+    a.u = u; a.v = v; a.w = w;
+    a.dxi = dxi; a.dyi = dyi; a.rho0i = 1.0 / rho0; a.f_t12 = dt;
+    a.f1 = 1.0 + (dt / f_t12_o);
+    a.f2 = (dt / f_t12_o);
+    a.g = g;
+    TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(a); }));
+  }
+  // ghosts of u*,v*,w* as the app leaves them before fillps (bounduvw)
+  if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
   TRY(pl->phi.ensure(pb));
   double *phi = pl->phi.as<double>();
   InFillps in;
-  in.u = su.d; in.v = sv.d; in.w = sw.d;
-  in.dzfi = sfi.d + (nh_d - 1);
+  in.u = u; in.v = v; in.w = w;
+  in.dzfi = dzfi_d + (nh_d - 1);
   in.dti = 1.0 / dt; in.dtidxi = in.dti * dxi; in.dtidyi = in.dti * dyi; in.rho0 = rho0;
   in.rhsbx = pl->rhsb[0].as<double>(); in.rhsby = pl->rhsb[1].as<double>(); in.rhsbz = pl->rhsb[2].as<double>();
   in.q1 = in.q2 = in.q3 = 0;
@@ -1034,22 +1186,59 @@ int flutas_gb300_projection(void *plan, int nh_u, double dxi, double dyi, const 
                        pl->pin_zero_mode));
     TRY(inv_xy<double>(pl, S, OutHalo{phi, pl->normfft, gp}, pl->tx64, pl->ty64, pl->path64));
   } else {
-    k_fillps<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(in, phi);
-    CK(cudaGetLastError());
-    rc = solve_mixed_dev(pl, phi, tol, max_iter, nullptr, nullptr);
+    TRY(launch("k_fillps", st, [&] { k_fillps<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(in, phi); }));
+    rc = solve_mixed_dev(pl, phi, tol, max_iter, &pl->last_relres, &pl->last_iters);
     if (rc != 0 && rc != FLUTAS_EITER) return rc;
   }
   const double dl[3] = {1.0 / dxi, 1.0 / dyi, 0.0};
   const double dzc0 = 1.0 / pl->dzci_h[0 - 1 + nh_d], dzcn = 1.0 / pl->dzci_h[nz - 1 + nh_d];
   TRY(boundp_dev(phi, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
   CorrecAddArgs ca;
-  ca.phi = phi; ca.dzci = sci.d + (nh_d - 1);
-  ca.u = su.d; ca.v = sv.d; ca.w = sw.d; ca.p = sp.d;
+  ca.phi = phi; ca.dzci = dzci_d + (nh_d - 1);
+  ca.u = u; ca.v = v; ca.w = w; ca.p = p;
   ca.factori = dt * dxi; ca.factorj = dt * dyi; ca.dt = dt; ca.rho0i = 1.0 / rho0;
   ca.g = g;
-  k_correc_padd<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(ca);
-  CK(cudaGetLastError());
-  TRY(boundp_dev(sp.d, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
+  TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(ca); }));
+  if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
+  TRY(boundp_dev(p, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
+  return rc;
+}
+
+int projection_entry(void *plan, int nh_u, double dxi, double dyi, const double *dzci, const double *dzfi,
+                     const double bcpre[6], double dt, double rho0, double *u, double *v, double *w, double *p,
+                     int precision, double tol, int max_iter, const double *rho, const double *pold,
+                     double f_t12_o, const char *cbcvel, const double *bcvel) {
+  flutas_plan *pl;
+  TRY(check_plan(plan, &pl));
+  if (!dzci || !dzfi || !bcpre || !u || !v || !w || !p) return fail(FLUTAS_EINVAL, "projection: null argument");
+  if (nh_u < 1 || dt == 0.0 || rho0 == 0.0) return fail(FLUTAS_EINVAL, "projection: bad nh_u/dt/rho0");
+  if (precision == 1 && (!(tol > 0.0) || max_iter < 1)) return fail(FLUTAS_EINVAL, "projection: need tol > 0, max_iter >= 1");
+  for (int i = 0; i < 6; i++)
+    if (bcpre[i] != pl->bc[i]) return fail(FLUTAS_EINVAL, "projection: bcpre differs from initsolver's bc");
+  if (cbcvel) {
+    TRY(check_cbcvel(cbcvel));
+    if (!bcvel) return fail(FLUTAS_EINVAL, "projection: cbcvel given without bcvel");
+    if (nh_u > 4 || pl->nh_d < nh_u) return fail(FLUTAS_EINVAL, "projection: bad nh_u for bounduvw");
+  }
+  const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2], nh_d = pl->nh_d;
+  cudaStream_t st = pl->stream;
+  pl->mir.reset();
+  const size_t ub = sizeof(double) * (size_t)(nx + 2 * nh_u) * (ny + 2 * nh_u) * (nz + 2 * nh_u);
+  const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+  Staged su, sv, sw, sp, sci, sfi, sr, so;
+  TRY(stage_in(pl->mir, u, ub, true, true, st, &su));
+  TRY(stage_in(pl->mir, v, ub, true, true, st, &sv));
+  TRY(stage_in(pl->mir, w, ub, true, true, st, &sw));
+  TRY(stage_in(pl->mir, p, pb, true, true, st, &sp));
+  TRY(stage_in(pl->mir, dzci, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sci));
+  TRY(stage_in(pl->mir, dzfi, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sfi));
+  if (rho) {
+    TRY(stage_in(pl->mir, rho, pb, true, false, st, &sr));
+    TRY(stage_in(pl->mir, pold, pb, true, false, st, &so));
+  }
+  int rc = projection_dev(pl, nh_u, dxi, dyi, sci.d, sfi.d, dt, rho0, su.d, sv.d, sw.d, sp.d, precision, tol,
+                          max_iter, rho ? sr.d : nullptr, rho ? so.d : nullptr, f_t12_o, cbcvel, bcvel);
+  if (rc != 0 && rc != FLUTAS_EITER) return rc;
   TRY(stage_out(su, st));
   TRY(stage_out(sv, st));
   TRY(stage_out(sw, st));
@@ -1057,6 +1246,86 @@ int flutas_gb300_projection(void *plan, int nh_u, double dxi, double dyi, const 
   if (su.host || sp.host) CK(cudaStreamSynchronize(st));
   TRY(finish(pl));
   return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int flutas_gb300_projection(void *plan, int nh_u, double dxi, double dyi, const double *dzci, const double *dzfi,
+                            const double bcpre[6], const char *cbcvel, const double *bcvel, double dt, double rho0,
+                            double *u, double *v, double *w, double *p, int precision, double tol, int max_iter) {
+  // fillps -> updt_rhs_b -> solver -> boundp -> correc -> p = pold + p -> boundp
+  // (src/apps/single_phase/main__single_phase.f90:705-747)
+  return projection_entry(plan, nh_u, dxi, dyi, dzci, dzfi, bcpre, dt, rho0, u, v, w, p, precision, tol, max_iter,
+                          nullptr, nullptr, 0.0, cbcvel, bcvel);
+}
+
+int flutas_gb300_projection_df(void *plan, int nh_u, double dxi, double dyi, const double *dzci,
+                               const double *dzfi, const double bcpre[6], const char *cbcvel,
+                               const double *bcvel, double f_t12, double f_t12_o,
+                               double rho0, const double *rho, const double *pold, double *u, double *v,
+                               double *w, double *p, int precision, double tol, int max_iter) {
+  // pres_tw_src (src/source.f90:247-309) then the projection of
+  // src/apps/two_phase_inc_isot/main__two_phase_inc_isot.f90:624,655-716
+  if (!rho || !pold) return fail(FLUTAS_EINVAL, "projection_df: null rho/pold");
+  if (f_t12_o == 0.0) return fail(FLUTAS_EINVAL, "projection_df: f_t12_o == 0");
+  return projection_entry(plan, nh_u, dxi, dyi, dzci, dzfi, bcpre, f_t12, rho0, u, v, w, p, precision, tol,
+                          max_iter, rho, pold, f_t12_o, cbcvel, bcvel);
+}
+
+int flutas_gb300_last_solve(void *plan, double *relres, int *iters) {
+  flutas_plan *pl;
+  TRY(check_plan(plan, &pl));
+  if (relres) *relres = pl->last_relres;
+  if (iters) *iters = pl->last_iters;
+  return FLUTAS_OK;
+}
+
+}  // extern "C"
+
+
+extern "C" {
+
+int flutas_gb300_launch_count(unsigned long long *count) {
+  if (!count) return fail(FLUTAS_EINVAL, "launch_count: null");
+  *count = g_launches.load();
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_profile(int enable) {
+  std::lock_guard<std::mutex> lk(g_prof.mu);
+  g_prof.on = enable != 0;
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_profile_report(char *buf, int len, int reset) {
+  if (!buf || len <= 0) return fail(FLUTAS_EINVAL, "profile_report: bad buffer");
+  std::lock_guard<std::mutex> lk(g_prof.mu);
+  std::map<std::string, std::pair<long, double>> agg;
+  for (auto &r : g_prof.recs) {
+    float ms = 0.f;
+    CK(cudaEventSynchronize(r.b));
+    CK(cudaEventElapsedTime(&ms, r.a, r.b));
+    auto &e = agg[r.name];
+    e.first += 1;
+    e.second += ms;
+  }
+  std::string out;
+  char line[256];
+  for (auto &kv : agg) {
+    snprintf(line, sizeof line, "%s %ld %.6f\n", kv.first.c_str(), kv.second.first, kv.second.second);
+    out += line;
+  }
+  snprintf(buf, (size_t)len, "%s", out.c_str());
+  if (reset) {
+    for (auto &r : g_prof.recs) {
+      g_prof.pool.push_back(r.a);
+      g_prof.pool.push_back(r.b);
+    }
+    g_prof.recs.clear();
+  }
+  return (int)out.size() < len ? FLUTAS_OK : FLUTAS_EINVAL;
 }
 
 }  // extern "C"

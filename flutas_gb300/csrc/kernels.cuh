@@ -37,12 +37,14 @@ struct Geo {
 // ------------------------------------------------------- forward input modes
 // All take 0-based interior coordinates (i0,j0,k0) and return the RHS value.
 struct InHalo {  // p(1:nx,1:ny,1:nz) of a halo-1 array
+  static constexpr const char *tag = "halo";
   const double *p;
   Geo g;
   __device__ double operator()(int i0, int j0, int k0) const { return p[g.pidx(i0 + 1, j0 + 1, k0 + 1)]; }
 };
 
 struct InPlain {  // contiguous (nx,ny,nz) FP64 array
+  static constexpr const char *tag = "plain";
   const double *f;
   Geo g;
   __device__ double operator()(int i0, int j0, int k0) const { return f[g.sidx(i0, j0, k0)]; }
@@ -50,6 +52,7 @@ struct InPlain {  // contiguous (nx,ny,nz) FP64 array
 
 // fillps (src/fillps.f90:50-57) + optional updt_rhs_b (src/bound.f90:829-944)
 struct InFillps {
+  static constexpr const char *tag = "fillps";
   const double *u, *v, *w, *dzfi;  // dzfi is (1-nh_d:), already offset so dzfi[k] = dzfi(k)
   double dti, dtidxi, dtidyi, rho0;
   const double *rhsbx, *rhsby, *rhsbz;  // nullable
@@ -78,6 +81,7 @@ struct InFillps {
 // solver inverts (ghost rules of src/initsolver.f90:188-246 tridmatrix and the
 // x/y eigenvalues: P wrap, N p0=p1, D p0=-p1).  f and x are halo-1 arrays.
 struct InResidual {
+  static constexpr const char *tag = "residual";
   const double *f, *x;
   const double *dzci, *dzfi;  // offset so that dzci[k] = dzci(k)
   double dxi2, dyi2;
@@ -102,12 +106,14 @@ struct InResidual {
 
 // ------------------------------------------------------ inverse output modes
 struct OutHalo {  // p(i,j,k) = v * scale
+  static constexpr const char *tag = "halo";
   double *p;
   double scale;
   Geo g;
   __device__ void operator()(int i0, int j0, int k0, double v) const { p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = v * scale; }
 };
 struct OutHaloAdd {  // p(i,j,k) += v * scale  (iterative-refinement update, FP64)
+  static constexpr const char *tag = "haloadd";
   double *p;
   double scale;
   Geo g;
@@ -662,6 +668,55 @@ __global__ void k_correc_padd(CorrecAddArgs a) {
     a.v[ui] = a.v[ui] - a.factorj * (a.phi[g.pidx(i, j + 1, k)] - ph) * a.rho0i;
     a.w[ui] = a.w[ui] - a.dt * a.dzci[k] * (a.phi[g.pidx(i, j, k + 1)] - ph) * a.rho0i;
     a.p[pc] = a.p[pc] + ph;
+  }
+}
+
+}  // namespace fg
+
+namespace fg {
+
+// set_bc (src/bound.f90:227-646) for any halo h, centred or not.  One thread per
+// point of the face (halo range of the two other axes); the ghost layers
+// q = 0..h-1 are written in order by that thread, as the reference loops.
+struct SetBcArgs {
+  double *p;
+  int nx, ny, nz, h;
+  int idir, ibound, centered;
+  char ctype;
+  double factor[4];
+  double sgn;
+};
+__global__ void k_set_bc(SetBcArgs s) {
+  const int n = s.idir == 1 ? s.nx : (s.idir == 2 ? s.ny : s.nz);
+  const int na = s.idir == 1 ? s.ny : s.nx, nb = s.idir == 3 ? s.ny : s.nz;
+  const long HX = s.nx + 2 * s.h, HY = s.ny + 2 * s.h;
+  const long wa = na + 2 * s.h, wb = nb + 2 * s.h;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < wa * wb; t += (long)gridDim.x * blockDim.x) {
+    const int a = (int)(t % wa) + 1 - s.h, b = (int)(t / wa) + 1 - s.h;
+    auto at = [&](int tt) -> long {
+      int i, j, k;
+      if (s.idir == 1) { i = tt; j = a; k = b; }
+      else if (s.idir == 2) { i = a; j = tt; k = b; }
+      else { i = a; j = b; k = tt; }
+      return (long)(i - 1 + s.h) + HX * ((long)(j - 1 + s.h) + HY * (long)(k - 1 + s.h));
+    };
+    double *p = s.p;
+    for (int q = 0; q < s.h; q++) {
+      const double f = s.factor[q];
+      if (s.ctype == 'P') {
+        p[at(0 - q)] = p[at(n - q)];
+        p[at(n + 1 + q)] = p[at(1 + q)];
+      } else if (s.centered) {
+        if (s.ibound == 0) p[at(0 - q)] = f + s.sgn * p[at(1 + q)];
+        else p[at(n + 1 + q)] = f + s.sgn * p[at(n - q)];
+      } else if (s.ctype == 'D') {
+        if (s.ibound == 0) p[at(0 - q)] = f;
+        else { p[at(n + q)] = f; p[at(n + 1 + q)] = p[at(n - 1 - q)]; }
+      } else {
+        if (s.ibound == 0) p[at(0 - q)] = 1.0 * f + p[at(1 + q)];
+        else { p[at(n + q)] = 1.0 * f + p[at(n - 1 - q)]; p[at(n + 1 + q)] = 2.0 * f + p[at(n - 1 - q)]; }
+      }
+    }
   }
 }
 

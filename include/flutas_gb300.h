@@ -85,6 +85,15 @@ FLUTAS_API int flutas_gb300_boundp(const char cbc[6], const int n[3], const doub
                         const int halo[3], const double dl[3], const double *dzc,
                         const double *dzf, double *p);
 
+/* Replaces bounduvw (src/bound.f90:17) for a single domain: velocity ghosts per
+ * set_bc (src/bound.f90:227-646), the face-normal component non-centred.
+ * cbcvel/bcvel are cbcvel/bcvel(0:1,1:3,1:3) in memory order; outflow
+ * boundaries (isoutflow, src/bound.f90:648+) return FLUTAS_EUNSUPPORTED. */
+FLUTAS_API int flutas_gb300_bounduvw(const char cbcvel[18], const int n[3], const double bcvel[18],
+                                     int nh_d, int nh_u, const int halo[3], const int isoutflow[6],
+                                     const double dl[3], const double *dzc, const double *dzf,
+                                     double *u, double *v, double *w);
+
 /* Replaces updt_rhs_b (src/bound.f90:829): adds the inhomogeneous-BC terms
  * rhsbx/rhsby/rhsbz (host or device) to the boundary planes of p. */
 FLUTAS_API int flutas_gb300_updt_rhs_b(int nx, int ny, int nz, const char c_or_f[3], const char cbc[6],
@@ -127,17 +136,44 @@ FLUTAS_API int flutas_gb300_solve_mixed(void *plan, double *p, double tol, int m
                              int *iters);
 
 /* Fused projection (one call for the steps of src/apps/<app>/main__<app>.f90: fillps ->
- * updt_rhs_b -> solver -> boundp -> correc -> p = pold + p -> boundp):
+ * updt_rhs_b -> solver -> boundp -> correc -> bounduvw -> p = pold + p -> boundp):
  * on exit u,v,w are projected and p holds pold + phi.  precision: 0 = FP64,
- * 1 = mixed to tol.  dzci/dzfi: (1-nh_d:nz+nh_d).  bcpre = bc(0:1,1:3). */
+ * 1 = mixed to tol.  dzci/dzfi: (1-nh_d:nz+nh_d).  bcpre = bc(0:1,1:3).
+ * cbcvel/bcvel (nullable): velocity BCs; when given, bounduvw is applied
+ * after correc. */
 FLUTAS_API int flutas_gb300_projection(void *plan, int nh_u, double dxi, double dyi, const double *dzci,
-                            const double *dzfi, const double bcpre[6], double dt, double rho0,
+                            const double *dzfi, const double bcpre[6], const char *cbcvel,
+                            const double *bcvel, double dt, double rho0,
                             double *u, double *v, double *w, double *p, int precision,
                             double tol, int max_iter);
+
+/* Two-phase fused projection: pres_tw_src (src/source.f90:247-309, the
+ * Dodd-Ferrante constant-coefficient split: explicit (1/rho - 1/rho0) terms
+ * built from p and pold) applied to u*,v*,w*, bounduvw (when cbcvel is
+ * given), then the projection above with dt = f_t12.  rho, pold: (0:n+1) halo-1 arrays; p holds p^n on entry and
+ * p^n + phi on exit (src/apps/two_phase_inc_isot/main__two_phase_inc_isot.f90:624-716). */
+FLUTAS_API int flutas_gb300_projection_df(void *plan, int nh_u, double dxi, double dyi,
+                                          const double *dzci, const double *dzfi,
+                                          const double bcpre[6], const char *cbcvel,
+                                          const double *bcvel, double f_t12, double f_t12_o,
+                                          double rho0, const double *rho, const double *pold,
+                                          double *u, double *v, double *w, double *p, int precision,
+                                          double tol, int max_iter);
+
+/* Relative residual and number of FP32 solves of the plan's last mixed solve. */
+FLUTAS_API int flutas_gb300_last_solve(void *plan, double *relres, int *iters);
 
 /* Plan introspection: bytes of device memory held by the plan, and which
  * transform path it uses (0 = separate x/y passes, 1 = fused plane kernel). */
 FLUTAS_API int flutas_gb300_plan_info(void *plan, size_t *device_bytes, int *xy_path_fp64, int *xy_path_fp32);
+
+/* Number of kernels this library has launched in the process (all plans). */
+FLUTAS_API int flutas_gb300_launch_count(unsigned long long *count);
+
+/* Per-kernel timing: when enabled, every launch is bracketed by CUDA events
+ * on its own stream.  The report lists "kernel launches total_ms" lines. */
+FLUTAS_API int flutas_gb300_profile(int enable);
+FLUTAS_API int flutas_gb300_profile_report(char *buf, int len, int reset);
 
 #ifdef __cplusplus
 }

@@ -529,38 +529,71 @@ void or_correc(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, double dy
       }
 }
 
+/* set_bc (bound.f90:227-646) on a field with halo h (Fortran index 1-h..n+h),
+ * dr[q] per ghost layer, q = 0..h-1 in order, as the reference loops. */
+static void set_bc_h(int nx, int ny, int nz, int h, char ctype, int ibound, int idir, int centered,
+                     double rvalue, const double *dr, double *p) {
+  const long HX = nx + 2 * h, HY = ny + 2 * h;
+#define HIDX(i, j, k) ((long)((i) - 1 + h) + HX * ((long)((j) - 1 + h) + HY * (long)((k) - 1 + h)))
+  double factor[8], sgn = 0.0;
+  for (int q = 0; q < h; q++) factor[q] = rvalue;
+  if (ctype == 'D' && centered) { for (int q = 0; q < h; q++) factor[q] = 2.0 * factor[q]; sgn = -1.0; }
+  if (ctype == 'N') {
+    for (int q = 0; q < h; q++) factor[q] = ibound == 0 ? -dr[q] * factor[q] : dr[q] * factor[q];
+    sgn = 1.0;
+  }
+  const int n = idir == 1 ? nx : (idir == 2 ? ny : nz);
+  const int na = idir == 1 ? ny : nx, nb = idir == 3 ? ny : nz; /* the two other axes */
+  for (int q = 0; q < h; q++)
+    for (int b = 1 - h; b <= nb + h; b++)
+      for (int a = 1 - h; a <= na + h; a++) {
+#define AT(t) (idir == 1 ? HIDX(t, a, b) : (idir == 2 ? HIDX(a, t, b) : HIDX(a, b, t)))
+        if (ctype == 'P') {
+          p[AT(0 - q)] = p[AT(n - q)];
+          p[AT(n + 1 + q)] = p[AT(1 + q)];
+        } else if (centered) {
+          if (ibound == 0) p[AT(0 - q)] = factor[q] + sgn * p[AT(1 + q)];
+          else p[AT(n + 1 + q)] = factor[q] + sgn * p[AT(n - q)];
+        } else if (ctype == 'D') {
+          if (ibound == 0) p[AT(0 - q)] = factor[q];
+          else { p[AT(n + q)] = factor[q]; p[AT(n + 1 + q)] = p[AT(n - 1 - q)]; }
+        } else { /* non-centred N */
+          if (ibound == 0) p[AT(0 - q)] = 1.0 * factor[q] + p[AT(1 + q)];
+          else { p[AT(n + q)] = 1.0 * factor[q] + p[AT(n - 1 - q)]; p[AT(n + 1 + q)] = 2.0 * factor[q] + p[AT(n - 1 - q)]; }
+        }
+#undef AT
+      }
+#undef HIDX
+}
+
 static void set_bc(int nx, int ny, int nz, char ctype, int ibound, int idir, double rvalue, double dr, double *p) {
-  /* bound.f90:227-646, centered = .true., nh_p = 1 (qq_d = 0) */
-  const long NX = nx + 2, NY = ny + 2;
-  double factor = rvalue, sgn = 0.0;
-  if (ctype == 'D') { factor = 2.0 * factor; sgn = -1.0; }
-  if (ctype == 'N') { factor = ibound == 0 ? -dr * factor : dr * factor; sgn = 1.0; }
-  if (ctype == 'P') {
-    if (idir == 1) {
-      for (int k = 0; k <= nz + 1; k++) for (int j = 0; j <= ny + 1; j++) {
-        p[PIDX(0, j, k)] = p[PIDX(nx, j, k)]; p[PIDX(nx + 1, j, k)] = p[PIDX(1, j, k)]; }
-    } else if (idir == 2) {
-      for (int k = 0; k <= nz + 1; k++) for (int i = 0; i <= nx + 1; i++) {
-        p[PIDX(i, 0, k)] = p[PIDX(i, ny, k)]; p[PIDX(i, ny + 1, k)] = p[PIDX(i, 1, k)]; }
-    } else {
-      for (int j = 0; j <= ny + 1; j++) for (int i = 0; i <= nx + 1; i++) {
-        p[PIDX(i, j, 0)] = p[PIDX(i, j, nz)]; p[PIDX(i, j, nz + 1)] = p[PIDX(i, j, 1)]; }
-    }
-    return;
-  }
-  if (idir == 1) {
-    for (int k = 0; k <= nz + 1; k++) for (int j = 0; j <= ny + 1; j++) {
-      if (ibound == 0) p[PIDX(0, j, k)] = factor + sgn * p[PIDX(1, j, k)];
-      else p[PIDX(nx + 1, j, k)] = factor + sgn * p[PIDX(nx, j, k)]; }
-  } else if (idir == 2) {
-    for (int k = 0; k <= nz + 1; k++) for (int i = 0; i <= nx + 1; i++) {
-      if (ibound == 0) p[PIDX(i, 0, k)] = factor + sgn * p[PIDX(i, 1, k)];
-      else p[PIDX(i, ny + 1, k)] = factor + sgn * p[PIDX(i, ny, k)]; }
-  } else {
-    for (int j = 0; j <= ny + 1; j++) for (int i = 0; i <= nx + 1; i++) {
-      if (ibound == 0) p[PIDX(i, j, 0)] = factor + sgn * p[PIDX(i, j, 1)];
-      else p[PIDX(i, j, nz + 1)] = factor + sgn * p[PIDX(i, j, nz)]; }
-  }
+  set_bc_h(nx, ny, nz, 1, ctype, ibound, idir, 1, rvalue, &dr, p);
+}
+
+void or_bounduvw(const char cbc[18], const int n[3], const double bc[18], int nh_d, int nh_u,
+                 const double dl[3], const double *dzc, const double *dzf, double *u, double *v, double *w) {
+  /* bound.f90:17-144 (single domain, no outflow); cbc/bc are (0:1,3,3): [ib + 2*dir + 6*comp] */
+  const int nx = n[0], ny = n[1], nz = n[2], h = nh_u;
+  double *f[3] = {u, v, w};
+  double dr[8];
+#define CB(ib, d, c) cbc[(ib) + 2 * (d) + 6 * (c)]
+#define BV(ib, d, c) bc[(ib) + 2 * (d) + 6 * (c)]
+  for (int q = 0; q < h; q++) dr[q] = dl[0];
+  for (int ib = 0; ib < 2; ib++)
+    for (int c = 0; c < 3; c++) set_bc_h(nx, ny, nz, h, CB(ib, 0, c), ib, 1, c != 0, BV(ib, 0, c), dr, f[c]);
+  for (int q = 0; q < h; q++) dr[q] = dl[1];
+  for (int ib = 0; ib < 2; ib++)
+    for (int c = 0; c < 3; c++) set_bc_h(nx, ny, nz, h, CB(ib, 1, c), ib, 2, c != 1, BV(ib, 1, c), dr, f[c]);
+  for (int q = 0; q < h; q++) dr[q] = dzc[-q - 1 + nh_d];
+  for (int c = 0; c < 2; c++) set_bc_h(nx, ny, nz, h, CB(0, 2, c), 0, 3, 1, BV(0, 2, c), dr, f[c]);
+  for (int q = 0; q < h; q++) dr[q] = dzf[-q - 1 + nh_d];
+  set_bc_h(nx, ny, nz, h, CB(0, 2, 2), 0, 3, 0, BV(0, 2, 2), dr, w);
+  for (int q = 0; q < h; q++) dr[q] = dzc[nz + q - 1 + nh_d];
+  for (int c = 0; c < 2; c++) set_bc_h(nx, ny, nz, h, CB(1, 2, c), 1, 3, 1, BV(1, 2, c), dr, f[c]);
+  for (int q = 0; q < h; q++) dr[q] = dzf[nz + q - 1 + nh_d];
+  set_bc_h(nx, ny, nz, h, CB(1, 2, 2), 1, 3, 0, BV(1, 2, 2), dr, w);
+#undef CB
+#undef BV
 }
 
 void or_boundp(const char cbc[6], const int n[3], const double bc[6], int nh_d, const double dl[3],

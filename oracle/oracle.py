@@ -65,6 +65,8 @@ def lib():
                                                                       _dp, _dp, _dp, _dp]
         L.or_boundp.argtypes = [C.c_char_p, C.c_int * 3, C.c_double * 6, C.c_int, C.c_double * 3,
                                 _dp, _dp, _dp]
+        L.or_bounduvw.argtypes = [C.c_char_p, C.c_int * 3, C.c_double * 18, C.c_int, C.c_int,
+                                  C.c_double * 3, _dp, _dp, _dp, _dp, _dp]
         L.or_updt_rhs_b.argtypes = [C.c_int] * 3 + [C.c_char_p, C.c_char_p, _dp, _dp, _dp, _dp]
         L.or_chkdiv.argtypes = [C.c_int] * 3 + [C.c_double] * 3 + [C.c_int] * 2 + [
             _dp, _dp, _dp, _dp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -162,6 +164,12 @@ def correc(n, nh_d, nh_u, dxi, dyi, dzi, dzci, dt, rho0, p, u, v, w):
 def boundp(cbc, n, bc, nh_d, dl, dzc, dzf, p):
     lib().or_boundp(_b(cbc), (C.c_int * 3)(*n), (C.c_double * 6)(*bc), nh_d,
                     (C.c_double * 3)(*dl), dzc, dzf, p)
+
+
+def bounduvw(cbcvel, n, bcvel, nh_d, nh_u, dl, dzc, dzf, u, v, w):
+    """cbcvel: 18 characters in Fortran (0:1,1:3,1:3) memory order."""
+    lib().or_bounduvw(_b(cbcvel), (C.c_int * 3)(*n), (C.c_double * 18)(*bcvel), nh_d, nh_u,
+                      (C.c_double * 3)(*dl), dzc, dzf, u, v, w)
 
 
 def updt_rhs_b(n, c_or_f, cbc, rhsbx, rhsby, rhsbz, p):

@@ -200,3 +200,60 @@ def test_gpu_mixed_precision_refinement(lib, oracle, n, cbc, gr, tol):
     assert np.linalg.norm(r) / np.linalg.norm(f[1:-1, 1:-1, 1:-1]) <= tol * 1.01
     err = rel_l2(p[1:-1, 1:-1, 1:-1], ref[1:-1, 1:-1, 1:-1], remove_mean=singular(cbc))
     assert err <= max(1e3 * tol, 1e-12), err
+
+
+VEL_BCS = ["PPPPDD" * 3, "DDPPDD" * 3, "NNDDND" * 3, "PPNNDD" * 3]
+
+
+@pytest.mark.parametrize("cbcvel", VEL_BCS)
+@pytest.mark.parametrize("nh_u", [1, 3])
+def test_gpu_bounduvw_matches_oracle(lib, oracle, cbcvel, nh_u):
+    n = [12, 10, 8]
+    rng = np.random.default_rng(nh_u)
+    dzci, dzfi, dzc, dzf = zgrid(n[2], 1.3, nh_d=nh_u)
+    bcvel = list(rng.uniform(-1, 1, 18))
+    u, v, w = random_velocity(rng, n, nh_u)
+    uo, vo, wo = u.copy(), v.copy(), w.copy()
+    dl = [1 / 12, 1 / 10, 1 / 8]
+    oracle.bounduvw(cbcvel, n, bcvel, nh_u, nh_u, dl, dzc, dzf, uo, vo, wo)
+    lib.bounduvw(cbcvel, n, bcvel, nh_u, nh_u, dl, dzc, dzf, u, v, w)
+    for a, b in ((u, uo), (v, vo), (w, wo)):
+        assert np.abs(a - b).max() <= 1e-15 * max(1.0, np.abs(b).max())
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_gpu_two_phase_projection_df(lib, oracle, precision):
+    """pres_tw_src + bounduvw + projection of a two-phase field == the oracle sequence."""
+    n, cbc, cbcvel = [32, 24, 16], "PPPPNN", "PPPPDD" * 3
+    rng = np.random.default_rng(51)
+    dzci, dzfi, dzc, dzf = zgrid(n[2], 0.0)
+    dxi, dyi, dt = 32.0, 24.0, 1e-3
+    P = lib.initsolver(n, [dxi, dyi, 16.0], 1, dzci, dzfi, cbc, [0] * 6, "ccc")
+    S = oracle.SolverSetup(n, [dxi, dyi, 16.0], 1, dzci, dzfi, cbc, [0] * 6, "ccc")
+    shp = (n[2] + 2, n[1] + 2, n[0] + 2)
+    u, v, w = random_velocity(rng, n, 1)
+    p, pold = rng.standard_normal(shp), rng.standard_normal(shp)
+    oracle.boundp(cbc, n, [0] * 6, 1, [1 / dxi, 1 / dyi, 1.0], dzc, dzf, p)
+    oracle.boundp(cbc, n, [0] * 6, 1, [1 / dxi, 1 / dyi, 1.0], dzc, dzf, pold)
+    psi = (rng.uniform(0, 1, shp) > 0.7).astype(np.float64)
+    rho = oracle.update_property(n, 1000.0, 1.0, psi)
+    dl = [1 / dxi, 1 / dyi, 0.0]
+    uo, vo, wo, po = u.copy(), v.copy(), w.copy(), p.copy()
+    oracle.pres_tw_src(n, dxi, dyi, 16.0, 1, 1, dzci, 1.0, dt, dt, po, pold, rho, uo, vo, wo)
+    oracle.bounduvw(cbcvel, n, [0] * 18, 1, 1, dl, dzc, dzf, uo, vo, wo)
+    phi = np.zeros(shp)
+    oracle.fillps(n, 1, 1, dxi, dyi, 16.0, dzfi, 1 / dt, 1.0, uo, vo, wo, phi)
+    S.solve(phi)
+    oracle.boundp(cbc, n, [0] * 6, 1, dl, dzc, dzf, phi)
+    oracle.correc(n, 1, 1, dxi, dyi, 16.0, dzci, dt, 1.0, phi, uo, vo, wo)
+    oracle.bounduvw(cbcvel, n, [0] * 18, 1, 1, dl, dzc, dzf, uo, vo, wo)
+    po[1:-1, 1:-1, 1:-1] += phi[1:-1, 1:-1, 1:-1]
+    oracle.boundp(cbc, n, [0] * 6, 1, dl, dzc, dzf, po)
+    P.projection_df(1, dxi, dyi, dzci, dzfi, [0] * 6, dt, dt, 1.0, rho, pold, u, v, w, p,
+                    precision=precision, tol=1e-11, max_iter=10, cbcvel=cbcvel, bcvel=[0] * 18)
+    tol = 1e-12 if precision == 0 else 1e-8
+    for a, b in ((u, uo), (v, vo), (w, wo)):
+        assert rel_l2(a, b) <= tol
+    assert rel_l2(p - pold, po - pold, remove_mean=True) <= tol * 100
+    tot, mx = lib.chkdiv(n, dxi, dyi, 16.0, 1, 1, dzfi, u, v, w)
+    assert mx <= 1e-11 * dxi
