@@ -56,15 +56,16 @@ METRIC = "Poisson solves/s at <=1e-6 & <=1e-10 rel. residual, mixed vs FP64; p50
 BYTES_PER_CELL = {
     "k_pres_tw_src": 72,            # R p,pold,rho,u,v,w ; W u,v,w
     "k_fillps": 32,                 # R u,v,w ; W rhs
-    "k_sumsq_halo": 8,
-    "k_ressq": 16,                  # R f, x
     "k_correc_padd": 72,            # R phi ; RW u,v,w ; RW p
-    "k_xfwd<f32,halocopy>": 20,     # R f(8) W f-copy(8) W S(4)
+    "k_xfwd<f32,keep-fillps>": 36,  # R u,v,w (24) W f-copy (8) W S (4)
+    "k_xfwd<f32,keep-halo>": 20,    # R f (8) W f-copy (8) W S (4)
     "k_xfwd<f32,residual>": 20,     # R f, x (16) W S (4)
-    "k_xyfwd_plane<f32,halocopy>": 20,
+    "k_xyfwd_plane<f32,keep-fillps>": 36,
+    "k_xyfwd_plane<f32,keep-halo>": 20,
     "k_xyfwd_plane<f32,residual>": 20,
     "k_ypass_fwd<f32>": 8,
     "k_ypass_inv<f32>": 8,
+    "k_zstream<f32>": 8,            # R S W S (eliminated values stay in L2)
     "k_zsolve<f32>": 8,
     "k_xinv<f32,halo>": 12,         # R S(4) W p(8)
     "k_xinv<f32,haloadd>": 20,      # R S(4) RW p(16)
@@ -74,6 +75,7 @@ BYTES_PER_CELL = {
     "k_xyfwd_plane<f64,fillps>": 32,
     "k_ypass_fwd<f64>": 16,
     "k_ypass_inv<f64>": 16,
+    "k_zstream<f64>": 16,
     "k_zsolve<f64>": 16,
     "k_xinv<f64,halo>": 16,
     "k_xyinv_plane<f64,halo>": 16,

@@ -63,6 +63,17 @@ struct AxisPlan {
 // Makhoul reordering: v_m = x_perm(m).
 FG_HD int mperm(int m, int n) { return m < (n + 1) / 2 ? 2 * m : 2 * (n - 1 - m) + 1; }
 
+// Division by a runtime constant: shift/mask when it is a power of two.
+struct FastDiv {
+  int d, sh;
+  bool p2;
+  FG_HD explicit FastDiv(int d_) : d(d_), sh(0), p2((d_ & (d_ - 1)) == 0) {
+    while ((1 << (sh + 1)) <= d_) sh++;
+  }
+  FG_HD int div(int x) const { return p2 ? (x >> sh) : x / d; }
+  FG_HD int mod(int x) const { return p2 ? (x & (d - 1)) : x % d; }
+};
+
 // ---------------------------------------------------------------------------
 // radix-R DFT kernels on registers (forward: exp(-2 pi i/R), INV: exp(+..)).
 // ---------------------------------------------------------------------------
@@ -99,33 +110,43 @@ template <typename T, bool INV> FG_HD void dft8(C2<T> *a) {
   dft4<T, INV>(a[0], a[2], a[4], a[6]);
   dft4<T, INV>(a[1], a[3], a[5], a[7]);
   // twiddle b1[s] *= W8^s
+#pragma unroll
   for (int s = 1; s < 4; s++) a[1 + 2 * s] = cmul<T>(a[1 + 2 * s], w16<T>(2 * s, INV));
   C2<T> o[8];
+#pragma unroll
   for (int s = 0; s < 4; s++) {
     C2<T> x0 = a[2 * s], x1 = a[1 + 2 * s];
     o[s] = cadd<T>(x0, x1);
     o[s + 4] = csub<T>(x0, x1);
   }
+#pragma unroll
   for (int i = 0; i < 8; i++) a[i] = o[i];
 }
 
 template <typename T, bool INV> FG_HD void dft16(C2<T> *a) {
   // m = q + 4p ; k = s + 4t ; b_q = DFT4 over p of a[q+4p]
+#pragma unroll
   for (int q = 0; q < 4; q++) dft4<T, INV>(a[q], a[q + 4], a[q + 8], a[q + 12]);
   // after dft4, a[q + 4s] holds b_q[s]; twiddle W16^{q s}
+#pragma unroll
   for (int q = 1; q < 4; q++)
+#pragma unroll
     for (int s = 1; s < 4; s++) a[q + 4 * s] = cmul<T>(a[q + 4 * s], w16<T>(q * s, INV));
   C2<T> o[16];
+#pragma unroll
   for (int s = 0; s < 4; s++) {
     C2<T> x0 = a[0 + 4 * s], x1 = a[1 + 4 * s], x2 = a[2 + 4 * s], x3 = a[3 + 4 * s];
     dft4<T, INV>(x0, x1, x2, x3);
     o[s] = x0; o[s + 4] = x1; o[s + 8] = x2; o[s + 12] = x3;
   }
+#pragma unroll
   for (int i = 0; i < 16; i++) a[i] = o[i];
 }
 
-template <typename T> FG_HD C2<T> twid(const C2<T> *W, int N, long e, bool inv) {
-  C2<T> w = W[e % N];
+// W_N^e for 0 <= e < N (every caller stays in range), conjugated for INV.
+template <typename T> FG_HD C2<T> twid(const C2<T> *W, int N, int e, bool inv) {
+  (void)N;
+  const C2<T> w = W[e];
   return inv ? mk<T>(w.x, -w.y) : w;
 }
 
@@ -133,11 +154,14 @@ template <typename T> FG_HD C2<T> twid(const C2<T> *W, int N, long e, bool inv) 
 template <typename T, int R, bool INV> FG_HD void dftR(C2<T> *a, const C2<T> *W, int N) {
   C2<T> o[R];
   const int step = N / R;
+#pragma unroll
   for (int q = 0; q < R; q++) {
     C2<T> acc = a[0];
-    for (int r = 1; r < R; r++) acc = cadd<T>(acc, cmul<T>(a[r], twid<T>(W, N, (long)((r * q) % R) * step, INV)));
+#pragma unroll
+    for (int r = 1; r < R; r++) acc = cadd<T>(acc, cmul<T>(a[r], twid<T>(W, N, ((r * q) % R) * step, INV)));
     o[q] = acc;
   }
+#pragma unroll
   for (int q = 0; q < R; q++) a[q] = o[q];
 }
 
@@ -160,15 +184,16 @@ FG_HD void stage_pass(const C2<T> *in, C2<T> *out, int N, int B, int ldb, int Ns
   const int NR = N / R;
   const int total = B * NR;
   const int tws = N / (Ns * R);
+  const FastDiv fb(B), fn(Ns);
   for (int bf = tid; bf < total; bf += nth) {
-    const int c = bf % B, j = bf / B;
-    const int kk = j % Ns;
+    const int c = fb.mod(bf), j = fb.div(bf);
+    const int kk = fn.mod(j);
     C2<T> a[R];
 #pragma unroll
     for (int r = 0; r < R; r++) a[r] = in[(long)(j + r * NR) * ldb + c];
     if (Ns > 1) {
 #pragma unroll
-      for (int r = 1; r < R; r++) a[r] = cmul<T>(a[r], twid<T>(W, N, (long)kk * r * tws, INV));
+      for (int r = 1; r < R; r++) a[r] = cmul<T>(a[r], twid<T>(W, N, kk * r * tws, INV));
     }
     dft_any<T, R, INV>(a, W, N);
     const int idxD = (j - kk) * R + kk;
@@ -232,8 +257,9 @@ FG_HD void pre_fwd(const AxisPlan &ap, const T *Rb, long ls, long es, int M, C2<
   const int n = ap.n;
   if (paired(ap.pair)) {
     const int B = M / 2, tot = B * n;
+    const FastDiv fb(B);
     for (int idx = tid; idx < tot; idx += nth) {
-      const int c = idx % B, m = idx / B;
+      const int c = fb.mod(idx), m = fb.div(idx);
       const int src = ap.pair == BC_PP ? m : mperm(m, n);
       T x0 = Rb[(2L * c) * ls + src * es], x1 = Rb[(2L * c + 1) * ls + src * es];
       if (ap.pair == BC_DD && (src & 1)) { x0 = -x0; x1 = -x1; }
@@ -243,8 +269,9 @@ FG_HD void pre_fwd(const AxisPlan &ap, const T *Rb, long ls, long es, int M, C2<
     const int h = n / 2, tot = M * h;
     const C2<T> *Q = (const C2<T> *)ap.Q;
     const T sgn = (ap.pair == BC_DN && ((n - 1) & 1)) ? (T)-1 : (T)1;
+    const FastDiv fm(M);
     for (int idx = tid; idx < tot; idx += nth) {
-      const int c = idx % M, j = idx / M;
+      const int c = fm.mod(idx), j = fm.div(idx);
       T xa = Rb[(long)c * ls + (2L * j) * es];
       T xb = Rb[(long)c * ls + (long)(n - 1 - 2 * j) * es];
       if (ap.pair == BC_DN) xb = sgn * xb;  // (-1)^(n-1-2j) = (-1)^(n-1)
@@ -264,8 +291,9 @@ FG_HD void post_fwd(const AxisPlan &ap, const C2<T> *F, int ldb, int M, Store &s
     const C2<T> *Q = (const C2<T> *)ap.Q;
     const int kmax = ap.pair == BC_PP ? n / 2 + 1 : n;
     const int tot = B * kmax;
+    const FastDiv fb(B);
     for (int idx = tid; idx < tot; idx += nth) {
-      const int c = idx % B, k = idx / B;
+      const int c = fb.mod(idx), k = fb.div(idx);
       const C2<T> Zk = F[(long)k * ldb + c];
       const C2<T> Zm = F[(long)((n - k) % n) * ldb + c];
       const T h = (T)0.5;
@@ -284,8 +312,9 @@ FG_HD void post_fwd(const AxisPlan &ap, const C2<T> *F, int ldb, int M, Store &s
   } else {
     const int h = n / 2, tot = M * h;
     const C2<T> *Q = (const C2<T> *)ap.Q + h;
+    const FastDiv fm(M);
     for (int idx = tid; idx < tot; idx += nth) {
-      const int c = idx % M, k = idx / M;
+      const int c = fm.mod(idx), k = fm.div(idx);
       C2<T> u = cmul<T>(F[(long)k * ldb + c], Q[k]);
       if (ap.pair == BC_ND) {
         st.single(c, 2 * k, (T)2 * u.x);
@@ -305,8 +334,9 @@ FG_HD void pre_bwd(const AxisPlan &ap, const T *Rb, long ls, long es, int M, C2<
   if (!paired(ap.pair)) { pre_fwd<T>(ap, Rb, ls, es, M, Cb, ldb, tid, nth); return; }
   const int n = ap.n, B = M / 2, tot = B * n;
   const C2<T> *Q = (const C2<T> *)ap.Q;
+  const FastDiv fb(B);
   for (int idx = tid; idx < tot; idx += nth) {
-    const int c = idx % B, k = idx / B;
+    const int c = fb.mod(idx), k = fb.div(idx);
     const T *r0 = Rb + (2L * c) * ls, *r1 = Rb + (2L * c + 1) * ls;
     C2<T> V0, V1;
     if (ap.pair == BC_PP) {
@@ -340,8 +370,9 @@ FG_HD void post_bwd(const AxisPlan &ap, const C2<T> *F, int ldb, int M, Store &s
                     int nth) {
   if (!paired(ap.pair)) { post_fwd<T, Store>(ap, F, ldb, M, st, tid, nth); return; }
   const int n = ap.n, B = M / 2, tot = B * n;
+  const FastDiv fb(B);
   for (int idx = tid; idx < tot; idx += nth) {
-    const int c = idx % B, m = idx / B;
+    const int c = fb.mod(idx), m = fb.div(idx);
     const C2<T> z = F[(long)m * ldb + c];
     if (ap.pair == BC_PP) {
       st.pair(c, m, z.x, z.y);

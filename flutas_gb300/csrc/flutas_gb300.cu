@@ -10,6 +10,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -315,14 +316,15 @@ template <int KID, typename T, typename F> const char *kname() {
 // forward (x,y) transform of one field into S, reading through functor In.
 // --------------------------------------------------------------------------
 template <typename T, typename In>
-int fwd_xy(flutas_plan *pl, const In &in, T *S, const AxisTables &tx, const AxisTables &ty, int path) {
+int fwd_xy(flutas_plan *pl, const In &in, T *S, const AxisTables &tx, const AxisTables &ty, int path,
+           double *nrm = nullptr) {
   Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
   cudaStream_t st = pl->stream;
   if (path == 1) {
     const size_t sm = plane_smem<T>(g.nx, g.ny);
     int grid = grid_for(k_xyfwd_plane<T, In>, 512, sm, g.nz);
     if (grid < 0) return grid;
-    TRY(launch(kname<KID_XYFWD, T, In>(), st, [&] { k_xyfwd_plane<T, In><<<grid, 512, sm, st>>>(tx.ap, ty.ap, in, S, g); }));
+    TRY(launch(kname<KID_XYFWD, T, In>(), st, [&] { k_xyfwd_plane<T, In><<<grid, 512, sm, st>>>(tx.ap, ty.ap, in, S, g, nrm); }));
     return 0;
   }
   // x pass
@@ -335,7 +337,7 @@ int fwd_xy(flutas_plan *pl, const In &in, T *S, const AxisTables &tx, const Axis
     const long rows = (long)g.ny * g.nz;
     int grid = grid_for(k_xfwd<T, In>, 256, sm, (rows + M - 1) / M);
     if (grid < 0) return grid;
-    TRY(launch(kname<KID_XFWD, T, In>(), st, [&] { k_xfwd<T, In><<<grid, 256, sm, st>>>(tx.ap, in, S, g, M); }));
+    TRY(launch(kname<KID_XFWD, T, In>(), st, [&] { k_xfwd<T, In><<<grid, 256, sm, st>>>(tx.ap, in, S, g, M, nrm); }));
   }
   // y pass
   {
@@ -399,12 +401,28 @@ int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const doub
   // only a singular z operator (N/N or P/P) has a null space to pin
   const bool zsing = (pl->cbc[4] == 'N' && pl->cbc[5] == 'N') || (pl->cbc[4] == 'P' && pl->cbc[5] == 'P');
   za.pin = (pin && zsing) ? 1 : 0;
-  int TC = sizeof(T) == 8 ? 32 : 64;
-  const size_t sm = sizeof(T) * (size_t)(za.periodic ? 3 : 2) * za.nz * TC;
-  if ((int)sm > max_smem_optin()) {
-    TC = 32;
+  if (!za.periodic) {
+    constexpr int CH = 16;
+    const int nt = 128;
+    const int nch = (za.nn + CH - 1) / CH;
+    const size_t sm = sizeof(T) * (size_t)nch * nt;
+    if ((int)sm > max_smem_optin()) return fail(FLUTAS_EUNSUPPORTED, "nz=%d too large for the z kernel", za.nz);
+    CK(cudaFuncSetAttribute(k_zstream<T, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    // launch in column batches whose eliminated values (one column of T per
+    // column) stay L2-resident between the two sweeps
+    const long per_batch = std::max<long>(nt, (long)(80.0e6 / (sizeof(T) * (double)za.nn)) / nt * nt);
+    for (long q0 = 0; q0 < za.nq; q0 += per_batch) {
+      const long q1 = std::min<long>(za.nq, q0 + per_batch);
+      const int grid = (int)((q1 - q0 + nt - 1) / nt);
+      TRY(launch(sizeof(T) == 8 ? "k_zstream<f64>" : "k_zstream<f32>", pl->stream,
+                 [&] { k_zstream<T, CH><<<grid, nt, sm, pl->stream>>>(za, S, q0, q1); }));
+    }
+    return 0;
   }
-  const size_t sm2 = sizeof(T) * (size_t)(za.periodic ? 3 : 2) * za.nz * TC;
+  int TC = sizeof(T) == 8 ? 32 : 64;
+  const size_t sm = sizeof(T) * (size_t)3 * za.nz * TC;
+  if ((int)sm > max_smem_optin()) TC = 32;
+  const size_t sm2 = sizeof(T) * (size_t)3 * za.nz * TC;
   if ((int)sm2 > max_smem_optin()) return fail(FLUTAS_EUNSUPPORTED, "nz=%d too large for the z kernel", za.nz);
   int grid = grid_for(k_zsolve<T>, TC, sm2, ((long)za.nq + TC - 1) / TC);
   if (grid < 0) return grid;
@@ -428,47 +446,6 @@ struct InHaloCopyNorm {  // value = p interior; also fbuf = value
 };
 
 }  // namespace
-
-// norm kernels (sum of squares of the interior of a halo-1 array) -----------
-__global__ void k_sumsq_halo(const double *f, Geo g, double *acc) {
-  const long N = (long)g.nx * g.ny * g.nz;
-  double s = 0.0;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
-    const double v = f[g.pidx(i, j, k)];
-    s += v * v;
-  }
-  block_add(s, acc);
-}
-
-// residual sum of squares (FP64), r = f - A x
-__global__ void k_ressq(InResidual r, double *acc) {
-  const Geo &g = r.g;
-  const long N = (long)g.nx * g.ny * g.nz;
-  double s = 0.0;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
-    const int i0 = (int)(t % g.nx), j0 = (int)((t / g.nx) % g.ny), k0 = (int)(t / ((long)g.nx * g.ny));
-    const double v = r(i0, j0, k0);
-    s += v * v;
-  }
-  block_add(s, acc);
-}
-
-__global__ void k_copy_interior(const double *src, double *dst, Geo g) {
-  const long N = (long)g.nx * g.ny * g.nz;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
-    dst[g.pidx(i, j, k)] = src[g.pidx(i, j, k)];
-  }
-}
-
-__global__ void k_add_interior(const double *src, double *dst, Geo g) {
-  const long N = (long)g.nx * g.ny * g.nz;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
-    dst[g.pidx(i, j, k)] += src[g.pidx(i, j, k)];
-  }
-}
 
 namespace {
 
@@ -496,8 +473,15 @@ int solve_fp64_dev(flutas_plan *pl, double *p, const double *lam, const double *
   return 0;
 }
 
-// Mixed solve on a device halo array p (RHS in, solution out).
-int solve_mixed_dev(flutas_plan *pl, double *p, double tol, int max_iter, double *relres, int *iters) {
+// Mixed solve.  The first pass evaluates the RHS through `first` (the halo
+// array x itself, or fillps of u,v,w), keeps an FP64 copy of it in fbuf and
+// accumulates ||f||^2; every later pass evaluates the FP64 residual
+// r = f - A x, accumulates ||r||^2 and transforms it.  x (halo 1) receives
+// the solution.  The norm of the residual decides on the host whether the
+// FP32 correction of that pass is applied.
+template <typename First>
+int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, int max_iter, double *relres,
+                    int *iters) {
   Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
   const size_t halo_bytes = sizeof(double) * (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
   TRY(pl->S32.ensure(sizeof(float) * (size_t)g.nx * g.ny * g.nz));
@@ -508,14 +492,12 @@ int solve_mixed_dev(flutas_plan *pl, double *p, double tol, int max_iter, double
   double *nrm = pl->nrm.as<double>();
   cudaStream_t st = pl->stream;
   const double *lam = pl->lam.as<double>(), *a = pl->a.as<double>(), *b = pl->b.as<double>(), *c = pl->c.as<double>();
-  CK(cudaMemsetAsync(nrm, 0, sizeof(double) * 4, st));
-  // ||f||^2 and the first FP32 solve (fbuf <- f copy fused into the load)
-  TRY(launch("k_sumsq_halo", st, [&] { k_sumsq_halo<<<stream_grid((long)g.nx * g.ny * g.nz), 256, 0, st>>>(p, g, nrm + 0); }));
-  TRY(fwd_xy<float>(pl, InHaloCopyNorm{p, f, g}, S, pl->tx32, pl->ty32, pl->path32));
+  CK(cudaMemsetAsync(nrm, 0, sizeof(double) * 2, st));
+  TRY(fwd_xy<float>(pl, InKeep<First>{first, f, g}, S, pl->tx32, pl->ty32, pl->path32, nrm + 0));
   TRY(zsolve<float>(pl, S, lam, a, b, c, true));
-  TRY(inv_xy<float>(pl, S, OutHalo{p, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
+  TRY(inv_xy<float>(pl, S, OutHalo{x, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
   InResidual R;
-  R.f = f; R.x = p;
+  R.f = f; R.x = x;
   R.dzci = pl->dzci.as<double>() + (pl->nh_d - 1);
   R.dzfi = pl->dzfi.as<double>() + (pl->nh_d - 1);
   R.dxi2 = pl->dli[0] * pl->dli[0];
@@ -523,23 +505,20 @@ int solve_mixed_dev(flutas_plan *pl, double *p, double tol, int max_iter, double
   memcpy(R.bc, pl->cbc, 6);
   R.g = g;
   int it = 1;
-  double fn2 = 0.0, rn2 = 0.0, rel = 0.0;
+  double rel = 0.0;
   for (;;) {
     CK(cudaMemsetAsync(nrm + 1, 0, sizeof(double), st));
-    TRY(launch("k_ressq", st, [&] { k_ressq<<<stream_grid((long)g.nx * g.ny * g.nz), 256, 0, st>>>(R, nrm + 1); }));
+    TRY(fwd_xy<float>(pl, R, S, pl->tx32, pl->ty32, pl->path32, nrm + 1));
     double h[2];
     CK(cudaMemcpyAsync(h, nrm, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    fn2 = h[0];
-    rn2 = h[1];
-    if (!std::isfinite(rn2) || !std::isfinite(fn2))
+    if (!std::isfinite(h[1]) || !std::isfinite(h[0]))
       return fail(FLUTAS_ENONFINITE, "non-finite residual in mixed solve");
-    rel = fn2 > 0 ? std::sqrt(rn2 / fn2) : std::sqrt(rn2);
+    rel = h[0] > 0 ? std::sqrt(h[1] / h[0]) : std::sqrt(h[1]);
     if (rel <= tol || it >= max_iter) break;
-    // correction: e = A^-1 r in FP32, p += e (FP64)
-    TRY(fwd_xy<float>(pl, R, S, pl->tx32, pl->ty32, pl->path32));
+    // correction of this pass: e = A^-1 r in FP32, x += e in FP64
     TRY(zsolve<float>(pl, S, lam, a, b, c, true));
-    TRY(inv_xy<float>(pl, S, OutHaloAdd{p, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
+    TRY(inv_xy<float>(pl, S, OutHaloAdd{x, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
     it++;
   }
   if (relres) *relres = rel;
@@ -772,7 +751,8 @@ int flutas_gb300_solve_mixed(void *plan, double *p, double tol, int max_iter, do
   Staged sp;
   const size_t pbytes = sizeof(double) * (size_t)(pl->n[0] + 2) * (pl->n[1] + 2) * (pl->n[2] + 2);
   TRY(stage_in(pl->mir, p, pbytes, true, true, pl->stream, &sp));
-  int rc = solve_mixed_dev(pl, sp.d, tol, max_iter, &pl->last_relres, &pl->last_iters);
+  const Geo gh{pl->n[0], pl->n[1], pl->n[2], 1};
+  int rc = solve_mixed_dev(pl, InHalo{sp.d, gh}, sp.d, tol, max_iter, &pl->last_relres, &pl->last_iters);
   if (relres) *relres = pl->last_relres;
   if (iters) *iters = pl->last_iters;
   if (rc != 0 && rc != FLUTAS_EITER) return rc;
@@ -818,7 +798,7 @@ int flutas_gb300_fillps(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, 
   in.rhsbx = in.rhsby = in.rhsbz = nullptr;
   in.q1 = in.q2 = in.q3 = 0;
   in.g = Geo{nx, ny, nz, nh_u};
-  TRY(launch("k_fillps", st, [&] { k_fillps<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(in, sp.d); }));
+  TRY(launch("k_fillps", st, [&] { k_fillps<<<grid_cells(in.g), 256, 0, st>>>(in, sp.d); }));
   TRY(stage_out(sp, st));
   CK(cudaStreamSynchronize(st));
   return FLUTAS_OK;
@@ -848,7 +828,7 @@ int flutas_gb300_correc(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, 
   ca.u = su.d; ca.v = sv.d; ca.w = sw.d;
   ca.factori = dt * dxi; ca.factorj = dt * dyi; ca.dt = dt; ca.rho0i = 1.0 / rho0;
   ca.g = Geo{nx, ny, nz, nh_u};
-  TRY(launch("k_correc", st, [&] { k_correc<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(ca); }));
+  TRY(launch("k_correc", st, [&] { k_correc<<<grid_cells(ca.g), 256, 0, st>>>(ca); }));
   TRY(stage_out(su, st));
   TRY(stage_out(sv, st));
   TRY(stage_out(sw, st));
@@ -919,13 +899,17 @@ int flutas_gb300_chkdiv(int nx, int ny, int nz, double dxi, double dyi, double d
   TRY(stage_in(g_ctx_mir, v, ub, true, false, st, &sv));
   TRY(stage_in(g_ctx_mir, w, ub, true, false, st, &sw));
   TRY(stage_in(g_ctx_mir, dzfi, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sz));
-  const int grid = stream_grid((long)nx * ny * nz);
+  const Geo gd{nx, ny, nz, nh_u};
+  dim3 grid3 = grid_cells(gd);
+  grid3.y = std::min<unsigned>(grid3.y, 64u);
+  grid3.z = std::min<unsigned>(grid3.z, 64u);
+  const int grid = (int)(grid3.x * grid3.y * grid3.z);
   TRY(g_ctx_small[0].ensure(sizeof(double) * 2 * grid));
   DivArgs da;
   da.u = su.d; da.v = sv.d; da.w = sw.d; da.dzfi = sz.d + (nh_d - 1);
   da.dxi = dxi; da.dyi = dyi;
   da.g = Geo{nx, ny, nz, nh_u};
-  TRY(launch("k_chkdiv", st, [&] { k_chkdiv<<<grid, 256, 0, st>>>(da, g_ctx_small[0].as<double>()); }));
+  TRY(launch("k_chkdiv", st, [&] { k_chkdiv<<<grid3, 256, 0, st>>>(da, g_ctx_small[0].as<double>()); }));
   std::vector<double> part(2 * grid);
   CK(cudaMemcpyAsync(part.data(), g_ctx_small[0].p, sizeof(double) * 2 * grid, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -1032,7 +1016,7 @@ int flutas_gb300_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, dou
   a.f1 = 1.0 + (f_t12 / f_t12_o);
   a.f2 = (f_t12 / f_t12_o);
   a.g = Geo{nx, ny, nz, nh_u};
-  TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(a); }));
+  TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<grid_cells(a.g), 256, 0, st>>>(a); }));
   TRY(stage_out(su, st));
   TRY(stage_out(sv, st));
   TRY(stage_out(sw, st));
@@ -1063,27 +1047,41 @@ int set_bc_dev(double *p, int nx, int ny, int nz, int h, char ctype, int ibound,
   return 0;
 }
 
-// bounduvw (src/bound.f90:17-144), single domain, no outflow.  dzc/dzf host values.
+// bounduvw (src/bound.f90:17-144), single domain, no outflow.  dzc/dzf host
+// values.  One launch per direction (x, then y, then z, as the reference).
 int bounduvw_dev(const char *cbc, const double *bc, int nx, int ny, int nz, int nh_d, int h, const double dl[3],
                  const double *dzc_h, const double *dzf_h, double *u, double *v, double *w, cudaStream_t st) {
-  double *f[3] = {u, v, w};
-  double dr[4];
+  if (h < 1 || h > 4) return fail(FLUTAS_EUNSUPPORTED, "bounduvw: halo %d not in 1..4", h);
   auto CB = [&](int ib, int d, int c) { return cbc[ib + 2 * d + 6 * c]; };
   auto BV = [&](int ib, int d, int c) { return bc[ib + 2 * d + 6 * c]; };
-  for (int q = 0; q < h; q++) dr[q] = dl[0];
-  for (int ib = 0; ib < 2; ib++)
-    for (int c = 0; c < 3; c++) TRY(set_bc_dev(f[c], nx, ny, nz, h, CB(ib, 0, c), ib, 1, c != 0, BV(ib, 0, c), dr, st));
-  for (int q = 0; q < h; q++) dr[q] = dl[1];
-  for (int ib = 0; ib < 2; ib++)
-    for (int c = 0; c < 3; c++) TRY(set_bc_dev(f[c], nx, ny, nz, h, CB(ib, 1, c), ib, 2, c != 1, BV(ib, 1, c), dr, st));
-  for (int q = 0; q < h; q++) dr[q] = dzc_h[-q - 1 + nh_d];
-  for (int c = 0; c < 2; c++) TRY(set_bc_dev(f[c], nx, ny, nz, h, CB(0, 2, c), 0, 3, 1, BV(0, 2, c), dr, st));
-  for (int q = 0; q < h; q++) dr[q] = dzf_h[-q - 1 + nh_d];
-  TRY(set_bc_dev(w, nx, ny, nz, h, CB(0, 2, 2), 0, 3, 0, BV(0, 2, 2), dr, st));
-  for (int q = 0; q < h; q++) dr[q] = dzc_h[nz + q - 1 + nh_d];
-  for (int c = 0; c < 2; c++) TRY(set_bc_dev(f[c], nx, ny, nz, h, CB(1, 2, c), 1, 3, 1, BV(1, 2, c), dr, st));
-  for (int q = 0; q < h; q++) dr[q] = dzf_h[nz + q - 1 + nh_d];
-  TRY(set_bc_dev(w, nx, ny, nz, h, CB(1, 2, 2), 1, 3, 0, BV(1, 2, 2), dr, st));
+  for (int d = 0; d < 3; d++) {
+    SetBc3Args a;
+    a.f[0] = u; a.f[1] = v; a.f[2] = w;
+    a.nx = nx; a.ny = ny; a.nz = nz; a.h = h; a.idir = d + 1;
+    for (int c = 0; c < 3; c++)
+      for (int ib = 0; ib < 2; ib++) {
+        BcSide &sd = a.side[c][ib];
+        sd.ctype = CB(ib, d, c);
+        sd.centered = (c != d) ? 1 : 0;  // the face-normal component is not centred
+        double dr[4];
+        for (int q = 0; q < h; q++) {
+          if (d < 2) dr[q] = dl[d];
+          else if (c < 2) dr[q] = ib == 0 ? dzc_h[-q - 1 + nh_d] : dzc_h[nz + q - 1 + nh_d];
+          else dr[q] = ib == 0 ? dzf_h[-q - 1 + nh_d] : dzf_h[nz + q - 1 + nh_d];
+        }
+        const double rv = BV(ib, d, c);
+        sd.sgn = 0.0;
+        for (int q = 0; q < h; q++) sd.factor[q] = rv;
+        if (sd.ctype == 'D' && sd.centered) { for (int q = 0; q < h; q++) sd.factor[q] = 2.0 * rv; sd.sgn = -1.0; }
+        if (sd.ctype == 'N') {
+          for (int q = 0; q < h; q++) sd.factor[q] = ib == 0 ? -dr[q] * rv : dr[q] * rv;
+          sd.sgn = 1.0;
+        }
+      }
+    const int na = d == 0 ? ny : nx, nb = d == 2 ? ny : nz;
+    const long cnt = (long)(na + 2 * h) * (nb + 2 * h);
+    TRY(launch("k_set_bc3", st, [&] { k_set_bc3<<<stream_grid(cnt), 256, 0, st>>>(a); }));
+  }
   return 0;
 }
 
@@ -1163,7 +1161,7 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     a.f1 = 1.0 + (dt / f_t12_o);
     a.f2 = (dt / f_t12_o);
     a.g = g;
-    TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(a); }));
+    TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<grid_cells(a.g), 256, 0, st>>>(a); }));
   }
   // ghosts of u*,v*,w* as the app leaves them before fillps (bounduvw)
   if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
@@ -1186,8 +1184,7 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
                        pl->pin_zero_mode));
     TRY(inv_xy<double>(pl, S, OutHalo{phi, pl->normfft, gp}, pl->tx64, pl->ty64, pl->path64));
   } else {
-    TRY(launch("k_fillps", st, [&] { k_fillps<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(in, phi); }));
-    rc = solve_mixed_dev(pl, phi, tol, max_iter, &pl->last_relres, &pl->last_iters);
+    rc = solve_mixed_dev(pl, in, phi, tol, max_iter, &pl->last_relres, &pl->last_iters);
     if (rc != 0 && rc != FLUTAS_EITER) return rc;
   }
   const double dl[3] = {1.0 / dxi, 1.0 / dyi, 0.0};
@@ -1198,7 +1195,7 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   ca.u = u; ca.v = v; ca.w = w; ca.p = p;
   ca.factori = dt * dxi; ca.factorj = dt * dyi; ca.dt = dt; ca.rho0i = 1.0 / rho0;
   ca.g = g;
-  TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<stream_grid((long)nx * ny * nz), 256, 0, st>>>(ca); }));
+  TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<grid_cells(ca.g), 256, 0, st>>>(ca); }));
   if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
   TRY(boundp_dev(p, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
   return rc;

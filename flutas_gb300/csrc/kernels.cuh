@@ -34,10 +34,33 @@ struct Geo {
   }
 };
 
+// Cell loop of the stencil kernels: i along threads, j and k along grid y / z
+// (no 64-bit division per cell).  Launch with grid_cells().
+template <typename F> __device__ __forceinline__ void for_cells(const Geo &g, F &&f) {
+  for (int k0 = blockIdx.z; k0 < g.nz; k0 += gridDim.z)
+    for (int j0 = blockIdx.y; j0 < g.ny; j0 += gridDim.y)
+      for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < g.nx; i0 += gridDim.x * blockDim.x) f(i0, j0, k0);
+}
+inline dim3 grid_cells(const Geo &g, int threads = 256) {
+  int gx = (g.nx + threads - 1) / threads;
+  return dim3(gx, g.ny < 65535 ? g.ny : 65535, g.nz < 65535 ? g.nz : 65535);
+}
+
+// Reciprocal in FP64: FP32 seed refined by two Newton-Raphson steps
+// y <- y (2 - x y); each step squares the relative error (2^-23 -> 2^-46 -> ~1 ulp).
+// Valid for the positive, normal arguments it is used on (densities).
+__device__ __forceinline__ double rcp64(double x) {
+  double y = (double)__frcp_rn((float)x);
+  y = y * fma(-x, y, 2.0);
+  y = y * fma(-x, y, 2.0);
+  return y;
+}
+
 // ------------------------------------------------------- forward input modes
 // All take 0-based interior coordinates (i0,j0,k0) and return the RHS value.
 struct InHalo {  // p(1:nx,1:ny,1:nz) of a halo-1 array
   static constexpr const char *tag = "halo";
+  static constexpr const char *keep_tag = "keep-halo";
   const double *p;
   Geo g;
   __device__ double operator()(int i0, int j0, int k0) const { return p[g.pidx(i0 + 1, j0 + 1, k0 + 1)]; }
@@ -53,6 +76,7 @@ struct InPlain {  // contiguous (nx,ny,nz) FP64 array
 // fillps (src/fillps.f90:50-57) + optional updt_rhs_b (src/bound.f90:829-944)
 struct InFillps {
   static constexpr const char *tag = "fillps";
+  static constexpr const char *keep_tag = "keep-fillps";
   const double *u, *v, *w, *dzfi;  // dzfi is (1-nh_d:), already offset so dzfi[k] = dzfi(k)
   double dti, dtidxi, dtidyi, rho0;
   const double *rhsbx, *rhsby, *rhsbz;  // nullable
@@ -104,6 +128,20 @@ struct InResidual {
   }
 };
 
+// Wrapper: evaluates the inner RHS functor and keeps an FP64 copy of it in the
+// interior of a halo-1 array (the RHS the mixed-precision residual needs).
+template <typename Inner> struct InKeep {
+  static constexpr const char *tag = Inner::keep_tag;
+  Inner inner;
+  double *keep;
+  Geo g;  // halo-1 geometry of keep
+  __device__ double operator()(int i0, int j0, int k0) const {
+    const double v = inner(i0, j0, k0);
+    keep[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = v;
+    return v;
+  }
+};
+
 // ------------------------------------------------------ inverse output modes
 struct OutHalo {  // p(i,j,k) = v * scale
   static constexpr const char *tag = "halo";
@@ -145,8 +183,23 @@ struct StoreRowsS {  // store into S rows: line l of this batch -> global row ro
   }
 };
 
+// Block sum of v, added atomically to *acc (all threads of the block call it).
+__device__ __forceinline__ void block_sum_add(double v, double *acc) {
+  __shared__ double part[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) part[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) atomicAdd(acc, v);
+  }
+}
+
 template <typename T, typename In>
-__global__ void __launch_bounds__(256) k_xfwd(AxisPlan ax, In in, T *S, Geo g, int M) {
+__global__ void __launch_bounds__(256) k_xfwd(AxisPlan ax, In in, T *S, Geo g, int M, double *nrm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nx = g.nx, P = xpitch(nx);
   T *A = (T *)smem_raw;
@@ -155,13 +208,15 @@ __global__ void __launch_bounds__(256) k_xfwd(AxisPlan ax, In in, T *S, Geo g, i
   const long rows = (long)g.ny * g.nz;
   const int tid = threadIdx.x, nth = blockDim.x;
   const int B = cbatch(ax.pair, M);
+  double ss = 0.0;
   for (long row0 = (long)blockIdx.x * M; row0 < rows; row0 += (long)gridDim.x * M) {
     for (int idx = tid; idx < M * nx; idx += nth) {
       const int m = idx / nx, x = idx % nx;
       const long r = row0 + m;
-      T v = (T)0;
-      if (r < rows) v = (T)in(x, (int)(r % g.ny), (int)(r / g.ny));
-      A[m * P + x] = v;
+      double v = 0.0;
+      if (r < rows) v = in(x, (int)(r % g.ny), (int)(r / g.ny));
+      ss += v * v;
+      A[m * P + x] = (T)v;
     }
     __syncthreads();
     pre_fwd<T>(ax, A, P, 1, M, C1, B, tid, nth);
@@ -178,6 +233,7 @@ __global__ void __launch_bounds__(256) k_xfwd(AxisPlan ax, In in, T *S, Geo g, i
     post_fwd<T>(ax, cur, B, M, st, tid, nth);
     __syncthreads();
   }
+  if (nrm) block_sum_add(ss, nrm);
 }
 
 // x pass (inverse): spectral rows -> output functor, times normfft
@@ -327,16 +383,19 @@ __device__ __forceinline__ C2<T> *run_stages(const AxisPlan &ap, C2<T> *cur, C2<
 }
 
 template <typename T, typename In>
-__global__ void __launch_bounds__(512) k_xyfwd_plane(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g) {
+__global__ void __launch_bounds__(512) k_xyfwd_plane(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nx = g.nx, ny = g.ny, P = xpitch(nx);
   T *A = (T *)smem_raw;  // ny x P
   T *Bu = (T *)(smem_raw + align_up<T>(sizeof(T) * (size_t)ny * P));  // nx*ny reals
   const int tid = threadIdx.x, nth = blockDim.x;
+  double ss = 0.0;
   for (int k = blockIdx.x; k < g.nz; k += gridDim.x) {
     for (int idx = tid; idx < nx * ny; idx += nth) {
       const int y = idx / nx, x = idx % nx;
-      A[y * P + x] = (T)in(x, y, k);
+      const double v = in(x, y, k);
+      ss += v * v;
+      A[y * P + x] = (T)v;
     }
     __syncthreads();
     // ---- x transform: lines = rows of A
@@ -359,6 +418,7 @@ __global__ void __launch_bounds__(512) k_xyfwd_plane(AxisPlan ax, AxisPlan ay, I
     post_fwd<T>(ay, fy, By, nx, st, tid, nth);
     __syncthreads();
   }
+  if (nrm) block_sum_add(ss, nrm);
 }
 
 template <typename T, typename Out>
@@ -487,11 +547,7 @@ __global__ void __launch_bounds__(128) k_zsolve(ZArgs za, T *S) {
 // ===========================================================================
 __global__ void k_fillps(InFillps in, double *p) {
   const Geo &g = in.g;
-  const long N = (long)g.nx * g.ny * g.nz;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
-    const int i0 = (int)(t % g.nx), j0 = (int)((t / g.nx) % g.ny), k0 = (int)(t / ((long)g.nx * g.ny));
-    p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = in(i0, j0, k0);
-  }
+  for_cells(g, [&](int i0, int j0, int k0) { p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = in(i0, j0, k0); });
 }
 
 struct CorrecArgs {
@@ -503,15 +559,14 @@ struct CorrecArgs {
 __global__ void k_correc(CorrecArgs a) {
   // src/correc.f90:57-60
   const Geo &g = a.g;
-  const long N = (long)g.nx * g.ny * g.nz;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
+  for_cells(g, [&](int i0, int j0, int k0) {
+    const int i = i0 + 1, j = j0 + 1, k = k0 + 1;
     const double pc = a.p[g.pidx(i, j, k)];
     const long ui = g.uidx(i, j, k);
     a.u[ui] = a.u[ui] - a.factori * (a.p[g.pidx(i + 1, j, k)] - pc) * a.rho0i;
     a.v[ui] = a.v[ui] - a.factorj * (a.p[g.pidx(i, j + 1, k)] - pc) * a.rho0i;
     a.w[ui] = a.w[ui] - a.dt * a.dzci[k] * (a.p[g.pidx(i, j, k + 1)] - pc) * a.rho0i;
-  }
+  });
 }
 
 // boundp for one direction: set_bc (src/bound.f90:227-646), centred, nh_p = 1.
@@ -557,16 +612,15 @@ struct DivArgs {
 };
 __global__ void k_chkdiv(DivArgs a, double *partial) {
   const Geo &g = a.g;
-  const long N = (long)g.nx * g.ny * g.nz;
   double tot = 0.0, mx = 0.0;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
+  for_cells(g, [&](int i0, int j0, int k0) {
+    const int i = i0 + 1, j = j0 + 1, k = k0 + 1;
     const double div = (a.w[g.uidx(i, j, k)] - a.w[g.uidx(i, j, k - 1)]) * a.dzfi[k] +
                        (a.v[g.uidx(i, j, k)] - a.v[g.uidx(i, j - 1, k)]) * a.dyi +
                        (a.u[g.uidx(i, j, k)] - a.u[g.uidx(i - 1, j, k)]) * a.dxi;
     tot += div;
     mx = fmax(mx, fabs(div));
-  }
+  });
   __shared__ double s_tot[32], s_mx[32];
   for (int o = 16; o > 0; o >>= 1) {
     tot += __shfl_down_sync(0xffffffffu, tot, o);
@@ -583,7 +637,8 @@ __global__ void k_chkdiv(DivArgs a, double *partial) {
       tot += __shfl_down_sync(0xffffffffu, tot, o);
       mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
     }
-    if (lane == 0) { partial[2 * blockIdx.x] = tot; partial[2 * blockIdx.x + 1] = mx; }
+    const long bid = blockIdx.x + (long)gridDim.x * (blockIdx.y + (long)gridDim.y * blockIdx.z);
+    if (lane == 0) { partial[2 * bid] = tot; partial[2 * bid + 1] = mx; }
   }
 }
 
@@ -626,9 +681,9 @@ struct PresTwArgs {
 __device__ __forceinline__ void pres_tw_cell(const PresTwArgs &a, int i, int j, int k) {
   const Geo &g = a.g;
   const long c0 = g.pidx(i, j, k), cx = g.pidx(i + 1, j, k), cy = g.pidx(i, j + 1, k), cz = g.pidx(i, j, k + 1);
-  const double rhoxi = 1.0 / (0.5 * (a.rho[cx] + a.rho[c0]));
-  const double rhoyi = 1.0 / (0.5 * (a.rho[cy] + a.rho[c0]));
-  const double rhozi = 1.0 / (0.5 * (a.rho[cz] + a.rho[c0]));
+  const double rhoxi = rcp64(0.5 * (a.rho[cx] + a.rho[c0]));
+  const double rhoyi = rcp64(0.5 * (a.rho[cy] + a.rho[c0]));
+  const double rhozi = rcp64(0.5 * (a.rho[cz] + a.rho[c0]));
   const double dzc = a.dzci[k];
   const double q0 = a.f1 * a.p[c0] - a.f2 * a.pold[c0];
   const long ui = g.uidx(i, j, k);
@@ -640,12 +695,7 @@ __device__ __forceinline__ void pres_tw_cell(const PresTwArgs &a, int i, int j, 
                                  (rhozi - a.rho0i) * ((a.f1 * a.p[cz] - a.f2 * a.pold[cz]) - q0) * dzc);
 }
 __global__ void k_pres_tw_src(PresTwArgs a) {
-  const Geo &g = a.g;
-  const long N = (long)g.nx * g.ny * g.nz;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
-    pres_tw_cell(a, i, j, k);
-  }
+  for_cells(a.g, [&](int i0, int j0, int k0) { pres_tw_cell(a, i0 + 1, j0 + 1, k0 + 1); });
 }
 
 // correc with the pressure increment phi, fused with p = p + phi
@@ -658,9 +708,8 @@ struct CorrecAddArgs {
 };
 __global__ void k_correc_padd(CorrecAddArgs a) {
   const Geo &g = a.g;
-  const long N = (long)g.nx * g.ny * g.nz;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % g.nx) + 1, j = (int)((t / g.nx) % g.ny) + 1, k = (int)(t / ((long)g.nx * g.ny)) + 1;
+  for_cells(g, [&](int i0, int j0, int k0) {
+    const int i = i0 + 1, j = j0 + 1, k = k0 + 1;
     const long pc = g.pidx(i, j, k);
     const double ph = a.phi[pc];
     const long ui = g.uidx(i, j, k);
@@ -668,7 +717,7 @@ __global__ void k_correc_padd(CorrecAddArgs a) {
     a.v[ui] = a.v[ui] - a.factorj * (a.phi[g.pidx(i, j + 1, k)] - ph) * a.rho0i;
     a.w[ui] = a.w[ui] - a.dt * a.dzci[k] * (a.phi[g.pidx(i, j, k + 1)] - ph) * a.rho0i;
     a.p[pc] = a.p[pc] + ph;
-  }
+  });
 }
 
 }  // namespace fg
@@ -717,6 +766,171 @@ __global__ void k_set_bc(SetBcArgs s) {
         else { p[at(n + q)] = 1.0 * f + p[at(n - 1 - q)]; p[at(n + 1 + q)] = 2.0 * f + p[at(n - 1 - q)]; }
       }
     }
+  }
+}
+
+}  // namespace fg
+
+namespace fg {
+
+// ===========================================================================
+// Streaming z solve (non-periodic z): one thread per (kx,ky) column, columns
+// coalesced across the warp, z levels processed in chunks of CH with the next
+// chunk prefetched into registers.  The forward sweep of dgtsv_homebrewed
+// (src/solver_cpu.f90:187-223) writes its eliminated values y_k back into S
+// (the line stays in L2 until the backward sweep overwrites it with x_k);
+// the elimination factors d_k are not stored: the backward sweep recomputes
+// them chunk by chunk from d at the chunk start, kept in shared memory.
+// ===========================================================================
+template <typename T>
+__device__ __forceinline__ T zpivot(T bb, T a, T dprev, bool first) {
+  return first ? bb : fma(-a, dprev, bb);
+}
+
+template <typename T, int CH>
+__global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, long q_begin, long q_end) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *chk = (T *)smem_raw;  // [nchunks][blockDim.x]: d_{k0-1} of each chunk
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const long q = q_begin + (long)blockIdx.x * nt + tid;
+  const bool act = q < q_end;
+  const int n = za.nn;
+  const long plane = za.nq;
+  const double lam = act ? za.lam[q] : 1.0;
+  const bool pin = za.pin && lam == 0.0;
+  T *col = S + (act ? q : 0);
+  const int nch = (n + CH - 1) / CH;
+  // ---- forward elimination
+  T r[CH], rn[CH];
+#pragma unroll
+  for (int i = 0; i < CH; i++) r[i] = (act && i < n) ? col[(long)i * plane] : (T)0;
+  T dprev = (T)0, yprev = (T)0;
+  for (int m = 0; m < nch; m++) {
+    const int k0 = m * CH;
+#pragma unroll
+    for (int i = 0; i < CH; i++) {
+      const int k = k0 + CH + i;
+      rn[i] = (act && k < n) ? col[(long)k * plane] : (T)0;
+    }
+    chk[m * nt + tid] = dprev;
+#pragma unroll
+    for (int i = 0; i < CH; i++) {
+      const int k = k0 + i;
+      if (k < n) {
+        const T bb = (T)(za.b[k] + lam);
+        const T ak = (T)za.a[k];
+        T y, d;
+        if (k < n - 1) {
+          const T z = (T)1 / zpivot<T>(bb, ak, dprev, k == 0);
+          d = (T)za.c[k] * z;
+          y = (k == 0 ? r[i] : fma(-ak, yprev, r[i])) * z;
+        } else {
+          const T zl = zpivot<T>(bb, ak, dprev, k == 0);
+          y = (zl != (T)0 && !pin) ? fma(-ak, yprev, r[i]) / zl : (T)0;
+          d = (T)0;
+        }
+        if (act) col[(long)k * plane] = y;
+        dprev = d;
+        yprev = y;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < CH; i++) r[i] = rn[i];
+  }
+  // ---- back substitution, chunks from the top
+  T xnext = (T)0;
+  {
+    const int k0 = (nch - 1) * CH;
+#pragma unroll
+    for (int i = 0; i < CH; i++) r[i] = (act && k0 + i < n) ? col[(long)(k0 + i) * plane] : (T)0;
+  }
+  for (int m = nch - 1; m >= 0; m--) {
+    const int k0 = m * CH;
+#pragma unroll
+    for (int i = 0; i < CH; i++) {
+      const int k = k0 - CH + i;
+      rn[i] = (act && m > 0 && k >= 0) ? col[(long)k * plane] : (T)0;
+    }
+    T dd[CH];
+    T dp = chk[m * nt + tid];
+#pragma unroll
+    for (int i = 0; i < CH; i++) {
+      const int k = k0 + i;
+      if (k < n - 1) {
+        const T bb = (T)(za.b[k] + lam);
+        const T z = (T)1 / zpivot<T>(bb, (T)za.a[k], dp, k == 0);
+        dd[i] = (T)za.c[k] * z;
+        dp = dd[i];
+      } else {
+        dd[i] = (T)0;
+      }
+    }
+#pragma unroll
+    for (int i = CH - 1; i >= 0; i--) {
+      const int k = k0 + i;
+      if (k < n) {
+        const T x = (k == n - 1) ? r[i] : fma(-dd[i], xnext, r[i]);
+        if (act) col[(long)k * plane] = x;
+        xnext = x;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < CH; i++) r[i] = rn[i];
+  }
+}
+
+}  // namespace fg
+
+namespace fg {
+
+// One direction of bounduvw (src/bound.f90:17-144): both ends, all three
+// velocity components; one thread per face point, ghost layers in order.
+struct BcSide {
+  char ctype;
+  int centered;
+  double factor[4];
+  double sgn;
+};
+struct SetBc3Args {
+  double *f[3];
+  int nx, ny, nz, h, idir;
+  BcSide side[3][2];  // [component][ibound]
+};
+__global__ void k_set_bc3(SetBc3Args s) {
+  const int n = s.idir == 1 ? s.nx : (s.idir == 2 ? s.ny : s.nz);
+  const int na = s.idir == 1 ? s.ny : s.nx, nb = s.idir == 3 ? s.ny : s.nz;
+  const long HX = s.nx + 2 * s.h, HY = s.ny + 2 * s.h;
+  const long wa = na + 2 * s.h, wb = nb + 2 * s.h;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < wa * wb; t += (long)gridDim.x * blockDim.x) {
+    const int a = (int)(t % wa) + 1 - s.h, b = (int)(t / wa) + 1 - s.h;
+    auto at = [&](int tt) -> long {
+      int i, j, k;
+      if (s.idir == 1) { i = tt; j = a; k = b; }
+      else if (s.idir == 2) { i = a; j = tt; k = b; }
+      else { i = a; j = b; k = tt; }
+      return (long)(i - 1 + s.h) + HX * ((long)(j - 1 + s.h) + HY * (long)(k - 1 + s.h));
+    };
+    for (int ib = 0; ib < 2; ib++)
+      for (int c = 0; c < 3; c++) {
+        double *p = s.f[c];
+        const BcSide &sd = s.side[c][ib];
+        for (int q = 0; q < s.h; q++) {
+          const double f = sd.factor[q];
+          if (sd.ctype == 'P') {
+            p[at(0 - q)] = p[at(n - q)];
+            p[at(n + 1 + q)] = p[at(1 + q)];
+          } else if (sd.centered) {
+            if (ib == 0) p[at(0 - q)] = f + sd.sgn * p[at(1 + q)];
+            else p[at(n + 1 + q)] = f + sd.sgn * p[at(n - q)];
+          } else if (sd.ctype == 'D') {
+            if (ib == 0) p[at(0 - q)] = f;
+            else { p[at(n + q)] = f; p[at(n + 1 + q)] = p[at(n - 1 - q)]; }
+          } else {
+            if (ib == 0) p[at(0 - q)] = 1.0 * f + p[at(1 + q)];
+            else { p[at(n + q)] = 1.0 * f + p[at(n - 1 - q)]; p[at(n + 1 + q)] = 2.0 * f + p[at(n - 1 - q)]; }
+          }
+        }
+      }
   }
 }
 
