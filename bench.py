@@ -268,6 +268,15 @@ def run_ours(args, rank, world, local_rank):
         rep = F.profile_report(reset=True) if profile else None
         return total, lat, iters, launches, rep, f
 
+    if args.single:
+        tol = 1e-10 if args.precision == 1 else 0.0
+        t, lat, its, launches, _, _ = timed(args.precision, tol, args.steps, args.warmup)
+        if rank == 0:
+            return {"mode": "single", "precision": args.precision, "grid": [n, n, n], "steps": args.steps,
+                    "ms_per_step": round(t / args.steps, 4), "gpu_launches": launches,
+                    "fp32_solves_per_step": float(np.mean(its)) if its else None}
+        return None
+
     clk = ClockSampler(local_rank)
     clk.start()
     t_mix, lat_mix, it_mix, launches, rep, f_mix = timed(1, 1e-10, args.steps, args.warmup, profile=True)
@@ -491,6 +500,10 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--single", action="store_true",
+                    help="only the headline mode (for profiler captures): W warm-up + K steps, no extra modes, "
+                         "no e2e, no CPU baseline")
+    ap.add_argument("--precision", type=int, default=1, help="with --single: 1 mixed to 1e-10, 0 FP64")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

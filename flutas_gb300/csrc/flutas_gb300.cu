@@ -280,6 +280,9 @@ struct flutas_plan {
   std::vector<double> lam_h, a_h, b_h, c_h, dzci_h, dzfi_h;
   const void *host_lam = nullptr, *host_a = nullptr, *host_b = nullptr, *host_c = nullptr;
   DBuf lam, a, b, c, dzci, dzfi, rhsb[3];
+  DBuf a32, b32, c32;  // z coefficients rounded to FP32 (the mixed solve's arithmetic)
+  DBuf zres;           // per-level coefficients of the FP64 residual (3 per level)
+  DBuf czf;            // folded fillps factors dti*rho0*dzfi(k)
   AxisTables tx64, ty64, tx32, ty32;
   DBuf S64, S32, fbuf, phi, nrm;
   Mirrors mir;
@@ -394,6 +397,8 @@ template <typename T>
 int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const double *b, const double *c, bool pin) {
   ZArgs za;
   za.a = a; za.b = b; za.c = c; za.lam = lam;
+  if (sizeof(T) == 8) { za.at = a; za.bt = b; za.ct = c; }
+  else { za.at = pl->a32.p; za.bt = pl->b32.p; za.ct = pl->c32.p; }
   za.nq = pl->n[0] * pl->n[1];
   za.nz = pl->n[2];
   za.nn = pl->nn;
@@ -498,8 +503,7 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
   TRY(inv_xy<float>(pl, S, OutHalo{x, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
   InResidual R;
   R.f = f; R.x = x;
-  R.dzci = pl->dzci.as<double>() + (pl->nh_d - 1);
-  R.dzfi = pl->dzfi.as<double>() + (pl->nh_d - 1);
+  R.zc = pl->zres.as<double>();
   R.dxi2 = pl->dli[0] * pl->dli[0];
   R.dyi2 = pl->dli[1] * pl->dli[1];
   memcpy(R.bc, pl->cbc, 6);
@@ -647,7 +651,32 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
   };
   if ((rc = up(pl->lam, lambdaxy, (size_t)nx * ny))) return bail(rc);
   if ((rc = up(pl->a, a, nz)) || (rc = up(pl->b, b, nz)) || (rc = up(pl->c, c, nz))) return bail(rc);
+  {
+    // the FP64 coefficients rounded once to FP32 for the bulk solve
+    std::vector<float> f32(nz);
+    DBuf *dst[3] = {&pl->a32, &pl->b32, &pl->c32};
+    const double *src[3] = {a, b, c};
+    for (int t = 0; t < 3; t++) {
+      for (int k = 0; k < nz; k++) f32[k] = (float)src[t][k];
+      if ((rc = dst[t]->ensure(sizeof(float) * nz))) return bail(rc);
+      if (cudaMemcpy(dst[t]->p, f32.data(), sizeof(float) * nz, cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(fail(FLUTAS_ECUDA, "initsolver: upload of FP32 coefficients failed"));
+    }
+  }
   if ((rc = up(pl->dzci, dzci, nz + 2 * nh_d)) || (rc = up(pl->dzfi, dzfi, nz + 2 * nh_d))) return bail(rc);
+  {
+    // residual coefficients of level k (1-based): czm = dzfi(k)dzci(k-1),
+    // czp = dzfi(k)dzci(k), cc = -2 dxi^2 - 2 dyi^2 - czm - czp
+    std::vector<double> zr(3 * (size_t)nz);
+    const double dxi2 = dli[0] * dli[0], dyi2 = dli[1] * dli[1];
+    for (int k = 1; k <= nz; k++) {
+      const double czm = DZFI(k) * DZCI(k - 1), czp = DZFI(k) * DZCI(k);
+      zr[3 * (k - 1)] = czm;
+      zr[3 * (k - 1) + 1] = czp;
+      zr[3 * (k - 1) + 2] = -2.0 * dxi2 - 2.0 * dyi2 - czm - czp;
+    }
+    if ((rc = up(pl->zres, zr.data(), zr.size()))) return bail(rc);
+  }
   if ((rc = up(pl->rhsb[0], rhsbx, 2 * (size_t)ny * nz)) || (rc = up(pl->rhsb[1], rhsby, 2 * (size_t)nx * nz)) ||
       (rc = up(pl->rhsb[2], rhsbz, 2 * (size_t)nx * ny)))
     return bail(rc);
@@ -667,7 +696,7 @@ int flutas_gb300_fftend(void **arrplan) {
   flutas_plan *pl;
   TRY(check_plan(arrplan[0], &pl));
   cudaStreamSynchronize(pl->stream);
-  DBuf *bufs[] = {&pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
+  DBuf *bufs[] = {&pl->zres, &pl->czf, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
                   &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W, &pl->tx32.Q, &pl->ty32.W,
                   &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->nrm};
   for (DBuf *d : bufs) d->release();
@@ -691,7 +720,7 @@ int flutas_gb300_plan_info(void *plan, size_t *device_bytes, int *xy_path_fp64, 
   TRY(check_plan(plan, &pl));
   if (device_bytes) {
     size_t s = 0;
-    const DBuf *bufs[] = {&pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1],
+    const DBuf *bufs[] = {&pl->zres, &pl->czf, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1],
                           &pl->rhsb[2], &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W,
                           &pl->tx32.Q, &pl->ty32.W, &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->nrm};
     for (const DBuf *d : bufs) s += d->bytes;
@@ -791,10 +820,13 @@ int flutas_gb300_fillps(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, 
   TRY(stage_in(g_ctx_mir, w, ub, true, false, st, &sw));
   TRY(stage_in(g_ctx_mir, dzfi, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sz));
   TRY(stage_in(g_ctx_mir, p, pb, true, true, st, &sp));
+  TRY(g_ctx_small[1].ensure(sizeof(double) * (nz + 2 * nh_d)));
+  double *cz = g_ctx_small[1].as<double>();
+  TRY(launch("k_scale_vec", st, [&] { k_scale_vec<<<1, 256, 0, st>>>(sz.d, dti * rho0, cz, nz + 2 * nh_d); }));
   InFillps in;
   in.u = su.d; in.v = sv.d; in.w = sw.d;
-  in.dzfi = sz.d + (nh_d - 1);
-  in.dti = dti; in.dtidxi = dti * dxi; in.dtidyi = dti * dyi; in.rho0 = rho0;
+  in.cz = cz + (nh_d - 1);
+  in.cx = dti * dxi * rho0; in.cy = dti * dyi * rho0;
   in.rhsbx = in.rhsby = in.rhsbz = nullptr;
   in.q1 = in.q2 = in.q3 = 0;
   in.g = Geo{nx, ny, nz, nh_u};
@@ -1167,10 +1199,13 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
   TRY(pl->phi.ensure(pb));
   double *phi = pl->phi.as<double>();
+  TRY(pl->czf.ensure(sizeof(double) * (nz + 2 * nh_d)));
+  const double dti = 1.0 / dt;
+  TRY(launch("k_scale_vec", st, [&] { k_scale_vec<<<1, 256, 0, st>>>(dzfi_d, dti * rho0, pl->czf.as<double>(), nz + 2 * nh_d); }));
   InFillps in;
   in.u = u; in.v = v; in.w = w;
-  in.dzfi = dzfi_d + (nh_d - 1);
-  in.dti = 1.0 / dt; in.dtidxi = in.dti * dxi; in.dtidyi = in.dti * dyi; in.rho0 = rho0;
+  in.cz = pl->czf.as<double>() + (nh_d - 1);
+  in.cx = dti * dxi * rho0; in.cy = dti * dyi * rho0;
   in.rhsbx = pl->rhsb[0].as<double>(); in.rhsby = pl->rhsb[1].as<double>(); in.rhsbz = pl->rhsb[2].as<double>();
   in.q1 = in.q2 = in.q3 = 0;
   in.g = g;

@@ -73,21 +73,23 @@ struct InPlain {  // contiguous (nx,ny,nz) FP64 array
   __device__ double operator()(int i0, int j0, int k0) const { return f[g.sidx(i0, j0, k0)]; }
 };
 
-// fillps (src/fillps.f90:50-57) + optional updt_rhs_b (src/bound.f90:829-944)
+// fillps (src/fillps.f90:50-57) + optional updt_rhs_b (src/bound.f90:829-944).
+// The factors dti*dzfi(k)*rho0, dti*dyi*rho0, dti*dxi*rho0 are folded (FP64
+// instructions are the scarce resource on this GPU).
 struct InFillps {
   static constexpr const char *tag = "fillps";
   static constexpr const char *keep_tag = "keep-fillps";
-  const double *u, *v, *w, *dzfi;  // dzfi is (1-nh_d:), already offset so dzfi[k] = dzfi(k)
-  double dti, dtidxi, dtidyi, rho0;
+  const double *u, *v, *w;
+  const double *cz;  // cz[k] = dti*dzfi(k)*rho0 for k = 1..nz (index k)
+  double cy, cx;     // dti*dyi*rho0, dti*dxi*rho0
   const double *rhsbx, *rhsby, *rhsbz;  // nullable
   int q1, q2, q3;
   Geo g;
   __device__ double operator()(int i0, int j0, int k0) const {
     const int i = i0 + 1, j = j0 + 1, k = k0 + 1;
-    double val = ((w[g.uidx(i, j, k)] - w[g.uidx(i, j, k - 1)]) * dti * dzfi[k] +
-                  (v[g.uidx(i, j, k)] - v[g.uidx(i, j - 1, k)]) * dtidyi +
-                  (u[g.uidx(i, j, k)] - u[g.uidx(i - 1, j, k)]) * dtidxi);
-    val = val * rho0;
+    const long c = g.uidx(i, j, k);
+    const long sy = g.nx + 2 * g.h, sz = (long)(g.nx + 2 * g.h) * (g.ny + 2 * g.h);
+    double val = fma(w[c] - w[c - sz], cz[k], fma(v[c] - v[c - sy], cy, (u[c] - u[c - 1]) * cx));
     if (rhsbx) {
       const int nx = g.nx, ny = g.ny, nz = g.nz;
       if (i == 1) val += rhsbx[(j - 1) + (long)ny * (k - 1)];
@@ -107,24 +109,31 @@ struct InFillps {
 struct InResidual {
   static constexpr const char *tag = "residual";
   const double *f, *x;
-  const double *dzci, *dzfi;  // offset so that dzci[k] = dzci(k)
+  const double *zc;  // per level k (0-based): [3k] czm = dzfi*dzci(k-1), [3k+1] czp = dzfi*dzci(k), [3k+2] cc
   double dxi2, dyi2;
   char bc[6];
   Geo g;
   __device__ double ghost(char b, double pc, double pw) const { return b == 'P' ? pw : (b == 'N' ? pc : -pc); }
   __device__ double operator()(int i0, int j0, int k0) const {
     const int i = i0 + 1, j = j0 + 1, k = k0 + 1, nx = g.nx, ny = g.ny, nz = g.nz;
-    const double pc = x[g.pidx(i, j, k)];
-    const double pw = i > 1 ? x[g.pidx(i - 1, j, k)] : ghost(bc[0], pc, x[g.pidx(nx, j, k)]);
-    const double pe = i < nx ? x[g.pidx(i + 1, j, k)] : ghost(bc[1], pc, x[g.pidx(1, j, k)]);
-    const double ps = j > 1 ? x[g.pidx(i, j - 1, k)] : ghost(bc[2], pc, x[g.pidx(i, ny, k)]);
-    const double pn = j < ny ? x[g.pidx(i, j + 1, k)] : ghost(bc[3], pc, x[g.pidx(i, 1, k)]);
-    const double pb = k > 1 ? x[g.pidx(i, j, k - 1)] : ghost(bc[4], pc, x[g.pidx(i, j, nz)]);
-    const double pt = k < nz ? x[g.pidx(i, j, k + 1)] : ghost(bc[5], pc, x[g.pidx(i, j, 1)]);
-    const double ax = ((pe - pc) - (pc - pw)) * dxi2;
-    const double ay = ((pn - pc) - (pc - ps)) * dyi2;
-    const double az = ((pt - pc) * dzci[k] - (pc - pb) * dzci[k - 1]) * dzfi[k];
-    return f[g.pidx(i, j, k)] - (ax + ay + az);
+    const long c = g.pidx(i, j, k);
+    const long sx = 1, sy = nx + 2, sz = (long)(nx + 2) * (ny + 2);
+    const double pc = x[c];
+    double pw, pe, ps, pn, pb, pt;
+    if (i > 1 && i < nx && j > 1 && j < ny && k > 1 && k < nz) {
+      pw = x[c - sx]; pe = x[c + sx]; ps = x[c - sy]; pn = x[c + sy]; pb = x[c - sz]; pt = x[c + sz];
+    } else {
+      pw = i > 1 ? x[c - sx] : ghost(bc[0], pc, x[g.pidx(nx, j, k)]);
+      pe = i < nx ? x[c + sx] : ghost(bc[1], pc, x[g.pidx(1, j, k)]);
+      ps = j > 1 ? x[c - sy] : ghost(bc[2], pc, x[g.pidx(i, ny, k)]);
+      pn = j < ny ? x[c + sy] : ghost(bc[3], pc, x[g.pidx(i, 1, k)]);
+      pb = k > 1 ? x[c - sz] : ghost(bc[4], pc, x[g.pidx(i, j, nz)]);
+      pt = k < nz ? x[c + sz] : ghost(bc[5], pc, x[g.pidx(i, j, 1)]);
+    }
+    const double czm = zc[3 * k0], czp = zc[3 * k0 + 1], cc = zc[3 * k0 + 2];
+    double ax = fma(dxi2, pe + pw, dyi2 * (pn + ps));
+    ax = fma(czp, pt, fma(czm, pb, fma(cc, pc, ax)));
+    return f[c] - ax;
   }
 };
 
@@ -143,19 +152,25 @@ template <typename Inner> struct InKeep {
 };
 
 // ------------------------------------------------------ inverse output modes
-struct OutHalo {  // p(i,j,k) = v * scale
+struct OutHalo {  // p(i,j,k) = v * scale   (scale applied in the arithmetic type of the pass)
   static constexpr const char *tag = "halo";
   double *p;
   double scale;
   Geo g;
   __device__ void operator()(int i0, int j0, int k0, double v) const { p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = v * scale; }
+  __device__ void operator()(int i0, int j0, int k0, float v) const {
+    p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = (double)(v * (float)scale);
+  }
 };
-struct OutHaloAdd {  // p(i,j,k) += v * scale  (iterative-refinement update, FP64)
+struct OutHaloAdd {  // p(i,j,k) += v * scale  (iterative-refinement update, accumulated in FP64)
   static constexpr const char *tag = "haloadd";
   double *p;
   double scale;
   Geo g;
   __device__ void operator()(int i0, int j0, int k0, double v) const { p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] += v * scale; }
+  __device__ void operator()(int i0, int j0, int k0, float v) const {
+    p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] += (double)(v * (float)scale);
+  }
 };
 
 // ---------------------------------------------------------------- smem sizes
@@ -208,15 +223,15 @@ __global__ void __launch_bounds__(256) k_xfwd(AxisPlan ax, In in, T *S, Geo g, i
   const long rows = (long)g.ny * g.nz;
   const int tid = threadIdx.x, nth = blockDim.x;
   const int B = cbatch(ax.pair, M);
-  double ss = 0.0;
+  float ss = 0.0f;  // sum of squares for convergence checks (FP32 per thread)
   for (long row0 = (long)blockIdx.x * M; row0 < rows; row0 += (long)gridDim.x * M) {
     for (int idx = tid; idx < M * nx; idx += nth) {
       const int m = idx / nx, x = idx % nx;
       const long r = row0 + m;
-      double v = 0.0;
-      if (r < rows) v = in(x, (int)(r % g.ny), (int)(r / g.ny));
-      ss += v * v;
-      A[m * P + x] = (T)v;
+      T v = (T)0;
+      if (r < rows) v = (T)in(x, (int)(r % g.ny), (int)(r / g.ny));
+      ss = fma((float)v, (float)v, ss);
+      A[m * P + x] = v;
     }
     __syncthreads();
     pre_fwd<T>(ax, A, P, 1, M, C1, B, tid, nth);
@@ -233,7 +248,7 @@ __global__ void __launch_bounds__(256) k_xfwd(AxisPlan ax, In in, T *S, Geo g, i
     post_fwd<T>(ax, cur, B, M, st, tid, nth);
     __syncthreads();
   }
-  if (nrm) block_sum_add(ss, nrm);
+  if (nrm) block_sum_add((double)ss, nrm);
 }
 
 // x pass (inverse): spectral rows -> output functor, times normfft
@@ -243,7 +258,7 @@ struct StoreRowsOut {
   long row0, rows;
   int ny;
   __device__ void put(long r, int t, T v) {
-    if (r < rows) out(t, (int)(r % ny), (int)(r / ny), (double)v);
+    if (r < rows) out(t, (int)(r % ny), (int)(r / ny), v);
   }
   __device__ void pair(int c, int t, T v0, T v1) { put(row0 + 2 * c, t, v0); put(row0 + 2 * c + 1, t, v1); }
   __device__ void single(int c, int t, T v) { put(row0 + c, t, v); }
@@ -389,13 +404,13 @@ __global__ void __launch_bounds__(512) k_xyfwd_plane(AxisPlan ax, AxisPlan ay, I
   T *A = (T *)smem_raw;  // ny x P
   T *Bu = (T *)(smem_raw + align_up<T>(sizeof(T) * (size_t)ny * P));  // nx*ny reals
   const int tid = threadIdx.x, nth = blockDim.x;
-  double ss = 0.0;
+  float ss = 0.0f;  // sum of squares for convergence checks (FP32 per thread)
   for (int k = blockIdx.x; k < g.nz; k += gridDim.x) {
     for (int idx = tid; idx < nx * ny; idx += nth) {
       const int y = idx / nx, x = idx % nx;
-      const double v = in(x, y, k);
-      ss += v * v;
-      A[y * P + x] = (T)v;
+      const T v = (T)in(x, y, k);
+      ss = fma((float)v, (float)v, ss);
+      A[y * P + x] = v;
     }
     __syncthreads();
     // ---- x transform: lines = rows of A
@@ -418,7 +433,7 @@ __global__ void __launch_bounds__(512) k_xyfwd_plane(AxisPlan ax, AxisPlan ay, I
     post_fwd<T>(ay, fy, By, nx, st, tid, nth);
     __syncthreads();
   }
-  if (nrm) block_sum_add(ss, nrm);
+  if (nrm) block_sum_add((double)ss, nrm);
 }
 
 template <typename T, typename Out>
@@ -466,7 +481,8 @@ __global__ void __launch_bounds__(512) k_xyinv_plane(AxisPlan ax, AxisPlan ay, c
 // Columns are indexed q = kx + nx*ky; element (q,k) at S[q + nx*ny*k].
 // ===========================================================================
 struct ZArgs {
-  const double *a, *b, *c;   // tridmatrix coefficients (nz)
+  const double *a, *b, *c;   // tridmatrix coefficients (nz), FP64
+  const void *at, *bt, *ct;  // the same, rounded to the arithmetic type of the kernel
   const double *lam;         // lambdaxy (nx*ny)
   int nq;                    // nx*ny columns
   int nz;                    // full nz
@@ -672,27 +688,35 @@ __global__ void k_updt_rhs_b_dir(RhsbArgs a) {
 }
 
 // pres_tw_src (src/source.f90:247-309), _CONSTANT_COEFFS_POISSON branch.
+// With f1 = 1 + f2, dp = p(+) - p, dq = pold(+) - pold and t = dp - dq, the
+// increment f_t12*[-dp*dli/rho0 - (1/rho_f - 1/rho0)*(f1*dp - f2*dq)*dli]
+// equals f_t12*dli*[(f2/rho0)*t - (1/rho_f)*(dp + f2*t)]; 1/rho_f = 2/(rho+rho(+)).
 struct PresTwArgs {
   const double *p, *pold, *rho, *dzci;  // dzci[k] = dzci(k)
   double *u, *v, *w;
   double dxi, dyi, rho0i, f_t12, f1, f2;
   Geo g;
 };
+__device__ __forceinline__ double rcp64_1(double x) {
+  const double y = (double)__frcp_rn((float)x);  // FP32 seed, error <= 2^-24
+  return y * fma(-x, y, 2.0);                      // one Newton step: error ~2^-48
+}
+__device__ __forceinline__ double df_incr(double dp, double dq, double rs, double A, double B, double f2) {
+  const double t = dp - dq;
+  const double dg = fma(f2, t, dp);
+  return fma(A, t, -B * (rcp64_1(rs) * dg));
+}
 __device__ __forceinline__ void pres_tw_cell(const PresTwArgs &a, int i, int j, int k) {
   const Geo &g = a.g;
-  const long c0 = g.pidx(i, j, k), cx = g.pidx(i + 1, j, k), cy = g.pidx(i, j + 1, k), cz = g.pidx(i, j, k + 1);
-  const double rhoxi = rcp64(0.5 * (a.rho[cx] + a.rho[c0]));
-  const double rhoyi = rcp64(0.5 * (a.rho[cy] + a.rho[c0]));
-  const double rhozi = rcp64(0.5 * (a.rho[cz] + a.rho[c0]));
-  const double dzc = a.dzci[k];
-  const double q0 = a.f1 * a.p[c0] - a.f2 * a.pold[c0];
+  const long c0 = g.pidx(i, j, k), cx = c0 + 1, cy = c0 + (g.nx + 2), cz = c0 + (long)(g.nx + 2) * (g.ny + 2);
+  const double p0 = a.p[c0], q0 = a.pold[c0], r0 = a.rho[c0];
   const long ui = g.uidx(i, j, k);
-  a.u[ui] = a.u[ui] + a.f_t12 * ((-(a.p[cx] - a.p[c0]) * a.dxi) * a.rho0i -
-                                 (rhoxi - a.rho0i) * ((a.f1 * a.p[cx] - a.f2 * a.pold[cx]) - q0) * a.dxi);
-  a.v[ui] = a.v[ui] + a.f_t12 * ((-(a.p[cy] - a.p[c0]) * a.dyi) * a.rho0i -
-                                 (rhoyi - a.rho0i) * ((a.f1 * a.p[cy] - a.f2 * a.pold[cy]) - q0) * a.dyi);
-  a.w[ui] = a.w[ui] + a.f_t12 * ((-(a.p[cz] - a.p[c0]) * dzc) * a.rho0i -
-                                 (rhozi - a.rho0i) * ((a.f1 * a.p[cz] - a.f2 * a.pold[cz]) - q0) * dzc);
+  const double dzc = a.dzci[k];
+  // A = f_t12*dli*f2*rho0i, B = 2*f_t12*dli
+  const double ax = a.f_t12 * a.dxi, ay = a.f_t12 * a.dyi, az = a.f_t12 * dzc;
+  a.u[ui] += df_incr(a.p[cx] - p0, a.pold[cx] - q0, a.rho[cx] + r0, ax * a.f2 * a.rho0i, 2.0 * ax, a.f2);
+  a.v[ui] += df_incr(a.p[cy] - p0, a.pold[cy] - q0, a.rho[cy] + r0, ay * a.f2 * a.rho0i, 2.0 * ay, a.f2);
+  a.w[ui] += df_incr(a.p[cz] - p0, a.pold[cz] - q0, a.rho[cz] + r0, az * a.f2 * a.rho0i, 2.0 * az, a.f2);
 }
 __global__ void k_pres_tw_src(PresTwArgs a) {
   for_cells(a.g, [&](int i0, int j0, int k0) { pres_tw_cell(a, i0 + 1, j0 + 1, k0 + 1); });
@@ -703,7 +727,7 @@ __global__ void k_pres_tw_src(PresTwArgs a) {
 struct CorrecAddArgs {
   const double *phi, *dzci;
   double *u, *v, *w, *p;
-  double factori, factorj, dt, rho0i;
+  double factori, factorj, dt, rho0i;  // cx = factori*rho0i etc. folded in the kernel
   Geo g;
 };
 __global__ void k_correc_padd(CorrecAddArgs a) {
@@ -713,9 +737,10 @@ __global__ void k_correc_padd(CorrecAddArgs a) {
     const long pc = g.pidx(i, j, k);
     const double ph = a.phi[pc];
     const long ui = g.uidx(i, j, k);
-    a.u[ui] = a.u[ui] - a.factori * (a.phi[g.pidx(i + 1, j, k)] - ph) * a.rho0i;
-    a.v[ui] = a.v[ui] - a.factorj * (a.phi[g.pidx(i, j + 1, k)] - ph) * a.rho0i;
-    a.w[ui] = a.w[ui] - a.dt * a.dzci[k] * (a.phi[g.pidx(i, j, k + 1)] - ph) * a.rho0i;
+    const double cx = a.factori * a.rho0i, cy = a.factorj * a.rho0i, cz = a.dt * a.rho0i * a.dzci[k];
+    a.u[ui] = fma(-cx, a.phi[pc + 1] - ph, a.u[ui]);
+    a.v[ui] = fma(-cy, a.phi[pc + (g.nx + 2)] - ph, a.v[ui]);
+    a.w[ui] = fma(-cz, a.phi[pc + (long)(g.nx + 2) * (g.ny + 2)] - ph, a.w[ui]);
     a.p[pc] = a.p[pc] + ph;
   });
 }
@@ -786,6 +811,10 @@ template <typename T>
 __device__ __forceinline__ T zpivot(T bb, T a, T dprev, bool first) {
   return first ? bb : fma(-a, dprev, bb);
 }
+// 1/x: the SFU reciprocal in FP32 (the FP32 solve is refined in FP64), a
+// correctly rounded division in FP64.
+__device__ __forceinline__ float zrcp(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double zrcp(double x) { return 1.0 / x; }
 
 template <typename T, int CH>
 __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, long q_begin, long q_end) {
@@ -796,8 +825,10 @@ __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, lo
   const bool act = q < q_end;
   const int n = za.nn;
   const long plane = za.nq;
-  const double lam = act ? za.lam[q] : 1.0;
-  const bool pin = za.pin && lam == 0.0;
+  const double lam64 = act ? za.lam[q] : 1.0;
+  const bool pin = za.pin && lam64 == 0.0;
+  const T lam = (T)lam64;
+  const T *__restrict__ ca = (const T *)za.at, *__restrict__ cb = (const T *)za.bt, *__restrict__ cc = (const T *)za.ct;
   T *col = S + (act ? q : 0);
   const int nch = (n + CH - 1) / CH;
   // ---- forward elimination
@@ -817,12 +848,12 @@ __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, lo
     for (int i = 0; i < CH; i++) {
       const int k = k0 + i;
       if (k < n) {
-        const T bb = (T)(za.b[k] + lam);
-        const T ak = (T)za.a[k];
+        const T bb = cb[k] + lam;
+        const T ak = ca[k];
         T y, d;
         if (k < n - 1) {
-          const T z = (T)1 / zpivot<T>(bb, ak, dprev, k == 0);
-          d = (T)za.c[k] * z;
+          const T z = zrcp(zpivot<T>(bb, ak, dprev, k == 0));
+          d = cc[k] * z;
           y = (k == 0 ? r[i] : fma(-ak, yprev, r[i])) * z;
         } else {
           const T zl = zpivot<T>(bb, ak, dprev, k == 0);
@@ -857,9 +888,9 @@ __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, lo
     for (int i = 0; i < CH; i++) {
       const int k = k0 + i;
       if (k < n - 1) {
-        const T bb = (T)(za.b[k] + lam);
-        const T z = (T)1 / zpivot<T>(bb, (T)za.a[k], dp, k == 0);
-        dd[i] = (T)za.c[k] * z;
+        const T bb = cb[k] + lam;
+        const T z = zrcp(zpivot<T>(bb, ca[k], dp, k == 0));
+        dd[i] = cc[k] * z;
         dp = dd[i];
       } else {
         dd[i] = (T)0;
@@ -934,4 +965,11 @@ __global__ void k_set_bc3(SetBc3Args s) {
   }
 }
 
+}  // namespace fg
+
+namespace fg {
+// out[k] = s * in[k] for k in [0, n): folded z factors (e.g. dti*rho0*dzfi(k))
+__global__ void k_scale_vec(const double *in, double s, double *out, int n) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) out[k] = s * in[k];
+}
 }  // namespace fg
