@@ -18,7 +18,8 @@ inline int fill_axis_tables(int n, int pair, AxisPlan *ap, std::vector<C2<T>> &W
   const bool pr = pair <= BC_DD;
   if (!pr && (n % 2)) return -1;
   ap->N = pr ? n : n / 2;
-  const int ns = ap->N == 1 ? 0 : make_radix_plan(ap->N, ap->radix);
+  // FP64 butterflies are capped at radix 8 (register pressure of 16 complex doubles)
+  const int ns = ap->N == 1 ? 0 : make_radix_plan(ap->N, ap->radix, sizeof(T) == 8 ? 3 : 4);
   if (ns < 0) return -1;
   ap->nst = ns;
   const long double PI = 3.141592653589793238462643383279502884L;

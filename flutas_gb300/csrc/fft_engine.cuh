@@ -219,15 +219,15 @@ FG_HD void stage_dispatch(int R, const C2<T> *in, C2<T> *out, int N, int B, int 
   }
 }
 
-// Radix plan for a length-N FFT: powers of two in balanced stages of <= 16,
-// then the odd factors 3,5,7,11,13.  Returns number of stages, or -1 if N has
-// another prime factor.
-inline int make_radix_plan(int N, int *radix) {
+// Radix plan for a length-N FFT: powers of two in balanced stages of at most
+// 2^maxe (16 by default), then the odd factors 3,5,7,11,13.  Returns the
+// number of stages, or -1 if N has another prime factor.
+inline int make_radix_plan(int N, int *radix, int maxe = 4) {
   int e = 0, m = N;
   while (m % 2 == 0) { m /= 2; e++; }
   int ns = 0;
   if (e > 0) {
-    int nst = (e + 3) / 4;
+    int nst = (e + maxe - 1) / maxe;
     for (int s = 0; s < nst; s++) {
       int es = e / nst + (s < e % nst ? 1 : 0);
       radix[ns++] = 1 << es;

@@ -283,6 +283,7 @@ struct flutas_plan {
   DBuf a32, b32, c32;  // z coefficients rounded to FP32 (the mixed solve's arithmetic)
   DBuf zres;           // per-level coefficients of the FP64 residual (3 per level)
   DBuf czf;            // folded fillps factors dti*rho0*dzfi(k)
+  DBuf zdf;            // per-level factors of the Dodd-Ferrante term
   AxisTables tx64, ty64, tx32, ty32;
   DBuf S64, S32, fbuf, phi, nrm;
   Mirrors mir;
@@ -696,7 +697,7 @@ int flutas_gb300_fftend(void **arrplan) {
   flutas_plan *pl;
   TRY(check_plan(arrplan[0], &pl));
   cudaStreamSynchronize(pl->stream);
-  DBuf *bufs[] = {&pl->zres, &pl->czf, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
+  DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
                   &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W, &pl->tx32.Q, &pl->ty32.W,
                   &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->nrm};
   for (DBuf *d : bufs) d->release();
@@ -720,7 +721,7 @@ int flutas_gb300_plan_info(void *plan, size_t *device_bytes, int *xy_path_fp64, 
   TRY(check_plan(plan, &pl));
   if (device_bytes) {
     size_t s = 0;
-    const DBuf *bufs[] = {&pl->zres, &pl->czf, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1],
+    const DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1],
                           &pl->rhsb[2], &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W,
                           &pl->tx32.Q, &pl->ty32.W, &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->nrm};
     for (const DBuf *d : bufs) s += d->bytes;
@@ -984,6 +985,24 @@ int boundp_dev(double *p, const int n[3], const char cbc[6], const double bc[6],
   return 0;
 }
 
+// Constants of the Dodd-Ferrante increment (see PresTwArgs): x/y scalars and
+// the per-level z factors zA = f_t12*f2/rho0*dzci(k), zB = 2*f_t12*dzci(k)
+// computed on the device into zab (2*(nz+2nh_d) doubles); dzci_d is (1-nh_d:).
+int presw_consts(PresTwArgs *a, const double *dzci_d, int nh_d, int nz, double dxi, double dyi, double rho0i,
+                 double f_t12, double f2, double *zab, cudaStream_t st) {
+  const int len = nz + 2 * nh_d;
+  a->f2 = f2;
+  a->xA = f_t12 * dxi * f2 * rho0i;
+  a->xB = 2.0 * f_t12 * dxi;
+  a->yA = f_t12 * dyi * f2 * rho0i;
+  a->yB = 2.0 * f_t12 * dyi;
+  TRY(launch("k_scale_vec", st, [&] { k_scale_vec<<<1, 256, 0, st>>>(dzci_d, f_t12 * f2 * rho0i, zab, len); }));
+  TRY(launch("k_scale_vec", st, [&] { k_scale_vec<<<1, 256, 0, st>>>(dzci_d, 2.0 * f_t12, zab + len, len); }));
+  a->zA = zab + (nh_d - 1);
+  a->zB = zab + len + (nh_d - 1);
+  return 0;
+}
+
 int updt_rhs_b_dev(double *p, Geo g, const double *rx, const double *ry, const double *rz, int q1, int q2, int q3,
                    cudaStream_t st) {
   const double *r[3] = {rx, ry, rz};
@@ -1041,12 +1060,13 @@ int flutas_gb300_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, dou
   TRY(stage_in(g_ctx_mir, pold, pb, true, false, st, &so));
   TRY(stage_in(g_ctx_mir, rho, pb, true, false, st, &sr));
   TRY(stage_in(g_ctx_mir, dzci, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sz));
+  const double f2 = (f_t12 / f_t12_o);
+  TRY(g_ctx_small[2].ensure(sizeof(double) * 2 * (nz + 2 * nh_d)));
+  double *zab = g_ctx_small[2].as<double>();
   PresTwArgs a;
-  a.p = sp.d; a.pold = so.d; a.rho = sr.d; a.dzci = sz.d + (nh_d - 1);
+  a.p = sp.d; a.pold = so.d; a.rho = sr.d;
   a.u = su.d; a.v = sv.d; a.w = sw.d;
-  a.dxi = dxi; a.dyi = dyi; a.rho0i = rho0i; a.f_t12 = f_t12;
-  a.f1 = 1.0 + (f_t12 / f_t12_o);
-  a.f2 = (f_t12 / f_t12_o);
+  TRY(presw_consts(&a, sz.d, nh_d, nz, dxi, dyi, rho0i, f_t12, f2, zab, st));
   a.g = Geo{nx, ny, nz, nh_u};
   TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<grid_cells(a.g), 256, 0, st>>>(a); }));
   TRY(stage_out(su, st));
@@ -1186,12 +1206,11 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   cudaStream_t st = pl->stream;
   const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
   if (rho) {
+    TRY(pl->zdf.ensure(sizeof(double) * 2 * (nz + 2 * nh_d)));
     PresTwArgs a;
-    a.p = p; a.pold = pold; a.rho = rho; a.dzci = dzci_d + (nh_d - 1);
+    a.p = p; a.pold = pold; a.rho = rho;
     a.u = u; a.v = v; a.w = w;
-    a.dxi = dxi; a.dyi = dyi; a.rho0i = 1.0 / rho0; a.f_t12 = dt;
-    a.f1 = 1.0 + (dt / f_t12_o);
-    a.f2 = (dt / f_t12_o);
+    TRY(presw_consts(&a, dzci_d, nh_d, nz, dxi, dyi, 1.0 / rho0, dt, dt / f_t12_o, pl->zdf.as<double>(), st));
     a.g = g;
     TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<grid_cells(a.g), 256, 0, st>>>(a); }));
   }

@@ -692,9 +692,11 @@ __global__ void k_updt_rhs_b_dir(RhsbArgs a) {
 // increment f_t12*[-dp*dli/rho0 - (1/rho_f - 1/rho0)*(f1*dp - f2*dq)*dli]
 // equals f_t12*dli*[(f2/rho0)*t - (1/rho_f)*(dp + f2*t)]; 1/rho_f = 2/(rho+rho(+)).
 struct PresTwArgs {
-  const double *p, *pold, *rho, *dzci;  // dzci[k] = dzci(k)
+  const double *p, *pold, *rho;
   double *u, *v, *w;
-  double dxi, dyi, rho0i, f_t12, f1, f2;
+  const double *zA, *zB;  // per level k: f_t12*dzci(k)*f2/rho0 and 2*f_t12*dzci(k)
+  double xA, xB, yA, yB;  // the same with dxi, dyi
+  double f2;
   Geo g;
 };
 __device__ __forceinline__ double rcp64_1(double x) {
@@ -711,12 +713,9 @@ __device__ __forceinline__ void pres_tw_cell(const PresTwArgs &a, int i, int j, 
   const long c0 = g.pidx(i, j, k), cx = c0 + 1, cy = c0 + (g.nx + 2), cz = c0 + (long)(g.nx + 2) * (g.ny + 2);
   const double p0 = a.p[c0], q0 = a.pold[c0], r0 = a.rho[c0];
   const long ui = g.uidx(i, j, k);
-  const double dzc = a.dzci[k];
-  // A = f_t12*dli*f2*rho0i, B = 2*f_t12*dli
-  const double ax = a.f_t12 * a.dxi, ay = a.f_t12 * a.dyi, az = a.f_t12 * dzc;
-  a.u[ui] += df_incr(a.p[cx] - p0, a.pold[cx] - q0, a.rho[cx] + r0, ax * a.f2 * a.rho0i, 2.0 * ax, a.f2);
-  a.v[ui] += df_incr(a.p[cy] - p0, a.pold[cy] - q0, a.rho[cy] + r0, ay * a.f2 * a.rho0i, 2.0 * ay, a.f2);
-  a.w[ui] += df_incr(a.p[cz] - p0, a.pold[cz] - q0, a.rho[cz] + r0, az * a.f2 * a.rho0i, 2.0 * az, a.f2);
+  a.u[ui] += df_incr(a.p[cx] - p0, a.pold[cx] - q0, a.rho[cx] + r0, a.xA, a.xB, a.f2);
+  a.v[ui] += df_incr(a.p[cy] - p0, a.pold[cy] - q0, a.rho[cy] + r0, a.yA, a.yB, a.f2);
+  a.w[ui] += df_incr(a.p[cz] - p0, a.pold[cz] - q0, a.rho[cz] + r0, a.zA[k], a.zB[k], a.f2);
 }
 __global__ void k_pres_tw_src(PresTwArgs a) {
   for_cells(a.g, [&](int i0, int j0, int k0) { pres_tw_cell(a, i0 + 1, j0 + 1, k0 + 1); });
