@@ -160,6 +160,22 @@ def zgrid(n):
     return 1.0 / dz, 1.0 / dz, dz
 
 
+# ----------------------------------------------------------------- replicas
+def reduce_max(x: float, world: int, device="cpu") -> float:
+    """Max of a per-rank scalar over all ranks (timing only; no data-path collective)."""
+    if world == 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(steps_per_rank: int, world: int, max_ms: float) -> float:
+    """Whole-job rate: every replica ran `steps_per_rank` steps; the slowest rank's time counts."""
+    return world * steps_per_rank / (max_ms / 1e3)
+
+
 # ----------------------------------------------------------------- clocks
 class ClockSampler:
     def __init__(self, gpu_index: int):
@@ -319,19 +335,13 @@ def run_ours(args, rank, world, local_rank):
     field_bytes = (n + 2) ** 3 * 8
 
     # max over ranks
-    def agg_max(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-    t_mix, t_m6, t_64, t_e2e = (agg_max(x) for x in (t_mix, t_m6, t_64, t_e2e))
+    t_mix, t_m6, t_64, t_e2e = (reduce_max(x, world, dev) for x in (t_mix, t_m6, t_64, t_e2e))
 
     res = None
     if rank == 0:
         ncell = n ** 3
         steps = args.steps
-        value = world * steps / (t_mix / 1e3)
+        value = replica_rate(steps, world, t_mix)
         # roofline of the dominant kernel
         hbm, src = peaks()
         dom = max(rep.items(), key=lambda kv: kv[1][1]) if rep else None

@@ -213,41 +213,49 @@ __device__ __forceinline__ void block_sum_add(double v, double *acc) {
   }
 }
 
+// One tile of the x pass: M rows starting at global row row0 (row = j + ny*k).
+// smem: M*P reals + M*nx reals.  Accumulates the squares of the inputs in ss.
 template <typename T, typename In>
-__global__ void __launch_bounds__(256) k_xfwd(AxisPlan ax, In in, T *S, Geo g, int M, double *nrm) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void xfwd_tile(const AxisPlan &ax, const In &in, T *S, const Geo &g, int M, long row0,
+                                          unsigned char *smem, float &ss) {
   const int nx = g.nx, P = xpitch(nx);
-  T *A = (T *)smem_raw;
-  C2<T> *C1 = (C2<T> *)(smem_raw + align_up<T>(sizeof(T) * (size_t)M * P));
+  T *A = (T *)smem;
+  C2<T> *C1 = (C2<T> *)(smem + align_up<T>(sizeof(T) * (size_t)M * P));
   C2<T> *C2b = (C2<T> *)A;  // ping-pong partner aliases the input rows
   const long rows = (long)g.ny * g.nz;
   const int tid = threadIdx.x, nth = blockDim.x;
   const int B = cbatch(ax.pair, M);
-  float ss = 0.0f;  // sum of squares for convergence checks (FP32 per thread)
-  for (long row0 = (long)blockIdx.x * M; row0 < rows; row0 += (long)gridDim.x * M) {
-    for (int idx = tid; idx < M * nx; idx += nth) {
-      const int m = idx / nx, x = idx % nx;
-      const long r = row0 + m;
-      T v = (T)0;
-      if (r < rows) v = (T)in(x, (int)(r % g.ny), (int)(r / g.ny));
-      ss = fma((float)v, (float)v, ss);
-      A[m * P + x] = v;
-    }
-    __syncthreads();
-    pre_fwd<T>(ax, A, P, 1, M, C1, B, tid, nth);
-    __syncthreads();
-    C2<T> *cur = C1, *nxt = C2b;
-    int Ns = 1;
-    for (int s = 0; s < ax.nst; s++) {
-      stage_dispatch<T, false>(ax.radix[s], cur, nxt, ax.N, B, B, Ns, (const C2<T> *)ax.W, tid, nth);
-      Ns *= ax.radix[s];
-      C2<T> *t = cur; cur = nxt; nxt = t;
-      __syncthreads();
-    }
-    StoreRowsS<T> st{S, row0, rows, nx};
-    post_fwd<T>(ax, cur, B, M, st, tid, nth);
+  for (int idx = tid; idx < M * nx; idx += nth) {
+    const int m = idx / nx, x = idx % nx;
+    const long r = row0 + m;
+    T v = (T)0;
+    if (r < rows) v = (T)in(x, (int)(r % g.ny), (int)(r / g.ny));
+    ss = fma((float)v, (float)v, ss);
+    A[m * P + x] = v;
+  }
+  __syncthreads();
+  pre_fwd<T>(ax, A, P, 1, M, C1, B, tid, nth);
+  __syncthreads();
+  C2<T> *cur = C1, *nxt = C2b;
+  int Ns = 1;
+  for (int s = 0; s < ax.nst; s++) {
+    stage_dispatch<T, false>(ax.radix[s], cur, nxt, ax.N, B, B, Ns, (const C2<T> *)ax.W, tid, nth);
+    Ns *= ax.radix[s];
+    C2<T> *t = cur; cur = nxt; nxt = t;
     __syncthreads();
   }
+  StoreRowsS<T> st{S, row0, rows, nx};
+  post_fwd<T>(ax, cur, B, M, st, tid, nth);
+  __syncthreads();
+}
+
+template <typename T, typename In>
+__global__ void __launch_bounds__(256) k_xfwd(AxisPlan ax, In in, T *S, Geo g, int M, double *nrm) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const long rows = (long)g.ny * g.nz;
+  float ss = 0.0f;  // sum of squares for convergence checks (FP32 per thread)
+  for (long row0 = (long)blockIdx.x * M; row0 < rows; row0 += (long)gridDim.x * M)
+    xfwd_tile<T, In>(ax, in, S, g, M, row0, smem_raw, ss);
   if (nrm) block_sum_add((double)ss, nrm);
 }
 
@@ -265,38 +273,44 @@ struct StoreRowsOut {
 };
 
 template <typename T, typename Out>
-__global__ void __launch_bounds__(256) k_xinv(AxisPlan ax, const T *S, Out out, Geo g, int M) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void xinv_tile(const AxisPlan &ax, const T *S, const Out &out, const Geo &g, int M,
+                                          long row0, unsigned char *smem) {
   const int nx = g.nx, P = xpitch(nx);
-  T *A = (T *)smem_raw;
-  C2<T> *C1 = (C2<T> *)(smem_raw + align_up<T>(sizeof(T) * (size_t)M * P));
+  T *A = (T *)smem;
+  C2<T> *C1 = (C2<T> *)(smem + align_up<T>(sizeof(T) * (size_t)M * P));
   C2<T> *C2b = (C2<T> *)A;
   const long rows = (long)g.ny * g.nz;
   const int tid = threadIdx.x, nth = blockDim.x;
   const int B = cbatch(ax.pair, M);
   const bool inv = fft_inverse(ax.pair, true);
-  for (long row0 = (long)blockIdx.x * M; row0 < rows; row0 += (long)gridDim.x * M) {
-    for (int idx = tid; idx < M * nx; idx += nth) {
-      const int m = idx / nx, x = idx % nx;
-      const long r = row0 + m;
-      A[m * P + x] = r < rows ? S[r * nx + x] : (T)0;
-    }
-    __syncthreads();
-    pre_bwd<T>(ax, A, P, 1, M, C1, B, tid, nth);
-    __syncthreads();
-    C2<T> *cur = C1, *nxt = C2b;
-    int Ns = 1;
-    for (int s = 0; s < ax.nst; s++) {
-      if (inv) stage_dispatch<T, true>(ax.radix[s], cur, nxt, ax.N, B, B, Ns, (const C2<T> *)ax.W, tid, nth);
-      else stage_dispatch<T, false>(ax.radix[s], cur, nxt, ax.N, B, B, Ns, (const C2<T> *)ax.W, tid, nth);
-      Ns *= ax.radix[s];
-      C2<T> *t = cur; cur = nxt; nxt = t;
-      __syncthreads();
-    }
-    StoreRowsOut<T, Out> st{out, row0, rows, g.ny};
-    post_bwd<T>(ax, cur, B, M, st, tid, nth);
+  for (int idx = tid; idx < M * nx; idx += nth) {
+    const int m = idx / nx, x = idx % nx;
+    const long r = row0 + m;
+    A[m * P + x] = r < rows ? S[r * nx + x] : (T)0;
+  }
+  __syncthreads();
+  pre_bwd<T>(ax, A, P, 1, M, C1, B, tid, nth);
+  __syncthreads();
+  C2<T> *cur = C1, *nxt = C2b;
+  int Ns = 1;
+  for (int s = 0; s < ax.nst; s++) {
+    if (inv) stage_dispatch<T, true>(ax.radix[s], cur, nxt, ax.N, B, B, Ns, (const C2<T> *)ax.W, tid, nth);
+    else stage_dispatch<T, false>(ax.radix[s], cur, nxt, ax.N, B, B, Ns, (const C2<T> *)ax.W, tid, nth);
+    Ns *= ax.radix[s];
+    C2<T> *t = cur; cur = nxt; nxt = t;
     __syncthreads();
   }
+  StoreRowsOut<T, Out> st{out, row0, rows, g.ny};
+  post_bwd<T>(ax, cur, B, M, st, tid, nth);
+  __syncthreads();
+}
+
+template <typename T, typename Out>
+__global__ void __launch_bounds__(256) k_xinv(AxisPlan ax, const T *S, Out out, Geo g, int M) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const long rows = (long)g.ny * g.nz;
+  for (long row0 = (long)blockIdx.x * M; row0 < rows; row0 += (long)gridDim.x * M)
+    xinv_tile<T, Out>(ax, S, out, g, M, row0, smem_raw);
 }
 
 // ===========================================================================
@@ -318,44 +332,49 @@ struct StoreColsS {  // line l of the tile = column x0+l; position t = row y
   }
 };
 
+// One tile of the y pass: columns [x0, x0+W) of plane k, all ny rows.
 template <typename T, bool BACKWARD>
-__global__ void __launch_bounds__(256) k_ypass(AxisPlan ay, T *S, Geo g, int W) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void ypass_tile(const AxisPlan &ay, T *S, const Geo &g, int W, long tile,
+                                           unsigned char *smem) {
   const int ny = g.ny, nx = g.nx;
-  T *A = (T *)smem_raw;  // ny rows x W
-  C2<T> *C1 = (C2<T> *)(smem_raw + align_up<T>(sizeof(T) * (size_t)W * ny));
+  T *A = (T *)smem;  // ny rows x W
+  C2<T> *C1 = (C2<T> *)(smem + align_up<T>(sizeof(T) * (size_t)W * ny));
   C2<T> *C2b = (C2<T> *)A;
   const int tid = threadIdx.x, nth = blockDim.x;
   const int tiles_x = (nx + W - 1) / W;
-  const long ntiles = (long)tiles_x * g.nz;
   const int B = cbatch(ay.pair, W);
   const bool inv = fft_inverse(ay.pair, BACKWARD);
-  for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int tx = (int)(tile % tiles_x), k = (int)(tile / tiles_x);
-    const int x0 = tx * W, Wv = min(W, nx - x0);
-    const long off = (long)k * nx * ny;
-    for (int idx = tid; idx < W * ny; idx += nth) {
-      const int y = idx / W, xx = idx % W;
-      A[idx] = xx < Wv ? S[off + (long)y * nx + x0 + xx] : (T)0;
-    }
-    __syncthreads();
-    if (BACKWARD) pre_bwd<T>(ay, A, 1, W, W, C1, B, tid, nth);
-    else pre_fwd<T>(ay, A, 1, W, W, C1, B, tid, nth);
-    __syncthreads();
-    C2<T> *cur = C1, *nxt = C2b;
-    int Ns = 1;
-    for (int s = 0; s < ay.nst; s++) {
-      if (inv) stage_dispatch<T, true>(ay.radix[s], cur, nxt, ay.N, B, B, Ns, (const C2<T> *)ay.W, tid, nth);
-      else stage_dispatch<T, false>(ay.radix[s], cur, nxt, ay.N, B, B, Ns, (const C2<T> *)ay.W, tid, nth);
-      Ns *= ay.radix[s];
-      C2<T> *t = cur; cur = nxt; nxt = t;
-      __syncthreads();
-    }
-    StoreColsS<T> st{S, off, nx, x0, Wv};
-    if (BACKWARD) post_bwd<T>(ay, cur, B, W, st, tid, nth);
-    else post_fwd<T>(ay, cur, B, W, st, tid, nth);
+  const int tx = (int)(tile % tiles_x), k = (int)(tile / tiles_x);
+  const int x0 = tx * W, Wv = min(W, nx - x0);
+  const long off = (long)k * nx * ny;
+  for (int idx = tid; idx < W * ny; idx += nth) {
+    const int y = idx / W, xx = idx % W;
+    A[idx] = xx < Wv ? S[off + (long)y * nx + x0 + xx] : (T)0;
+  }
+  __syncthreads();
+  if (BACKWARD) pre_bwd<T>(ay, A, 1, W, W, C1, B, tid, nth);
+  else pre_fwd<T>(ay, A, 1, W, W, C1, B, tid, nth);
+  __syncthreads();
+  C2<T> *cur = C1, *nxt = C2b;
+  int Ns = 1;
+  for (int s = 0; s < ay.nst; s++) {
+    if (inv) stage_dispatch<T, true>(ay.radix[s], cur, nxt, ay.N, B, B, Ns, (const C2<T> *)ay.W, tid, nth);
+    else stage_dispatch<T, false>(ay.radix[s], cur, nxt, ay.N, B, B, Ns, (const C2<T> *)ay.W, tid, nth);
+    Ns *= ay.radix[s];
+    C2<T> *t = cur; cur = nxt; nxt = t;
     __syncthreads();
   }
+  StoreColsS<T> st{S, off, nx, x0, Wv};
+  if (BACKWARD) post_bwd<T>(ay, cur, B, W, st, tid, nth);
+  else post_fwd<T>(ay, cur, B, W, st, tid, nth);
+  __syncthreads();
+}
+
+template <typename T, bool BACKWARD>
+__global__ void __launch_bounds__(256) k_ypass(AxisPlan ay, T *S, Geo g, int W) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const long ntiles = (long)((g.nx + W - 1) / W) * g.nz;
+  for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) ypass_tile<T, BACKWARD>(ay, S, g, W, tile, smem_raw);
 }
 
 // ===========================================================================
@@ -971,4 +990,242 @@ namespace fg {
 __global__ void k_scale_vec(const double *in, double s, double *out, int n) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) out[k] = s * in[k];
 }
+}  // namespace fg
+
+namespace fg {
+
+// ===========================================================================
+// Batched solves: many independent grids of different sizes and BCs.
+// Each pass is one persistent kernel that drains a (grid, tile) work queue
+// (an atomic counter over the concatenated tiles of all grids).  Grids that
+// have converged are skipped.  The pass sequence is captured in a CUDA graph.
+// ===========================================================================
+struct BatchGrid {
+  Geo g;                 // halo-1 geometry
+  AxisPlan ax, ay;       // FP32 transform plans
+  ZArgs za;              // FP32 z coefficients (at/bt/ct), lambda, pin, periodic
+  double *x, *f;         // FP64 halo arrays: solution (RHS on entry), RHS copy
+  float *S, *S2;         // spectral array, periodic-z scratch (nullable)
+  const double *zres;    // residual coefficients, 3 per level
+  double dxi2, dyi2, normfft;
+  char bc[6];
+  int M, W;              // x-pass rows per tile, y-pass columns per tile
+  double *nrm;           // [0] ||f||^2, [1] ||r||^2 of the current check
+  int *active;           // 1 while the grid still refines
+};
+
+struct BatchQueue {
+  const BatchGrid *grids;
+  const long *prefix;    // ngrids+1 running totals of tiles for this pass
+  int ngrids;
+  int *counter;          // work counter of this pass (zeroed before the pass)
+};
+
+__device__ __forceinline__ int batch_find(const long *prefix, int ng, long item) {
+  int lo = 0, hi = ng;  // prefix[lo] <= item < prefix[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= item) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Fetch the next work item for the whole block (thread 0 takes it, all read it).
+__device__ __forceinline__ long batch_next(int *counter) {
+  __shared__ long s_item;
+  __syncthreads();
+  if (threadIdx.x == 0) s_item = (long)atomicAdd(counter, 1);
+  __syncthreads();
+  return s_item;
+}
+
+// First pass (mode 0: RHS = x, keep f = x) or residual pass (mode 1: r = f - A x).
+__global__ void __launch_bounds__(256) kb_xfwd(BatchQueue q, int mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const long total = q.prefix[q.ngrids];
+  for (long item = batch_next(q.counter); item < total; item = batch_next(q.counter)) {
+    const int gi = batch_find(q.prefix, q.ngrids, item);
+    const BatchGrid &G = q.grids[gi];
+    if (!*G.active) continue;
+    const long row0 = (item - q.prefix[gi]) * G.M;
+    float ss = 0.0f;
+    if (mode == 0) {
+      InKeep<InHalo> in{InHalo{G.x, G.g}, G.f, G.g};
+      xfwd_tile<float, InKeep<InHalo>>(G.ax, in, G.S, G.g, G.M, row0, smem_raw, ss);
+    } else {
+      InResidual in;
+      in.f = G.f; in.x = G.x; in.zc = G.zres; in.dxi2 = G.dxi2; in.dyi2 = G.dyi2;
+      for (int t = 0; t < 6; t++) in.bc[t] = G.bc[t];
+      in.g = G.g;
+      xfwd_tile<float, InResidual>(G.ax, in, G.S, G.g, G.M, row0, smem_raw, ss);
+    }
+    block_sum_add((double)ss, G.nrm + (mode == 0 ? 0 : 1));
+  }
+}
+
+template <bool BACKWARD>
+__global__ void __launch_bounds__(256) kb_ypass(BatchQueue q) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const long total = q.prefix[q.ngrids];
+  for (long item = batch_next(q.counter); item < total; item = batch_next(q.counter)) {
+    const int gi = batch_find(q.prefix, q.ngrids, item);
+    const BatchGrid &G = q.grids[gi];
+    if (!*G.active) continue;
+    ypass_tile<float, BACKWARD>(G.ay, G.S, G.g, G.W, item - q.prefix[gi], smem_raw);
+  }
+}
+
+// mode 0: x = e * normfft; mode 1: x += e * normfft
+__global__ void __launch_bounds__(256) kb_xinv(BatchQueue q, int mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const long total = q.prefix[q.ngrids];
+  for (long item = batch_next(q.counter); item < total; item = batch_next(q.counter)) {
+    const int gi = batch_find(q.prefix, q.ngrids, item);
+    const BatchGrid &G = q.grids[gi];
+    if (!*G.active) continue;
+    const long row0 = (item - q.prefix[gi]) * G.M;
+    if (mode == 0) xinv_tile<float, OutHalo>(G.ax, G.S, OutHalo{G.x, G.normfft, G.g}, G.g, G.M, row0, smem_raw);
+    else xinv_tile<float, OutHaloAdd>(G.ax, G.S, OutHaloAdd{G.x, G.normfft, G.g}, G.g, G.M, row0, smem_raw);
+  }
+}
+
+// z solve of one column per thread (FP32).  Non-periodic: the forward sweep
+// writes the eliminated values into S, the backward sweep recomputes the
+// elimination factors from per-chunk checkpoints kept in shared memory
+// (chk[nchunk][blockDim]).  Periodic: the spike solution of gaussel_periodic
+// (src/solver_cpu.f90:147-185) goes through S2 and a third sweep combines.
+template <int CH>
+__device__ void zcol_f32(const ZArgs &za, float *S, float *S2, long q, bool act, float *chk) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const long plane = za.nq;
+  const double lam64 = act ? za.lam[q] : 1.0;
+  const bool pin = za.pin && lam64 == 0.0;
+  const float lam = (float)lam64;
+  const float *ca = (const float *)za.at, *cb = (const float *)za.bt, *cc = (const float *)za.ct;
+  float *col = S + (act ? q : 0);
+  float *col2 = S2 ? S2 + (act ? q : 0) : nullptr;
+  const bool per = za.periodic != 0;
+  const int n = per ? za.nn - 1 : za.nn;  // system solved by elimination
+  const int nch = (n + CH - 1) / CH;
+  // forward
+  float dprev = 0.f, yprev = 0.f, y2prev = 0.f;
+  for (int m = 0; m < nch; m++) {
+    const int k0 = m * CH;
+    chk[m * nt + tid] = dprev;
+    float r[CH];
+#pragma unroll
+    for (int i = 0; i < CH; i++) r[i] = (act && k0 + i < n) ? col[(long)(k0 + i) * plane] : 0.f;
+#pragma unroll
+    for (int i = 0; i < CH; i++) {
+      const int k = k0 + i;
+      if (k < n) {
+        const float bb = cb[k] + lam, ak = ca[k];
+        const float piv = k == 0 ? bb : fmaf(-ak, dprev, bb);
+        float y, d = 0.f;
+        if (k < n - 1 || per) {
+          const float z = __fdividef(1.0f, piv);
+          d = cc[k] * z;
+          y = (k == 0 ? r[i] : fmaf(-ak, yprev, r[i])) * z;
+          if (per) {
+            // spike RHS: -a(1) at the first level, -c(n-1) at the last of the n-1 system
+            float g = (k == 0 ? -ca[0] : 0.f) + (k == n - 1 ? -cc[n - 1] : 0.f);
+            const float y2 = (k == 0 ? g : fmaf(-ak, y2prev, g)) * z;
+            if (act) col2[(long)k * plane] = y2;
+            y2prev = y2;
+          }
+        } else {
+          y = (piv != 0.f && !pin) ? __fdividef(fmaf(-ak, yprev, r[i]), piv) : 0.f;
+        }
+        if (act) col[(long)k * plane] = y;
+        dprev = d;
+        yprev = y;
+      }
+    }
+  }
+  // backward
+  float xnext = 0.f, x2next = 0.f;
+  float x0 = 0.f, x20 = 0.f, xlast = 0.f, x2last = 0.f;
+  for (int m = nch - 1; m >= 0; m--) {
+    const int k0 = m * CH;
+    float dd[CH];
+    float dp = chk[m * nt + tid];
+#pragma unroll
+    for (int i = 0; i < CH; i++) {
+      const int k = k0 + i;
+      if (k < n - 1) {
+        const float bb = cb[k] + lam;
+        const float z = __fdividef(1.0f, k == 0 ? bb : fmaf(-ca[k], dp, bb));
+        dd[i] = cc[k] * z;
+        dp = dd[i];
+      } else {
+        dd[i] = 0.f;
+      }
+    }
+#pragma unroll
+    for (int i = CH - 1; i >= 0; i--) {
+      const int k = k0 + i;
+      if (k < n) {
+        const float yk = act ? col[(long)k * plane] : 0.f;
+        const float x = (k == n - 1) ? yk : fmaf(-dd[i], xnext, yk);
+        if (act) col[(long)k * plane] = x;
+        xnext = x;
+        if (k == n - 1) xlast = x;
+        if (k == 0) x0 = x;
+        if (per) {
+          const float y2k = act ? col2[(long)k * plane] : 0.f;
+          const float x2 = (k == n - 1) ? y2k : fmaf(-dd[i], x2next, y2k);
+          if (act) col2[(long)k * plane] = x2;
+          x2next = x2;
+          if (k == n - 1) x2last = x2;
+          if (k == 0) x20 = x2;
+        }
+      }
+    }
+  }
+  if (per && act) {
+    const int nn = za.nn;
+    const float rn = col[(long)(nn - 1) * plane];
+    const float num = rn - cc[nn - 1] * x0 - ca[nn - 1] * xlast;
+    const float den = (cb[nn - 1] + lam) + cc[nn - 1] * x20 + ca[nn - 1] * x2last;
+    const float pn = ((za.pin && lam64 == 0.0) || den == 0.f) ? 0.f : num / den;
+    col[(long)(nn - 1) * plane] = pn;
+    for (int k = 0; k < nn - 1; k++) col[(long)k * plane] = fmaf(col2[(long)k * plane], pn, col[(long)k * plane]);
+  }
+}
+
+__global__ void __launch_bounds__(128) kb_z(BatchQueue q) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *chk = (float *)smem_raw;
+  const long total = q.prefix[q.ngrids];
+  for (long item = batch_next(q.counter); item < total; item = batch_next(q.counter)) {
+    const int gi = batch_find(q.prefix, q.ngrids, item);
+    const BatchGrid &G = q.grids[gi];
+    if (!*G.active) continue;
+    const long qcol = (item - q.prefix[gi]) * blockDim.x + threadIdx.x;
+    zcol_f32<16>(G.za, G.S, G.S2, qcol, qcol < G.za.nq, chk);
+  }
+}
+
+// Per-grid convergence after a residual pass: relres[g], active[g], iters[g].
+__global__ void kb_update(BatchGrid *grids, int ng, double tol, int it, int max_iter, double *relres, int *iters) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    BatchGrid &G = grids[g];
+    if (!*G.active) continue;
+    const double f2 = G.nrm[0], r2 = G.nrm[1];
+    const double rel = f2 > 0.0 ? sqrt(r2 / f2) : sqrt(r2);
+    relres[g] = rel;
+    iters[g] = it;
+    if (!(rel > tol) || it >= max_iter) *G.active = 0;  // NaN also stops
+    G.nrm[1] = 0.0;
+  }
+}
+
+__global__ void kb_reset(BatchGrid *grids, int ng) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    *grids[g].active = 1;
+    grids[g].nrm[0] = 0.0;
+    grids[g].nrm[1] = 0.0;
+  }
+}
+
 }  // namespace fg
