@@ -41,7 +41,7 @@ EXPORTED = [
     "flutas_gb300_plan_set_stream", "flutas_gb300_solve_mixed", "flutas_gb300_projection",
     "flutas_gb300_plan_info", "flutas_gb300_launch_count", "flutas_gb300_profile",
     "flutas_gb300_profile_report", "flutas_gb300_projection_df", "flutas_gb300_last_solve",
-    "flutas_gb300_bounduvw",
+    "flutas_gb300_bounduvw", "flutas_gb300_chkdiv_noalloc",
 ]
 
 
@@ -80,6 +80,7 @@ def load(path: str | None = None):
     L.flutas_gb300_solve_mixed.argtypes = [vp, vp, dp, ip, vp, vp]
     L.flutas_gb300_projection.argtypes = [vp, ip, dp, dp, vp, vp, vp, C.c_char_p, vp, dp, dp, vp, vp, vp,
                                           vp, ip, dp, ip]
+    L.flutas_gb300_chkdiv_noalloc.argtypes = [ip] * 3 + [dp] * 3 + [ip] * 2 + [vp, vp, vp, vp, vp, vp]
     L.flutas_gb300_bounduvw.argtypes = [C.c_char_p, vp, vp, ip, ip, vp, vp, vp, vp, vp, vp, vp, vp]
     L.flutas_gb300_plan_info.argtypes = [vp, vp, vp, vp]
     L.flutas_gb300_launch_count.argtypes = [vp]
@@ -300,6 +301,15 @@ def chkdiv(n, dxi, dyi, dzi, nh_d, nh_u, dzfi, u, v, w):
     _check(load().flutas_gb300_chkdiv(int(n[0]), int(n[1]), int(n[2]), float(dxi), float(dyi), float(dzi),
                                       int(nh_d), int(nh_u), _ptr(dzfi), _ptr(u), _ptr(v), _ptr(w),
                                       C.addressof(tot), C.addressof(mx)))
+    return tot.value, mx.value
+
+
+def chkdiv_noalloc(n, dxi, dyi, dzi, nh_d, nh_u, dzfi, u, v, w):
+    """chkdiv without any device allocation (device arrays only; ny*nz <= 65536)."""
+    tot, mx = C.c_double(), C.c_double()
+    _check(load().flutas_gb300_chkdiv_noalloc(int(n[0]), int(n[1]), int(n[2]), float(dxi), float(dyi),
+                                              float(dzi), int(nh_d), int(nh_u), _ptr(dzfi), _ptr(u), _ptr(v),
+                                              _ptr(w), C.addressof(tot), C.addressof(mx)))
     return tot.value, mx.value
 
 

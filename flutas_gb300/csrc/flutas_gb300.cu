@@ -1380,3 +1380,130 @@ int flutas_gb300_profile_report(char *buf, int len, int reset) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Divergence check that allocates nothing.
+//
+// Scratch: one (sum, max) pair per (j,k) row of cells, kept in a file-scope
+// device array of FLUTAS_NOALLOC_MAX_ROWS rows (1 MiB), which every GPU that
+// loads this library holds until the process exits.  Host code must not pass
+// the array's name to a kernel (on the host it is only a stand-in); the
+// device address is looked up once per device with cudaGetSymbolAddress.
+// ===========================================================================
+#define FLUTAS_NOALLOC_MAX_ROWS 65536
+static __device__ __align__(256) double g_noalloc_rows[2 * FLUTAS_NOALLOC_MAX_ROWS];
+
+namespace {
+
+// One block per (j,k) row (grid-stride): the row's divergence sum and max |div|
+// go to rows[2r], rows[2r+1].  Every row is written, so nothing needs clearing.
+__global__ void k_chkdiv_rows(DivArgs a, double *rows) {
+  const Geo &g = a.g;
+  const long nrow = (long)g.ny * g.nz;
+  __shared__ double s_tot[32], s_mx[32];
+  for (long r = blockIdx.x; r < nrow; r += gridDim.x) {
+    const int j = (int)(r % g.ny) + 1, k = (int)(r / g.ny) + 1;
+    double tot = 0.0, mx = 0.0;
+    for (int i = threadIdx.x + 1; i <= g.nx; i += blockDim.x) {
+      const double div = (a.w[g.uidx(i, j, k)] - a.w[g.uidx(i, j, k - 1)]) * a.dzfi[k] +
+                         (a.v[g.uidx(i, j, k)] - a.v[g.uidx(i, j - 1, k)]) * a.dyi +
+                         (a.u[g.uidx(i, j, k)] - a.u[g.uidx(i - 1, j, k)]) * a.dxi;
+      tot += div;
+      mx = fmax(mx, fabs(div));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      tot += __shfl_down_sync(0xffffffffu, tot, o);
+      mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) { s_tot[wid] = tot; s_mx[wid] = mx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0, m = 0.0;
+      for (int q = 0; q < nw; q++) { t += s_tot[q]; m = fmax(m, s_mx[q]); }
+      rows[2 * r] = t;
+      rows[2 * r + 1] = m;
+    }
+    __syncthreads();
+  }
+}
+
+// One block: fixed-order reduction of the row pairs into rows[0], rows[1].
+__global__ void k_chkdiv_rows_reduce(double *rows, long nrow) {
+  __shared__ double s_tot[1024], s_mx[1024];
+  double t = 0.0, m = 0.0;
+  for (long r = threadIdx.x; r < nrow; r += blockDim.x) {
+    t += rows[2 * r];
+    m = fmax(m, rows[2 * r + 1]);
+  }
+  s_tot[threadIdx.x] = t;
+  s_mx[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      s_tot[threadIdx.x] += s_tot[threadIdx.x + s];
+      s_mx[threadIdx.x] = fmax(s_mx[threadIdx.x], s_mx[threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    rows[0] = s_tot[0];
+    rows[1] = s_mx[0];
+  }
+}
+
+std::mutex g_noalloc_mu;
+double *g_noalloc_addr[64] = {};
+
+// Device address of g_noalloc_rows on the current device (looked up on the
+// first call made with that device current, then cached).
+int noalloc_rows(double **out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(FLUTAS_EUNSUPPORTED, "chkdiv_noalloc: device index %d above 63", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    CK(cudaGetSymbolAddress(&p, g_noalloc_rows));
+    g_noalloc_addr[dev] = (double *)p;
+  }
+  *out = g_noalloc_addr[dev];
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int flutas_gb300_chkdiv_noalloc(int nx, int ny, int nz, double dxi, double dyi, double dzi, int nh_d, int nh_u,
+                                const double *dzfi, const double *u, const double *v, const double *w,
+                                double *divtot, double *divmax) {
+  (void)dzi;
+  if (!divtot || !divmax || !dzfi || !u || !v || !w) return fail(FLUTAS_EINVAL, "chkdiv_noalloc: null argument");
+  if (nx < 1 || ny < 1 || nz < 1 || nh_u < 1 || nh_d < 1) return fail(FLUTAS_EINVAL, "chkdiv_noalloc: bad sizes");
+  if ((long)ny * nz > FLUTAS_NOALLOC_MAX_ROWS)
+    return fail(FLUTAS_EINVAL, "chkdiv_noalloc: ny*nz = %ld exceeds the %d rows of its fixed scratch",
+                (long)ny * nz, FLUTAS_NOALLOC_MAX_ROWS);
+  if (!is_device_ptr(u) || !is_device_ptr(v) || !is_device_ptr(w) || !is_device_ptr(dzfi))
+    return fail(FLUTAS_EINVAL, "chkdiv_noalloc: u, v, w and dzfi must be device (or managed) memory");
+  double *rows = nullptr;
+  TRY(noalloc_rows(&rows));
+  DivArgs da;
+  da.u = u; da.v = v; da.w = w; da.dzfi = dzfi + (nh_d - 1);
+  da.dxi = dxi; da.dyi = dyi;
+  da.g = Geo{nx, ny, nz, nh_u};
+  const long nrow = (long)ny * nz;
+  const int grid = (int)std::min<long>(nrow, (long)num_sms() * 16);
+  k_chkdiv_rows<<<grid, 128, 0, 0>>>(da, rows);
+  CK(cudaGetLastError());
+  k_chkdiv_rows_reduce<<<1, 1024, 0, 0>>>(rows, nrow);
+  CK(cudaGetLastError());
+  g_launches.fetch_add(2, std::memory_order_relaxed);
+  double res[2];
+  CK(cudaMemcpy(res, rows, sizeof res, cudaMemcpyDeviceToHost));
+  *divtot = res[0];
+  *divmax = res[1];
+  return FLUTAS_OK;
+}
+
+}  // extern "C"

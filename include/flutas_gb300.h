@@ -167,6 +167,23 @@ FLUTAS_API int flutas_gb300_last_solve(void *plan, double *relres, int *iters);
  * transform path it uses (0 = separate x/y passes, 1 = fused plane kernel). */
 FLUTAS_API int flutas_gb300_plan_info(void *plan, size_t *device_bytes, int *xy_path_fp64, int *xy_path_fp32);
 
+/* Divergence check that allocates nothing (no counterpart in the reference).
+ * Same arguments and result as flutas_gb300_chkdiv, for callers that must not
+ * allocate device memory at the point of the call: an application that gives
+ * the whole device to its own memory pool, or a diagnostic run after an
+ * out-of-memory error, when a cudaMalloc would fail.  u, v, w and dzfi must
+ * be device or managed memory (host arrays would need staging buffers).  Its
+ * scratch is a fixed 1 MiB device array inside the library, one (sum, max)
+ * pair per (j,k) row of cells, so ny*nz may not exceed 65536 (FLUTAS_EINVAL
+ * otherwise).  The first call made on a device looks the array's address up
+ * for that device.  All calls share the array: calls that overlap on the GPU
+ * (several host threads, or several streams) race and must be serialised by
+ * the caller.  Synchronous: returns after the result is on the host. */
+FLUTAS_API int flutas_gb300_chkdiv_noalloc(int nx, int ny, int nz, double dxi, double dyi, double dzi,
+                                           int nh_d, int nh_u, const double *dzfi, const double *u,
+                                           const double *v, const double *w, double *divtot,
+                                           double *divmax);
+
 /* Number of kernels this library has launched in the process (all plans). */
 FLUTAS_API int flutas_gb300_launch_count(unsigned long long *count);
 
