@@ -41,7 +41,9 @@ EXPORTED = [
     "flutas_gb300_plan_set_stream", "flutas_gb300_solve_mixed", "flutas_gb300_projection",
     "flutas_gb300_plan_info", "flutas_gb300_launch_count", "flutas_gb300_profile",
     "flutas_gb300_profile_report", "flutas_gb300_projection_df", "flutas_gb300_last_solve",
-    "flutas_gb300_bounduvw", "flutas_gb300_chkdiv_noalloc",
+    "flutas_gb300_bounduvw", "flutas_gb300_chkdiv_noalloc", "flutas_gb300_batch_create",
+    "flutas_gb300_batch_field", "flutas_gb300_batch_solve", "flutas_gb300_batch_report",
+    "flutas_gb300_batch_destroy", "flutas_gb300_batch_set", "flutas_gb300_batch_get",
 ]
 
 
@@ -81,6 +83,13 @@ def load(path: str | None = None):
     L.flutas_gb300_projection.argtypes = [vp, ip, dp, dp, vp, vp, vp, C.c_char_p, vp, dp, dp, vp, vp, vp,
                                           vp, ip, dp, ip]
     L.flutas_gb300_chkdiv_noalloc.argtypes = [ip] * 3 + [dp] * 3 + [ip] * 2 + [vp, vp, vp, vp, vp, vp]
+    L.flutas_gb300_batch_create.argtypes = [ip, vp, vp, ip, vp, vp, C.c_char_p, ip, vp]
+    L.flutas_gb300_batch_field.argtypes = [vp, ip, vp]
+    L.flutas_gb300_batch_solve.argtypes = [vp, dp, ip, vp, vp]
+    L.flutas_gb300_batch_report.argtypes = [vp, C.c_char_p, ip]
+    L.flutas_gb300_batch_set.argtypes = [vp, ip, vp]
+    L.flutas_gb300_batch_get.argtypes = [vp, ip, vp]
+    L.flutas_gb300_batch_destroy.argtypes = [vp]
     L.flutas_gb300_bounduvw.argtypes = [C.c_char_p, vp, vp, ip, ip, vp, vp, vp, vp, vp, vp, vp, vp]
     L.flutas_gb300_plan_info.argtypes = [vp, vp, vp, vp]
     L.flutas_gb300_launch_count.argtypes = [vp]
@@ -339,3 +348,64 @@ def profile_report(reset: bool = True) -> dict:
         name, cnt, ms = line.rsplit(" ", 2)
         out[name] = (int(cnt), float(ms))
     return out
+
+
+class Batch:
+    """Many independent grids solved together (mixed precision, one CUDA graph per solve).
+
+    grids: list of dicts with keys n (3 ints), dli (3), dzci, dzfi (numpy, nz+2*nh_d), cbc (6 chars).
+    """
+
+    def __init__(self, grids, nh_d=1, autotune=True):
+        L = load()
+        self.ng = len(grids)
+        n = (C.c_int * (3 * self.ng))(*[int(v) for g in grids for v in g["n"]])
+        dli = (C.c_double * (3 * self.ng))(*[float(v) for g in grids for v in g["dli"]])
+        self._z = [(np.ascontiguousarray(g["dzci"], dtype=np.float64),
+                    np.ascontiguousarray(g["dzfi"], dtype=np.float64)) for g in grids]
+        zci = (C.c_void_p * self.ng)(*[z[0].ctypes.data for z in self._z])
+        zfi = (C.c_void_p * self.ng)(*[z[1].ctypes.data for z in self._z])
+        cbc = "".join(g["cbc"] for g in grids).encode()
+        self.n = [list(g["n"]) for g in grids]
+        self.handle = C.c_void_p()
+        _check(L.flutas_gb300_batch_create(self.ng, C.cast(n, C.c_void_p), C.cast(dli, C.c_void_p), int(nh_d),
+                                           C.cast(zci, C.c_void_p), C.cast(zfi, C.c_void_p), cbc,
+                                           1 if autotune else 0, C.addressof(self.handle)))
+
+    def field_ptr(self, g: int) -> int:
+        p = C.c_void_p()
+        _check(load().flutas_gb300_batch_field(self.handle, int(g), C.addressof(p)))
+        return p.value
+
+    def set(self, g: int, arr):
+        _check(load().flutas_gb300_batch_set(self.handle, int(g), _ptr(arr)))
+
+    def get(self, g: int, out=None):
+        nx, ny, nz = self.n[g]
+        out = np.empty((nz + 2, ny + 2, nx + 2)) if out is None else out
+        _check(load().flutas_gb300_batch_get(self.handle, int(g), _ptr(out)))
+        return out
+
+    def solve(self, tol=1e-10, max_iter=8, allow_unconverged=False):
+        rr = np.zeros(self.ng)
+        it = np.zeros(self.ng, dtype=np.int32)
+        _check(load().flutas_gb300_batch_solve(self.handle, float(tol), int(max_iter), rr.ctypes.data, it.ctypes.data),
+               allow=(FLUTAS_EITER,) if allow_unconverged else ())
+        return rr, it
+
+    def report(self) -> str:
+        buf = C.create_string_buffer(1 << 20)
+        _check(load().flutas_gb300_batch_report(self.handle, buf, 1 << 20))
+        return buf.value.decode()
+
+    def destroy(self):
+        if self.handle:
+            _check(load().flutas_gb300_batch_destroy(self.handle))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if _lib is not None and self.handle:
+                _lib.flutas_gb300_batch_destroy(self.handle)
+        except Exception:
+            pass

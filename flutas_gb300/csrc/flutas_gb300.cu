@@ -18,6 +18,8 @@
 #include <atomic>
 #include <map>
 #include <mutex>
+#include <sstream>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -1503,6 +1505,410 @@ int flutas_gb300_chkdiv_noalloc(int nx, int ny, int nz, double dxi, double dyi, 
   CK(cudaMemcpy(res, rows, sizeof res, cudaMemcpyDeviceToHost));
   *divtot = res[0];
   *divmax = res[1];
+  return FLUTAS_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batched solves (many independent grids of uneven sizes and BCs)
+// ===========================================================================
+struct flutas_batch {
+  static constexpr unsigned MAGIC = 0xBA7C4u;
+  unsigned magic = MAGIC;
+  int ng = 0;
+  std::vector<void *> plans;  // one plan per grid (tables, coefficients)
+  DBuf arena;                 // x, f (FP64 halo), S, S2 (FP32) of every grid
+  std::vector<double *> x;    // device halo arrays handed to the caller
+  DBuf d_grids, d_prefix, d_counters, d_nrm, d_active, d_relres, d_iters;
+  std::vector<BatchGrid> grids;
+  size_t smem_x = 0, smem_y = 0, smem_z = 0;
+  int grid_x = 0, grid_y = 0, grid_z = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  double g_tol = -1.0;
+  int g_maxit = -1;
+  int nodes = 0;
+  std::string report;
+};
+
+namespace {
+
+// ------------------------------------------------------------- autotuner
+// Picks, per (axis length, BC pair, other-axis length), the radix cap of the
+// FP32 transform plan and the tile shape of its pass (rows per x tile, columns
+// per y tile) by timing the candidates on scratch data with CUDA events.
+struct TuneKey {
+  int pass, n, pair, other;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(pass, n, pair, other) < std::tie(o.pass, o.n, o.pair, o.other);
+  }
+};
+struct TuneVal {
+  int maxe, tile;
+  float ms;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneVal> g_tune;
+
+size_t smem_xpass(int nx, int M) { return align_up<float>(sizeof(float) * (size_t)M * xpitch(nx)) + sizeof(float) * (size_t)M * nx; }
+size_t smem_ypass(int ny, int W) { return align_up<float>(sizeof(float) * (size_t)W * ny) + sizeof(float) * (size_t)W * ny; }
+
+int build_axis32(int n, int pair, int maxe, AxisTables *t) {
+  AxisPlan ap{};
+  std::vector<C2<float>> W, Q;
+  if (fill_axis_tables<float>(n, pair, &ap, W, Q) != 0) return fail(FLUTAS_EUNSUPPORTED, "axis of length %d not supported", n);
+  if (ap.N > 1) {
+    const int ns = make_radix_plan(ap.N, ap.radix, maxe);
+    if (ns < 0) return fail(FLUTAS_EUNSUPPORTED, "axis of length %d not supported", n);
+    ap.nst = ns;
+  }
+  TRY(t->W.ensure(sizeof(C2<float>) * W.size()));
+  TRY(t->Q.ensure(sizeof(C2<float>) * Q.size()));
+  CK(cudaMemcpy(t->W.p, W.data(), sizeof(C2<float>) * W.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(t->Q.p, Q.data(), sizeof(C2<float>) * Q.size(), cudaMemcpyHostToDevice));
+  ap.W = t->W.p;
+  ap.Q = t->Q.p;
+  t->ap = ap;
+  t->ok = true;
+  return 0;
+}
+
+// pass 0: x pass over (n = nx, other = ny*nz rows); pass 1: y pass (n = ny, other = nx*nz)
+int autotune(int pass, int n, int pair, int other, size_t smem_budget, TuneVal *out, bool enabled) {
+  TuneKey key{pass, n, pair, enabled ? other : -1};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) { *out = it->second; return 0; }
+  }
+  std::vector<int> tiles;
+  for (int t : {4, 8, 16, 32, 64}) {
+    const size_t sm = pass == 0 ? smem_xpass(n, t) : smem_ypass(n, t);
+    if (sm <= smem_budget) tiles.push_back(t);
+  }
+  if (tiles.empty()) return fail(FLUTAS_EUNSUPPORTED, "axis of length %d does not fit the tile budget", n);
+  TuneVal best{4, tiles.size() > 2 ? tiles[2] : tiles.back(), 0.f};
+  if (enabled) {
+    // scratch problem: `other` lines of length n (capped): FP64 input, FP32 output
+    const long lines = std::max<long>(2, std::min<long>(other, 1L << 15));
+    DBuf buf, in64;
+    TRY(buf.ensure(sizeof(float) * (size_t)n * lines + 256));
+    TRY(in64.ensure(sizeof(double) * (size_t)n * lines + 256));
+    CK(cudaMemset(buf.p, 0, sizeof(float) * (size_t)n * lines));
+    CK(cudaMemset(in64.p, 0, sizeof(double) * (size_t)n * lines));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    for (int maxe : {4, 3}) {
+      AxisTables t;
+      if (build_axis32(n, pair, maxe, &t) != 0) continue;
+      for (int tile : tiles) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 3; rep++) {
+          if (pass == 0) {
+            const Geo g{n, (int)lines, 1, 1};
+            const size_t sm = smem_xpass(n, tile);
+            int grid = grid_for(k_xfwd<float, InPlain>, 256, sm, (lines + tile - 1) / tile);
+            if (grid < 0) break;
+            const InPlain in{(const double *)in64.p, g};
+            CK(cudaEventRecord(e0));
+            k_xfwd<float, InPlain><<<grid, 256, sm>>>(t.ap, in, (float *)buf.p, g, tile, nullptr);
+            CK(cudaEventRecord(e1));
+          } else {
+            Geo g{(int)std::min<long>(lines, 4096), n, 1, 1};
+            const size_t sm = smem_ypass(n, tile);
+            int grid = grid_for(k_ypass<float, false>, 256, sm, (g.nx + tile - 1) / tile);
+            if (grid < 0) break;
+            CK(cudaEventRecord(e0));
+            k_ypass<float, false><<<grid, 256, sm>>>(t.ap, (float *)buf.p, g, tile);
+            CK(cudaEventRecord(e1));
+          }
+          CK(cudaEventSynchronize(e1));
+          float m = 0.f;
+          CK(cudaEventElapsedTime(&m, e0, e1));
+          if (rep > 0) ms += m;
+        }
+        if (ms > 0.f && ms < best_ms) {
+          best_ms = ms;
+          best = TuneVal{maxe, tile, ms};
+        }
+      }
+      t.W.release();
+      t.Q.release();
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    buf.release();
+    in64.release();
+  }
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = best;
+  *out = best;
+  return 0;
+}
+
+int check_batch(void *b, flutas_batch **out) {
+  flutas_batch *bt = (flutas_batch *)b;
+  if (!bt || bt->magic != flutas_batch::MAGIC) return fail(FLUTAS_EINVAL, "invalid batch handle");
+  *out = bt;
+  return 0;
+}
+
+void batch_free(flutas_batch *bt) {
+  if (bt->exec) cudaGraphExecDestroy(bt->exec);
+  for (void *p : bt->plans) {
+    void *arr[4] = {p, nullptr, nullptr, nullptr};
+    if (p) flutas_gb300_fftend(arr);
+  }
+  DBuf *bufs[] = {&bt->arena, &bt->d_grids, &bt->d_prefix, &bt->d_counters, &bt->d_nrm, &bt->d_active,
+                  &bt->d_relres, &bt->d_iters};
+  for (DBuf *d : bufs) d->release();
+  if (bt->stream) cudaStreamDestroy(bt->stream);
+  bt->magic = 0;
+  delete bt;
+}
+
+int batch_capture(flutas_batch *bt, double tol, int max_iter) {
+  if (bt->exec) {
+    cudaGraphExecDestroy(bt->exec);
+    bt->exec = nullptr;
+  }
+  const int ng = bt->ng;
+  const int npass = 5 + 5 * max_iter;
+  TRY(bt->d_counters.ensure(sizeof(int) * npass));
+  BatchGrid *dg = bt->d_grids.as<BatchGrid>();
+  const long *px = bt->d_prefix.as<long>(), *py = px + (ng + 1), *pz = py + (ng + 1);
+  int *cnt = bt->d_counters.as<int>();
+  double *relres = bt->d_relres.as<double>();
+  int *iters = bt->d_iters.as<int>();
+  cudaStream_t st = bt->stream;
+  cudaGraph_t graph = nullptr;
+  int nodes = 0, c = 0;
+  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  auto Q = [&](const long *pre) { return BatchQueue{dg, pre, ng, cnt + (c++)}; };
+  auto fwd_chain = [&](int xmode, int outmode) {
+    kb_xfwd<<<bt->grid_x, 256, bt->smem_x, st>>>(Q(px), xmode);
+    nodes++;
+    (void)outmode;
+  };
+  auto rest_chain = [&](int outmode) {
+    kb_ypass<false><<<bt->grid_y, 256, bt->smem_y, st>>>(Q(py));
+    kb_z<<<bt->grid_z, 128, bt->smem_z, st>>>(Q(pz));
+    kb_ypass<true><<<bt->grid_y, 256, bt->smem_y, st>>>(Q(py));
+    kb_xinv<<<bt->grid_x, 256, bt->smem_x, st>>>(Q(px), outmode);
+    nodes += 4;
+  };
+  cudaMemsetAsync(cnt, 0, sizeof(int) * npass, st);
+  kb_reset<<<(ng + 255) / 256, 256, 0, st>>>(dg, ng);
+  nodes += 1;
+  fwd_chain(0, 0);
+  rest_chain(0);
+  for (int it = 1; it <= max_iter; it++) {
+    fwd_chain(1, 1);
+    kb_update<<<(ng + 255) / 256, 256, 0, st>>>(dg, ng, tol, it, max_iter, relres, iters);
+    nodes++;
+    if (it < max_iter) rest_chain(1);
+  }
+  cudaError_t e = cudaStreamEndCapture(st, &graph);
+  if (e != cudaSuccess) return fail(FLUTAS_ECUDA, "batch graph capture failed: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&bt->exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(FLUTAS_ECUDA, "batch graph instantiation failed: %s", cudaGetErrorString(e));
+  bt->g_tol = tol;
+  bt->g_maxit = max_iter;
+  bt->nodes = nodes;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int nh_d, const double *const *dzci,
+                              const double *const *dzfi, const char *cbc, int autotune_tiles, void **batch) {
+  if (ngrids < 1 || !n || !dli || !dzci || !dzfi || !cbc || !batch) return fail(FLUTAS_EINVAL, "batch_create: bad arguments");
+  flutas_batch *bt = new flutas_batch();
+  bt->ng = ngrids;
+  auto bail = [&](int rc) { batch_free(bt); return rc; };
+  int rc = 0;
+  if (cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(FLUTAS_ECUDA, "batch_create: stream creation failed"));
+  bt->plans.assign(ngrids, nullptr);
+  bt->grids.resize(ngrids);
+  const size_t budget = 96 * 1024;
+  // plans and tile choices
+  std::vector<size_t> sx(ngrids), sf(ngrids), sS(ngrids), sS2(ngrids);
+  size_t total = 0;
+  auto take = [&](size_t bytes) { size_t o = total; total += (bytes + 255) & ~(size_t)255; return o; };
+  std::vector<long> tx(ngrids), ty(ngrids), tz(ngrids);
+  std::ostringstream rep;
+  for (int g = 0; g < ngrids; g++) {
+    const int *ng3 = n + 3 * g;
+    const int nx = ng3[0], ny = ng3[1], nz = ng3[2];
+    std::vector<double> lam((size_t)nx * ny), a(nz), b(nz), c(nz), rx(2 * (size_t)ny * nz), ry(2 * (size_t)nx * nz),
+        rz(2 * (size_t)nx * ny);
+    void *arr[4] = {};
+    double nf = 0.0, bc6[6] = {0, 0, 0, 0, 0, 0};
+    if ((rc = flutas_gb300_initsolver(ng3, dli + 3 * g, nh_d, dzci[g], dzfi[g], cbc + 6 * g, bc6, "ccc", lam.data(),
+                                      a.data(), b.data(), c.data(), arr, &nf, rx.data(), ry.data(), rz.data())))
+      return bail(rc);
+    bt->plans[g] = arr[0];
+    flutas_plan *pl = (flutas_plan *)arr[0];
+    BatchGrid &G = bt->grids[g];
+    G.g = Geo{nx, ny, nz, 1};
+    // tuned transform plans and tiles
+    TuneVal vx, vy;
+    if ((rc = autotune(0, nx, pair_code(pl->cbc[0], pl->cbc[1]), ny * nz, budget, &vx, autotune_tiles != 0)) ||
+        (rc = autotune(1, ny, pair_code(pl->cbc[2], pl->cbc[3]), nx * nz, budget, &vy, autotune_tiles != 0)))
+      return bail(rc);
+    if ((rc = build_axis32(nx, pair_code(pl->cbc[0], pl->cbc[1]), vx.maxe, &pl->tx32)) ||
+        (rc = build_axis32(ny, pair_code(pl->cbc[2], pl->cbc[3]), vy.maxe, &pl->ty32)))
+      return bail(rc);
+    G.ax = pl->tx32.ap;
+    G.ay = pl->ty32.ap;
+    G.M = vx.tile;
+    G.W = vy.tile;
+    rep << "grid " << g << " n=" << nx << "x" << ny << "x" << nz << " cbc=" << std::string(pl->cbc, 6) << " x:maxe=" << vx.maxe
+        << ",M=" << vx.tile << " y:maxe=" << vy.maxe << ",W=" << vy.tile << "\n";
+    ZArgs za;
+    za.a = pl->a.as<double>(); za.b = pl->b.as<double>(); za.c = pl->c.as<double>();
+    za.at = pl->a32.p; za.bt = pl->b32.p; za.ct = pl->c32.p;
+    za.lam = pl->lam.as<double>();
+    za.nq = nx * ny;
+    za.nz = nz;
+    za.nn = nz;
+    za.periodic = (pl->cbc[4] == 'P' && pl->cbc[5] == 'P') ? 1 : 0;
+    const bool zsing = (pl->cbc[4] == 'N' && pl->cbc[5] == 'N') || za.periodic;
+    za.pin = zsing ? 1 : 0;
+    G.za = za;
+    G.zres = pl->zres.as<double>();
+    G.dxi2 = pl->dli[0] * pl->dli[0];
+    G.dyi2 = pl->dli[1] * pl->dli[1];
+    G.normfft = pl->normfft;
+    memcpy(G.bc, pl->cbc, 6);
+    const size_t halo = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+    sx[g] = take(halo);
+    sf[g] = take(halo);
+    sS[g] = take(sizeof(float) * (size_t)nx * ny * nz);
+    sS2[g] = za.periodic ? take(sizeof(float) * (size_t)nx * ny * nz) : (size_t)-1;
+    tx[g] = ((long)ny * nz + G.M - 1) / G.M;
+    ty[g] = (long)((nx + G.W - 1) / G.W) * nz;
+    tz[g] = ((long)nx * ny + 127) / 128;
+    bt->smem_x = std::max(bt->smem_x, smem_xpass(nx, G.M));
+    bt->smem_y = std::max(bt->smem_y, smem_ypass(ny, G.W));
+    bt->smem_z = std::max(bt->smem_z, sizeof(float) * (size_t)((nz + 15) / 16) * 128);
+  }
+  bt->report = rep.str();
+  if ((rc = bt->arena.ensure(total))) return bail(rc);
+  if (cudaMemset(bt->arena.p, 0, total) != cudaSuccess) return bail(fail(FLUTAS_ECUDA, "batch_create: memset failed"));
+  if ((rc = bt->d_nrm.ensure(sizeof(double) * 2 * ngrids)) || (rc = bt->d_active.ensure(sizeof(int) * ngrids)) ||
+      (rc = bt->d_relres.ensure(sizeof(double) * ngrids)) || (rc = bt->d_iters.ensure(sizeof(int) * ngrids)))
+    return bail(rc);
+  unsigned char *base = (unsigned char *)bt->arena.p;
+  bt->x.resize(ngrids);
+  for (int g = 0; g < ngrids; g++) {
+    BatchGrid &G = bt->grids[g];
+    G.x = (double *)(base + sx[g]);
+    G.f = (double *)(base + sf[g]);
+    G.S = (float *)(base + sS[g]);
+    G.S2 = sS2[g] == (size_t)-1 ? nullptr : (float *)(base + sS2[g]);
+    G.nrm = bt->d_nrm.as<double>() + 2 * g;
+    G.active = bt->d_active.as<int>() + g;
+    bt->x[g] = G.x;
+  }
+  std::vector<long> pre(3 * (size_t)(ngrids + 1), 0);
+  for (int g = 0; g < ngrids; g++) {
+    pre[g + 1] = pre[g] + tx[g];
+    pre[(ngrids + 1) + g + 1] = pre[(ngrids + 1) + g] + ty[g];
+    pre[2 * (ngrids + 1) + g + 1] = pre[2 * (ngrids + 1) + g] + tz[g];
+  }
+  if ((rc = bt->d_prefix.ensure(sizeof(long) * pre.size())) || (rc = bt->d_grids.ensure(sizeof(BatchGrid) * ngrids)))
+    return bail(rc);
+  if (cudaMemcpy(bt->d_prefix.p, pre.data(), sizeof(long) * pre.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(bt->d_grids.p, bt->grids.data(), sizeof(BatchGrid) * ngrids, cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(FLUTAS_ECUDA, "batch_create: upload failed"));
+  if ((int)std::max({bt->smem_x, bt->smem_y, bt->smem_z}) > max_smem_optin())
+    return bail(fail(FLUTAS_EUNSUPPORTED, "batch_create: tiles exceed shared memory"));
+  int g1, g2, g3;
+  if ((g1 = grid_for(kb_xfwd, 256, bt->smem_x, pre[ngrids])) < 0) return bail(g1);
+  if ((g2 = grid_for(kb_ypass<false>, 256, bt->smem_y, pre[2 * ngrids + 1])) < 0) return bail(g2);
+  if ((g3 = grid_for(kb_z, 128, bt->smem_z, pre[3 * ngrids + 2])) < 0) return bail(g3);
+  CK(cudaFuncSetAttribute(kb_xinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem_x));
+  CK(cudaFuncSetAttribute(kb_ypass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem_y));
+  bt->grid_x = g1;
+  bt->grid_y = g2;
+  bt->grid_z = g3;
+  *batch = bt;
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_batch_field(void *batch, int g, double **p) {
+  flutas_batch *bt;
+  TRY(check_batch(batch, &bt));
+  if (g < 0 || g >= bt->ng || !p) return fail(FLUTAS_EINVAL, "batch_field: bad grid index");
+  *p = bt->x[g];
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_batch_solve(void *batch, double tol, int max_iter, double *relres, int *iters) {
+  flutas_batch *bt;
+  TRY(check_batch(batch, &bt));
+  if (!(tol > 0.0) || max_iter < 1 || max_iter > 32) return fail(FLUTAS_EINVAL, "batch_solve: need tol > 0 and 1 <= max_iter <= 32");
+  if (!bt->exec || bt->g_tol != tol || bt->g_maxit != max_iter) TRY(batch_capture(bt, tol, max_iter));
+  CK(cudaGraphLaunch(bt->exec, bt->stream));
+  g_launches.fetch_add((unsigned long long)bt->nodes, std::memory_order_relaxed);
+  std::vector<double> rr(bt->ng);
+  std::vector<int> it(bt->ng);
+  CK(cudaMemcpyAsync(rr.data(), bt->d_relres.p, sizeof(double) * bt->ng, cudaMemcpyDeviceToHost, bt->stream));
+  CK(cudaMemcpyAsync(it.data(), bt->d_iters.p, sizeof(int) * bt->ng, cudaMemcpyDeviceToHost, bt->stream));
+  CK(cudaStreamSynchronize(bt->stream));
+  int rc = FLUTAS_OK;
+  for (int g = 0; g < bt->ng; g++) {
+    if (relres) relres[g] = rr[g];
+    if (iters) iters[g] = it[g];
+    if (!(rr[g] <= tol)) rc = FLUTAS_EITER;
+  }
+  if (rc) fail(rc, "batch_solve: some grids did not reach tol in %d solves", max_iter);
+  return rc;
+}
+
+int flutas_gb300_batch_set(void *batch, int g, const double *src) {
+  flutas_batch *bt;
+  TRY(check_batch(batch, &bt));
+  if (g < 0 || g >= bt->ng || !src) return fail(FLUTAS_EINVAL, "batch_set: bad arguments");
+  const Geo &G = bt->grids[g].g;
+  const size_t bytes = sizeof(double) * (size_t)(G.nx + 2) * (G.ny + 2) * (G.nz + 2);
+  CK(cudaMemcpyAsync(bt->x[g], src, bytes, cudaMemcpyDefault, bt->stream));
+  CK(cudaStreamSynchronize(bt->stream));
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_batch_get(void *batch, int g, double *dst) {
+  flutas_batch *bt;
+  TRY(check_batch(batch, &bt));
+  if (g < 0 || g >= bt->ng || !dst) return fail(FLUTAS_EINVAL, "batch_get: bad arguments");
+  const Geo &G = bt->grids[g].g;
+  const size_t bytes = sizeof(double) * (size_t)(G.nx + 2) * (G.ny + 2) * (G.nz + 2);
+  CK(cudaMemcpyAsync(dst, bt->x[g], bytes, cudaMemcpyDefault, bt->stream));
+  CK(cudaStreamSynchronize(bt->stream));
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_batch_report(void *batch, char *buf, int len) {
+  flutas_batch *bt;
+  TRY(check_batch(batch, &bt));
+  if (!buf || len <= 0) return fail(FLUTAS_EINVAL, "batch_report: bad buffer");
+  snprintf(buf, (size_t)len, "%s", bt->report.c_str());
+  return FLUTAS_OK;
+}
+
+int flutas_gb300_batch_destroy(void *batch) {
+  flutas_batch *bt;
+  TRY(check_batch(batch, &bt));
+  cudaStreamSynchronize(bt->stream);
+  batch_free(bt);
   return FLUTAS_OK;
 }
 

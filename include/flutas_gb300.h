@@ -184,6 +184,29 @@ FLUTAS_API int flutas_gb300_chkdiv_noalloc(int nx, int ny, int nz, double dxi, d
                                            const double *v, const double *w, double *divtot,
                                            double *divmax);
 
+/* Batched mixed-precision solves of many independent grids (uneven sizes and
+ * BCs; no counterpart in the reference, which solves one grid per call).
+ * n, dli: 3 per grid; dzci, dzfi: one (1-nh_d:nz+nh_d) host array per grid;
+ * cbc: 6 characters per grid.  Each pass of the refinement (x transform, y
+ * transform, z solve, inverse transforms, FP64 residual) is one persistent
+ * kernel draining a (grid, tile) work queue over all grids; the whole
+ * sequence is captured in a CUDA graph and replayed by batch_solve.  With
+ * autotune != 0, the radix plan and tile shape of each axis signature are
+ * chosen by timing candidates on the device (cached per process).  The batch
+ * owns one device halo array per grid (batch_field): the RHS on entry of
+ * batch_solve, the solution on exit.  relres/iters (nullable, one per grid)
+ * receive the achieved relative residual and the FP32 solves used. */
+FLUTAS_API int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int nh_d,
+                                         const double *const *dzci, const double *const *dzfi,
+                                         const char *cbc, int autotune, void **batch);
+FLUTAS_API int flutas_gb300_batch_field(void *batch, int grid, double **p);
+/* Copy a grid's halo array in (RHS) or out (solution); host or device memory. */
+FLUTAS_API int flutas_gb300_batch_set(void *batch, int grid, const double *src);
+FLUTAS_API int flutas_gb300_batch_get(void *batch, int grid, double *dst);
+FLUTAS_API int flutas_gb300_batch_solve(void *batch, double tol, int max_iter, double *relres, int *iters);
+FLUTAS_API int flutas_gb300_batch_report(void *batch, char *buf, int len);
+FLUTAS_API int flutas_gb300_batch_destroy(void *batch);
+
 /* Number of kernels this library has launched in the process (all plans). */
 FLUTAS_API int flutas_gb300_launch_count(unsigned long long *count);
 

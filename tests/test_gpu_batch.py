@@ -1,0 +1,75 @@
+"""Batched mixed-precision solves: many grids of uneven sizes and BCs in one
+graph-replayed sequence of persistent pass kernels.  Each grid must reach the
+requested relative residual, agree with the FP64 oracle within the error that
+residual allows, and give the same answer alone (single-grid mixed solve) as in
+the batch."""
+import numpy as np
+import pytest
+
+from conftest import compatible_rhs, rel_l2, singular, zgrid
+
+pytestmark = pytest.mark.gpu
+
+GRIDS = [
+    ((32, 48, 16), "PPPPNN", 0.0),
+    ((48, 32, 24), "NNPPNN", 1.5),
+    ((64, 64, 32), "DDNNDD", 2.0),
+    ((80, 48, 16), "PPDDPP", 0.0),
+    ((112, 32, 20), "NNNNND", 1.0),
+    ((96, 80, 12), "DDPPDD", 2.5),
+    ((32, 32, 32), "PPPPPP", 0.0),
+    ((144, 16, 8), "PPNNNN", 1.2),
+]
+
+
+def _batch_inputs():
+    rng = np.random.default_rng(123)
+    grids, rhs = [], []
+    for n, cbc, gr in GRIDS:
+        dzci, dzfi, dzc, dzf = zgrid(n[2], gr)
+        grids.append(dict(n=n, dli=[n[0] * 1.0, n[1] * 1.1, 1.0], dzci=dzci, dzfi=dzfi, cbc=cbc))
+        rhs.append(compatible_rhs(rng, n, cbc, dzf))
+    return grids, rhs
+
+
+@pytest.mark.parametrize("tol", [1e-6, 1e-10])
+def test_batch_matches_oracle_and_single(lib, oracle, tol):
+    grids, rhs = _batch_inputs()
+    B = lib.Batch(grids, autotune=True)
+    for g, r in enumerate(rhs):
+        B.set(g, r)
+    relres, iters = B.solve(tol=tol, max_iter=8)
+    assert np.all(relres <= tol), relres
+    assert np.all(iters >= 1)
+    for g, (gd, r) in enumerate(zip(grids, rhs)):
+        got = B.get(g)
+        S = oracle.SolverSetup(gd["n"], gd["dli"], 1, gd["dzci"], gd["dzfi"], gd["cbc"], [0] * 6, "ccc")
+        ref = r.copy()
+        S.solve(ref)
+        sing = singular(gd["cbc"])
+        e = rel_l2(got[1:-1, 1:-1, 1:-1], ref[1:-1, 1:-1, 1:-1], remove_mean=sing)
+        assert e <= max(1e3 * tol, 1e-12), (g, e)
+        # alone: the single-grid mixed solve of the same problem
+        P = lib.initsolver(gd["n"], gd["dli"], 1, gd["dzci"], gd["dzfi"], gd["cbc"], [0.0] * 6, "ccc")
+        alone = r.copy()
+        rr, _ = P.solve_mixed(alone, tol=tol, max_iter=8)
+        assert rr <= tol
+        d = rel_l2(got[1:-1, 1:-1, 1:-1], alone[1:-1, 1:-1, 1:-1], remove_mean=sing)
+        assert d <= max(1e3 * tol, 1e-12), (g, d)
+    assert "maxe" in B.report()
+    B.destroy()
+
+
+def test_batch_second_solve_reuses_graph(lib):
+    grids, rhs = _batch_inputs()
+    B = lib.Batch(grids[:3], autotune=False)
+    for g in range(3):
+        B.set(g, rhs[g])
+    r1, _ = B.solve(tol=1e-8)
+    sol1 = [B.get(g) for g in range(3)]
+    for g in range(3):
+        B.set(g, rhs[g])
+    r2, _ = B.solve(tol=1e-8)
+    for g in range(3):
+        assert np.array_equal(sol1[g], B.get(g))
+    assert np.array_equal(r1, r2)
