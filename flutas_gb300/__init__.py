@@ -44,7 +44,19 @@ EXPORTED = [
     "flutas_gb300_bounduvw", "flutas_gb300_chkdiv_noalloc", "flutas_gb300_batch_create",
     "flutas_gb300_batch_field", "flutas_gb300_batch_solve", "flutas_gb300_batch_report",
     "flutas_gb300_batch_destroy", "flutas_gb300_batch_set", "flutas_gb300_batch_get",
+    "flutas_gb300_server_create", "flutas_gb300_server_submit", "flutas_gb300_server_wait",
+    "flutas_gb300_server_stats", "flutas_gb300_server_reset_stats", "flutas_gb300_server_destroy",
 ]
+
+
+class Request(C.Structure):
+    """flutas_request of include/flutas_gb300.h."""
+    _fields_ = [("kind", C.c_int), ("n", C.c_int * 3), ("dli", C.c_double * 3), ("nh_d", C.c_int),
+                ("dzci", C.c_void_p), ("dzfi", C.c_void_p), ("cbc", C.c_char * 6), ("bcpre", C.c_void_p),
+                ("tol", C.c_double), ("max_iter", C.c_int), ("rhs", C.c_void_p), ("p", C.c_void_p),
+                ("u", C.c_void_p), ("v", C.c_void_p), ("w", C.c_void_p), ("rho", C.c_void_p),
+                ("pold", C.c_void_p), ("nh_u", C.c_int), ("dt", C.c_double), ("dt_old", C.c_double),
+                ("rho0", C.c_double), ("cbcvel", C.c_void_p), ("bcvel", C.c_void_p)]
 
 
 class FlutasError(RuntimeError):
@@ -88,6 +100,12 @@ def load(path: str | None = None):
     L.flutas_gb300_batch_solve.argtypes = [vp, dp, ip, vp, vp]
     L.flutas_gb300_batch_report.argtypes = [vp, C.c_char_p, ip]
     L.flutas_gb300_batch_set.argtypes = [vp, ip, vp]
+    L.flutas_gb300_server_create.argtypes = [C.c_size_t, ip, vp]
+    L.flutas_gb300_server_submit.argtypes = [vp, C.POINTER(Request), vp]
+    L.flutas_gb300_server_wait.argtypes = [vp, C.c_longlong, vp, vp, vp]
+    L.flutas_gb300_server_stats.argtypes = [vp, C.c_char_p, ip]
+    L.flutas_gb300_server_reset_stats.argtypes = [vp]
+    L.flutas_gb300_server_destroy.argtypes = [vp]
     L.flutas_gb300_batch_get.argtypes = [vp, ip, vp]
     L.flutas_gb300_batch_destroy.argtypes = [vp]
     L.flutas_gb300_bounduvw.argtypes = [C.c_char_p, vp, vp, ip, ip, vp, vp, vp, vp, vp, vp, vp, vp]
@@ -407,5 +425,87 @@ class Batch:
         try:
             if _lib is not None and self.handle:
                 _lib.flutas_gb300_batch_destroy(self.handle)
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching request loop (flutas_gb300_server_*).
+
+    submit_solve / submit_projection return a ticket; wait(ticket) blocks until
+    that request is done and returns (status, relres, fp32_solves, latency_ms).
+    Arrays passed to submit_* must stay alive until wait() returns.
+    """
+
+    def __init__(self, hbm_budget_bytes: int, slots: int = 4):
+        self.handle = C.c_void_p()
+        _check(load().flutas_gb300_server_create(int(hbm_budget_bytes), int(slots), C.addressof(self.handle)))
+        self._keep = {}
+
+    def _submit(self, req, keep):
+        t = C.c_longlong()
+        _check(load().flutas_gb300_server_submit(self.handle, C.byref(req), C.addressof(t)))
+        self._keep[t.value] = (req, keep)
+        return t.value
+
+    @staticmethod
+    def _grid(req, n, dli, nh_d, dzci, dzfi, cbc, tol, max_iter):
+        req.n = (C.c_int * 3)(*[int(x) for x in n])
+        req.dli = (C.c_double * 3)(*[float(x) for x in dli])
+        req.nh_d = int(nh_d)
+        req.dzci, req.dzfi = _ptr(dzci), _ptr(dzfi)
+        req.cbc = _chars(cbc, 6)
+        req.tol, req.max_iter = float(tol), int(max_iter)
+
+    def submit_solve(self, n, dli, dzci, dzfi, cbc, rhs, out, tol=1e-10, max_iter=8, nh_d=1):
+        dzci, dzfi = np.ascontiguousarray(dzci, dtype=np.float64), np.ascontiguousarray(dzfi, dtype=np.float64)
+        req = Request()
+        req.kind = 0
+        self._grid(req, n, dli, nh_d, dzci, dzfi, cbc, tol, max_iter)
+        req.rhs, req.p = _ptr(rhs), _ptr(out)
+        return self._submit(req, (dzci, dzfi, rhs, out))
+
+    def submit_projection(self, n, dli, dzci, dzfi, cbc, u, v, w, p, dt, rho0=1.0, nh_u=1, rho=None, pold=None,
+                          dt_old=None, tol=1e-10, max_iter=8, cbcvel=None, bcvel=None, nh_d=1):
+        dzci, dzfi = np.ascontiguousarray(dzci, dtype=np.float64), np.ascontiguousarray(dzfi, dtype=np.float64)
+        req = Request()
+        req.kind = 1
+        self._grid(req, n, dli, nh_d, dzci, dzfi, cbc, tol, max_iter)
+        req.u, req.v, req.w, req.p = _ptr(u), _ptr(v), _ptr(w), _ptr(p)
+        req.rho, req.pold = _ptr(rho), _ptr(pold)
+        req.nh_u, req.dt, req.dt_old, req.rho0 = int(nh_u), float(dt), float(dt_old or dt), float(rho0)
+        keep = [dzci, dzfi, u, v, w, p, rho, pold]
+        if cbcvel is not None:
+            cv = C.create_string_buffer(_chars(cbcvel, 18), 18)
+            bv = (C.c_double * 18)(*[float(x) for x in (bcvel if bcvel is not None else [0.0] * 18)])
+            req.cbcvel, req.bcvel = C.cast(cv, C.c_void_p), C.cast(bv, C.c_void_p)
+            keep += [cv, bv]
+        return self._submit(req, keep)
+
+    def wait(self, ticket):
+        rr, it, lat = C.c_double(), C.c_int(), C.c_double()
+        rc = load().flutas_gb300_server_wait(self.handle, C.c_longlong(ticket), C.addressof(rr), C.addressof(it),
+                                             C.addressof(lat))
+        self._keep.pop(ticket, None)
+        return rc, rr.value, it.value, lat.value
+
+    def stats(self) -> dict:
+        import json
+        buf = C.create_string_buffer(4096)
+        _check(load().flutas_gb300_server_stats(self.handle, buf, 4096))
+        return json.loads(buf.value.decode())
+
+    def reset_stats(self):
+        _check(load().flutas_gb300_server_reset_stats(self.handle))
+
+    def close(self):
+        if self.handle:
+            _check(load().flutas_gb300_server_destroy(self.handle))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if _lib is not None and self.handle:
+                _lib.flutas_gb300_server_destroy(self.handle)
         except Exception:
             pass

@@ -151,22 +151,26 @@ int stage_out(const Staged &s, cudaStream_t st) {
 }
 
 int num_sms() {
-  static int sms = 0;
+  static std::atomic<int> cache{0};
+  int sms = cache.load();
   if (!sms) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
+    cache.store(sms);
   }
   return sms;
 }
 
 int max_smem_optin() {
-  static int v = 0;
+  static std::atomic<int> cache{0};
+  int v = cache.load();
   if (!v) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cache.store(v);
   }
   return v;
 }

@@ -207,6 +207,46 @@ FLUTAS_API int flutas_gb300_batch_solve(void *batch, double tol, int max_iter, d
 FLUTAS_API int flutas_gb300_batch_report(void *batch, char *buf, int len);
 FLUTAS_API int flutas_gb300_batch_destroy(void *batch);
 
+/* ---------------------------------------------------------------------------
+ * Serving (no counterpart in the reference): a continuous-batching request
+ * loop.  Requests of any size are submitted at any time; `slots` workers, each
+ * with its own CUDA stream, admit them in arrival order as soon as a slot is
+ * free and the HBM budget covers the request's fields and plan, so admitted
+ * requests overlap on the device.  Plans stay resident between requests of
+ * the same grid and are evicted least-recently-used when the budget needs
+ * room.  The caller's arrays must stay valid until server_wait returns.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int kind;                    /* 0: Poisson solve rhs -> p; 1: projection of u,v,w,p */
+  int n[3];
+  double dli[3];
+  int nh_d;
+  const double *dzci, *dzfi;   /* (1-nh_d:nz+nh_d), host memory */
+  char cbc[6];
+  const double *bcpre;         /* nullable: homogeneous BC values */
+  double tol;                  /* kind 0: > 0 (mixed precision); kind 1: > 0 mixed, 0 FP64 */
+  int max_iter;
+  const double *rhs;           /* kind 0: RHS, halo-1 array */
+  double *p;                   /* kind 0: solution out; kind 1: pressure in/out (p^n -> p^n + phi) */
+  double *u, *v, *w;           /* kind 1: velocities (halo nh_u), in/out */
+  const double *rho, *pold;    /* kind 1: two-phase Dodd-Ferrante split when non-null */
+  int nh_u;
+  double dt, dt_old, rho0;
+  const char *cbcvel;          /* nullable: 18 velocity BC characters (bounduvw) */
+  const double *bcvel;         /* 18 values when cbcvel is given */
+} flutas_request;
+
+FLUTAS_API int flutas_gb300_server_create(size_t hbm_budget_bytes, int slots, void **server);
+FLUTAS_API int flutas_gb300_server_submit(void *server, const flutas_request *req, long long *ticket);
+/* Blocks until the request is done; returns its status (FLUTAS_EITER when tol was not reached). */
+FLUTAS_API int flutas_gb300_server_wait(void *server, long long ticket, double *relres, int *iters,
+                                        double *latency_ms);
+/* JSON text: completed, p50_ms, p99_ms (submit-to-result latency), span_s, budget use. */
+FLUTAS_API int flutas_gb300_server_stats(void *server, char *buf, int len);
+FLUTAS_API int flutas_gb300_server_reset_stats(void *server);
+/* Waits for every queued request, then stops the workers and frees the plans. */
+FLUTAS_API int flutas_gb300_server_destroy(void *server);
+
 /* Number of kernels this library has launched in the process (all plans). */
 FLUTAS_API int flutas_gb300_launch_count(unsigned long long *count);
 
