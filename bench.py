@@ -500,6 +500,216 @@ def run_reference(args, rank):
     }
 
 
+# ----------------------------------------------------------------- batch mode
+def batch_grids(count, seed):
+    """Uneven grids: each axis 16*m log-uniform in [32,192], BCs per axis from
+    {PP,NN,DD}, z uniform or tanh-clustered (factor U[1,2.5])."""
+    rng = np.random.default_rng(seed)
+    grids = []
+    for _ in range(count):
+        n = [int(16 * round(np.exp(rng.uniform(np.log(32), np.log(192))) / 16)) for _ in range(3)]
+        cbc = "".join(rng.choice(["PP", "NN", "DD"]) for _ in range(3))
+        gr = 0.0 if (rng.uniform() < 0.5 or cbc[4:6] == "PP") else float(rng.uniform(1.0, 2.5))
+        k = np.arange(0, n[2] + 1) / n[2]
+        zf = 0.5 * (1 + np.tanh((k - 0.5) * gr) / np.tanh(gr / 2)) if gr else k
+        dzf = np.empty(n[2] + 2)
+        dzf[1:-1] = np.diff(zf)
+        dzf[0], dzf[-1] = dzf[1], dzf[-2]
+        dzc = np.empty(n[2] + 2)
+        dzc[:-1] = 0.5 * (dzf[:-1] + dzf[1:])
+        dzc[-1] = dzc[-2]
+        grids.append(dict(n=n, dli=[float(n[0]), float(n[1]), 1.0], dzci=1.0 / dzc, dzfi=1.0 / dzf, cbc=cbc,
+                          dzf=dzf))
+    return grids
+
+
+def run_batch(args):
+    import torch
+    import flutas_gb300 as F
+    F.load()
+    grids = batch_grids(args.grids, args.seed)
+    cells = sum(int(np.prod(g["n"])) for g in grids)
+    t0 = time.perf_counter()
+    B = F.Batch(grids, autotune=True)
+    t_create = time.perf_counter() - t0
+    rng = np.random.default_rng(args.seed + 1)
+    rhs = []
+    for g in grids:
+        nx, ny, nz = g["n"]
+        f = rng.uniform(-1, 1, (nz, ny, nx))
+        w = g["dzf"][1:-1][:, None, None]
+        f -= (f * w).sum() / (w.sum() * nx * ny)  # compatible with every BC (zero weighted mean)
+        h = np.zeros((nz + 2, ny + 2, nx + 2))
+        h[1:-1, 1:-1, 1:-1] = f
+        rhs.append(torch.from_numpy(h).cuda())
+    torch.cuda.synchronize()
+    def load_rhs():
+        for i, r in enumerate(rhs):
+            B.set(i, r)
+    for _ in range(args.warmup):
+        load_rhs()
+        B.solve(tol=1e-10, max_iter=8)
+    times, iters, rels = [], [], []
+    l0 = F.launch_count()
+    for _ in range(args.steps):
+        load_rhs()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rr, it = B.solve(tol=1e-10, max_iter=8)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+        iters.append(it)
+        rels.append(rr)
+    launches = (F.launch_count() - l0) // max(1, args.steps)
+    # the same grids one by one with the single-grid paths (a sample)
+    sample = list(range(0, len(grids), max(1, len(grids) // 24)))
+    t_seq_mixed = t_seq_fp64 = 0.0
+    for i in sample:
+        g = grids[i]
+        P = F.initsolver(g["n"], g["dli"], 1, g["dzci"], g["dzfi"], g["cbc"], [0.0] * 6, "ccc")
+        x = rhs[i].clone()
+        P.solve_mixed(x, tol=1e-10, max_iter=8)  # warm
+        for mode in ("mixed", "fp64"):
+            x = rhs[i].clone()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            if mode == "mixed":
+                P.solve_mixed(x, tol=1e-10, max_iter=8)
+            else:
+                P.solver(x)
+            torch.cuda.synchronize()
+            dt_ = time.perf_counter() - t1
+            if mode == "mixed":
+                t_seq_mixed += dt_
+            else:
+                t_seq_fp64 += dt_
+        P.fftend()
+    ms = float(np.median(times))
+    scale = len(grids) / len(sample)
+    return {"mode": "batch", "metric": "grids solved/s (mixed precision to 1e-10)", "grids": len(grids),
+            "cells": cells, "value": round(len(grids) / (ms / 1e3), 2), "unit": "grids/s",
+            "ms_per_batch": round(ms, 3), "cells_per_s": round(cells / (ms / 1e3), 1),
+            "max_relres": float(np.max(rels)), "fp32_solves_per_grid": {
+                "mean": float(np.mean(iters)), "max": int(np.max(iters))},
+            "gpu_launches_per_batch": int(launches), "create_s": round(t_create, 2),
+            "sequential_single_grid": {"mixed_grids_per_s": round(len(sample) / t_seq_mixed, 2),
+                                       "fp64_grids_per_s": round(len(sample) / t_seq_fp64, 2),
+                                       "sample_grids": len(sample), "est_batch_equivalent_ms":
+                                           round(t_seq_mixed * scale * 1e3, 2)},
+            "steps": args.steps, "warmup": args.warmup,
+            "timing": "CUDA events around each batch solve; RHS reloaded (device copies) between solves, untimed"}
+
+
+# ----------------------------------------------------------------- serving mode
+def serve_sizes(rng, count):
+    """Sizes 64^3..384^3 (volume log-uniform), aspect up to 4:1, axes multiples of 32."""
+    out = []
+    while len(out) < count:
+        vol = np.exp(rng.uniform(np.log(64 ** 3), np.log(384 ** 3)))
+        a = np.exp(rng.uniform(-np.log(2), np.log(2), 3))
+        a = a / np.prod(a) ** (1 / 3)
+        n = [int(max(32, min(512, 32 * round(vol ** (1 / 3) * x / 32)))) for x in a]
+        if max(n) / min(n) <= 4.0:
+            out.append(n)
+    return out
+
+
+def run_serve(args):
+    import torch
+    import flutas_gb300 as F
+    F.load()
+    rng = np.random.default_rng(args.seed)
+    # 16 grid shapes drawn log-uniformly in volume (64^3..384^3, aspect <= 4:1);
+    # requests pick a shape uniformly, so their volumes stay log-uniform
+    classes = sorted({tuple(s) for s in serve_sizes(rng, 16)})
+    sizes = [classes[i] for i in rng.integers(0, len(classes), args.requests)]
+    # one single-phase and one two-phase RHS per size class (pinned host memory)
+    rhs = {}
+    for c in classes:
+        nx, ny, nz = c
+        for kind in ("1p", "2p"):
+            f = torch.empty((nz + 2, ny + 2, nx + 2), dtype=torch.float64).pin_memory()
+            g = rng.uniform(-1, 1, (nz, ny, nx))
+            if kind == "2p":  # density-jump structure of a two-phase RHS: large values inside drops
+                zz, yy, xx = np.meshgrid(*(np.linspace(0, 1, m) for m in (nz, ny, nx)), indexing="ij")
+                drop = ((xx - 0.5) ** 2 + (yy - 0.5) ** 2 + (zz - 0.5) ** 2) < 0.04
+                g = g * np.where(drop, float(np.exp(rng.uniform(np.log(10), np.log(1000)))), 1.0)
+            g -= g.mean()
+            f.zero_()
+            f[1:-1, 1:-1, 1:-1] = torch.from_numpy(g)
+            rhs[(c, kind)] = f
+    outs = {c: [torch.empty((c[2] + 2, c[1] + 2, c[0] + 2), dtype=torch.float64).pin_memory() for _ in range(4)]
+            for c in classes}
+    dz = {c: np.full(c[2] + 2, float(c[2])) for c in classes}
+    reqs = []
+    for i, s in enumerate(sizes):
+        kind = "2p" if rng.uniform() < 0.3 else "1p"
+        tol = 1e-6 if rng.uniform() < 0.5 else 1e-10
+        reqs.append((tuple(s), kind, tol))
+    S = F.Server(hbm_budget_bytes=int(args.budget_gb * (1 << 30)), slots=args.slots)
+
+    def submit(c, kind, tol, k):
+        return S.submit_solve(c, [float(c[0]), float(c[1]), float(c[2])], dz[c], dz[c], "PPPPNN",
+                              rhs[(c, kind)].numpy(), outs[c][k % 4].numpy(), tol=tol, max_iter=8)
+
+    # warm: one request per class (plans become resident)
+    for j, c in enumerate(classes):
+        S.wait(submit(c, "1p", 1e-6, j))
+    # capacity: everything submitted at once
+    S.reset_stats()
+    t0 = time.perf_counter()
+    ts = [submit(c, kind, tol, i) for i, (c, kind, tol) in enumerate(reqs)]
+    for t in ts:
+        S.wait(t)
+    cap_span = time.perf_counter() - t0
+    capacity = len(reqs) / cap_span
+    sweep = []
+    for frac in args.rates:
+        rate = frac * capacity
+        S.reset_stats()
+        gaps = rng.exponential(1.0 / rate, len(reqs))
+        t0 = time.perf_counter()
+        tick = t0
+        ts = []
+        for i, (c, kind, tol) in enumerate(reqs):
+            tick += gaps[i]
+            dt_ = tick - time.perf_counter()
+            if dt_ > 0:
+                time.sleep(dt_)
+            ts.append(submit(c, kind, tol, i))
+        stat = [S.wait(t) for t in ts]
+        span = time.perf_counter() - t0
+        st = S.stats()
+        sweep.append({"offered_per_s": round(rate, 2), "solves_per_s": round(len(reqs) / span, 2),
+                      "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                      "errors": int(sum(1 for x in stat if x[0] != 0))})
+    S.close()
+    # the plain FP64 single-solve path on the same request sizes (sequential, device-resident)
+    sample = reqs[: min(len(reqs), 40)]
+    plans = {}
+    t_fp64 = 0.0
+    for c, kind, tol in sample:
+        if c not in plans:
+            plans[c] = F.initsolver(c, [float(c[0]), float(c[1]), float(c[2])], 1, dz[c], dz[c], "PPPPNN", [0.0] * 6)
+            x = rhs[(c, kind)].cuda()
+            plans[c].solver(x)
+        x = rhs[(c, kind)].cuda()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        plans[c].solver(x)
+        torch.cuda.synchronize()
+        t_fp64 += time.perf_counter() - t1
+    return {"mode": "serve", "metric": "projection solves/s and p50/p99 latency under a mixed-size stream",
+            "requests": len(reqs), "size_classes": len(classes), "two_phase_frac": 0.3,
+            "tolerances": "1e-6 / 1e-10 (50/50)", "budget_gb": args.budget_gb, "slots": args.slots,
+            "capacity_solves_per_s": round(capacity, 2), "sweep": sweep,
+            "fp64_single_solve_per_s": round(len(sample) / t_fp64, 2),
+            "timing": "host clock; latency = submit to result on host (includes H2D of the RHS and D2H of the "
+                      "solution); Poisson arrivals"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -514,13 +724,23 @@ def main():
                     help="only the headline mode (for profiler captures): W warm-up + K steps, no extra modes, "
                          "no e2e, no CPU baseline")
     ap.add_argument("--precision", type=int, default=1, help="with --single: 1 mixed to 1e-10, 0 FP64")
+    ap.add_argument("--mode", choices=["projection", "batch", "serve"], default="projection",
+                    help="projection: the headline two-phase step; batch: 512 uneven grids in one graph; "
+                         "serve: Poisson request stream through the continuous-batching server")
+    ap.add_argument("--grids", type=int, default=512)
+    ap.add_argument("--requests", type=int, default=1000)
+    ap.add_argument("--slots", type=int, default=4)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--rates", type=float, nargs="+", default=[0.5, 0.8, 1.0, 1.2])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
+    if args.impl == "ours" and args.mode != "projection":
+        res = run_batch(args) if args.mode == "batch" else run_serve(args)
+    elif args.impl == "reference":
         res = run_reference(args, rank)
     else:
         if world > 1:
