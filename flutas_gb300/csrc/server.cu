@@ -165,6 +165,10 @@ int run_request(flutas_server *s, Request *q, PlanEntry *pe, cudaStream_t st) {
   void *plan = pe->arr[0];
   int rc = flutas_gb300_plan_set_stream(plan, st, 1);
   if (rc) return rc;
+  struct Restore {  // every exit path hands the plan back on the default stream
+    void *plan;
+    ~Restore() { flutas_gb300_plan_set_stream(plan, nullptr, 1); }
+  } restore{plan};
   const size_t pb = sizeof(double) * cells_halo(r.n, 1);
   auto dmalloc = [&](size_t bytes, double **out) -> int {
     if (cudaMallocAsync((void **)out, bytes, st) != cudaSuccess) {
