@@ -295,7 +295,8 @@ struct flutas_plan {
   Mirrors mir;
   cudaStream_t stream = 0;
   bool sync = true;
-  int path64 = 0, path32 = 0;  // 0 separate passes, 1 fused plane kernel
+  int path64 = 0, path32 = 0;  // 0 separate passes, 1 fused plane kernel, 2 cluster plane kernel
+  int clus64 = 0, clus32 = 0;  // cluster size of path 2
   bool pin_zero_mode = false;  // singular (lam == 0, z in N/N or P/P) column
   double last_relres = 0.0;    // relative residual / FP32 solves of the last mixed solve
   int last_iters = 0;
@@ -314,10 +315,68 @@ template <typename T> size_t plane_smem(int nx, int ny) {
   return align_up<T>(sizeof(T) * (size_t)ny * xpitch(nx)) + sizeof(T) * (size_t)nx * ny;
 }
 
+// Cluster plane kernels: smallest cluster (2..16 CTAs) whose per-CTA share of
+// the plane fits two CTAs per SM; 0 when the plane does not split evenly.
+constexpr int CLUSTER_THREADS = 256;
+template <typename T> int cluster_size_for(int nx, int ny, int smax) {
+  for (int C = 2; C <= 16; C *= 2) {
+    if (nx % C || ny % C || (nx / C) % 2 || (ny / C) % 2) continue;
+    const size_t sm = cluster_plane_smem(nx, ny, C, sizeof(T));
+    if (sm <= (size_t)smax / 2 - 1024) return C;
+  }
+  return 0;
+}
+
+template <typename K> int cluster_prepare(K kernel, size_t smem, int C) {
+  CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (C > 8) CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  return 0;
+}
+
+template <typename K, typename... Args>
+cudaError_t cluster_launch(K kernel, int clusters, int C, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(clusters * C));
+  cfg.blockDim = dim3(CLUSTER_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+// Co-resident clusters of a kernel (0 when a cluster of C cannot be placed).
+template <typename K> int cluster_capacity(K kernel, size_t smem, int C) {
+  if (cluster_prepare(kernel, smem, C)) return 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)C);
+  cfg.blockDim = dim3(CLUSTER_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kernel, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
 // Launch name "<base><f32|f64,tag>" per kernel, precision and functor.
-enum KId { KID_XYFWD, KID_XFWD, KID_XYINV, KID_XINV };
+enum KId { KID_XYFWD, KID_XFWD, KID_XYINV, KID_XINV, KID_XYFWD_CL, KID_XYINV_CL };
 template <int KID, typename T, typename F> const char *kname() {
-  static const char *base[] = {"k_xyfwd_plane", "k_xfwd", "k_xyinv_plane", "k_xinv"};
+  static const char *base[] = {"k_xyfwd_plane", "k_xfwd", "k_xyinv_plane", "k_xinv", "k_xyfwd_cluster",
+                               "k_xyinv_cluster"};
   static const std::string s = std::string(base[KID]) + (sizeof(T) == 8 ? "<f64," : "<f32,") + F::tag + ">";
   return s.c_str();
 }
@@ -335,6 +394,16 @@ int fwd_xy(flutas_plan *pl, const In &in, T *S, const AxisTables &tx, const Axis
     int grid = grid_for(k_xyfwd_plane<T, In>, 512, sm, g.nz);
     if (grid < 0) return grid;
     TRY(launch(kname<KID_XYFWD, T, In>(), st, [&] { k_xyfwd_plane<T, In><<<grid, 512, sm, st>>>(tx.ap, ty.ap, in, S, g, nrm); }));
+    return 0;
+  }
+  if (path == 2) {
+    const int C = sizeof(T) == 8 ? pl->clus64 : pl->clus32;
+    const size_t sm = cluster_plane_smem(g.nx, g.ny, C, sizeof(T));
+    TRY(cluster_prepare(k_xyfwd_cluster<T, In>, sm, C));
+    cudaError_t e = cudaSuccess;
+    TRY(launch(kname<KID_XYFWD_CL, T, In>(), st,
+               [&] { e = cluster_launch(k_xyfwd_cluster<T, In>, g.nz, C, sm, st, tx.ap, ty.ap, in, S, g, nrm); }));
+    if (e != cudaSuccess) return fail(FLUTAS_ECUDA, "cluster launch failed: %s", cudaGetErrorString(e));
     return 0;
   }
   // x pass
@@ -373,6 +442,16 @@ int inv_xy(flutas_plan *pl, const T *S, const Out &out, const AxisTables &tx, co
     int grid = grid_for(k_xyinv_plane<T, Out>, 512, sm, g.nz);
     if (grid < 0) return grid;
     TRY(launch(kname<KID_XYINV, T, Out>(), st, [&] { k_xyinv_plane<T, Out><<<grid, 512, sm, st>>>(tx.ap, ty.ap, S, out, g); }));
+    return 0;
+  }
+  if (path == 2) {
+    const int C = sizeof(T) == 8 ? pl->clus64 : pl->clus32;
+    const size_t sm = cluster_plane_smem(g.nx, g.ny, C, sizeof(T));
+    TRY(cluster_prepare(k_xyinv_cluster<T, Out>, sm, C));
+    cudaError_t e = cudaSuccess;
+    TRY(launch(kname<KID_XYINV_CL, T, Out>(), st,
+               [&] { e = cluster_launch(k_xyinv_cluster<T, Out>, g.nz, C, sm, st, tx.ap, ty.ap, S, out, g); }));
+    if (e != cudaSuccess) return fail(FLUTAS_ECUDA, "cluster launch failed: %s", cudaGetErrorString(e));
     return 0;
   }
   {
@@ -693,6 +772,15 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
   const int smax = max_smem_optin();
   pl->path64 = (nx % 2 == 0 && ny % 2 == 0 && (int)plane_smem<double>(nx, ny) <= smax) ? 1 : 0;
   pl->path32 = (nx % 2 == 0 && ny % 2 == 0 && (int)plane_smem<float>(nx, ny) <= smax) ? 1 : 0;
+  if (!pl->path64 && (pl->clus64 = cluster_size_for<double>(nx, ny, smax)) &&
+      cluster_capacity(k_xyinv_cluster<double, OutHalo>, cluster_plane_smem(nx, ny, pl->clus64, 8), pl->clus64) > 0)
+    pl->path64 = 2;
+  if (!pl->path32 && (pl->clus32 = cluster_size_for<float>(nx, ny, smax)) &&
+      cluster_capacity(k_xyinv_cluster<float, OutHalo>, cluster_plane_smem(nx, ny, pl->clus32, 4), pl->clus32) > 0)
+    pl->path32 = 2;
+  if (const char *e = getenv("FLUTAS_GB300_XY_PATH")) {  // 0 forces separate passes (A/B timing)
+    if (atoi(e) == 0) pl->path64 = pl->path32 = 0;
+  }
   arrplan[0] = pl;
   arrplan[1] = arrplan[2] = arrplan[3] = nullptr;
   return FLUTAS_OK;
@@ -1073,6 +1161,7 @@ int flutas_gb300_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, dou
   a.p = sp.d; a.pold = so.d; a.rho = sr.d;
   a.u = su.d; a.v = sv.d; a.w = sw.d;
   TRY(presw_consts(&a, sz.d, nh_d, nz, dxi, dyi, rho0i, f_t12, f2, zab, st));
+  a.fp32 = 0;
   a.g = Geo{nx, ny, nz, nh_u};
   TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<grid_cells(a.g), 256, 0, st>>>(a); }));
   TRY(stage_out(su, st));
@@ -1217,6 +1306,7 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     a.p = p; a.pold = pold; a.rho = rho;
     a.u = u; a.v = v; a.w = w;
     TRY(presw_consts(&a, dzci_d, nh_d, nz, dxi, dyi, 1.0 / rho0, dt, dt / f_t12_o, pl->zdf.as<double>(), st));
+    a.fp32 = precision == 1 ? 1 : 0;  // FP32 increment in the mixed path, FP64 in the FP64 path
     a.g = g;
     TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<grid_cells(a.g), 256, 0, st>>>(a); }));
   }

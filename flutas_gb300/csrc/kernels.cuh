@@ -716,6 +716,7 @@ struct PresTwArgs {
   const double *zA, *zB;  // per level k: f_t12*dzci(k)*f2/rho0 and 2*f_t12*dzci(k)
   double xA, xB, yA, yB;  // the same with dxi, dyi
   double f2;
+  int fp32;               // 1: increment evaluated in FP32 from FP64 differences (mixed path)
   Geo g;
 };
 __device__ __forceinline__ double rcp64_1(double x) {
@@ -727,6 +728,24 @@ __device__ __forceinline__ double df_incr(double dp, double dq, double rs, doubl
   const double dg = fma(f2, t, dp);
   return fma(A, t, -B * (rcp64_1(rs) * dg));
 }
+// FP32 increment from FP64 differences: the differences of p and pold (which
+// cancel) are taken in FP64, the rest (relative error ~1e-7 of an increment
+// that is itself small against u) in FP32; the update u += delta stays FP64.
+__device__ __forceinline__ double df_incr32(double dp64, double dq64, float rs, float A, float B, float f2) {
+  const float dp = (float)dp64, t = (float)(dp64 - dq64);
+  const float dg = fmaf(f2, t, dp);
+  return (double)fmaf(A, t, -B * (__frcp_rn(rs) * dg));
+}
+__device__ __forceinline__ void pres_tw_cell32(const PresTwArgs &a, int i, int j, int k) {
+  const Geo &g = a.g;
+  const long c0 = g.pidx(i, j, k), cx = c0 + 1, cy = c0 + (g.nx + 2), cz = c0 + (long)(g.nx + 2) * (g.ny + 2);
+  const double p0 = a.p[c0], q0 = a.pold[c0];
+  const float r0 = (float)a.rho[c0], f2 = (float)a.f2;
+  const long ui = g.uidx(i, j, k);
+  a.u[ui] += df_incr32(a.p[cx] - p0, a.pold[cx] - q0, (float)a.rho[cx] + r0, (float)a.xA, (float)a.xB, f2);
+  a.v[ui] += df_incr32(a.p[cy] - p0, a.pold[cy] - q0, (float)a.rho[cy] + r0, (float)a.yA, (float)a.yB, f2);
+  a.w[ui] += df_incr32(a.p[cz] - p0, a.pold[cz] - q0, (float)a.rho[cz] + r0, (float)a.zA[k], (float)a.zB[k], f2);
+}
 __device__ __forceinline__ void pres_tw_cell(const PresTwArgs &a, int i, int j, int k) {
   const Geo &g = a.g;
   const long c0 = g.pidx(i, j, k), cx = c0 + 1, cy = c0 + (g.nx + 2), cz = c0 + (long)(g.nx + 2) * (g.ny + 2);
@@ -737,7 +756,8 @@ __device__ __forceinline__ void pres_tw_cell(const PresTwArgs &a, int i, int j, 
   a.w[ui] += df_incr(a.p[cz] - p0, a.pold[cz] - q0, a.rho[cz] + r0, a.zA[k], a.zB[k], a.f2);
 }
 __global__ void k_pres_tw_src(PresTwArgs a) {
-  for_cells(a.g, [&](int i0, int j0, int k0) { pres_tw_cell(a, i0 + 1, j0 + 1, k0 + 1); });
+  if (a.fp32) for_cells(a.g, [&](int i0, int j0, int k0) { pres_tw_cell32(a, i0 + 1, j0 + 1, k0 + 1); });
+  else for_cells(a.g, [&](int i0, int j0, int k0) { pres_tw_cell(a, i0 + 1, j0 + 1, k0 + 1); });
 }
 
 // correc with the pressure increment phi, fused with p = p + phi
@@ -1225,6 +1245,179 @@ __global__ void kb_reset(BatchGrid *grids, int ng) {
     *grids[g].active = 1;
     grids[g].nrm[0] = 0.0;
     grids[g].nrm[1] = 0.0;
+  }
+}
+
+}  // namespace fg
+
+#include <cooperative_groups.h>
+
+namespace fg {
+
+namespace cg = cooperative_groups;
+
+// ===========================================================================
+// Cluster plane passes: a z-plane too large for one CTA's shared memory is
+// shared by a thread-block cluster of C CTAs.  CTA r transforms rows
+// [r*ny/C, (r+1)*ny/C) along x, the cluster exchanges the x-spectrum through
+// distributed shared memory so that CTA r holds columns [r*nx/C, (r+1)*nx/C)
+// of every row, then transforms those along y.  The inverse runs the same in
+// reverse order.  Shared memory per CTA: three buffers of (plane/C) values.
+// ===========================================================================
+template <typename T> struct ClusterPlane {
+  int nx, ny, C;
+  int rows, cols;       // ny/C, nx/C
+  int P;                // row pitch of the slab buffer (nx + 1)
+  size_t bufsz;         // bytes of one buffer (>= rows*P and >= ny*cols reals)
+  __device__ ClusterPlane(int nx_, int ny_, int C_) : nx(nx_), ny(ny_), C(C_) {
+    rows = ny / C;
+    cols = nx / C;
+    P = xpitch(nx);
+    size_t a = (size_t)rows * P, b = (size_t)ny * cols;
+    bufsz = align_up<T>(sizeof(T) * (a > b ? a : b));
+  }
+};
+
+inline size_t cluster_plane_smem(int nx, int ny, int C, size_t tsize) {
+  const size_t rows = ny / C, cols = nx / C, P = nx + 1;
+  const size_t a = rows * P, b = (size_t)ny * cols;
+  const size_t one = ((tsize * (a > b ? a : b)) + 255) & ~(size_t)255;
+  return 3 * one;
+}
+
+template <typename T>
+struct StoreColBlock {  // y-phase lines = columns of the local column block (row-major ny x cols)
+  T *R;
+  int pitch;
+  __device__ void pair(int c, int t, T v0, T v1) {
+    R[(long)t * pitch + 2 * c] = v0;
+    R[(long)t * pitch + 2 * c + 1] = v1;
+  }
+  __device__ void single(int c, int t, T v) { R[(long)t * pitch + c] = v; }
+};
+
+// x-spectrum rows (slab of each CTA, pitch gp, in buffer `slab`) -> this CTA's
+// column block (ny x cols, row-major) in `blk`.
+template <typename T>
+__device__ __forceinline__ void cluster_gather_cols(cg::cluster_group &cluster, const ClusterPlane<T> &cp, T *slab,
+                                                    int gp, T *blk) {
+  const int r = (int)cluster.block_rank();
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int x0 = r * cp.cols;
+  for (int s = 0; s < cp.C; s++) {
+    const T *rem = cluster.map_shared_rank(slab, s);
+    const int tot = cp.rows * cp.cols;
+    for (int idx = tid; idx < tot; idx += nth) {
+      const int lr = idx / cp.cols, xc = idx % cp.cols;
+      blk[(long)(s * cp.rows + lr) * cp.cols + xc] = rem[(long)lr * gp + x0 + xc];
+    }
+  }
+}
+
+// this CTA's column block (ny x cols) -> its row slab (rows x nx, pitch P) from every CTA's block.
+template <typename T>
+__device__ __forceinline__ void cluster_gather_rows(cg::cluster_group &cluster, const ClusterPlane<T> &cp, T *blk,
+                                                    T *slab) {
+  const int r = (int)cluster.block_rank();
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int s = 0; s < cp.C; s++) {
+    const T *rem = cluster.map_shared_rank(blk, s);
+    const int tot = cp.rows * cp.cols;
+    for (int idx = tid; idx < tot; idx += nth) {
+      const int lr = idx / cp.cols, xc = idx % cp.cols;
+      slab[(long)lr * cp.P + s * cp.cols + xc] = rem[(long)(r * cp.rows + lr) * cp.cols + xc];
+    }
+  }
+}
+
+template <typename T, typename In>
+__global__ void __launch_bounds__(256, 2) k_xyfwd_cluster(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int r = (int)cluster.block_rank();
+  const ClusterPlane<T> cp(g.nx, g.ny, C);
+  T *B0 = (T *)smem_raw;
+  T *B1 = (T *)(smem_raw + cp.bufsz);
+  T *B2 = (T *)(smem_raw + 2 * cp.bufsz);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int nclusters = gridDim.x / C;
+  const int cid = blockIdx.x / C;
+  float ss = 0.0f;
+  for (int k = cid; k < g.nz; k += nclusters) {
+    // ---- x transform of this CTA's rows
+    const int y0 = r * cp.rows;
+    for (int idx = tid; idx < cp.rows * g.nx; idx += nth) {
+      const int ly = idx / g.nx, x = idx % g.nx;
+      const T v = (T)in(x, y0 + ly, k);
+      ss = fma((float)v, (float)v, ss);
+      B0[ly * cp.P + x] = v;
+    }
+    __syncthreads();
+    const int Bx = cbatch(ax.pair, cp.rows);
+    pre_fwd<T>(ax, B0, cp.P, 1, cp.rows, (C2<T> *)B1, Bx, tid, nth);
+    __syncthreads();
+    C2<T> *fin = run_stages<T, false>(ax, (C2<T> *)B1, (C2<T> *)B0, Bx, tid, nth);
+    T *G = (fin == (C2<T> *)B1) ? B0 : B1;  // real x-spectrum rows, pitch P
+    StorePlaneReal<T> sx{G, cp.P, 0};
+    post_fwd<T>(ax, fin, Bx, cp.rows, sx, tid, nth);
+    cluster.sync();  // every slab complete
+    cluster_gather_cols<T>(cluster, cp, G, cp.P, B2);
+    cluster.sync();  // every CTA has read the slabs
+    // ---- y transform of this CTA's columns (lines = columns of B2)
+    const int By = cbatch(ay.pair, cp.cols);
+    pre_fwd<T>(ay, B2, 1, cp.cols, cp.cols, (C2<T> *)B0, By, tid, nth);
+    __syncthreads();
+    C2<T> *fy = run_stages<T, false>(ay, (C2<T> *)B0, (C2<T> *)B1, By, tid, nth);
+    StoreColsS<T> st{S, (long)k * g.nx * g.ny, g.nx, r * cp.cols, cp.cols};
+    post_fwd<T>(ay, fy, By, cp.cols, st, tid, nth);
+    __syncthreads();
+  }
+  if (nrm) block_sum_add((double)ss, nrm);
+}
+
+template <typename T, typename Out>
+__global__ void __launch_bounds__(256, 2) k_xyinv_cluster(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int r = (int)cluster.block_rank();
+  const ClusterPlane<T> cp(g.nx, g.ny, C);
+  T *B0 = (T *)smem_raw;
+  T *B1 = (T *)(smem_raw + cp.bufsz);
+  T *B2 = (T *)(smem_raw + 2 * cp.bufsz);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const bool invx = fft_inverse(ax.pair, true), invy = fft_inverse(ay.pair, true);
+  const int nclusters = gridDim.x / C;
+  const int cid = blockIdx.x / C;
+  for (int k = cid; k < g.nz; k += nclusters) {
+    // ---- y^-1 of this CTA's columns
+    const T *Sp = S + (long)k * g.nx * g.ny + r * cp.cols;
+    for (int idx = tid; idx < g.ny * cp.cols; idx += nth) {
+      const int y = idx / cp.cols, xc = idx % cp.cols;
+      B0[idx] = Sp[(long)y * g.nx + xc];
+    }
+    __syncthreads();
+    const int By = cbatch(ay.pair, cp.cols);
+    pre_bwd<T>(ay, B0, 1, cp.cols, cp.cols, (C2<T> *)B1, By, tid, nth);
+    __syncthreads();
+    C2<T> *fy = invy ? run_stages<T, true>(ay, (C2<T> *)B1, (C2<T> *)B0, By, tid, nth)
+                     : run_stages<T, false>(ay, (C2<T> *)B1, (C2<T> *)B0, By, tid, nth);
+    StoreColBlock<T> sy{B2, cp.cols};
+    post_bwd<T>(ay, fy, By, cp.cols, sy, tid, nth);
+    cluster.sync();  // every column block complete
+    cluster_gather_rows<T>(cluster, cp, B2, B0);
+    cluster.sync();  // every CTA has read the blocks
+    // ---- x^-1 of this CTA's rows (B0, pitch P)
+    const int Bx = cbatch(ax.pair, cp.rows);
+    pre_bwd<T>(ax, B0, cp.P, 1, cp.rows, (C2<T> *)B1, Bx, tid, nth);
+    __syncthreads();
+    C2<T> *fx = invx ? run_stages<T, true>(ax, (C2<T> *)B1, (C2<T> *)B0, Bx, tid, nth)
+                     : run_stages<T, false>(ax, (C2<T> *)B1, (C2<T> *)B0, Bx, tid, nth);
+    const long row0 = (long)k * g.ny + r * cp.rows;
+    StoreRowsOut<T, Out> st{out, row0, row0 + cp.rows, g.ny};
+    post_bwd<T>(ax, fx, Bx, cp.rows, st, tid, nth);
+    __syncthreads();
   }
 }
 

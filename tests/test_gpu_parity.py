@@ -202,6 +202,41 @@ def test_gpu_mixed_precision_refinement(lib, oracle, n, cbc, gr, tol):
     assert err <= max(1e3 * tol, 1e-12), err
 
 
+# z-planes larger than one CTA's shared memory: the x and y transforms of a
+# plane run in a thread-block cluster that exchanges the plane through
+# distributed shared memory (xy path 2); 320x192 needs 16 CTAs in FP64.
+LARGE_PLANES = [((256, 256, 4), "PPPPNN", 0.0), ((320, 192, 6), "NNPPDD", 1.0),
+                ((256, 128, 5), "DDNNPP", 0.0), ((192, 256, 3), "NDPPNN", 0.5)]
+
+
+@pytest.mark.parametrize("n,cbc,gr", LARGE_PLANES, ids=[f"{c}-{n[0]}x{n[1]}x{n[2]}" for n, c, _ in LARGE_PLANES])
+def test_gpu_cluster_plane_path(lib, oracle, n, cbc, gr, monkeypatch):
+    rng = np.random.default_rng(7 + sum(n))
+    P, dzci, dzfi, dzc, dzf, dli = plan_for(lib, n, cbc, gr)
+    info = P.info()
+    assert info["xy_path_fp64"] == 2 and info["xy_path_fp32"] == 2, info
+    S = oracle.SolverSetup(n, dli, 1, dzci, dzfi, cbc, [0] * 6, "ccc")
+    p = compatible_rhs(rng, n, cbc, dzf)
+    f = p.copy()
+    ref = p.copy()
+    S.solve(ref)
+    got = p.copy()
+    P.solver(got)
+    assert rel_l2(got[1:-1, 1:-1, 1:-1], ref[1:-1, 1:-1, 1:-1], remove_mean=singular(cbc)) <= 1e-12
+    mixed = p.copy()
+    relres, _ = P.solve_mixed(mixed, tol=1e-10, max_iter=10)
+    assert relres <= 1e-10
+    r = oracle.residual(n, cbc, dli[0], dli[1], 1, dzci, dzfi, f, mixed)
+    assert np.linalg.norm(r) / np.linalg.norm(f[1:-1, 1:-1, 1:-1]) <= 1e-10 * 1.01
+    # the same solve with separate x and y passes (path 0) agrees to rounding
+    monkeypatch.setenv("FLUTAS_GB300_XY_PATH", "0")
+    Q = plan_for(lib, n, cbc, gr)[0]
+    assert Q.info()["xy_path_fp64"] == 0 and Q.info()["xy_path_fp32"] == 0
+    sep = p.copy()
+    Q.solver(sep)
+    assert rel_l2(got[1:-1, 1:-1, 1:-1], sep[1:-1, 1:-1, 1:-1], remove_mean=singular(cbc)) <= 1e-13
+
+
 VEL_BCS = ["PPPPDD" * 3, "DDPPDD" * 3, "NNDDND" * 3, "PPNNDD" * 3]
 
 
