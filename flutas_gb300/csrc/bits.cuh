@@ -1,0 +1,88 @@
+// bits.cuh -- FP64 <-> FP32 conversions by integer bit operations.
+//
+// A conversion instruction between FP64 and FP32 issues on the FP64 pipe, the
+// scarce unit of the part (about 1/57 of the FP32 rate); these run on the
+// integer ALUs instead.  __host__ __device__ so the CPU tests run the same code.
+//
+// f32_of truncates the mantissa toward zero (relative error < 2^-23), flushes
+// magnitudes below 2^-126 to a signed zero and turns finite values above the
+// FP32 range into infinities; NaN stays NaN.  f64_of is exact for normal FP32
+// values (FP32 subnormals become a signed zero).
+#pragma once
+#include <cstring>
+
+#ifndef FG_HD
+#define FG_HD __host__ __device__ __forceinline__
+#endif
+
+namespace fg {
+
+FG_HD unsigned hi_word(double x) {
+#ifdef __CUDA_ARCH__
+  return (unsigned)__double2hiint(x);
+#else
+  unsigned long long b;
+  memcpy(&b, &x, 8);
+  return (unsigned)(b >> 32);
+#endif
+}
+FG_HD unsigned lo_word(double x) {
+#ifdef __CUDA_ARCH__
+  return (unsigned)__double2loint(x);
+#else
+  unsigned long long b;
+  memcpy(&b, &x, 8);
+  return (unsigned)b;
+#endif
+}
+FG_HD double from_words(unsigned hi, unsigned lo) {
+#ifdef __CUDA_ARCH__
+  return __hiloint2double((int)hi, (int)lo);
+#else
+  const unsigned long long b = ((unsigned long long)hi << 32) | lo;
+  double x;
+  memcpy(&x, &b, 8);
+  return x;
+#endif
+}
+FG_HD float float_of_bits(unsigned f) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(f);
+#else
+  float x;
+  memcpy(&x, &f, 4);
+  return x;
+#endif
+}
+FG_HD unsigned bits_of_float(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  unsigned f;
+  memcpy(&f, &x, 4);
+  return f;
+#endif
+}
+
+FG_HD float f32_of(double x) {
+  const unsigned hi = hi_word(x), lo = lo_word(x);
+  const unsigned sign = hi & 0x80000000u, ex = (hi >> 20) & 0x7ffu;
+  const int e = (int)ex - 896;  // FP32 biased exponent
+  unsigned f = sign | ((unsigned)e << 23) | (((hi << 3) | (lo >> 29)) & 0x7fffffu);
+  if (e <= 0) f = sign;
+  if (e >= 255) f = sign | 0x7f800000u | ((ex == 0x7ffu && ((hi & 0xfffffu) | lo)) ? 0x400000u : 0u);
+  return float_of_bits(f);
+}
+
+FG_HD double f64_of(float x) {
+  const unsigned f = bits_of_float(x), e = (f >> 23) & 0xffu;
+  unsigned hi = (f & 0x80000000u) | ((e + 896u) << 20) | ((f >> 3) & 0xfffffu), lo = f << 29;
+  if (e == 0) {
+    hi = f & 0x80000000u;
+    lo = 0u;
+  }
+  if (e == 255) hi = (f & 0x80000000u) | 0x7ff00000u | ((f >> 3) & 0xfffffu);
+  return from_words(hi, lo);
+}
+
+}  // namespace fg

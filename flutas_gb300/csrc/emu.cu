@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "axis_tables.cuh"
+#include "bits.cuh"
 #include "fft_engine.cuh"
 
 using namespace fg;
@@ -68,4 +69,12 @@ extern "C" __attribute__((visibility("default"))) int fg_emu_lines(int dbl, int 
 
 extern "C" __attribute__((visibility("default"))) int fg_emu_radix_plan(int N, int *radix) {
   return make_radix_plan(N, radix);
+}
+
+// The bit-operation conversions of bits.cuh, element by element.
+extern "C" __attribute__((visibility("default"))) void fg_emu_f32_of(const double *x, float *y, long n) {
+  for (long i = 0; i < n; i++) y[i] = f32_of(x[i]);
+}
+extern "C" __attribute__((visibility("default"))) void fg_emu_f64_of(const float *x, double *y, long n) {
+  for (long i = 0; i < n; i++) y[i] = f64_of(x[i]);
 }

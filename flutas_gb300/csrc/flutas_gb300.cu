@@ -316,13 +316,14 @@ template <typename T> size_t plane_smem(int nx, int ny) {
 }
 
 // Cluster plane kernels: smallest cluster (2..16 CTAs) whose per-CTA share of
-// the plane fits two CTAs per SM; 0 when the plane does not split evenly.
+// the plane fits two CTAs per SM (FP32: 128 registers) or one (FP64: up to
+// 255 registers); 0 when the plane does not split evenly.
 constexpr int CLUSTER_THREADS = 256;
 template <typename T> int cluster_size_for(int nx, int ny, int smax) {
   for (int C = 2; C <= 16; C *= 2) {
     if (nx % C || ny % C || (nx / C) % 2 || (ny / C) % 2) continue;
     const size_t sm = cluster_plane_smem(nx, ny, C, sizeof(T));
-    if (sm <= (size_t)smax / 2 - 1024) return C;
+    if (sm <= (sizeof(T) == 4 ? (size_t)smax / 2 - 1024 : (size_t)smax)) return C;
   }
   return 0;
 }
@@ -1090,6 +1091,8 @@ int presw_consts(PresTwArgs *a, const double *dzci_d, int nh_d, int nz, double d
   a->xB = 2.0 * f_t12 * dxi;
   a->yA = f_t12 * dyi * f2 * rho0i;
   a->yB = 2.0 * f_t12 * dyi;
+  a->xA32 = (float)a->xA; a->xB32 = (float)a->xB; a->yA32 = (float)a->yA; a->yB32 = (float)a->yB;
+  a->f2_32 = (float)f2;
   TRY(launch("k_scale_vec", st, [&] { k_scale_vec<<<1, 256, 0, st>>>(dzci_d, f_t12 * f2 * rho0i, zab, len); }));
   TRY(launch("k_scale_vec", st, [&] { k_scale_vec<<<1, 256, 0, st>>>(dzci_d, 2.0 * f_t12, zab + len, len); }));
   a->zA = zab + (nh_d - 1);

@@ -16,6 +16,7 @@
 //   spectral S     (nx, ny, nz) no halo             T (double or float)
 #pragma once
 #include "fft_engine.cuh"
+#include "bits.cuh"
 
 namespace fg {
 
@@ -55,6 +56,14 @@ __device__ __forceinline__ double rcp64(double x) {
   y = y * fma(-x, y, 2.0);
   return y;
 }
+
+// Value of an FP64 RHS in the arithmetic type of a pass, and the FP32 value
+// used for the norms (integer-ALU conversions, bits.cuh).
+template <typename T> __device__ __forceinline__ T to_pass(double v);
+template <> __device__ __forceinline__ float to_pass<float>(double v) { return f32_of(v); }
+template <> __device__ __forceinline__ double to_pass<double>(double v) { return v; }
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(double v) { return f32_of(v); }
 
 // ------------------------------------------------------- forward input modes
 // All take 0-based interior coordinates (i0,j0,k0) and return the RHS value.
@@ -159,7 +168,7 @@ struct OutHalo {  // p(i,j,k) = v * scale   (scale applied in the arithmetic typ
   Geo g;
   __device__ void operator()(int i0, int j0, int k0, double v) const { p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = v * scale; }
   __device__ void operator()(int i0, int j0, int k0, float v) const {
-    p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = (double)(v * (float)scale);
+    p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = f64_of(v * f32_of(scale));
   }
 };
 struct OutHaloAdd {  // p(i,j,k) += v * scale  (iterative-refinement update, accumulated in FP64)
@@ -169,7 +178,7 @@ struct OutHaloAdd {  // p(i,j,k) += v * scale  (iterative-refinement update, acc
   Geo g;
   __device__ void operator()(int i0, int j0, int k0, double v) const { p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] += v * scale; }
   __device__ void operator()(int i0, int j0, int k0, float v) const {
-    p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] += (double)(v * (float)scale);
+    p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] += f64_of(v * f32_of(scale));
   }
 };
 
@@ -177,6 +186,8 @@ struct OutHaloAdd {  // p(i,j,k) += v * scale  (iterative-refinement update, acc
 template <typename T> FG_HD size_t align_up(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // Row-batch geometry for the x pass: M rows (even) of length nx, pitch P.
+// The FP32 transform kernels are held to 128 registers (two 256-thread CTAs
+// per SM, no spills); the FP64 ones keep up to 255 (they spill at 128).
 FG_HD int xpitch(int nx) { return nx + 1; }
 
 // ===========================================================================
@@ -229,8 +240,9 @@ __device__ __forceinline__ void xfwd_tile(const AxisPlan &ax, const In &in, T *S
     const int m = idx / nx, x = idx % nx;
     const long r = row0 + m;
     T v = (T)0;
-    if (r < rows) v = (T)in(x, (int)(r % g.ny), (int)(r / g.ny));
-    ss = fma((float)v, (float)v, ss);
+    if (r < rows) v = to_pass<T>(in(x, (int)(r % g.ny), (int)(r / g.ny)));
+    const float vf = to_f32(v);
+    ss = fmaf(vf, vf, ss);
     A[m * P + x] = v;
   }
   __syncthreads();
@@ -250,7 +262,7 @@ __device__ __forceinline__ void xfwd_tile(const AxisPlan &ax, const In &in, T *S
 }
 
 template <typename T, typename In>
-__global__ void __launch_bounds__(256) k_xfwd(AxisPlan ax, In in, T *S, Geo g, int M, double *nrm) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xfwd(AxisPlan ax, In in, T *S, Geo g, int M, double *nrm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const long rows = (long)g.ny * g.nz;
   float ss = 0.0f;  // sum of squares for convergence checks (FP32 per thread)
@@ -306,7 +318,7 @@ __device__ __forceinline__ void xinv_tile(const AxisPlan &ax, const T *S, const 
 }
 
 template <typename T, typename Out>
-__global__ void __launch_bounds__(256) k_xinv(AxisPlan ax, const T *S, Out out, Geo g, int M) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xinv(AxisPlan ax, const T *S, Out out, Geo g, int M) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const long rows = (long)g.ny * g.nz;
   for (long row0 = (long)blockIdx.x * M; row0 < rows; row0 += (long)gridDim.x * M)
@@ -371,7 +383,7 @@ __device__ __forceinline__ void ypass_tile(const AxisPlan &ay, T *S, const Geo &
 }
 
 template <typename T, bool BACKWARD>
-__global__ void __launch_bounds__(256) k_ypass(AxisPlan ay, T *S, Geo g, int W) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_ypass(AxisPlan ay, T *S, Geo g, int W) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const long ntiles = (long)((g.nx + W - 1) / W) * g.nz;
   for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) ypass_tile<T, BACKWARD>(ay, S, g, W, tile, smem_raw);
@@ -427,8 +439,9 @@ __global__ void __launch_bounds__(512) k_xyfwd_plane(AxisPlan ax, AxisPlan ay, I
   for (int k = blockIdx.x; k < g.nz; k += gridDim.x) {
     for (int idx = tid; idx < nx * ny; idx += nth) {
       const int y = idx / nx, x = idx % nx;
-      const T v = (T)in(x, y, k);
-      ss = fma((float)v, (float)v, ss);
+      const T v = to_pass<T>(in(x, y, k));
+      const float vf = to_f32(v);
+      ss = fmaf(vf, vf, ss);
       A[y * P + x] = v;
     }
     __syncthreads();
@@ -716,6 +729,7 @@ struct PresTwArgs {
   const double *zA, *zB;  // per level k: f_t12*dzci(k)*f2/rho0 and 2*f_t12*dzci(k)
   double xA, xB, yA, yB;  // the same with dxi, dyi
   double f2;
+  float xA32, xB32, yA32, yB32, f2_32;  // FP32 copies for the mixed path
   int fp32;               // 1: increment evaluated in FP32 from FP64 differences (mixed path)
   Geo g;
 };
@@ -728,23 +742,25 @@ __device__ __forceinline__ double df_incr(double dp, double dq, double rs, doubl
   const double dg = fma(f2, t, dp);
   return fma(A, t, -B * (rcp64_1(rs) * dg));
 }
-// FP32 increment from FP64 differences: the differences of p and pold (which
-// cancel) are taken in FP64, the rest (relative error ~1e-7 of an increment
-// that is itself small against u) in FP32; the update u += delta stays FP64.
+// FP32 increment (mixed path): the differences of p and of pold, which cancel,
+// are taken in FP64; the rest of the Dodd-Ferrante increment (relative error
+// ~1e-7 of a term that is itself small against u) in FP32; the update
+// u += delta stays FP64.  Only the differences and the update use the FP64 pipe.
 __device__ __forceinline__ double df_incr32(double dp64, double dq64, float rs, float A, float B, float f2) {
-  const float dp = (float)dp64, t = (float)(dp64 - dq64);
+  const float dp = f32_of(dp64), t = dp - f32_of(dq64);
   const float dg = fmaf(f2, t, dp);
-  return (double)fmaf(A, t, -B * (__frcp_rn(rs) * dg));
+  return f64_of(fmaf(A, t, -B * (__frcp_rn(rs) * dg)));
 }
 __device__ __forceinline__ void pres_tw_cell32(const PresTwArgs &a, int i, int j, int k) {
   const Geo &g = a.g;
   const long c0 = g.pidx(i, j, k), cx = c0 + 1, cy = c0 + (g.nx + 2), cz = c0 + (long)(g.nx + 2) * (g.ny + 2);
   const double p0 = a.p[c0], q0 = a.pold[c0];
-  const float r0 = (float)a.rho[c0], f2 = (float)a.f2;
+  const float r0 = f32_of(a.rho[c0]);
   const long ui = g.uidx(i, j, k);
-  a.u[ui] += df_incr32(a.p[cx] - p0, a.pold[cx] - q0, (float)a.rho[cx] + r0, (float)a.xA, (float)a.xB, f2);
-  a.v[ui] += df_incr32(a.p[cy] - p0, a.pold[cy] - q0, (float)a.rho[cy] + r0, (float)a.yA, (float)a.yB, f2);
-  a.w[ui] += df_incr32(a.p[cz] - p0, a.pold[cz] - q0, (float)a.rho[cz] + r0, (float)a.zA[k], (float)a.zB[k], f2);
+  a.u[ui] += df_incr32(a.p[cx] - p0, a.pold[cx] - q0, f32_of(a.rho[cx]) + r0, a.xA32, a.xB32, a.f2_32);
+  a.v[ui] += df_incr32(a.p[cy] - p0, a.pold[cy] - q0, f32_of(a.rho[cy]) + r0, a.yA32, a.yB32, a.f2_32);
+  a.w[ui] += df_incr32(a.p[cz] - p0, a.pold[cz] - q0, f32_of(a.rho[cz]) + r0, f32_of(a.zA[k]), f32_of(a.zB[k]),
+                       a.f2_32);
 }
 __device__ __forceinline__ void pres_tw_cell(const PresTwArgs &a, int i, int j, int k) {
   const Geo &g = a.g;
@@ -1331,7 +1347,7 @@ __device__ __forceinline__ void cluster_gather_rows(cg::cluster_group &cluster, 
 }
 
 template <typename T, typename In>
-__global__ void __launch_bounds__(256, 2) k_xyfwd_cluster(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xyfwd_cluster(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
@@ -1349,8 +1365,9 @@ __global__ void __launch_bounds__(256, 2) k_xyfwd_cluster(AxisPlan ax, AxisPlan 
     const int y0 = r * cp.rows;
     for (int idx = tid; idx < cp.rows * g.nx; idx += nth) {
       const int ly = idx / g.nx, x = idx % g.nx;
-      const T v = (T)in(x, y0 + ly, k);
-      ss = fma((float)v, (float)v, ss);
+      const T v = to_pass<T>(in(x, y0 + ly, k));
+      const float vf = to_f32(v);
+      ss = fmaf(vf, vf, ss);
       B0[ly * cp.P + x] = v;
     }
     __syncthreads();
@@ -1377,7 +1394,7 @@ __global__ void __launch_bounds__(256, 2) k_xyfwd_cluster(AxisPlan ax, AxisPlan 
 }
 
 template <typename T, typename Out>
-__global__ void __launch_bounds__(256, 2) k_xyinv_cluster(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xyinv_cluster(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();

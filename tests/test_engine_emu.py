@@ -56,3 +56,39 @@ def test_passes_match_oracle(emu, oracle, dbl, pair):
                 tol = 1e-14 if dbl else 4e-6
                 err = np.abs(got - ref).max() / np.abs(ref).max()
                 assert err <= tol, (n, cols, bwd, err)
+
+
+def _trunc_f32(x):
+    """FP32 value of x with the mantissa truncated toward zero (numpy reference)."""
+    b = x.view(np.uint64) & ~np.uint64((1 << 29) - 1)
+    with np.errstate(over="ignore"):
+        t = b.view(np.float64).astype(np.float32)
+    return np.where(np.abs(x) < 2.0 ** -126, np.copysign(np.float32(0), x).astype(np.float32), t)
+
+
+def test_bit_conversions(emu):
+    """f32_of / f64_of (bits.cuh), the integer-ALU conversions of the FP32 Dodd-Ferrante path."""
+    dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+    fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+    emu.fg_emu_f32_of.argtypes = [dp, fp, C.c_long]
+    emu.fg_emu_f64_of.argtypes = [fp, dp, C.c_long]
+    rng = np.random.default_rng(5)
+    x = np.concatenate([rng.standard_normal(4000) * 10.0 ** rng.integers(-30, 30, 4000),
+                        np.array([0.0, -0.0, 1.0, -1.0, 3.0e38, -3.0e38, 1.5e-38, 2.0 ** -126, 2.0 ** -127])])
+    y = np.empty(len(x), np.float32)
+    emu.fg_emu_f32_of(x, y, len(x))
+    assert np.array_equal(y.view(np.uint32), _trunc_f32(x).view(np.uint32))
+    nrm = np.abs(x) >= 2.0 ** -126
+    assert np.all(np.abs(y[nrm] - x[nrm]) <= np.abs(x[nrm]) * 2.0 ** -23)
+    # out of range: below 2^-126 -> signed zero, above FP32 max -> inf, NaN stays NaN
+    z = np.array([1e-40, -1e-300, 1e39, -1e300, np.inf, -np.inf, np.nan])
+    w = np.empty(len(z), np.float32)
+    emu.fg_emu_f32_of(z, w, len(z))
+    assert w[0] == 0.0 and np.signbit(w[1]) and w[1] == 0.0
+    assert w[2] == np.inf and w[3] == -np.inf and w[4] == np.inf and w[5] == -np.inf and np.isnan(w[6])
+    f = np.concatenate([y[np.isfinite(y)], np.array([np.inf, -np.inf, np.nan], np.float32)])
+    d = np.empty(len(f), np.float64)
+    emu.fg_emu_f64_of(np.ascontiguousarray(f), d, len(f))
+    normal = (np.abs(f) >= 2.0 ** -126) | (f == 0) | ~np.isfinite(f)
+    ok = np.isnan(f) & np.isnan(d) | (f.astype(np.float64) == d)
+    assert np.all(ok[normal])

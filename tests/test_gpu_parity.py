@@ -47,8 +47,8 @@ CASES = [
     ((48, 16, 8), "PPDDDN", 0.5),
     ((16, 12, 16), "NNNNPP", 0.0),
     ((18, 14, 7), "DNNDNN", 1.0),
-    ((128, 128, 12), "PPPPNN", 0.0),   # fused plane path in FP32, separate passes in FP64
-    ((256, 64, 6), "NNPPNN", 1.5),     # FP64 plane too large: separate x and y passes
+    ((128, 128, 12), "PPPPNN", 0.0),   # fused plane path in FP32, cluster path in FP64
+    ((256, 64, 6), "NNPPNN", 1.5),     # planes larger than one CTA: cluster path
     ((176, 144, 5), "PPNNDD", 0.0),    # radices 11, 9
 ]
 
@@ -204,7 +204,7 @@ def test_gpu_mixed_precision_refinement(lib, oracle, n, cbc, gr, tol):
 
 # z-planes larger than one CTA's shared memory: the x and y transforms of a
 # plane run in a thread-block cluster that exchanges the plane through
-# distributed shared memory (xy path 2); 320x192 needs 16 CTAs in FP64.
+# distributed shared memory (xy path 2), 4 to 8 CTAs per cluster here.
 LARGE_PLANES = [((256, 256, 4), "PPPPNN", 0.0), ((320, 192, 6), "NNPPDD", 1.0),
                 ((256, 128, 5), "DDNNPP", 0.0), ((192, 256, 3), "NDPPNN", 0.5)]
 
