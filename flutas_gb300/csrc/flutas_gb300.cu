@@ -39,6 +39,14 @@ int fail(int code, const char *fmt, ...) {
   return code;
 }
 
+}  // namespace
+
+// Sets the calling thread's error text (the server hands a worker's message to
+// the thread that waits for the request).  Library-internal.
+void fg_set_error_text(const char *msg) { g_err = msg ? msg : ""; }
+
+namespace {
+
 #define CK(call)                                                                                  \
   do {                                                                                            \
     cudaError_t e_ = (call);                                                                      \
@@ -175,8 +183,32 @@ int max_smem_optin() {
   return v;
 }
 
+// The dynamic shared-memory limit of a kernel belongs to the function and is
+// shared by every host thread and plan: it is raised once per device, to the
+// device maximum, under a lock.  (Setting it to each launch's own size raced:
+// a thread launching a large plan could find the limit lowered by another.)
+int allow_smem_fn(const void *kernel, bool nonportable_cluster) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, bool> done;
+  std::lock_guard<std::mutex> lk(mu);
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  const auto key = std::make_pair(kernel, dev);
+  if (done.count(key)) return 0;
+  cudaFuncAttributes fa;
+  CK(cudaFuncGetAttributes(&fa, kernel));  // static shared memory counts against the same limit
+  CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          max_smem_optin() - (int)fa.sharedSizeBytes));
+  if (nonportable_cluster) CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  done[key] = true;
+  return 0;
+}
+template <typename K> int allow_smem(K kernel, bool nonportable_cluster = false) {
+  return allow_smem_fn((const void *)kernel, nonportable_cluster);
+}
+
 template <typename K> int grid_for(K kernel, int threads, size_t smem, long work_items) {
-  CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  TRY(allow_smem(kernel));
   int per_sm = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
   if (per_sm < 1) return fail(FLUTAS_EUNSUPPORTED, "kernel does not fit on an SM (smem %zu)", smem);
@@ -329,9 +361,9 @@ template <typename T> int cluster_size_for(int nx, int ny, int smax) {
 }
 
 template <typename K> int cluster_prepare(K kernel, size_t smem, int C) {
-  CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if (C > 8) CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-  return 0;
+  (void)smem;
+  (void)C;
+  return allow_smem(kernel, true);
 }
 
 template <typename K, typename... Args>
@@ -499,7 +531,7 @@ int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const doub
     const int nch = (za.nn + CH - 1) / CH;
     const size_t sm = sizeof(T) * (size_t)nch * nt;
     if ((int)sm > max_smem_optin()) return fail(FLUTAS_EUNSUPPORTED, "nz=%d too large for the z kernel", za.nz);
-    CK(cudaFuncSetAttribute(k_zstream<T, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    TRY(allow_smem(k_zstream<T, CH>));
     // launch in column batches whose eliminated values (one column of T per
     // column) stay L2-resident between the two sweeps
     const long per_batch = std::max<long>(nt, (long)(80.0e6 / (sizeof(T) * (double)za.nn)) / nt * nt);
@@ -1932,8 +1964,7 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
   if ((g1 = grid_for(kb_xfwd, 256, bt->smem_x, pre[ngrids])) < 0) return bail(g1);
   if ((g2 = grid_for(kb_ypass<false>, 256, bt->smem_y, pre[2 * ngrids + 1])) < 0) return bail(g2);
   if ((g3 = grid_for(kb_z, 128, bt->smem_z, pre[3 * ngrids + 2])) < 0) return bail(g3);
-  CK(cudaFuncSetAttribute(kb_xinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem_x));
-  CK(cudaFuncSetAttribute(kb_ypass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem_y));
+  if ((rc = allow_smem(kb_xinv)) || (rc = allow_smem(kb_ypass<true>))) return bail(rc);
   bt->grid_x = g1;
   bt->grid_y = g2;
   bt->grid_z = g3;

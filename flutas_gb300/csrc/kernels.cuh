@@ -73,6 +73,7 @@ struct InHalo {  // p(1:nx,1:ny,1:nz) of a halo-1 array
   const double *p;
   Geo g;
   __device__ double operator()(int i0, int j0, int k0) const { return p[g.pidx(i0 + 1, j0 + 1, k0 + 1)]; }
+  __device__ void keep(int, int, int, double) const {}
 };
 
 struct InPlain {  // contiguous (nx,ny,nz) FP64 array
@@ -80,6 +81,7 @@ struct InPlain {  // contiguous (nx,ny,nz) FP64 array
   const double *f;
   Geo g;
   __device__ double operator()(int i0, int j0, int k0) const { return f[g.sidx(i0, j0, k0)]; }
+  __device__ void keep(int, int, int, double) const {}
 };
 
 // fillps (src/fillps.f90:50-57) + optional updt_rhs_b (src/bound.f90:829-944).
@@ -110,6 +112,7 @@ struct InFillps {
     }
     return val;
   }
+  __device__ void keep(int, int, int, double) const {}
 };
 
 // FP64 residual r = f - A x of the cell-centred 7-point operator that the
@@ -144,20 +147,19 @@ struct InResidual {
     ax = fma(czp, pt, fma(czm, pb, fma(cc, pc, ax)));
     return f[c] - ax;
   }
+  __device__ void keep(int, int, int, double) const {}
 };
 
 // Wrapper: evaluates the inner RHS functor and keeps an FP64 copy of it in the
 // interior of a halo-1 array (the RHS the mixed-precision residual needs).
+// The loaders call keep() after the evaluations of a batch of cells.
 template <typename Inner> struct InKeep {
   static constexpr const char *tag = Inner::keep_tag;
   Inner inner;
-  double *keep;
-  Geo g;  // halo-1 geometry of keep
-  __device__ double operator()(int i0, int j0, int k0) const {
-    const double v = inner(i0, j0, k0);
-    keep[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = v;
-    return v;
-  }
+  double *kept;
+  Geo g;  // halo-1 geometry of kept
+  __device__ double operator()(int i0, int j0, int k0) const { return inner(i0, j0, k0); }
+  __device__ void keep(int i0, int j0, int k0, double v) const { kept[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = v; }
 };
 
 // ------------------------------------------------------ inverse output modes
@@ -170,6 +172,9 @@ struct OutHalo {  // p(i,j,k) = v * scale   (scale applied in the arithmetic typ
   __device__ void operator()(int i0, int j0, int k0, float v) const {
     p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = f64_of(v * f32_of(scale));
   }
+  __device__ double pre(int, int, int) const { return 0.0; }
+  __device__ void put(int i0, int j0, int k0, double, double v) const { (*this)(i0, j0, k0, v); }
+  __device__ void put(int i0, int j0, int k0, double, float v) const { (*this)(i0, j0, k0, v); }
 };
 struct OutHaloAdd {  // p(i,j,k) += v * scale  (iterative-refinement update, accumulated in FP64)
   static constexpr const char *tag = "haloadd";
@@ -180,7 +185,72 @@ struct OutHaloAdd {  // p(i,j,k) += v * scale  (iterative-refinement update, acc
   __device__ void operator()(int i0, int j0, int k0, float v) const {
     p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] += f64_of(v * f32_of(scale));
   }
+  __device__ double pre(int i0, int j0, int k0) const { return p[g.pidx(i0 + 1, j0 + 1, k0 + 1)]; }
+  __device__ void put(int i0, int j0, int k0, double old, double v) const {
+    p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = old + v * scale;
+  }
+  __device__ void put(int i0, int j0, int k0, double old, float v) const {
+    p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = old + f64_of(v * f32_of(scale));
+  }
 };
+
+// ---------------------------------------------------------------------------
+// Batched global loads and stores of the transform kernels.  Each thread
+// evaluates BATCH_U cells before it stores any of them, so that the loads of
+// BATCH_U cells are in flight together: a store between two evaluations would
+// keep the compiler from hoisting the later loads (it cannot prove that they do
+// not alias the store).  coord(idx, x, y, k) maps a slab index to 0-based
+// interior coordinates and returns false for padding entries.
+// ---------------------------------------------------------------------------
+constexpr int BATCH_U = 4;
+
+template <typename T, typename In, typename Coord, typename Dst>
+__device__ __forceinline__ void load_cells(const In &in, int tot, const Coord &coord, const Dst &dst, float &ss) {
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int b = tid; b < tot; b += BATCH_U * nth) {
+    double v[BATCH_U];
+    int xs[BATCH_U], ys[BATCH_U], ks[BATCH_U];
+    bool ok[BATCH_U];
+#pragma unroll
+    for (int u = 0; u < BATCH_U; u++) {
+      const int idx = b + u * nth;
+      ok[u] = idx < tot && coord(idx, xs[u], ys[u], ks[u]);
+      v[u] = ok[u] ? in(xs[u], ys[u], ks[u]) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < BATCH_U; u++) {
+      const int idx = b + u * nth;
+      if (idx < tot) {
+        if (ok[u]) in.keep(xs[u], ys[u], ks[u], v[u]);
+        const T t = to_pass<T>(v[u]);
+        const float f = to_f32(t);
+        ss = fmaf(f, f, ss);
+        dst(idx, t);
+      }
+    }
+  }
+}
+
+template <typename T, typename Out, typename Coord, typename Src>
+__device__ __forceinline__ void store_cells(const Out &out, int tot, const Coord &coord, const Src &src) {
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int b = tid; b < tot; b += BATCH_U * nth) {
+    double old[BATCH_U];
+    int xs[BATCH_U], ys[BATCH_U], ks[BATCH_U];
+    bool ok[BATCH_U];
+#pragma unroll
+    for (int u = 0; u < BATCH_U; u++) {
+      const int idx = b + u * nth;
+      ok[u] = idx < tot && coord(idx, xs[u], ys[u], ks[u]);
+      old[u] = ok[u] ? out.pre(xs[u], ys[u], ks[u]) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < BATCH_U; u++) {
+      const int idx = b + u * nth;
+      if (ok[u]) out.put(xs[u], ys[u], ks[u], old[u], (T)src(idx));
+    }
+  }
+}
 
 // ---------------------------------------------------------------- smem sizes
 template <typename T> FG_HD size_t align_up(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -207,6 +277,17 @@ struct StoreRowsS {  // store into S rows: line l of this batch -> global row ro
     const long r = row0 + c;
     if (r < rows) S[r * nx + t] = v;
   }
+};
+
+template <typename T>
+struct StorePlaneReal {  // write real plane (row-major y*pitch + x)
+  T *R;
+  int pitch, rowbase;  // line l = row rowbase + l for x lines
+  __device__ void pair(int c, int t, T v0, T v1) {
+    R[(long)(2 * c) * pitch + t] = v0;
+    R[(long)(2 * c + 1) * pitch + t] = v1;
+  }
+  __device__ void single(int c, int t, T v) { R[(long)c * pitch + t] = v; }
 };
 
 // Block sum of v, added atomically to *acc (all threads of the block call it).
@@ -236,14 +317,19 @@ __device__ __forceinline__ void xfwd_tile(const AxisPlan &ax, const In &in, T *S
   const long rows = (long)g.ny * g.nz;
   const int tid = threadIdx.x, nth = blockDim.x;
   const int B = cbatch(ax.pair, M);
-  for (int idx = tid; idx < M * nx; idx += nth) {
-    const int m = idx / nx, x = idx % nx;
-    const long r = row0 + m;
-    T v = (T)0;
-    if (r < rows) v = to_pass<T>(in(x, (int)(r % g.ny), (int)(r / g.ny)));
-    const float vf = to_f32(v);
-    ss = fmaf(vf, vf, ss);
-    A[m * P + x] = v;
+  {
+    const FastDiv fnx(nx), fny(g.ny);
+    const int r0 = (int)row0, nrows = (int)rows;  // ny*nz < 2^31
+    load_cells<T>(
+        in, M * nx,
+        [&](int idx, int &x, int &y, int &k) -> bool {
+          const int m = fnx.div(idx), r = r0 + m;
+          x = idx - m * nx;
+          k = fny.div(r);
+          y = r - k * g.ny;
+          return r < nrows;
+        },
+        [&](int idx, T t) { A[idx + fnx.div(idx)] = t; }, ss);
   }
   __syncthreads();
   pre_fwd<T>(ax, A, P, 1, M, C1, B, tid, nth);
@@ -272,17 +358,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xfwd(AxisPlan a
 }
 
 // x pass (inverse): spectral rows -> output functor, times normfft
-template <typename T, typename Out>
-struct StoreRowsOut {
-  Out out;
-  long row0, rows;
-  int ny;
-  __device__ void put(long r, int t, T v) {
-    if (r < rows) out(t, (int)(r % ny), (int)(r / ny), v);
-  }
-  __device__ void pair(int c, int t, T v0, T v1) { put(row0 + 2 * c, t, v0); put(row0 + 2 * c + 1, t, v1); }
-  __device__ void single(int c, int t, T v) { put(row0 + c, t, v); }
-};
 
 template <typename T, typename Out>
 __device__ __forceinline__ void xinv_tile(const AxisPlan &ax, const T *S, const Out &out, const Geo &g, int M,
@@ -312,8 +387,26 @@ __device__ __forceinline__ void xinv_tile(const AxisPlan &ax, const T *S, const 
     C2<T> *t = cur; cur = nxt; nxt = t;
     __syncthreads();
   }
-  StoreRowsOut<T, Out> st{out, row0, rows, g.ny};
-  post_bwd<T>(ax, cur, B, M, st, tid, nth);
+  // real rows into the free buffer, then the batched epilogue
+  T *R = (cur == C1) ? A : (T *)C1;
+  const int PR = (cur == C1) ? P : nx;
+  StorePlaneReal<T> sr{R, PR, 0};
+  post_bwd<T>(ax, cur, B, M, sr, tid, nth);
+  __syncthreads();
+  {
+    const FastDiv fnx(nx), fny(g.ny);
+    const int r0 = (int)row0, nrows = (int)rows;
+    store_cells<T>(
+        out, M * nx,
+        [&](int idx, int &x, int &y, int &k) -> bool {
+          const int m = fnx.div(idx), r = r0 + m;
+          x = idx - m * nx;
+          k = fny.div(r);
+          y = r - k * g.ny;
+          return r < nrows;
+        },
+        [&](int idx) { const int m = fnx.div(idx); return R[m * PR + (idx - m * nx)]; });
+  }
   __syncthreads();
 }
 
@@ -396,16 +489,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_ypass(AxisPlan 
 // Shared memory: two buffers of nx*ny reals (plus row padding of the first).
 // ===========================================================================
 template <typename T>
-struct StorePlaneReal {  // write real plane (row-major y*pitch + x)
-  T *R;
-  int pitch, rowbase;  // line l = row rowbase + l for x lines
-  __device__ void pair(int c, int t, T v0, T v1) {
-    R[(long)(2 * c) * pitch + t] = v0;
-    R[(long)(2 * c + 1) * pitch + t] = v1;
-  }
-  __device__ void single(int c, int t, T v) { R[(long)c * pitch + t] = v; }
-};
-template <typename T>
 struct StorePlaneRealCols {  // columns as lines: line l = column l, position t = row
   T *R;
   int pitch;
@@ -436,14 +519,17 @@ __global__ void __launch_bounds__(512) k_xyfwd_plane(AxisPlan ax, AxisPlan ay, I
   T *Bu = (T *)(smem_raw + align_up<T>(sizeof(T) * (size_t)ny * P));  // nx*ny reals
   const int tid = threadIdx.x, nth = blockDim.x;
   float ss = 0.0f;  // sum of squares for convergence checks (FP32 per thread)
+  const FastDiv fnx(nx);
   for (int k = blockIdx.x; k < g.nz; k += gridDim.x) {
-    for (int idx = tid; idx < nx * ny; idx += nth) {
-      const int y = idx / nx, x = idx % nx;
-      const T v = to_pass<T>(in(x, y, k));
-      const float vf = to_f32(v);
-      ss = fmaf(vf, vf, ss);
-      A[y * P + x] = v;
-    }
+    load_cells<T>(
+        in, nx * ny,
+        [&](int idx, int &x, int &y, int &kk) -> bool {
+          y = fnx.div(idx);
+          x = idx - y * nx;
+          kk = k;
+          return true;
+        },
+        [&](int idx, T t) { A[idx + fnx.div(idx)] = t; }, ss);
     __syncthreads();
     // ---- x transform: lines = rows of A
     const int Bx = cbatch(ax.pair, ny);
@@ -501,8 +587,22 @@ __global__ void __launch_bounds__(512) k_xyinv_plane(AxisPlan ax, AxisPlan ay, c
     __syncthreads();
     C2<T> *fx = invx ? run_stages<T, true>(ax, F, (C2<T> *)G, Bx, tid, nth)
                      : run_stages<T, false>(ax, F, (C2<T> *)G, Bx, tid, nth);
-    StoreRowsOut<T, Out> st{out, (long)k * ny, (long)(k + 1) * ny, ny};
-    post_bwd<T>(ax, fx, Bx, ny, st, tid, nth);
+    // real plane into the free buffer, then the batched epilogue
+    T *R = (fx == F) ? G : (T *)F;
+    const int PR = (R == A) ? P : nx;
+    StorePlaneReal<T> sr{R, PR, 0};
+    post_bwd<T>(ax, fx, Bx, ny, sr, tid, nth);
+    __syncthreads();
+    const FastDiv fnx(nx);
+    store_cells<T>(
+        out, nx * ny,
+        [&](int idx, int &x, int &y, int &kk) -> bool {
+          y = fnx.div(idx);
+          x = idx - y * nx;
+          kk = k;
+          return true;
+        },
+        [&](int idx) { const int y = fnx.div(idx); return R[y * PR + (idx - y * nx)]; });
     __syncthreads();
   }
 }
@@ -1312,36 +1412,60 @@ struct StoreColBlock {  // y-phase lines = columns of the local column block (ro
   __device__ void single(int c, int t, T v) { R[(long)t * pitch + c] = v; }
 };
 
+// Gathers through distributed shared memory, GATHER_U remote loads in flight
+// per thread before the local stores of a batch.
+constexpr int GATHER_U = 8;
+
 // x-spectrum rows (slab of each CTA, pitch gp, in buffer `slab`) -> this CTA's
-// column block (ny x cols, row-major) in `blk`.
+// column block (ny x cols, row-major) in `blk`.  Element idx of the block is row
+// gl = idx / cols (= s*rows + lr: row lr of CTA s), column x0 + idx % cols.
 template <typename T>
 __device__ __forceinline__ void cluster_gather_cols(cg::cluster_group &cluster, const ClusterPlane<T> &cp, T *slab,
                                                     int gp, T *blk) {
-  const int r = (int)cluster.block_rank();
-  const int tid = threadIdx.x, nth = blockDim.x;
-  const int x0 = r * cp.cols;
-  for (int s = 0; s < cp.C; s++) {
-    const T *rem = cluster.map_shared_rank(slab, s);
-    const int tot = cp.rows * cp.cols;
-    for (int idx = tid; idx < tot; idx += nth) {
-      const int lr = idx / cp.cols, xc = idx % cp.cols;
-      blk[(long)(s * cp.rows + lr) * cp.cols + xc] = rem[(long)lr * gp + x0 + xc];
+  const int x0 = (int)cluster.block_rank() * cp.cols;
+  const int tid = threadIdx.x, nth = blockDim.x, tot = cp.ny * cp.cols;
+  const FastDiv fc(cp.cols), fr(cp.rows);
+  for (int b = tid; b < tot; b += GATHER_U * nth) {
+    T v[GATHER_U];
+#pragma unroll
+    for (int u = 0; u < GATHER_U; u++) {
+      const int idx = b + u * nth;
+      if (idx < tot) {
+        const int gl = fc.div(idx), xc = idx - gl * cp.cols, s = fr.div(gl), lr = gl - s * cp.rows;
+        v[u] = cluster.map_shared_rank(slab, s)[lr * gp + x0 + xc];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < GATHER_U; u++) {
+      const int idx = b + u * nth;
+      if (idx < tot) blk[idx] = v[u];
     }
   }
 }
 
-// this CTA's column block (ny x cols) -> its row slab (rows x nx, pitch P) from every CTA's block.
+// this CTA's row slab (rows x nx, pitch P) from every CTA's column block (ny x
+// cols).  Element idx of the slab is row lr = idx / nx, column xg = idx % nx,
+// held by CTA s = xg / cols at (r*rows + lr, xg % cols).
 template <typename T>
 __device__ __forceinline__ void cluster_gather_rows(cg::cluster_group &cluster, const ClusterPlane<T> &cp, T *blk,
                                                     T *slab) {
   const int r = (int)cluster.block_rank();
-  const int tid = threadIdx.x, nth = blockDim.x;
-  for (int s = 0; s < cp.C; s++) {
-    const T *rem = cluster.map_shared_rank(blk, s);
-    const int tot = cp.rows * cp.cols;
-    for (int idx = tid; idx < tot; idx += nth) {
-      const int lr = idx / cp.cols, xc = idx % cp.cols;
-      slab[(long)lr * cp.P + s * cp.cols + xc] = rem[(long)(r * cp.rows + lr) * cp.cols + xc];
+  const int tid = threadIdx.x, nth = blockDim.x, tot = cp.rows * cp.nx;
+  const FastDiv fn(cp.nx), fc(cp.cols);
+  for (int b = tid; b < tot; b += GATHER_U * nth) {
+    T v[GATHER_U];
+#pragma unroll
+    for (int u = 0; u < GATHER_U; u++) {
+      const int idx = b + u * nth;
+      if (idx < tot) {
+        const int lr = fn.div(idx), xg = idx - lr * cp.nx, s = fc.div(xg), xc = xg - s * cp.cols;
+        v[u] = cluster.map_shared_rank(blk, s)[(r * cp.rows + lr) * cp.cols + xc];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < GATHER_U; u++) {
+      const int idx = b + u * nth;
+      if (idx < tot) slab[idx + fn.div(idx)] = v[u];  // lr*P + xg with P = nx + 1
     }
   }
 }
@@ -1359,17 +1483,21 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xyfwd_cluster(A
   const int tid = threadIdx.x, nth = blockDim.x;
   const int nclusters = gridDim.x / C;
   const int cid = blockIdx.x / C;
+  const FastDiv fnx(g.nx);
   float ss = 0.0f;
   for (int k = cid; k < g.nz; k += nclusters) {
     // ---- x transform of this CTA's rows
     const int y0 = r * cp.rows;
-    for (int idx = tid; idx < cp.rows * g.nx; idx += nth) {
-      const int ly = idx / g.nx, x = idx % g.nx;
-      const T v = to_pass<T>(in(x, y0 + ly, k));
-      const float vf = to_f32(v);
-      ss = fmaf(vf, vf, ss);
-      B0[ly * cp.P + x] = v;
-    }
+    load_cells<T>(
+        in, cp.rows * g.nx,
+        [&](int idx, int &x, int &y, int &kk) -> bool {
+          const int ly = fnx.div(idx);
+          x = idx - ly * g.nx;
+          y = y0 + ly;
+          kk = k;
+          return true;
+        },
+        [&](int idx, T t) { B0[idx + fnx.div(idx)] = t; }, ss);
     __syncthreads();
     const int Bx = cbatch(ax.pair, cp.rows);
     pre_fwd<T>(ax, B0, cp.P, 1, cp.rows, (C2<T> *)B1, Bx, tid, nth);
@@ -1407,6 +1535,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xyinv_cluster(A
   const bool invx = fft_inverse(ax.pair, true), invy = fft_inverse(ay.pair, true);
   const int nclusters = gridDim.x / C;
   const int cid = blockIdx.x / C;
+  const FastDiv fnx(g.nx);
   for (int k = cid; k < g.nz; k += nclusters) {
     // ---- y^-1 of this CTA's columns
     const T *Sp = S + (long)k * g.nx * g.ny + r * cp.cols;
@@ -1431,9 +1560,21 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xyinv_cluster(A
     __syncthreads();
     C2<T> *fx = invx ? run_stages<T, true>(ax, (C2<T> *)B1, (C2<T> *)B0, Bx, tid, nth)
                      : run_stages<T, false>(ax, (C2<T> *)B1, (C2<T> *)B0, Bx, tid, nth);
-    const long row0 = (long)k * g.ny + r * cp.rows;
-    StoreRowsOut<T, Out> st{out, row0, row0 + cp.rows, g.ny};
-    post_bwd<T>(ax, fx, Bx, cp.rows, st, tid, nth);
+    // real rows into B2 (free since the second cluster barrier), then the batched epilogue
+    StorePlaneReal<T> sr{B2, cp.P, 0};
+    post_bwd<T>(ax, fx, Bx, cp.rows, sr, tid, nth);
+    __syncthreads();
+    const int y0 = r * cp.rows;
+    store_cells<T>(
+        out, cp.rows * g.nx,
+        [&](int idx, int &x, int &y, int &kk) -> bool {
+          const int ly = fnx.div(idx);
+          x = idx - ly * g.nx;
+          y = y0 + ly;
+          kk = k;
+          return true;
+        },
+        [&](int idx) { return B2[idx + fnx.div(idx)]; });
     __syncthreads();
   }
 }

@@ -26,6 +26,8 @@
 #include <thread>
 #include <vector>
 
+void fg_set_error_text(const char *msg);  // flutas_gb300.cu
+
 namespace {
 
 using Clock = std::chrono::steady_clock;
@@ -380,6 +382,7 @@ int flutas_gb300_server_wait(void *srv, long long ticket, double *relres, int *i
   if (iters) *iters = q->iters;
   if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(q->t_done - q->t_submit).count();
   const int rc = q->rc;
+  if (rc) fg_set_error_text(q->err.c_str());
   s->reqs.erase(it);
   return rc;
 }

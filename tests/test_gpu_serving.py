@@ -39,9 +39,12 @@ def test_serving_results_match_alone(lib):
         o = np.zeros_like(r["rhs"])
         outs.append(o)
         tickets.append(S.submit_solve(r["n"], r["dli"], r["dzci"], r["dzfi"], r["cbc"], r["rhs"], o, tol=r["tol"]))
-    res = [S.wait(t) for t in tickets]
+    res, errs = [], []
+    for t in tickets:
+        res.append(S.wait(t))
+        errs.append(lib.last_error() if res[-1][0] else "")
     st = S.stats()
-    assert st["completed"] == len(reqs) and st["p99_ms"] >= st["p50_ms"] > 0
+    assert st["completed"] == len(reqs) and st["p99_ms"] >= st["p50_ms"] > 0, [(r[0], e) for r, e in zip(res, errs)]
     S.close()
     for r, o, (rc, rr, it, lat) in zip(reqs, outs, res):
         assert rc == 0 and rr <= r["tol"] and it >= 1 and lat > 0
