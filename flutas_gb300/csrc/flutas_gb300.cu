@@ -332,6 +332,7 @@ struct flutas_plan {
   bool pin_zero_mode = false;  // singular (lam == 0, z in N/N or P/P) column
   double last_relres = 0.0;    // relative residual / FP32 solves of the last mixed solve
   int last_iters = 0;
+  double contraction = 1e-3;   // residual reduction of one FP32 solve, last measured
 };
 
 namespace {
@@ -602,7 +603,10 @@ int solve_fp64_dev(flutas_plan *pl, double *p, const double *lam, const double *
 // accumulates ||f||^2; every later pass evaluates the FP64 residual
 // r = f - A x, accumulates ||r||^2 and transforms it.  x (halo 1) receives
 // the solution.  The norm of the residual decides on the host whether the
-// FP32 correction of that pass is applied.
+// FP32 correction of that pass is applied.  When the last measured reduction
+// per FP32 solve predicts that a check will end the solve (or the iteration
+// limit does), the check evaluates the residual norm alone (k_resnorm) and
+// the transform of the residual is made only if the prediction was wrong.
 template <typename First>
 int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, int max_iter, double *relres,
                     int *iters) {
@@ -628,21 +632,31 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
   memcpy(R.bc, pl->cbc, 6);
   R.g = g;
   int it = 1;
-  double rel = 0.0;
+  double rel = 0.0, before = 1.0;  // relative residual before the latest FP32 solve
   for (;;) {
+    const bool norm_only = it >= max_iter || before * pl->contraction <= 0.5 * tol;
     CK(cudaMemsetAsync(nrm + 1, 0, sizeof(double), st));
-    TRY(fwd_xy<float>(pl, R, S, pl->tx32, pl->ty32, pl->path32, nrm + 1));
+    if (norm_only) {
+      const int grid = grid_for(k_resnorm, 256, 0, ((long)g.nx * g.ny * g.nz + 1023) / 1024);
+      if (grid < 0) return grid;
+      TRY(launch("k_resnorm", st, [&] { k_resnorm<<<grid, 256, 0, st>>>(R, nrm + 1); }));
+    } else {
+      TRY(fwd_xy<float>(pl, R, S, pl->tx32, pl->ty32, pl->path32, nrm + 1));
+    }
     double h[2];
     CK(cudaMemcpyAsync(h, nrm, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (!std::isfinite(h[1]) || !std::isfinite(h[0]))
       return fail(FLUTAS_ENONFINITE, "non-finite residual in mixed solve");
     rel = h[0] > 0 ? std::sqrt(h[1] / h[0]) : std::sqrt(h[1]);
+    if (before > 0.0) pl->contraction = std::min(1.0, std::max(rel / before, 1e-12));
     if (rel <= tol || it >= max_iter) break;
+    if (norm_only) TRY(fwd_xy<float>(pl, R, S, pl->tx32, pl->ty32, pl->path32));  // prediction missed
     // correction of this pass: e = A^-1 r in FP32, x += e in FP64
     TRY(zsolve<float>(pl, S, lam, a, b, c, true));
     TRY(inv_xy<float>(pl, S, OutHaloAdd{x, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
     it++;
+    before = rel;
   }
   if (relres) *relres = rel;
   if (iters) *iters = it;

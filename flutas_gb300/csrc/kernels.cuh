@@ -305,6 +305,35 @@ __device__ __forceinline__ void block_sum_add(double v, double *acc) {
   }
 }
 
+// ||f - A x||^2 alone (FP32 sum of the FP32-truncated residual, as the fused
+// norms of the transform passes): the convergence check of a mixed solve whose
+// residual is not going to be transformed.  BATCH-style: four cells per thread
+// evaluated before any is accumulated.
+__global__ void __launch_bounds__(256) k_resnorm(InResidual R, double *nrm) {
+  const Geo &g = R.g;
+  const int tot = g.nx * g.ny * g.nz;  // < 2^31
+  const FastDiv fx(g.nx), fy(g.ny);
+  float ss = 0.0f;
+  for (int b = blockIdx.x * blockDim.x * 4 + threadIdx.x; b < tot; b += gridDim.x * blockDim.x * 4) {
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int idx = b + u * (int)blockDim.x;
+      v[u] = 0.0;
+      if (idx < tot) {
+        const int row = fx.div(idx), x = idx - row * g.nx, k = fy.div(row), y = row - k * g.ny;
+        v[u] = R(x, y, k);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const float f = f32_of(v[u]);
+      ss = fmaf(f, f, ss);
+    }
+  }
+  block_sum_add((double)ss, nrm);
+}
+
 // One tile of the x pass: M rows starting at global row row0 (row = j + ny*k).
 // smem: M*P reals + M*nx reals.  Accumulates the squares of the inputs in ss.
 template <typename T, typename In>

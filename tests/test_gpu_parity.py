@@ -292,3 +292,26 @@ def test_gpu_two_phase_projection_df(lib, oracle, precision):
     assert rel_l2(p - pold, po - pold, remove_mean=True) <= tol * 100
     tot, mx = lib.chkdiv(n, dxi, dyi, 16.0, 1, 1, dzfi, u, v, w)
     assert mx <= 1e-11 * dxi
+
+
+@pytest.mark.parametrize("n,cbc", [((64, 48, 32), "PPPPNN"), ((256, 256, 6), "NNPPDD")])
+def test_gpu_mixed_reported_residual(lib, oracle, n, cbc):
+    """The residual a mixed solve reports is the residual of the solution it returns.
+
+    An unattainable tolerance walks every branch of the refinement loop: full
+    residual passes, a norm-only check predicted to be the last, the transform
+    made after that prediction failed, and the final norm-only check at the
+    iteration limit."""
+    rng = np.random.default_rng(17)
+    P, dzci, dzfi, dzc, dzf, dli = plan_for(lib, n, cbc, 1.0)
+    f = compatible_rhs(rng, n, cbc, dzf)
+    for tol, max_iter in ((1e-6, 8), (1e-10, 8), (1e-15, 4)):
+        p = f.copy()
+        relres, iters = P.solve_mixed(p, tol=tol, max_iter=max_iter, allow_unconverged=True)
+        r = oracle.residual(n, cbc, dli[0], dli[1], 1, dzci, dzfi, f, p)
+        true = np.linalg.norm(r) / np.linalg.norm(f[1:-1, 1:-1, 1:-1])
+        # FP32 sums of FP32-truncated residuals: ~1e-5 relative; plus the FP64 rounding
+        # noise of two different evaluation orders of f - A x near the floor
+        assert abs(relres - true) <= 1e-3 * true + 1e-12, (tol, relres, true)
+        assert (relres <= tol) == (tol > 1e-14) and iters <= max_iter
+        assert relres <= max(tol, 1e-11)
