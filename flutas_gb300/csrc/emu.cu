@@ -10,6 +10,7 @@
 #include "axis_tables.cuh"
 #include "bits.cuh"
 #include "fft_engine.cuh"
+#include "fft_fixed.cuh"
 
 using namespace fg;
 
@@ -77,4 +78,52 @@ extern "C" __attribute__((visibility("default"))) void fg_emu_f32_of(const doubl
 }
 extern "C" __attribute__((visibility("default"))) void fg_emu_f64_of(const float *x, double *y, long n) {
   for (long i = 0; i < n; i++) y[i] = f64_of(x[i]);
+}
+
+namespace {
+
+template <typename T, int N, int PAIR, int M>
+int run_fixed(int backward, const double *in, double *out) {
+  constexpr int B = M / 2;
+  AxisPlan ap;
+  std::vector<C2<T>> W, Q;
+  if (fill_axis_tables<T>(N, PAIR, &ap, W, Q) != 0) return -1;
+  std::vector<T> R((size_t)M * N), O((size_t)M * N, (T)0);
+  for (size_t i = 0; i < R.size(); i++) R[i] = (T)in[i];
+  std::vector<C2<T>> b0((size_t)B * N), b1((size_t)B * N);
+  auto bar = [] {};
+  if (backward) {
+    fix::inverse<T, N, PAIR, B, 1>(R.data(), N, 1, O.data(), N, 1, b0.data(), b1.data(), W.data(), Q.data(), 0, bar);
+  } else {
+    HostStore<T> st{O.data(), N, 1};
+    fix::forward<T, N, PAIR, B, 1>(R.data(), N, 1, b0.data(), b1.data(), W.data(), Q.data(), st, 0, bar);
+  }
+  for (size_t i = 0; i < O.size(); i++) out[i] = (double)O[i];
+  return 0;
+}
+
+template <typename T, int N>
+int fixed_pairs(int pair, int backward, const double *in, double *out) {
+  switch (pair) {
+    case BC_PP: return run_fixed<T, N, BC_PP, 8>(backward, in, out);
+    case BC_NN: return run_fixed<T, N, BC_NN, 8>(backward, in, out);
+    case BC_DD: return run_fixed<T, N, BC_DD, 8>(backward, in, out);
+    default: return -1;
+  }
+}
+
+}  // namespace
+
+// The fixed-size passes (fft_fixed.cuh) on 8 real lines of length n (line l at
+// in[l*n + t]), n in {32, 64, 256, 512}, kinds PP/NN/DD.
+extern "C" __attribute__((visibility("default"))) int fg_emu_fixed(int dbl, int pair, int n, int backward,
+                                                                   const double *in, double *out) {
+#define FG_EMU_FIX(NN_)                                                                                  \
+  if (n == NN_) return dbl ? fixed_pairs<double, NN_>(pair, backward, in, out) : fixed_pairs<float, NN_>(pair, backward, in, out);
+  FG_EMU_FIX(32)
+  FG_EMU_FIX(64)
+  FG_EMU_FIX(256)
+  FG_EMU_FIX(512)
+#undef FG_EMU_FIX
+  return -1;
 }

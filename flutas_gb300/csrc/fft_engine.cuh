@@ -190,7 +190,7 @@ FG_HD void stage_pass(const C2<T> *in, C2<T> *out, int N, int B, int ldb, int Ns
     const int kk = fn.mod(j);
     C2<T> a[R];
 #pragma unroll
-    for (int r = 0; r < R; r++) a[r] = in[(long)(j + r * NR) * ldb + c];
+    for (int r = 0; r < R; r++) a[r] = in[(j + r * NR) * ldb + c];
     if (Ns > 1) {
 #pragma unroll
       for (int r = 1; r < R; r++) a[r] = cmul<T>(a[r], twid<T>(W, N, kk * r * tws, INV));
@@ -198,7 +198,7 @@ FG_HD void stage_pass(const C2<T> *in, C2<T> *out, int N, int B, int ldb, int Ns
     dft_any<T, R, INV>(a, W, N);
     const int idxD = (j - kk) * R + kk;
 #pragma unroll
-    for (int r = 0; r < R; r++) out[(long)(idxD + r * Ns) * ldb + c] = a[r];
+    for (int r = 0; r < R; r++) out[(idxD + r * Ns) * ldb + c] = a[r];
   }
 }
 
@@ -252,7 +252,7 @@ FG_HD bool paired(int pair) { return pair <= BC_DD; }
 
 // forward, real -> complex (before the FFT)
 template <typename T>
-FG_HD void pre_fwd(const AxisPlan &ap, const T *Rb, long ls, long es, int M, C2<T> *Cb, int ldb,
+FG_HD void pre_fwd(const AxisPlan &ap, const T *Rb, int ls, int es, int M, C2<T> *Cb, int ldb,
                    int tid, int nth) {
   const int n = ap.n;
   if (paired(ap.pair)) {
@@ -261,9 +261,9 @@ FG_HD void pre_fwd(const AxisPlan &ap, const T *Rb, long ls, long es, int M, C2<
     for (int idx = tid; idx < tot; idx += nth) {
       const int c = fb.mod(idx), m = fb.div(idx);
       const int src = ap.pair == BC_PP ? m : mperm(m, n);
-      T x0 = Rb[(2L * c) * ls + src * es], x1 = Rb[(2L * c + 1) * ls + src * es];
+      T x0 = Rb[(2 * c) * ls + src * es], x1 = Rb[(2 * c + 1) * ls + src * es];
       if (ap.pair == BC_DD && (src & 1)) { x0 = -x0; x1 = -x1; }
-      Cb[(long)m * ldb + c] = mk<T>(x0, x1);
+      Cb[m * ldb + c] = mk<T>(x0, x1);
     }
   } else {
     const int h = n / 2, tot = M * h;
@@ -272,10 +272,10 @@ FG_HD void pre_fwd(const AxisPlan &ap, const T *Rb, long ls, long es, int M, C2<
     const FastDiv fm(M);
     for (int idx = tid; idx < tot; idx += nth) {
       const int c = fm.mod(idx), j = fm.div(idx);
-      T xa = Rb[(long)c * ls + (2L * j) * es];
-      T xb = Rb[(long)c * ls + (long)(n - 1 - 2 * j) * es];
+      T xa = Rb[c * ls + (2L * j) * es];
+      T xb = Rb[c * ls + (n - 1 - 2 * j) * es];
       if (ap.pair == BC_DN) xb = sgn * xb;  // (-1)^(n-1-2j) = (-1)^(n-1)
-      Cb[(long)j * ldb + c] = cmul<T>(mk<T>(xa, xb), Q[j]);
+      Cb[j * ldb + c] = cmul<T>(mk<T>(xa, xb), Q[j]);
     }
   }
 }
@@ -294,8 +294,8 @@ FG_HD void post_fwd(const AxisPlan &ap, const C2<T> *F, int ldb, int M, Store &s
     const FastDiv fb(B);
     for (int idx = tid; idx < tot; idx += nth) {
       const int c = fb.mod(idx), k = fb.div(idx);
-      const C2<T> Zk = F[(long)k * ldb + c];
-      const C2<T> Zm = F[(long)((n - k) % n) * ldb + c];
+      const C2<T> Zk = F[k * ldb + c];
+      const C2<T> Zm = F[(k ? n - k : 0) * ldb + c];
       const T h = (T)0.5;
       C2<T> X0 = mk<T>(h * (Zk.x + Zm.x), h * (Zk.y - Zm.y));
       C2<T> X1 = mk<T>(h * (Zk.y + Zm.y), h * (Zm.x - Zk.x));
@@ -315,7 +315,7 @@ FG_HD void post_fwd(const AxisPlan &ap, const C2<T> *F, int ldb, int M, Store &s
     const FastDiv fm(M);
     for (int idx = tid; idx < tot; idx += nth) {
       const int c = fm.mod(idx), k = fm.div(idx);
-      C2<T> u = cmul<T>(F[(long)k * ldb + c], Q[k]);
+      C2<T> u = cmul<T>(F[k * ldb + c], Q[k]);
       if (ap.pair == BC_ND) {
         st.single(c, 2 * k, (T)2 * u.x);
         st.single(c, n - 1 - 2 * k, (T)-2 * u.y);
@@ -329,7 +329,7 @@ FG_HD void post_fwd(const AxisPlan &ap, const C2<T> *F, int ldb, int M, Store &s
 
 // backward, real spectral -> complex (before the inverse FFT)
 template <typename T>
-FG_HD void pre_bwd(const AxisPlan &ap, const T *Rb, long ls, long es, int M, C2<T> *Cb, int ldb,
+FG_HD void pre_bwd(const AxisPlan &ap, const T *Rb, int ls, int es, int M, C2<T> *Cb, int ldb,
                    int tid, int nth) {
   if (!paired(ap.pair)) { pre_fwd<T>(ap, Rb, ls, es, M, Cb, ldb, tid, nth); return; }
   const int n = ap.n, B = M / 2, tot = B * n;
@@ -337,31 +337,31 @@ FG_HD void pre_bwd(const AxisPlan &ap, const T *Rb, long ls, long es, int M, C2<
   const FastDiv fb(B);
   for (int idx = tid; idx < tot; idx += nth) {
     const int c = fb.mod(idx), k = fb.div(idx);
-    const T *r0 = Rb + (2L * c) * ls, *r1 = Rb + (2L * c + 1) * ls;
+    const T *r0 = Rb + (2 * c) * ls, *r1 = Rb + (2 * c + 1) * ls;
     C2<T> V0, V1;
     if (ap.pair == BC_PP) {
       if (k == 0 || 2 * k == n) {
         V0 = mk<T>(r0[k * es], (T)0); V1 = mk<T>(r1[k * es], (T)0);
       } else if (2 * k < n) {
-        V0 = mk<T>(r0[k * es], r0[(long)(n - k) * es]); V1 = mk<T>(r1[k * es], r1[(long)(n - k) * es]);
+        V0 = mk<T>(r0[k * es], r0[(n - k) * es]); V1 = mk<T>(r1[k * es], r1[(n - k) * es]);
       } else {
-        V0 = mk<T>(r0[(long)(n - k) * es], -r0[k * es]); V1 = mk<T>(r1[(long)(n - k) * es], -r1[k * es]);
+        V0 = mk<T>(r0[(n - k) * es], -r0[k * es]); V1 = mk<T>(r1[(n - k) * es], -r1[k * es]);
       }
     } else {
       T a0, b0, a1, b1;
       if (ap.pair == BC_NN) {
         a0 = r0[k * es]; a1 = r1[k * es];
-        b0 = k > 0 ? r0[(long)(n - k) * es] : (T)0; b1 = k > 0 ? r1[(long)(n - k) * es] : (T)0;
+        b0 = k > 0 ? r0[(n - k) * es] : (T)0; b1 = k > 0 ? r1[(n - k) * es] : (T)0;
       } else {  // DD: X~[k] = X[n-1-k]
-        a0 = r0[(long)(n - 1 - k) * es]; a1 = r1[(long)(n - 1 - k) * es];
-        b0 = k > 0 ? r0[(long)(k - 1) * es] : (T)0; b1 = k > 0 ? r1[(long)(k - 1) * es] : (T)0;
+        a0 = r0[(n - 1 - k) * es]; a1 = r1[(n - 1 - k) * es];
+        b0 = k > 0 ? r0[(k - 1) * es] : (T)0; b1 = k > 0 ? r1[(k - 1) * es] : (T)0;
       }
       const C2<T> q = Q[k];  // exp(-i pi k/2n); we need exp(+i ...) = conj
       // V = conj(q) * (a - i b)
       V0 = mk<T>(q.x * a0 - q.y * b0, -q.y * a0 - q.x * b0);
       V1 = mk<T>(q.x * a1 - q.y * b1, -q.y * a1 - q.x * b1);
     }
-    Cb[(long)k * ldb + c] = mk<T>(V0.x - V1.y, V0.y + V1.x);
+    Cb[k * ldb + c] = mk<T>(V0.x - V1.y, V0.y + V1.x);
   }
 }
 
@@ -373,7 +373,7 @@ FG_HD void post_bwd(const AxisPlan &ap, const C2<T> *F, int ldb, int M, Store &s
   const FastDiv fb(B);
   for (int idx = tid; idx < tot; idx += nth) {
     const int c = fb.mod(idx), m = fb.div(idx);
-    const C2<T> z = F[(long)m * ldb + c];
+    const C2<T> z = F[m * ldb + c];
     if (ap.pair == BC_PP) {
       st.pair(c, m, z.x, z.y);
     } else {

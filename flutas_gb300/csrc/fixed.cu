@@ -1,0 +1,290 @@
+// fixed.cu -- compile-time-sized cluster plane kernels.
+//
+// The x and y transforms of one z-plane, shared by a cluster of C CTAs as in
+// k_xyfwd_cluster / k_xyinv_cluster (kernels.cuh), with the plane size, the
+// cluster size and the BC pair kinds as template parameters, so that the
+// transforms use the fixed-size passes of fft_fixed.cuh (no run-time index
+// arithmetic, pre/post passes folded into the Stockham stages) and the
+// exchange through distributed shared memory has constant trip counts.
+// Twiddle and pre/post tables live in shared memory.
+#define FG_NO_PLAIN_KERNELS
+#include "fixed.h"
+#include "fft_fixed.cuh"
+
+#include <cstdlib>
+#include <mutex>
+#include <set>
+
+namespace fg {
+namespace {
+
+constexpr int FIX_NTH = 256;
+
+template <typename T, int N, int C> struct FixGeo {
+  static constexpr int ROWS = N / C, COLS = N / C, P = N + 1, BX = ROWS / 2, BY = COLS / 2;
+  static constexpr size_t A = (size_t)ROWS * P, BN = (size_t)N * COLS;
+  static constexpr size_t BUF = ((sizeof(T) * (A > BN ? A : BN)) + 255) & ~(size_t)255;
+  static constexpr size_t TAB = sizeof(C2<T>) * N;
+  static constexpr size_t SMEM = 3 * BUF + 3 * TAB;
+  static_assert(N % C == 0 && ROWS % 2 == 0, "plane must split into an even number of rows per CTA");
+};
+
+struct Barrier {
+  __device__ void operator()() const { __syncthreads(); }
+};
+
+// Columns [r*COLS, (r+1)*COLS) of every CTA's x-spectrum rows (pitch P) into
+// this CTA's column block (N x COLS, row-major).
+template <typename T, int N, int C>
+__device__ __forceinline__ void gather_cols(cg::cluster_group &cl, T *slab, T *blk, int r) {
+  using G = FixGeo<T, N, C>;
+  constexpr int TOT = N * G::COLS, U = 8;
+  const int x0 = r * G::COLS;
+  for (int b = threadIdx.x; b < TOT; b += FIX_NTH * U) {
+    T v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const unsigned idx = b + u * FIX_NTH;
+      if (idx < (unsigned)TOT) {
+        const unsigned gl = idx / G::COLS, xc = idx % G::COLS, s = gl / G::ROWS, lr = gl % G::ROWS;
+        v[u] = cl.map_shared_rank(slab, (int)s)[lr * G::P + x0 + xc];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const unsigned idx = b + u * FIX_NTH;
+      if (idx < (unsigned)TOT) blk[idx] = v[u];
+    }
+  }
+}
+
+// This CTA's rows (ROWS x N, pitch P) from every CTA's column block.
+template <typename T, int N, int C>
+__device__ __forceinline__ void gather_rows(cg::cluster_group &cl, T *blk, T *slab, int r) {
+  using G = FixGeo<T, N, C>;
+  constexpr int TOT = G::ROWS * N, U = 8;
+  for (int b = threadIdx.x; b < TOT; b += FIX_NTH * U) {
+    T v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const unsigned idx = b + u * FIX_NTH;
+      if (idx < (unsigned)TOT) {
+        const unsigned lr = idx / N, xg = idx % N, s = xg / G::COLS, xc = xg % G::COLS;
+        v[u] = cl.map_shared_rank(blk, (int)s)[(r * G::ROWS + lr) * G::COLS + xc];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const unsigned idx = b + u * FIX_NTH;
+      if (idx < (unsigned)TOT) slab[idx + idx / N] = v[u];
+    }
+  }
+}
+
+template <typename T, int N, int PX, int PY>
+__device__ __forceinline__ void load_tables(const AxisPlan &ax, const AxisPlan &ay, C2<T> *Wt, C2<T> *Qx, C2<T> *Qy) {
+  for (int i = threadIdx.x; i < N; i += FIX_NTH) {
+    Wt[i] = ((const C2<T> *)ax.W)[i];
+    if (PX != BC_PP) Qx[i] = ((const C2<T> *)ax.Q)[i];
+    if (PY != BC_PP) Qy[i] = ((const C2<T> *)ay.Q)[i];
+  }
+}
+
+template <typename T, int N, int C, int PX, int PY, typename In>
+__global__ void __launch_bounds__(FIX_NTH, 2) k_xyfwd_fix(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
+  using G = FixGeo<T, N, C>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank(), tid = threadIdx.x;
+  T *B0 = (T *)smem_raw, *B1 = (T *)(smem_raw + G::BUF), *B2 = (T *)(smem_raw + 2 * G::BUF);
+  C2<T> *Wt = (C2<T> *)(smem_raw + 3 * G::BUF), *Qx = Wt + N, *Qy = Qx + N;
+  load_tables<T, N, PX, PY>(ax, ay, Wt, Qx, Qy);
+  const Barrier bar;
+  const int y0 = r * G::ROWS;
+  float ss = 0.0f;
+  for (int k = blockIdx.x / C; k < g.nz; k += gridDim.x / C) {
+    load_cells<T>(
+        in, G::ROWS * N,
+        [&](int idx, int &x, int &y, int &kk) -> bool {
+          const unsigned u = idx;
+          x = (int)(u % N);
+          y = y0 + (int)(u / N);
+          kk = k;
+          return true;
+        },
+        [&](int idx, T t) {
+          const unsigned u = idx;
+          B0[u + u / N] = t;  // row ly = u / N at pitch P = N + 1
+        },
+        ss);
+    __syncthreads();
+    // x: rows in B0 -> stages in B1/B2 -> split into the x-spectrum rows, B0
+    fix::forward<T, N, PX, G::BX, FIX_NTH>(B0, G::P, 1, (C2<T> *)B1, (C2<T> *)B2, Wt, Qx,
+                                            StorePlaneReal<T>{B0, G::P, 0}, tid, bar);
+    cluster.sync();  // every CTA's x-spectrum rows are complete
+    gather_cols<T, N, C>(cluster, B0, B1, r);
+    cluster.sync();  // every CTA has read the rows
+    // y: columns in B1 -> stages in B2/B0 -> split into S
+    fix::forward<T, N, PY, G::BY, FIX_NTH>(B1, 1, G::COLS, (C2<T> *)B2, (C2<T> *)B0, Wt, Qy,
+                                            StoreColsS<T>{S, (long)k * N * N, N, r * G::COLS, G::COLS}, tid, bar);
+    __syncthreads();
+  }
+  if (nrm) block_sum_add((double)ss, nrm);
+}
+
+template <typename T, int N, int C, int PX, int PY, typename Out>
+__global__ void __launch_bounds__(FIX_NTH, 2) k_xyinv_fix(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
+  using G = FixGeo<T, N, C>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank(), tid = threadIdx.x;
+  T *B0 = (T *)smem_raw, *B1 = (T *)(smem_raw + G::BUF), *B2 = (T *)(smem_raw + 2 * G::BUF);
+  C2<T> *Wt = (C2<T> *)(smem_raw + 3 * G::BUF), *Qx = Wt + N, *Qy = Qx + N;
+  load_tables<T, N, PX, PY>(ax, ay, Wt, Qx, Qy);
+  const Barrier bar;
+  const int y0 = r * G::ROWS;
+  for (int k = blockIdx.x / C; k < g.nz; k += gridDim.x / C) {
+    const T *Sp = S + (long)k * N * N + r * G::COLS;
+    for (int i = tid; i < N * G::COLS; i += FIX_NTH) {
+      const unsigned u = i;
+      B0[i] = Sp[(u / G::COLS) * N + u % G::COLS];
+    }
+    __syncthreads();
+    // y^-1: columns in B0 -> stages in B1/B0 -> columns in B2
+    fix::inverse<T, N, PY, G::BY, FIX_NTH>(B0, 1, G::COLS, B2, 1, G::COLS, (C2<T> *)B1, (C2<T> *)B0, Wt, Qy, tid,
+                                            bar);
+    cluster.sync();  // every CTA's column block is complete
+    gather_rows<T, N, C>(cluster, B2, B0, r);
+    cluster.sync();  // every CTA has read the blocks
+    // x^-1: rows in B0 -> stages in B1/B0 -> rows in B2 (pitch P)
+    fix::inverse<T, N, PX, G::BX, FIX_NTH>(B0, G::P, 1, B2, G::P, 1, (C2<T> *)B1, (C2<T> *)B0, Wt, Qx, tid, bar);
+    __syncthreads();
+    store_cells<T>(
+        out, G::ROWS * N,
+        [&](int idx, int &x, int &y, int &kk) -> bool {
+          const unsigned u = idx;
+          x = (int)(u % N);
+          y = y0 + (int)(u / N);
+          kk = k;
+          return true;
+        },
+        [&](int idx) {
+          const unsigned u = idx;
+          return B2[u + u / N];
+        });
+    __syncthreads();
+  }
+}
+
+// Raises the kernel's dynamic shared-memory limit once per device.
+int prepare(const void *kernel, size_t smem) {
+  static std::mutex mu;
+  static std::set<std::pair<const void *, int>> done;
+  std::lock_guard<std::mutex> lk(mu);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+  if (done.count({kernel, dev})) return 0;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+  done.insert({kernel, dev});
+  return 0;
+}
+
+template <typename K, typename... Args>
+cudaError_t cluster_start(K kernel, size_t smem, int clusters, int C, cudaStream_t st, Args... args) {
+  if (prepare((const void *)kernel, smem)) return cudaErrorInvalidValue;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(clusters * C));
+  cfg.blockDim = dim3(FIX_NTH);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+bool kind_ok(int p) { return p == BC_PP || p == BC_NN; }
+
+template <int N, int C, typename In>
+cudaError_t fwd_pairs(const AxisPlan &ax, const AxisPlan &ay, const In &in, float *S, const Geo &g, double *nrm,
+                      cudaStream_t st) {
+  using G = FixGeo<float, N, C>;
+  const int px = ax.pair, py = ay.pair;
+#define FG_FIX_FWD(PX, PY)                                                                                      \
+  if (px == PX && py == PY)                                                                                     \
+    return cluster_start(k_xyfwd_fix<float, N, C, PX, PY, In>, G::SMEM, g.nz, C, st, ax, ay, in, S, g, nrm);
+  FG_FIX_FWD(BC_PP, BC_PP)
+  FG_FIX_FWD(BC_PP, BC_NN)
+  FG_FIX_FWD(BC_NN, BC_PP)
+  FG_FIX_FWD(BC_NN, BC_NN)
+#undef FG_FIX_FWD
+  return cudaErrorInvalidValue;
+}
+
+template <int N, int C, typename Out>
+cudaError_t inv_pairs(const AxisPlan &ax, const AxisPlan &ay, const float *S, const Out &out, const Geo &g,
+                      cudaStream_t st) {
+  using G = FixGeo<float, N, C>;
+  const int px = ax.pair, py = ay.pair;
+#define FG_FIX_INV(PX, PY)                                                                                      \
+  if (px == PX && py == PY)                                                                                     \
+    return cluster_start(k_xyinv_fix<float, N, C, PX, PY, Out>, G::SMEM, g.nz, C, st, ax, ay, S, out, g);
+  FG_FIX_INV(BC_PP, BC_PP)
+  FG_FIX_INV(BC_PP, BC_NN)
+  FG_FIX_INV(BC_NN, BC_PP)
+  FG_FIX_INV(BC_NN, BC_NN)
+#undef FG_FIX_INV
+  return cudaErrorInvalidValue;
+}
+
+template <typename In>
+cudaError_t fwd_dispatch(const AxisPlan &ax, const AxisPlan &ay, const In &in, float *S, const Geo &g, double *nrm,
+                         int C, cudaStream_t st, bool *handled) {
+  *handled = fixed_supported(g.nx, g.ny, C, ax.pair, ay.pair);
+  if (!*handled) return cudaSuccess;
+  return fwd_pairs<256, 8, In>(ax, ay, in, S, g, nrm, st);
+}
+
+template <typename Out>
+cudaError_t inv_dispatch(const AxisPlan &ax, const AxisPlan &ay, const float *S, const Out &out, const Geo &g, int C,
+                         cudaStream_t st, bool *handled) {
+  *handled = fixed_supported(g.nx, g.ny, C, ax.pair, ay.pair);
+  if (!*handled) return cudaSuccess;
+  return inv_pairs<256, 8, Out>(ax, ay, S, out, g, st);
+}
+
+}  // namespace
+
+bool fixed_supported(int nx, int ny, int C, int px, int py) {
+  if (const char *e = getenv("FLUTAS_GB300_FIXED")) {  // 0 disables the fixed-size kernels (A/B timing)
+    if (atoi(e) == 0) return false;
+  }
+  return nx == 256 && ny == 256 && C == 8 && kind_ok(px) && kind_ok(py);
+}
+
+cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InKeep<InFillps> &in, float *S, const Geo &g,
+                        double *nrm, int C, cudaStream_t st, bool *handled) {
+  return fwd_dispatch(ax, ay, in, S, g, nrm, C, st, handled);
+}
+cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InKeep<InHalo> &in, float *S, const Geo &g,
+                        double *nrm, int C, cudaStream_t st, bool *handled) {
+  return fwd_dispatch(ax, ay, in, S, g, nrm, C, st, handled);
+}
+cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InResidual &in, float *S, const Geo &g,
+                        double *nrm, int C, cudaStream_t st, bool *handled) {
+  return fwd_dispatch(ax, ay, in, S, g, nrm, C, st, handled);
+}
+cudaError_t xyinv_fixed(const AxisPlan &ax, const AxisPlan &ay, const float *S, const OutHalo &out, const Geo &g,
+                        int C, cudaStream_t st, bool *handled) {
+  return inv_dispatch(ax, ay, S, out, g, C, st, handled);
+}
+cudaError_t xyinv_fixed(const AxisPlan &ax, const AxisPlan &ay, const float *S, const OutHaloAdd &out, const Geo &g,
+                        int C, cudaStream_t st, bool *handled) {
+  return inv_dispatch(ax, ay, S, out, g, C, st, handled);
+}
+
+}  // namespace fg

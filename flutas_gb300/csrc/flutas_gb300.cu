@@ -7,6 +7,7 @@
 #include "../../include/flutas_gb300.h"
 #include "axis_tables.cuh"
 #include "kernels.cuh"
+#include "fixed.h"
 
 #include <cuda_runtime.h>
 
@@ -407,10 +408,10 @@ template <typename K> int cluster_capacity(K kernel, size_t smem, int C) {
 }
 
 // Launch name "<base><f32|f64,tag>" per kernel, precision and functor.
-enum KId { KID_XYFWD, KID_XFWD, KID_XYINV, KID_XINV, KID_XYFWD_CL, KID_XYINV_CL };
+enum KId { KID_XYFWD, KID_XFWD, KID_XYINV, KID_XINV, KID_XYFWD_CL, KID_XYINV_CL, KID_XYFWD_FIX, KID_XYINV_FIX };
 template <int KID, typename T, typename F> const char *kname() {
   static const char *base[] = {"k_xyfwd_plane", "k_xfwd", "k_xyinv_plane", "k_xinv", "k_xyfwd_cluster",
-                               "k_xyinv_cluster"};
+                               "k_xyinv_cluster", "k_xyfwd_fix", "k_xyinv_fix"};
   static const std::string s = std::string(base[KID]) + (sizeof(T) == 8 ? "<f64," : "<f32,") + F::tag + ">";
   return s.c_str();
 }
@@ -432,6 +433,14 @@ int fwd_xy(flutas_plan *pl, const In &in, T *S, const AxisTables &tx, const Axis
   }
   if (path == 2) {
     const int C = sizeof(T) == 8 ? pl->clus64 : pl->clus32;
+    if (sizeof(T) == 4 && fixed_supported(g.nx, g.ny, C, tx.ap.pair, ty.ap.pair)) {
+      cudaError_t e = cudaSuccess;
+      bool handled = false;
+      TRY(launch(kname<KID_XYFWD_FIX, T, In>(), st,
+                 [&] { e = xyfwd_fixed(tx.ap, ty.ap, in, S, g, nrm, C, st, &handled); }));
+      if (e != cudaSuccess) return fail(FLUTAS_ECUDA, "fixed-size launch failed: %s", cudaGetErrorString(e));
+      if (handled) return 0;
+    }
     const size_t sm = cluster_plane_smem(g.nx, g.ny, C, sizeof(T));
     TRY(cluster_prepare(k_xyfwd_cluster<T, In>, sm, C));
     cudaError_t e = cudaSuccess;
@@ -480,6 +489,14 @@ int inv_xy(flutas_plan *pl, const T *S, const Out &out, const AxisTables &tx, co
   }
   if (path == 2) {
     const int C = sizeof(T) == 8 ? pl->clus64 : pl->clus32;
+    if (sizeof(T) == 4 && fixed_supported(g.nx, g.ny, C, tx.ap.pair, ty.ap.pair)) {
+      cudaError_t e = cudaSuccess;
+      bool handled = false;
+      TRY(launch(kname<KID_XYINV_FIX, T, Out>(), st,
+                 [&] { e = xyinv_fixed(tx.ap, ty.ap, S, out, g, C, st, &handled); }));
+      if (e != cudaSuccess) return fail(FLUTAS_ECUDA, "fixed-size launch failed: %s", cudaGetErrorString(e));
+      if (handled) return 0;
+    }
     const size_t sm = cluster_plane_smem(g.nx, g.ny, C, sizeof(T));
     TRY(cluster_prepare(k_xyinv_cluster<T, Out>, sm, C));
     cudaError_t e = cudaSuccess;

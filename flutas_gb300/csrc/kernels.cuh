@@ -284,10 +284,10 @@ struct StorePlaneReal {  // write real plane (row-major y*pitch + x)
   T *R;
   int pitch, rowbase;  // line l = row rowbase + l for x lines
   __device__ void pair(int c, int t, T v0, T v1) {
-    R[(long)(2 * c) * pitch + t] = v0;
-    R[(long)(2 * c + 1) * pitch + t] = v1;
+    R[(2 * c) * pitch + t] = v0;
+    R[(2 * c + 1) * pitch + t] = v1;
   }
-  __device__ void single(int c, int t, T v) { R[(long)c * pitch + t] = v; }
+  __device__ void single(int c, int t, T v) { R[c * pitch + t] = v; }
 };
 
 // Block sum of v, added atomically to *acc (all threads of the block call it).
@@ -309,6 +309,7 @@ __device__ __forceinline__ void block_sum_add(double v, double *acc) {
 // norms of the transform passes): the convergence check of a mixed solve whose
 // residual is not going to be transformed.  BATCH-style: four cells per thread
 // evaluated before any is accumulated.
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void __launch_bounds__(256) k_resnorm(InResidual R, double *nrm) {
   const Geo &g = R.g;
   const int tot = g.nx * g.ny * g.nz;  // < 2^31
@@ -333,6 +334,7 @@ __global__ void __launch_bounds__(256) k_resnorm(InResidual R, double *nrm) {
   }
   block_sum_add((double)ss, nrm);
 }
+#endif
 
 // One tile of the x pass: M rows starting at global row row0 (row = j + ny*k).
 // smem: M*P reals + M*nx reals.  Accumulates the squares of the inputs in ss.
@@ -522,10 +524,10 @@ struct StorePlaneRealCols {  // columns as lines: line l = column l, position t 
   T *R;
   int pitch;
   __device__ void pair(int c, int t, T v0, T v1) {
-    R[(long)t * pitch + 2 * c] = v0;
-    R[(long)t * pitch + 2 * c + 1] = v1;
+    R[t * pitch + 2 * c] = v0;
+    R[t * pitch + 2 * c + 1] = v1;
   }
-  __device__ void single(int c, int t, T v) { R[(long)t * pitch + c] = v; }
+  __device__ void single(int c, int t, T v) { R[t * pitch + c] = v; }
 };
 
 template <typename T, bool INV>
@@ -722,10 +724,12 @@ __global__ void __launch_bounds__(128) k_zsolve(ZArgs za, T *S) {
 // ===========================================================================
 // Stencil kernels (drop-in entry points).  One thread per interior cell.
 // ===========================================================================
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void k_fillps(InFillps in, double *p) {
   const Geo &g = in.g;
   for_cells(g, [&](int i0, int j0, int k0) { p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = in(i0, j0, k0); });
 }
+#endif
 
 struct CorrecArgs {
   const double *p, *dzci;  // dzci offset: dzci[k] = dzci(k)
@@ -733,6 +737,7 @@ struct CorrecArgs {
   double factori, factorj, dt, rho0i;
   Geo g;
 };
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void k_correc(CorrecArgs a) {
   // src/correc.f90:57-60
   const Geo &g = a.g;
@@ -745,6 +750,7 @@ __global__ void k_correc(CorrecArgs a) {
     a.w[ui] = a.w[ui] - a.dt * a.dzci[k] * (a.p[g.pidx(i, j, k + 1)] - pc) * a.rho0i;
   });
 }
+#endif
 
 // boundp for one direction: set_bc (src/bound.f90:227-646), centred, nh_p = 1.
 struct BoundArgs {
@@ -754,6 +760,7 @@ struct BoundArgs {
   char ctype0, ctype1;
   double f0, s0, f1, s1;  // ghost = f + s * inner
 };
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void k_boundp_dir(BoundArgs a) {
   const Geo &g = a.g;
   const int nx = g.nx, ny = g.ny, nz = g.nz;
@@ -780,6 +787,7 @@ __global__ void k_boundp_dir(BoundArgs a) {
     a.p[hi] = phi;
   }
 }
+#endif
 
 // divergence check: per-block partial (sum, max) in double
 struct DivArgs {
@@ -787,6 +795,7 @@ struct DivArgs {
   double dxi, dyi;
   Geo g;
 };
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void k_chkdiv(DivArgs a, double *partial) {
   const Geo &g = a.g;
   double tot = 0.0, mx = 0.0;
@@ -818,6 +827,7 @@ __global__ void k_chkdiv(DivArgs a, double *partial) {
     if (lane == 0) { partial[2 * bid] = tot; partial[2 * bid + 1] = mx; }
   }
 }
+#endif
 
 }  // namespace fg
 
@@ -830,6 +840,7 @@ struct RhsbArgs {
   Geo g;
   int idir, q;
 };
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void k_updt_rhs_b_dir(RhsbArgs a) {
   const Geo &g = a.g;
   int n1, n2;
@@ -847,6 +858,7 @@ __global__ void k_updt_rhs_b_dir(RhsbArgs a) {
     a.p[hi] += a.rhs[t + N];
   }
 }
+#endif
 
 // pres_tw_src (src/source.f90:247-309), _CONSTANT_COEFFS_POISSON branch.
 // With f1 = 1 + f2, dp = p(+) - p, dq = pold(+) - pold and t = dp - dq, the
@@ -900,10 +912,12 @@ __device__ __forceinline__ void pres_tw_cell(const PresTwArgs &a, int i, int j, 
   a.v[ui] += df_incr(a.p[cy] - p0, a.pold[cy] - q0, a.rho[cy] + r0, a.yA, a.yB, a.f2);
   a.w[ui] += df_incr(a.p[cz] - p0, a.pold[cz] - q0, a.rho[cz] + r0, a.zA[k], a.zB[k], a.f2);
 }
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void k_pres_tw_src(PresTwArgs a) {
   if (a.fp32) for_cells(a.g, [&](int i0, int j0, int k0) { pres_tw_cell32(a, i0 + 1, j0 + 1, k0 + 1); });
   else for_cells(a.g, [&](int i0, int j0, int k0) { pres_tw_cell(a, i0 + 1, j0 + 1, k0 + 1); });
 }
+#endif
 
 // correc with the pressure increment phi, fused with p = p + phi
 // (src/correc.f90:57-60 and the update of src/apps/two_phase_inc_isot/main__two_phase_inc_isot.f90:698-714).
@@ -913,6 +927,7 @@ struct CorrecAddArgs {
   double factori, factorj, dt, rho0i;  // cx = factori*rho0i etc. folded in the kernel
   Geo g;
 };
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void k_correc_padd(CorrecAddArgs a) {
   const Geo &g = a.g;
   for_cells(g, [&](int i0, int j0, int k0) {
@@ -927,6 +942,7 @@ __global__ void k_correc_padd(CorrecAddArgs a) {
     a.p[pc] = a.p[pc] + ph;
   });
 }
+#endif
 
 }  // namespace fg
 
@@ -943,6 +959,7 @@ struct SetBcArgs {
   double factor[4];
   double sgn;
 };
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void k_set_bc(SetBcArgs s) {
   const int n = s.idir == 1 ? s.nx : (s.idir == 2 ? s.ny : s.nz);
   const int na = s.idir == 1 ? s.ny : s.nx, nb = s.idir == 3 ? s.ny : s.nz;
@@ -976,6 +993,7 @@ __global__ void k_set_bc(SetBcArgs s) {
     }
   }
 }
+#endif
 
 }  // namespace fg
 
@@ -1110,6 +1128,7 @@ struct SetBc3Args {
   int nx, ny, nz, h, idir;
   BcSide side[3][2];  // [component][ibound]
 };
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void k_set_bc3(SetBc3Args s) {
   const int n = s.idir == 1 ? s.nx : (s.idir == 2 ? s.ny : s.nz);
   const int na = s.idir == 1 ? s.ny : s.nx, nb = s.idir == 3 ? s.ny : s.nz;
@@ -1147,14 +1166,17 @@ __global__ void k_set_bc3(SetBc3Args s) {
       }
   }
 }
+#endif
 
 }  // namespace fg
 
 namespace fg {
 // out[k] = s * in[k] for k in [0, n): folded z factors (e.g. dti*rho0*dzfi(k))
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void k_scale_vec(const double *in, double s, double *out, int n) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) out[k] = s * in[k];
 }
+#endif
 }  // namespace fg
 
 namespace fg {
@@ -1205,6 +1227,7 @@ __device__ __forceinline__ long batch_next(int *counter) {
 }
 
 // First pass (mode 0: RHS = x, keep f = x) or residual pass (mode 1: r = f - A x).
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void __launch_bounds__(256) kb_xfwd(BatchQueue q, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const long total = q.prefix[q.ngrids];
@@ -1227,6 +1250,7 @@ __global__ void __launch_bounds__(256) kb_xfwd(BatchQueue q, int mode) {
     block_sum_add((double)ss, G.nrm + (mode == 0 ? 0 : 1));
   }
 }
+#endif
 
 template <bool BACKWARD>
 __global__ void __launch_bounds__(256) kb_ypass(BatchQueue q) {
@@ -1241,6 +1265,7 @@ __global__ void __launch_bounds__(256) kb_ypass(BatchQueue q) {
 }
 
 // mode 0: x = e * normfft; mode 1: x += e * normfft
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void __launch_bounds__(256) kb_xinv(BatchQueue q, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const long total = q.prefix[q.ngrids];
@@ -1253,6 +1278,7 @@ __global__ void __launch_bounds__(256) kb_xinv(BatchQueue q, int mode) {
     else xinv_tile<float, OutHaloAdd>(G.ax, G.S, OutHaloAdd{G.x, G.normfft, G.g}, G.g, G.M, row0, smem_raw);
   }
 }
+#endif
 
 // z solve of one column per thread (FP32).  Non-periodic: the forward sweep
 // writes the eliminated values into S, the backward sweep recomputes the
@@ -1260,7 +1286,7 @@ __global__ void __launch_bounds__(256) kb_xinv(BatchQueue q, int mode) {
 // (chk[nchunk][blockDim]).  Periodic: the spike solution of gaussel_periodic
 // (src/solver_cpu.f90:147-185) goes through S2 and a third sweep combines.
 template <int CH>
-__device__ void zcol_f32(const ZArgs &za, float *S, float *S2, long q, bool act, float *chk) {
+static __device__ void zcol_f32(const ZArgs &za, float *S, float *S2, long q, bool act, float *chk) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const long plane = za.nq;
   const double lam64 = act ? za.lam[q] : 1.0;
@@ -1358,6 +1384,7 @@ __device__ void zcol_f32(const ZArgs &za, float *S, float *S2, long q, bool act,
   }
 }
 
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void __launch_bounds__(128) kb_z(BatchQueue q) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float *chk = (float *)smem_raw;
@@ -1370,8 +1397,10 @@ __global__ void __launch_bounds__(128) kb_z(BatchQueue q) {
     zcol_f32<16>(G.za, G.S, G.S2, qcol, qcol < G.za.nq, chk);
   }
 }
+#endif
 
 // Per-grid convergence after a residual pass: relres[g], active[g], iters[g].
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void kb_update(BatchGrid *grids, int ng, double tol, int it, int max_iter, double *relres, int *iters) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
     BatchGrid &G = grids[g];
@@ -1384,7 +1413,9 @@ __global__ void kb_update(BatchGrid *grids, int ng, double tol, int it, int max_
     G.nrm[1] = 0.0;
   }
 }
+#endif
 
+#ifndef FG_NO_PLAIN_KERNELS
 __global__ void kb_reset(BatchGrid *grids, int ng) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
     *grids[g].active = 1;
@@ -1392,6 +1423,7 @@ __global__ void kb_reset(BatchGrid *grids, int ng) {
     grids[g].nrm[1] = 0.0;
   }
 }
+#endif
 
 }  // namespace fg
 
@@ -1435,10 +1467,10 @@ struct StoreColBlock {  // y-phase lines = columns of the local column block (ro
   T *R;
   int pitch;
   __device__ void pair(int c, int t, T v0, T v1) {
-    R[(long)t * pitch + 2 * c] = v0;
-    R[(long)t * pitch + 2 * c + 1] = v1;
+    R[t * pitch + 2 * c] = v0;
+    R[t * pitch + 2 * c + 1] = v1;
   }
-  __device__ void single(int c, int t, T v) { R[(long)t * pitch + c] = v; }
+  __device__ void single(int c, int t, T v) { R[t * pitch + c] = v; }
 };
 
 // Gathers through distributed shared memory, GATHER_U remote loads in flight

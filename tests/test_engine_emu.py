@@ -92,3 +92,22 @@ def test_bit_conversions(emu):
     normal = (np.abs(f) >= 2.0 ** -126) | (f == 0) | ~np.isfinite(f)
     ok = np.isnan(f) & np.isnan(d) | (f.astype(np.float64) == d)
     assert np.all(ok[normal])
+
+
+@pytest.mark.parametrize("dbl", [0, 1], ids=["f32", "f64"])
+@pytest.mark.parametrize("n", [32, 64, 256, 512])
+def test_fixed_size_passes_match_engine(emu, dbl, n):
+    """fft_fixed.cuh (compile-time N, pre/post folded into the stages) == the run-time engine."""
+    dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+    emu.fg_emu_fixed.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, dp, dp]
+    rng = np.random.default_rng(n + dbl)
+    M = 8
+    for pair in (0, 1, 2):
+        for bwd in (0, 1):
+            x = rng.standard_normal(M * n)
+            ref = np.empty_like(x)
+            got = np.empty_like(x)
+            assert emu.fg_emu_lines(dbl, pair, n, M, bwd, 0, x, ref) == 0
+            assert emu.fg_emu_fixed(dbl, pair, n, bwd, x, got) == 0
+            tol = 1e-13 if dbl else 2e-6
+            assert np.abs(got - ref).max() <= tol * np.abs(ref).max(), (pair, bwd)

@@ -315,3 +315,25 @@ def test_gpu_mixed_reported_residual(lib, oracle, n, cbc):
         assert abs(relres - true) <= 1e-3 * true + 1e-12, (tol, relres, true)
         assert (relres <= tol) == (tol > 1e-14) and iters <= max_iter
         assert relres <= max(tol, 1e-11)
+
+
+@pytest.mark.parametrize("cbc", ["PPPPNN", "NNPPDD", "PPNNNN", "NNNNPP"])
+def test_gpu_fixed_size_cluster_kernels(lib, oracle, cbc, monkeypatch):
+    """256^2 planes run the compile-time-sized cluster kernels in the mixed path;
+    the result matches the oracle and the run-time-sized kernels."""
+    n = (256, 256, 5)
+    rng = np.random.default_rng(3)
+    P, dzci, dzfi, dzc, dzf, dli = plan_for(lib, n, cbc, 0.5)
+    f = compatible_rhs(rng, n, cbc, dzf)
+    ref = f.copy()
+    oracle.SolverSetup(n, dli, 1, dzci, dzfi, cbc, [0] * 6, "ccc").solve(ref)
+    out = {}
+    for fixed in ("1", "0"):
+        monkeypatch.setenv("FLUTAS_GB300_FIXED", fixed)
+        p = f.copy()
+        relres, _ = P.solve_mixed(p, tol=1e-10, max_iter=8)
+        r = oracle.residual(n, cbc, dli[0], dli[1], 1, dzci, dzfi, f, p)
+        assert np.linalg.norm(r) / np.linalg.norm(f[1:-1, 1:-1, 1:-1]) <= 1.01e-10
+        assert rel_l2(p[1:-1, 1:-1, 1:-1], ref[1:-1, 1:-1, 1:-1], remove_mean=singular(cbc)) <= 1e-7
+        out[fixed] = p
+    assert rel_l2(out["1"][1:-1, 1:-1, 1:-1], out["0"][1:-1, 1:-1, 1:-1], remove_mean=singular(cbc)) <= 1e-7
