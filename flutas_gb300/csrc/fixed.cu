@@ -278,6 +278,10 @@ cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InResidual
                         double *nrm, int C, cudaStream_t st, bool *handled) {
   return fwd_dispatch(ax, ay, in, S, g, nrm, C, st, handled);
 }
+cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InF32 &in, float *S, const Geo &g,
+                        double *nrm, int C, cudaStream_t st, bool *handled) {
+  return fwd_dispatch(ax, ay, in, S, g, nrm, C, st, handled);
+}
 cudaError_t xyinv_fixed(const AxisPlan &ax, const AxisPlan &ay, const float *S, const OutHalo &out, const Geo &g,
                         int C, cudaStream_t st, bool *handled) {
   return inv_dispatch(ax, ay, S, out, g, C, st, handled);

@@ -24,6 +24,8 @@ cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InKeep<InH
                         double *nrm, int C, cudaStream_t st, bool *handled);
 cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InResidual &in, float *S, const Geo &g,
                         double *nrm, int C, cudaStream_t st, bool *handled);
+cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InF32 &in, float *S, const Geo &g,
+                        double *nrm, int C, cudaStream_t st, bool *handled);
 
 template <typename T, typename Out>
 cudaError_t xyinv_fixed(const AxisPlan &, const AxisPlan &, const T *, const Out &, const Geo &, int, cudaStream_t,

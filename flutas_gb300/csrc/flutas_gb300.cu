@@ -21,6 +21,7 @@
 #include <mutex>
 #include <sstream>
 #include <tuple>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -322,6 +323,7 @@ struct flutas_plan {
   DBuf a32, b32, c32;  // z coefficients rounded to FP32 (the mixed solve's arithmetic)
   DBuf zres;           // per-level coefficients of the FP64 residual (3 per level)
   DBuf czf;            // folded fillps factors dti*rho0*dzfi(k)
+  DBuf czc;            // folded correc factors dt*dzci(k)/rho0
   DBuf zdf;            // per-level factors of the Dodd-Ferrante term
   AxisTables tx64, ty64, tx32, ty32;
   DBuf S64, S32, fbuf, phi, nrm;
@@ -331,6 +333,7 @@ struct flutas_plan {
   int path64 = 0, path32 = 0;  // 0 separate passes, 1 fused plane kernel, 2 cluster plane kernel
   int clus64 = 0, clus32 = 0;  // cluster size of path 2
   bool pin_zero_mode = false;  // singular (lam == 0, z in N/N or P/P) column
+  bool rhsb_zero = false;      // every boundary-RHS value is 0 (homogeneous BCs): updt_rhs_b adds nothing
   double last_relres = 0.0;    // relative residual / FP32 solves of the last mixed solve
   int last_iters = 0;
   double contraction = 1e-3;   // residual reduction of one FP32 solve, last measured
@@ -624,6 +627,9 @@ int solve_fp64_dev(flutas_plan *pl, double *p, const double *lam, const double *
 // per FP32 solve predicts that a check will end the solve (or the iteration
 // limit does), the check evaluates the residual norm alone (k_resnorm) and
 // the transform of the residual is made only if the prediction was wrong.
+// With the fixed-size cluster kernels, the FP64 RHS (fillps, residual) is
+// evaluated by a stencil pass at full occupancy and the transform reads its
+// FP32 values in place; the other paths evaluate it in the transform's loads.
 template <typename First>
 int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, int max_iter, double *relres,
                     int *iters) {
@@ -637,8 +643,28 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
   double *nrm = pl->nrm.as<double>();
   cudaStream_t st = pl->stream;
   const double *lam = pl->lam.as<double>(), *a = pl->a.as<double>(), *b = pl->b.as<double>(), *c = pl->c.as<double>();
+  const bool split =
+      pl->path32 == 2 && fixed_supported(g.nx, g.ny, pl->clus32, pl->tx32.ap.pair, pl->ty32.ap.pair);
+  auto stencil = [&](const auto &in, double *keep, float *s32, double *acc) -> int {
+    using In = std::decay_t<decltype(in)>;
+    const int grid = grid_for(k_stencil_pass<In>, 256, 0, ((long)g.nx * g.ny * g.nz + 1023) / 1024);
+    if (grid < 0) return grid;
+    static const std::string name = std::string("k_stencil<") + In::tag + ">";
+    const char *nm = (keep || s32) ? name.c_str() : "k_resnorm";
+    return launch(nm, st, [&] { k_stencil_pass<In><<<grid, 256, 0, st>>>(in, g, keep, s32, acc); });
+  };
+  auto transform = [&](const InResidual &R, double *acc) -> int {  // residual -> S
+    if (!split) return fwd_xy<float>(pl, R, S, pl->tx32, pl->ty32, pl->path32, acc);
+    TRY(stencil(R, nullptr, S, acc));
+    return fwd_xy<float>(pl, InF32{S, g}, S, pl->tx32, pl->ty32, pl->path32);
+  };
   CK(cudaMemsetAsync(nrm, 0, sizeof(double) * 2, st));
-  TRY(fwd_xy<float>(pl, InKeep<First>{first, f, g}, S, pl->tx32, pl->ty32, pl->path32, nrm + 0));
+  if (split) {
+    TRY(stencil(first, f, S, nrm + 0));
+    TRY(fwd_xy<float>(pl, InF32{S, g}, S, pl->tx32, pl->ty32, pl->path32));
+  } else {
+    TRY(fwd_xy<float>(pl, InKeep<First>{first, f, g}, S, pl->tx32, pl->ty32, pl->path32, nrm + 0));
+  }
   TRY(zsolve<float>(pl, S, lam, a, b, c, true));
   TRY(inv_xy<float>(pl, S, OutHalo{x, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
   InResidual R;
@@ -653,13 +679,8 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
   for (;;) {
     const bool norm_only = it >= max_iter || before * pl->contraction <= 0.5 * tol;
     CK(cudaMemsetAsync(nrm + 1, 0, sizeof(double), st));
-    if (norm_only) {
-      const int grid = grid_for(k_resnorm, 256, 0, ((long)g.nx * g.ny * g.nz + 1023) / 1024);
-      if (grid < 0) return grid;
-      TRY(launch("k_resnorm", st, [&] { k_resnorm<<<grid, 256, 0, st>>>(R, nrm + 1); }));
-    } else {
-      TRY(fwd_xy<float>(pl, R, S, pl->tx32, pl->ty32, pl->path32, nrm + 1));
-    }
+    if (norm_only) TRY(stencil(R, nullptr, nullptr, nrm + 1));
+    else TRY(transform(R, nrm + 1));
     double h[2];
     CK(cudaMemcpyAsync(h, nrm, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -668,7 +689,7 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
     rel = h[0] > 0 ? std::sqrt(h[1] / h[0]) : std::sqrt(h[1]);
     if (before > 0.0) pl->contraction = std::min(1.0, std::max(rel / before, 1e-12));
     if (rel <= tol || it >= max_iter) break;
-    if (norm_only) TRY(fwd_xy<float>(pl, R, S, pl->tx32, pl->ty32, pl->path32));  // prediction missed
+    if (norm_only) TRY(transform(R, nullptr));  // prediction missed
     // correction of this pass: e = A^-1 r in FP32, x += e in FP64
     TRY(zsolve<float>(pl, S, lam, a, b, c, true));
     TRY(inv_xy<float>(pl, S, OutHaloAdd{x, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
@@ -827,6 +848,11 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
     }
     if ((rc = up(pl->zres, zr.data(), zr.size()))) return bail(rc);
   }
+  {
+    auto zero = [](const double *v, size_t n) { return std::all_of(v, v + n, [](double x) { return x == 0.0; }); };
+    pl->rhsb_zero = zero(rhsbx, 2 * (size_t)ny * nz) && zero(rhsby, 2 * (size_t)nx * nz) &&
+                    zero(rhsbz, 2 * (size_t)nx * ny);
+  }
   if ((rc = up(pl->rhsb[0], rhsbx, 2 * (size_t)ny * nz)) || (rc = up(pl->rhsb[1], rhsby, 2 * (size_t)nx * nz)) ||
       (rc = up(pl->rhsb[2], rhsbz, 2 * (size_t)nx * ny)))
     return bail(rc);
@@ -855,7 +881,7 @@ int flutas_gb300_fftend(void **arrplan) {
   flutas_plan *pl;
   TRY(check_plan(arrplan[0], &pl));
   cudaStreamSynchronize(pl->stream);
-  DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
+  DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->czc, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
                   &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W, &pl->tx32.Q, &pl->ty32.W,
                   &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->nrm};
   for (DBuf *d : bufs) d->release();
@@ -879,7 +905,7 @@ int flutas_gb300_plan_info(void *plan, size_t *device_bytes, int *xy_path_fp64, 
   TRY(check_plan(plan, &pl));
   if (device_bytes) {
     size_t s = 0;
-    const DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1],
+    const DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->czc, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1],
                           &pl->rhsb[2], &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W,
                           &pl->tx32.Q, &pl->ty32.W, &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->nrm};
     for (const DBuf *d : bufs) s += d->bytes;
@@ -1388,6 +1414,7 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   in.cz = pl->czf.as<double>() + (nh_d - 1);
   in.cx = dti * dxi * rho0; in.cy = dti * dyi * rho0;
   in.rhsbx = pl->rhsb[0].as<double>(); in.rhsby = pl->rhsb[1].as<double>(); in.rhsbz = pl->rhsb[2].as<double>();
+  if (pl->rhsb_zero) in.rhsbx = in.rhsby = in.rhsbz = nullptr;  // adding zeros changes nothing
   in.q1 = in.q2 = in.q3 = 0;
   in.g = g;
   const Geo gp{nx, ny, nz, 1};
@@ -1407,9 +1434,14 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   const double dzc0 = 1.0 / pl->dzci_h[0 - 1 + nh_d], dzcn = 1.0 / pl->dzci_h[nz - 1 + nh_d];
   TRY(boundp_dev(phi, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
   CorrecAddArgs ca;
-  ca.phi = phi; ca.dzci = dzci_d + (nh_d - 1);
+  const double rho0i = 1.0 / rho0;
+  TRY(pl->czc.ensure(sizeof(double) * (nz + 2 * nh_d)));
+  TRY(launch("k_scale_vec", st, [&] {
+    k_scale_vec<<<1, 256, 0, st>>>(dzci_d, dt * rho0i, pl->czc.as<double>(), nz + 2 * nh_d);
+  }));
+  ca.phi = phi; ca.cz = pl->czc.as<double>() + (nh_d - 1);
   ca.u = u; ca.v = v; ca.w = w; ca.p = p;
-  ca.factori = dt * dxi; ca.factorj = dt * dyi; ca.dt = dt; ca.rho0i = 1.0 / rho0;
+  ca.cx = (dt * dxi) * rho0i; ca.cy = (dt * dyi) * rho0i;
   ca.g = g;
   TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<grid_cells(ca.g), 256, 0, st>>>(ca); }));
   if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));

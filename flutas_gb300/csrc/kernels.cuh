@@ -62,6 +62,10 @@ __device__ __forceinline__ double rcp64(double x) {
 template <typename T> __device__ __forceinline__ T to_pass(double v);
 template <> __device__ __forceinline__ float to_pass<float>(double v) { return f32_of(v); }
 template <> __device__ __forceinline__ double to_pass<double>(double v) { return v; }
+__device__ __forceinline__ void to_pass_into(float &o, double v) { o = f32_of(v); }
+__device__ __forceinline__ void to_pass_into(float &o, float v) { o = v; }
+__device__ __forceinline__ void to_pass_into(double &o, double v) { o = v; }
+__device__ __forceinline__ void to_pass_into(double &o, float v) { o = f64_of(v); }
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(double v) { return f32_of(v); }
 
@@ -74,6 +78,14 @@ struct InHalo {  // p(1:nx,1:ny,1:nz) of a halo-1 array
   Geo g;
   __device__ double operator()(int i0, int j0, int k0) const { return p[g.pidx(i0 + 1, j0 + 1, k0 + 1)]; }
   __device__ void keep(int, int, int, double) const {}
+};
+
+struct InF32 {  // contiguous (nx,ny,nz) FP32 array (a RHS already evaluated by k_stencil_pass)
+  static constexpr const char *tag = "f32";
+  const float *f;
+  Geo g;
+  __device__ float operator()(int i0, int j0, int k0) const { return f[g.sidx(i0, j0, k0)]; }
+  __device__ void keep(int, int, int, float) const {}
 };
 
 struct InPlain {  // contiguous (nx,ny,nz) FP64 array
@@ -143,9 +155,12 @@ struct InResidual {
       pt = k < nz ? x[c + sz] : ghost(bc[5], pc, x[g.pidx(i, j, 1)]);
     }
     const double czm = zc[3 * k0], czp = zc[3 * k0 + 1], cc = zc[3 * k0 + 2];
-    double ax = fma(dxi2, pe + pw, dyi2 * (pn + ps));
-    ax = fma(czp, pt, fma(czm, pb, fma(cc, pc, ax)));
-    return f[c] - ax;
+    // f - A x accumulated into f: two adds and five FMAs (FP64 is the bound)
+    double r = fma(-cc, pc, f[c]);
+    r = fma(-dxi2, pe + pw, r);
+    r = fma(-dyi2, pn + ps, r);
+    r = fma(-czm, pb, r);
+    return fma(-czp, pt, r);
   }
   __device__ void keep(int, int, int, double) const {}
 };
@@ -207,22 +222,24 @@ constexpr int BATCH_U = 4;
 template <typename T, typename In, typename Coord, typename Dst>
 __device__ __forceinline__ void load_cells(const In &in, int tot, const Coord &coord, const Dst &dst, float &ss) {
   const int tid = threadIdx.x, nth = blockDim.x;
+  using V = decltype(in(0, 0, 0));  // double (FP64 functors) or float (InF32)
   for (int b = tid; b < tot; b += BATCH_U * nth) {
-    double v[BATCH_U];
+    V v[BATCH_U];
     int xs[BATCH_U], ys[BATCH_U], ks[BATCH_U];
     bool ok[BATCH_U];
 #pragma unroll
     for (int u = 0; u < BATCH_U; u++) {
       const int idx = b + u * nth;
       ok[u] = idx < tot && coord(idx, xs[u], ys[u], ks[u]);
-      v[u] = ok[u] ? in(xs[u], ys[u], ks[u]) : 0.0;
+      v[u] = ok[u] ? in(xs[u], ys[u], ks[u]) : (V)0;
     }
 #pragma unroll
     for (int u = 0; u < BATCH_U; u++) {
       const int idx = b + u * nth;
       if (idx < tot) {
         if (ok[u]) in.keep(xs[u], ys[u], ks[u], v[u]);
-        const T t = to_pass<T>(v[u]);
+        T t;
+        to_pass_into(t, v[u]);
         const float f = to_f32(t);
         ss = fmaf(f, f, ss);
         dst(idx, t);
@@ -305,36 +322,44 @@ __device__ __forceinline__ void block_sum_add(double v, double *acc) {
   }
 }
 
-// ||f - A x||^2 alone (FP32 sum of the FP32-truncated residual, as the fused
-// norms of the transform passes): the convergence check of a mixed solve whose
-// residual is not going to be transformed.  BATCH-style: four cells per thread
-// evaluated before any is accumulated.
-#ifndef FG_NO_PLAIN_KERNELS
-__global__ void __launch_bounds__(256) k_resnorm(InResidual R, double *nrm) {
-  const Geo &g = R.g;
+// Stencil pass of the mixed solve: evaluates an FP64 RHS functor (fillps,
+// or the residual f - A x) per cell, optionally keeps the FP64 value (halo-1
+// array `keep`) and writes the FP32-truncated value into `s32` (no halo, x
+// fastest: the input of the transform, which may run in place), and adds the
+// FP32 sum of squares of the FP32 values to *nrm (as the fused norms of the
+// transform passes).  With keep = s32 = nullptr it is the norm-only check.
+// Four cells per thread are evaluated before any is stored.
+template <typename In>
+__global__ void __launch_bounds__(256) k_stencil_pass(In in, Geo g, double *keep, float *s32, double *nrm) {
   const int tot = g.nx * g.ny * g.nz;  // < 2^31
   const FastDiv fx(g.nx), fy(g.ny);
   float ss = 0.0f;
   for (int b = blockIdx.x * blockDim.x * 4 + threadIdx.x; b < tot; b += gridDim.x * blockDim.x * 4) {
     double v[4];
+    int xs[4], ys[4], ks[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
       const int idx = b + u * (int)blockDim.x;
-      v[u] = 0.0;
-      if (idx < tot) {
-        const int row = fx.div(idx), x = idx - row * g.nx, k = fy.div(row), y = row - k * g.ny;
-        v[u] = R(x, y, k);
-      }
+      const int row = fx.div(idx), k = fy.div(row);
+      xs[u] = idx - row * g.nx;
+      ks[u] = k;
+      ys[u] = row - k * g.ny;
+      v[u] = idx < tot ? in(xs[u], ys[u], ks[u]) : 0.0;
     }
 #pragma unroll
     for (int u = 0; u < 4; u++) {
+      const int idx = b + u * (int)blockDim.x;
       const float f = f32_of(v[u]);
       ss = fmaf(f, f, ss);
+      if (idx < tot) {
+        if (keep) keep[g.pidx(xs[u] + 1, ys[u] + 1, ks[u] + 1)] = v[u];
+        if (s32) s32[idx] = f;
+      }
     }
   }
-  block_sum_add((double)ss, nrm);
+  if (nrm) block_sum_add((double)ss, nrm);
 }
-#endif
+
 
 // One tile of the x pass: M rows starting at global row row0 (row = j + ny*k).
 // smem: M*P reals + M*nx reals.  Accumulates the squares of the inputs in ss.
@@ -922,9 +947,10 @@ __global__ void k_pres_tw_src(PresTwArgs a) {
 // correc with the pressure increment phi, fused with p = p + phi
 // (src/correc.f90:57-60 and the update of src/apps/two_phase_inc_isot/main__two_phase_inc_isot.f90:698-714).
 struct CorrecAddArgs {
-  const double *phi, *dzci;
+  const double *phi;
+  const double *cz;  // cz[k] = dt*rho0i*dzci(k) (index k)
   double *u, *v, *w, *p;
-  double factori, factorj, dt, rho0i;  // cx = factori*rho0i etc. folded in the kernel
+  double cx, cy;     // dt*dxi*rho0i, dt*dyi*rho0i
   Geo g;
 };
 #ifndef FG_NO_PLAIN_KERNELS
@@ -935,10 +961,9 @@ __global__ void k_correc_padd(CorrecAddArgs a) {
     const long pc = g.pidx(i, j, k);
     const double ph = a.phi[pc];
     const long ui = g.uidx(i, j, k);
-    const double cx = a.factori * a.rho0i, cy = a.factorj * a.rho0i, cz = a.dt * a.rho0i * a.dzci[k];
-    a.u[ui] = fma(-cx, a.phi[pc + 1] - ph, a.u[ui]);
-    a.v[ui] = fma(-cy, a.phi[pc + (g.nx + 2)] - ph, a.v[ui]);
-    a.w[ui] = fma(-cz, a.phi[pc + (long)(g.nx + 2) * (g.ny + 2)] - ph, a.w[ui]);
+    a.u[ui] = fma(-a.cx, a.phi[pc + 1] - ph, a.u[ui]);
+    a.v[ui] = fma(-a.cy, a.phi[pc + (g.nx + 2)] - ph, a.v[ui]);
+    a.w[ui] = fma(-a.cz[k], a.phi[pc + (long)(g.nx + 2) * (g.ny + 2)] - ph, a.w[ui]);
     a.p[pc] = a.p[pc] + ph;
   });
 }
