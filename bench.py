@@ -79,7 +79,33 @@ BYTES_PER_CELL = {
     "k_zsolve<f64>": 16,
     "k_xinv<f64,halo>": 16,
     "k_xyinv_plane<f64,halo>": 16,
+    # stencil passes ahead of the fixed-size transforms, and the norm-only check
+    "k_stencil<fillps>": 36,        # R u,v,w (24) W f-copy FP64 (8) W S FP32 (4)
+    "k_stencil<residual>": 20,      # R f, x (16) W S (4)
+    "k_resnorm": 16,                # R f, x
+    # cluster plane kernels (run-time sized, and compile-time sized for 256^2)
+    "k_xyfwd_cluster<f32,keep-fillps>": 36,
+    "k_xyfwd_cluster<f32,keep-halo>": 20,
+    "k_xyfwd_cluster<f32,residual>": 20,
+    "k_xyinv_cluster<f32,halo>": 12,
+    "k_xyinv_cluster<f32,haloadd>": 20,
+    "k_xyfwd_cluster<f64,fillps>": 32,
+    "k_xyfwd_cluster<f64,halo>": 16,
+    "k_xyinv_cluster<f64,halo>": 16,
+    "k_xyfwd_fix<f32,f32>": 8,      # R S W S (in place)
+    "k_xyfwd_fix<f32,keep-fillps>": 36,
+    "k_xyfwd_fix<f32,keep-halo>": 20,
+    "k_xyfwd_fix<f32,residual>": 20,
+    "k_xyinv_fix<f32,halo>": 12,
+    "k_xyinv_fix<f32,haloadd>": 20,
 }
+
+# FP64 instructions per cell of the FP64-bound kernels (the part's FP64 rate,
+# not HBM, bounds them): DF increments 3x(2 sub + 1 add), fillps 3 sub + 1 mul
+# + 2 fma, residual 2 add + 5 fma, correc 3x(sub + fma) + 1 add.
+FP64_PER_CELL = {"k_pres_tw_src": 9, "k_stencil<fillps>": 6, "k_stencil<residual>": 7, "k_resnorm": 7,
+                 "k_correc_padd": 7}
+FP64_PEAK_TOPS = 0.60   # FP64 FMA instructions/s measured on this part (1.20 TFLOP/s counting an FMA as 2)
 
 
 def peaks():
@@ -359,6 +385,12 @@ def run_ours(args, rank, world, local_rank):
                         "unit": "GB/s", "frac": round(achieved / hbm, 4),
                         "peak_source": src, "bytes_per_launch": bpc * ncell,
                         "traffic": ncu_traffic(name, n)}
+                f64 = FP64_PER_CELL.get(name)
+                if f64:
+                    ops = f64 * ncell / (ms / cnt / 1e3) / 1e12
+                    roof["fp64"] = {"instr_per_cell": f64, "achieved_tinstr_s": round(ops, 4),
+                                    "peak_tinstr_s": FP64_PEAK_TOPS, "frac": round(ops / FP64_PEAK_TOPS, 4),
+                                    "note": "FP64 FMA/add instructions; the binding roof of this kernel"}
         res = {
             "metric": METRIC,
             "value": round(value, 3),
