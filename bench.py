@@ -755,6 +755,192 @@ def run_serve(args):
                       "solution); Poisson arrivals"}
 
 
+
+# ------------------------------------------------------------ configs C1, C3
+def zgrid_stretched(n, gr):
+    """dzci, dzfi (0:n+1) of src/initgrid.f90 steps 1-5 with two-end tanh
+    clustering (gr > 0; uniform for gr = 0), lz = 1, one ghost layer:
+    zf(k) = 0.5 (1 + tanh((k/n - 0.5) gr) / tanh(gr/2)), dzf(k) = zf(k) - zf(k-1),
+    dzc(k) = (dzf(k) + dzf(k+1)) / 2, and the ghost extension of step 5
+    (dzf(0) = dzf(1), dzf(n+1) = dzf(n-2), dzc(n+1) = dzc(n-1))."""
+    z0 = np.arange(1, n + 1, dtype=np.float64) / n
+    zf = 0.5 * (1.0 + np.tanh((z0 - 0.5) * gr) / np.tanh(gr / 2.0)) if gr != 0.0 else z0
+    dzf = np.empty(n + 2)
+    dzf[1:n + 1] = np.diff(np.concatenate([[0.0], zf]))
+    dzf[0], dzf[n + 1] = dzf[1], dzf[n]
+    dzc = np.empty(n + 2)
+    dzc[0:n + 1] = 0.5 * (dzf[0:n + 1] + dzf[1:n + 2])
+    dzc[n + 1] = dzc[n]
+    dzf[n + 1] = dzf[n - 2]     # step 5: dzf(k) = dzf(2n-k-1), dzc(k) = dzc(2n-k) for k = n+1
+    dzc[n + 1] = dzc[n - 1]
+    return 1.0 / dzc, 1.0 / dzf
+
+
+def run_config1(args):
+    """C1: plain single-phase FP64 projection, 128^3, periodic x,y, walls z (one
+    fillps -> solver -> boundp -> correc -> bounduvw), as drop-in calls and as one fused
+    call, device-resident and through host arrays, with the oracle restatement on
+    the host cores beside it."""
+    import torch
+    import flutas_gb300 as F
+    dev = torch.device("cuda:0")
+    n = 128
+    dzci, dzfi = zgrid_stretched(n, 0.0)
+    dxi = dyi = float(n)
+    P = F.initsolver([n, n, n], [dxi, dyi, float(n)], 1, dzci, dzfi, CBC, [0.0] * 6, "ccc")
+    g = torch.Generator(device="cpu").manual_seed(args.seed)
+    vel = [2 * torch.rand((n + 2,) * 3, generator=g, dtype=torch.float64) - 1 for _ in range(3)]
+    for f in vel:
+        f[:, :, 0] = f[:, :, n]; f[:, :, n + 1] = f[:, :, 1]
+        f[:, 0, :] = f[:, n, :]; f[:, n + 1, :] = f[:, 1, :]
+    for f in vel[:2]:
+        f[0] = -f[1]; f[n + 1] = -f[n]
+    vel[2][0] = 0.0; vel[2][n] = 0.0; vel[2][n + 1] = 0.0
+    pristine = {"u": vel[0], "v": vel[1], "w": vel[2], "p": torch.zeros((n + 2,) * 3, dtype=torch.float64)}
+    dd = {k: t.to(dev) for k, t in pristine.items()}
+    dzci_d, dzfi_d = torch.from_numpy(dzci).to(dev), torch.from_numpy(dzfi).to(dev)
+    dzc, dzf = 1.0 / dzci, 1.0 / dzfi
+
+    def fresh():
+        return {k: t.clone() for k, t in dd.items()}
+
+    def three_calls(f):
+        F.fillps([n, n, n], 1, 1, dxi, dyi, float(n), dzfi_d, 1.0 / DT, 1.0, f["u"], f["v"], f["w"], f["p"])
+        P.solver(f["p"])
+        F.boundp(CBC, [n, n, n], [0.0] * 6, 1, [1.0 / n] * 3, dzc, dzf, f["p"])
+        F.correc([n, n, n], 1, 1, dxi, dyi, float(n), dzci_d, DT, 1.0, f["p"], f["u"], f["v"], f["w"])
+        F.bounduvw(CBCVEL, [n, n, n], BCVEL, 1, 1, [1.0 / n] * 3, dzc, dzf, f["u"], f["v"], f["w"])
+
+    def fused(f):
+        P.projection(1, dxi, dyi, dzci_d, dzfi_d, [0.0] * 6, DT, 1.0, f["u"], f["v"], f["w"], f["p"], precision=0,
+                     cbcvel=CBCVEL, bcvel=BCVEL)
+
+    def timed(fn, steps):
+        fs = [fresh() for _ in range(steps + 3)]
+        for i in range(3):
+            fn(fs[i])
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for i in range(steps):
+            fn(fs[3 + i])
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps, fs[-1]
+
+    steps = max(args.steps, 10)
+    t3, f3 = timed(three_calls, steps)
+    tf, ff = timed(fused, steps)
+    _, div3 = F.chkdiv([n, n, n], dxi, dyi, float(n), 1, 1, dzfi_d, f3["u"], f3["v"], f3["w"])
+    _, divf = F.chkdiv([n, n, n], dxi, dyi, float(n), 1, 1, dzfi_d, ff["u"], ff["v"], ff["w"])
+    # e2e through host arrays (pinned)
+    host = {k: t.clone().pin_memory() for k, t in pristine.items()}
+    hnp = {k: t.numpy() for k, t in host.items()}
+    for _ in range(2):
+        P.projection(1, dxi, dyi, dzci, dzfi, [0.0] * 6, DT, 1.0, hnp["u"], hnp["v"], hnp["w"], hnp["p"],
+                     precision=0, cbcvel=CBCVEL, bcvel=BCVEL)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        P.projection(1, dxi, dyi, dzci, dzfi, [0.0] * 6, DT, 1.0, hnp["u"], hnp["v"], hnp["w"], hnp["p"],
+                     precision=0, cbcvel=CBCVEL, bcvel=BCVEL)
+    te = (time.perf_counter() - t0) * 1e3 / steps
+    # the oracle restatement of the same three calls on the host cores
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        S = O.SolverSetup([n, n, n], [dxi, dyi, float(n)], 1, dzci, dzfi, CBC, [0.0] * 6, "ccc")
+        f = {k: t.numpy().copy() for k, t in pristine.items()}
+        def cpu_once():
+            O.fillps([n, n, n], 1, 1, dxi, dyi, float(n), dzfi, 1.0 / DT, 1.0, f["u"], f["v"], f["w"], f["p"])
+            S.solve(f["p"])
+            O.boundp(CBC, [n, n, n], [0.0] * 6, 1, [1.0 / n] * 3, dzc, dzf, f["p"])
+            O.correc([n, n, n], 1, 1, dxi, dyi, float(n), dzci, DT, 1.0, f["p"], f["u"], f["v"], f["w"])
+            O.bounduvw(CBCVEL, [n, n, n], BCVEL, 1, 1, [1.0 / n] * 3, dzc, dzf, f["u"], f["v"], f["w"])
+        cpu_once()
+        reps, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < min(args.cpu_budget, 5.0) or reps < 3:
+            cpu_once()
+            reps += 1
+        tc = (time.perf_counter() - t0) / reps * 1e3
+        cpu = {"ms_per_projection": round(tc, 3), "projections_per_s": round(1e3 / tc, 2), "cores": O.get_threads(),
+               "kind": "port", "sample": f"{reps} FP64 fillps+solver+boundp+correc+bounduvw at 128^3"}
+    cells = n ** 3
+    return {"mode": "c1", "workload": "single-phase FP64 projection 128^3, periodic x,y, walls z, U[-1,1] velocities",
+            "three_calls": {"ms": round(t3, 4), "projections_per_s": round(1e3 / t3, 2),
+                            "hbm_gbs_136B": round(136 * cells / t3 / 1e6, 1)},
+            "fused": {"ms": round(tf, 4), "projections_per_s": round(1e3 / tf, 2),
+                      "hbm_gbs_112B": round(112 * cells / tf / 1e6, 1)},
+            "e2e_fused_host_arrays": {"ms": round(te, 3), "projections_per_s": round(1e3 / te, 2)},
+            "max_div_after": {"three_calls": div3, "fused": divf}, "div_bound": 1e-11 * dxi, "cpu_baseline": cpu,
+            "hbm_peak_gbs": peaks()[0]}
+
+
+def run_config3(args):
+    """C3: stretched-grid solve, 512x512x256, tanh two-end clustering (gr = 2) in z,
+    Neumann x (DCT-II), periodic y, Neumann bottom / Dirichlet top in z; RHS a
+    seeded Gaussian random field with a k^-5/3 spectrum, zero mean.  FP64 solver
+    against the mixed solve refined to 1e-6 and to 1e-10 (device-resident)."""
+    import torch
+    import flutas_gb300 as F
+    dev = torch.device("cuda:0")
+    nx, ny, nz = 512, 512, 256
+    cbc = "NNPPND"
+    dzci, dzfi = zgrid_stretched(nz, 2.0)
+    dli = [float(nx), float(ny), float(nz)]
+    P = F.initsolver([nx, ny, nz], dli, 1, dzci, dzfi, cbc, [0.0] * 6, "ccc")
+    g = torch.Generator(device=dev).manual_seed(args.seed)
+    white = torch.randn((nz, ny, nx), generator=g, dtype=torch.float64, device=dev)
+    spec = torch.fft.rfftn(white)
+    kz = torch.fft.fftfreq(nz, device=dev, dtype=torch.float64)[:, None, None] * nz
+    ky = torch.fft.fftfreq(ny, device=dev, dtype=torch.float64)[None, :, None] * ny
+    kx = torch.fft.rfftfreq(nx, device=dev, dtype=torch.float64)[None, None, :] * nx
+    k = torch.sqrt(kx * kx + ky * ky + kz * kz)
+    k[0, 0, 0] = 1.0
+    spec *= k ** (-5.0 / 6.0)       # power ~ k^-5/3
+    spec[0, 0, 0] = 0.0
+    field = torch.fft.irfftn(spec, s=(nz, ny, nx))
+    field -= field.mean()
+    field /= field.std()
+    rhs = torch.zeros((nz + 2, ny + 2, nx + 2), dtype=torch.float64, device=dev)
+    rhs[1:-1, 1:-1, 1:-1] = field
+    del white, spec, k, field
+
+    def timed(fn, steps):
+        bufs = [rhs.clone() for _ in range(2)]
+        out = None
+        for i in range(3):
+            bufs[i % 2].copy_(rhs)
+            out = fn(bufs[i % 2])
+        ts, extra = [], []
+        for i in range(steps):
+            b = bufs[i % 2]
+            b.copy_(rhs)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = fn(b)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+            extra.append(out)
+        return float(np.median(ts)), b, extra[-1]
+
+    steps = max(args.steps // 2, 8)
+    t64, p64, _ = timed(lambda b: P.solver(b), steps)
+    p64 = p64.clone()
+    res = {}
+    for tol in (1e-6, 1e-10):
+        tm, pm, (rr, its) = timed(lambda b: P.solve_mixed(b, tol=tol, max_iter=10), steps)
+        d = pm[1:-1, 1:-1, 1:-1] - p64[1:-1, 1:-1, 1:-1]
+        err = float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(p64[1:-1, 1:-1, 1:-1]))
+        res[f"mixed_{tol:g}"] = {"ms": round(tm, 4), "solves_per_s": round(1e3 / tm, 2), "relres": rr,
+                                 "fp32_solves": its, "rel_l2_vs_fp64": err}
+    info = P.info()
+    return {"mode": "c3", "workload": "Poisson solve 512x512x256, tanh-stretched z (gr 2), BC NN/PP/ND, k^-5/3 RHS",
+            "fp64": {"ms": round(t64, 4), "solves_per_s": round(1e3 / t64, 2),
+                     "hbm_gbs_48B": round(48 * nx * ny * nz / t64 / 1e6, 1)},
+            **res, "xy_path_fp32": info["xy_path_fp32"], "xy_path_fp64": info["xy_path_fp64"],
+            "timing": "CUDA events per solve (median), RHS reloaded untimed"}
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -769,7 +955,7 @@ def main():
                     help="only the headline mode (for profiler captures): W warm-up + K steps, no extra modes, "
                          "no e2e, no CPU baseline")
     ap.add_argument("--precision", type=int, default=1, help="with --single: 1 mixed to 1e-10, 0 FP64")
-    ap.add_argument("--mode", choices=["projection", "batch", "serve"], default="projection",
+    ap.add_argument("--mode", choices=["projection", "batch", "serve", "c1", "c3"], default="projection",
                     help="projection: the headline two-phase step; batch: 512 uneven grids in one graph; "
                          "serve: Poisson request stream through the continuous-batching server")
     ap.add_argument("--grids", type=int, default=512)
@@ -784,7 +970,7 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "ours" and args.mode != "projection":
-        res = run_batch(args) if args.mode == "batch" else run_serve(args)
+        res = {"batch": run_batch, "serve": run_serve, "c1": run_config1, "c3": run_config3}[args.mode](args)
     elif args.impl == "reference":
         res = run_reference(args, rank)
     else:

@@ -12,13 +12,12 @@
 #include "fft_fixed.cuh"
 
 #include <cstdlib>
+#include <type_traits>
 #include <mutex>
 #include <set>
 
 namespace fg {
 namespace {
-
-constexpr int FIX_NTH = 256;
 
 template <typename T, int N, int C> struct FixGeo {
   static constexpr int ROWS = N / C, COLS = N / C, P = N + 1, BX = ROWS / 2, BY = COLS / 2;
@@ -35,7 +34,7 @@ struct Barrier {
 
 // Columns [r*COLS, (r+1)*COLS) of every CTA's x-spectrum rows (pitch P) into
 // this CTA's column block (N x COLS, row-major).
-template <typename T, int N, int C>
+template <typename T, int N, int C, int FIX_NTH>
 __device__ __forceinline__ void gather_cols(cg::cluster_group &cl, T *slab, T *blk, int r) {
   using G = FixGeo<T, N, C>;
   constexpr int TOT = N * G::COLS, U = 8;
@@ -59,7 +58,7 @@ __device__ __forceinline__ void gather_cols(cg::cluster_group &cl, T *slab, T *b
 }
 
 // This CTA's rows (ROWS x N, pitch P) from every CTA's column block.
-template <typename T, int N, int C>
+template <typename T, int N, int C, int FIX_NTH>
 __device__ __forceinline__ void gather_rows(cg::cluster_group &cl, T *blk, T *slab, int r) {
   using G = FixGeo<T, N, C>;
   constexpr int TOT = G::ROWS * N, U = 8;
@@ -81,7 +80,7 @@ __device__ __forceinline__ void gather_rows(cg::cluster_group &cl, T *blk, T *sl
   }
 }
 
-template <typename T, int N, int PX, int PY>
+template <typename T, int N, int PX, int PY, int FIX_NTH>
 __device__ __forceinline__ void load_tables(const AxisPlan &ax, const AxisPlan &ay, C2<T> *Wt, C2<T> *Qx, C2<T> *Qy) {
   for (int i = threadIdx.x; i < N; i += FIX_NTH) {
     Wt[i] = ((const C2<T> *)ax.W)[i];
@@ -90,15 +89,15 @@ __device__ __forceinline__ void load_tables(const AxisPlan &ax, const AxisPlan &
   }
 }
 
-template <typename T, int N, int C, int PX, int PY, typename In>
-__global__ void __launch_bounds__(FIX_NTH, 2) k_xyfwd_fix(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
+template <typename T, int N, int C, int FIX_NTH, int PX, int PY, typename In>
+__global__ void __launch_bounds__(FIX_NTH, 512 / FIX_NTH) k_xyfwd_fix(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
   using G = FixGeo<T, N, C>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
   const int r = (int)cluster.block_rank(), tid = threadIdx.x;
   T *B0 = (T *)smem_raw, *B1 = (T *)(smem_raw + G::BUF), *B2 = (T *)(smem_raw + 2 * G::BUF);
   C2<T> *Wt = (C2<T> *)(smem_raw + 3 * G::BUF), *Qx = Wt + N, *Qy = Qx + N;
-  load_tables<T, N, PX, PY>(ax, ay, Wt, Qx, Qy);
+  load_tables<T, N, PX, PY, FIX_NTH>(ax, ay, Wt, Qx, Qy);
   const Barrier bar;
   const int y0 = r * G::ROWS;
   float ss = 0.0f;
@@ -122,7 +121,7 @@ __global__ void __launch_bounds__(FIX_NTH, 2) k_xyfwd_fix(AxisPlan ax, AxisPlan 
     fix::forward<T, N, PX, G::BX, FIX_NTH>(B0, G::P, 1, (C2<T> *)B1, (C2<T> *)B2, Wt, Qx,
                                             StorePlaneReal<T>{B0, G::P, 0}, tid, bar);
     cluster.sync();  // every CTA's x-spectrum rows are complete
-    gather_cols<T, N, C>(cluster, B0, B1, r);
+    gather_cols<T, N, C, FIX_NTH>(cluster, B0, B1, r);
     cluster.sync();  // every CTA has read the rows
     // y: columns in B1 -> stages in B2/B0 -> split into S
     fix::forward<T, N, PY, G::BY, FIX_NTH>(B1, 1, G::COLS, (C2<T> *)B2, (C2<T> *)B0, Wt, Qy,
@@ -132,15 +131,15 @@ __global__ void __launch_bounds__(FIX_NTH, 2) k_xyfwd_fix(AxisPlan ax, AxisPlan 
   if (nrm) block_sum_add((double)ss, nrm);
 }
 
-template <typename T, int N, int C, int PX, int PY, typename Out>
-__global__ void __launch_bounds__(FIX_NTH, 2) k_xyinv_fix(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
+template <typename T, int N, int C, int FIX_NTH, int PX, int PY, typename Out>
+__global__ void __launch_bounds__(FIX_NTH, 512 / FIX_NTH) k_xyinv_fix(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
   using G = FixGeo<T, N, C>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
   const int r = (int)cluster.block_rank(), tid = threadIdx.x;
   T *B0 = (T *)smem_raw, *B1 = (T *)(smem_raw + G::BUF), *B2 = (T *)(smem_raw + 2 * G::BUF);
   C2<T> *Wt = (C2<T> *)(smem_raw + 3 * G::BUF), *Qx = Wt + N, *Qy = Qx + N;
-  load_tables<T, N, PX, PY>(ax, ay, Wt, Qx, Qy);
+  load_tables<T, N, PX, PY, FIX_NTH>(ax, ay, Wt, Qx, Qy);
   const Barrier bar;
   const int y0 = r * G::ROWS;
   for (int k = blockIdx.x / C; k < g.nz; k += gridDim.x / C) {
@@ -154,7 +153,7 @@ __global__ void __launch_bounds__(FIX_NTH, 2) k_xyinv_fix(AxisPlan ax, AxisPlan 
     fix::inverse<T, N, PY, G::BY, FIX_NTH>(B0, 1, G::COLS, B2, 1, G::COLS, (C2<T> *)B1, (C2<T> *)B0, Wt, Qy, tid,
                                             bar);
     cluster.sync();  // every CTA's column block is complete
-    gather_rows<T, N, C>(cluster, B2, B0, r);
+    gather_rows<T, N, C, FIX_NTH>(cluster, B2, B0, r);
     cluster.sync();  // every CTA has read the blocks
     // x^-1: rows in B0 -> stages in B1/B0 -> rows in B2 (pitch P)
     fix::inverse<T, N, PX, G::BX, FIX_NTH>(B0, G::P, 1, B2, G::P, 1, (C2<T> *)B1, (C2<T> *)B0, Wt, Qx, tid, bar);
@@ -177,7 +176,7 @@ __global__ void __launch_bounds__(FIX_NTH, 2) k_xyinv_fix(AxisPlan ax, AxisPlan 
 }
 
 // Raises the kernel's dynamic shared-memory limit once per device.
-int prepare(const void *kernel, size_t smem) {
+int prepare(const void *kernel, size_t smem, int C) {
   static std::mutex mu;
   static std::set<std::pair<const void *, int>> done;
   std::lock_guard<std::mutex> lk(mu);
@@ -185,16 +184,18 @@ int prepare(const void *kernel, size_t smem) {
   if (cudaGetDevice(&dev) != cudaSuccess) return -1;
   if (done.count({kernel, dev})) return 0;
   if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+  if (C > 8 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+    return -1;
   done.insert({kernel, dev});
   return 0;
 }
 
 template <typename K, typename... Args>
-cudaError_t cluster_start(K kernel, size_t smem, int clusters, int C, cudaStream_t st, Args... args) {
-  if (prepare((const void *)kernel, smem)) return cudaErrorInvalidValue;
+cudaError_t cluster_start(K kernel, size_t smem, int clusters, int C, int nth, cudaStream_t st, Args... args) {
+  if (prepare((const void *)kernel, smem, C)) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(clusters * C));
-  cfg.blockDim = dim3(FIX_NTH);
+  cfg.blockDim = dim3((unsigned)nth);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute at[1];
@@ -209,52 +210,66 @@ cudaError_t cluster_start(K kernel, size_t smem, int clusters, int C, cudaStream
 
 bool kind_ok(int p) { return p == BC_PP || p == BC_NN; }
 
-template <int N, int C, typename In>
-cudaError_t fwd_pairs(const AxisPlan &ax, const AxisPlan &ay, const In &in, float *S, const Geo &g, double *nrm,
-                      cudaStream_t st) {
-  using G = FixGeo<float, N, C>;
-  const int px = ax.pair, py = ay.pair;
-#define FG_FIX_FWD(PX, PY)                                                                                      \
-  if (px == PX && py == PY)                                                                                     \
-    return cluster_start(k_xyfwd_fix<float, N, C, PX, PY, In>, G::SMEM, g.nz, C, st, ax, ay, in, S, g, nrm);
-  FG_FIX_FWD(BC_PP, BC_PP)
-  FG_FIX_FWD(BC_PP, BC_NN)
-  FG_FIX_FWD(BC_NN, BC_PP)
-  FG_FIX_FWD(BC_NN, BC_NN)
-#undef FG_FIX_FWD
+// Built variants: (N, C, threads) = (256, 8, 256) with two CTAs per SM and
+// (512, 16, 512) with one (non-portable cluster size).
+template <int N> struct FixCfg;
+template <> struct FixCfg<256> { static constexpr int C = 8, NTH = 256; };
+template <> struct FixCfg<512> { static constexpr int C = 16, NTH = 512; };
+
+template <int N, typename F> cudaError_t with_kinds(int px, int py, F &&f) {
+  if (px == BC_PP && py == BC_PP) return f(std::integral_constant<int, BC_PP>(), std::integral_constant<int, BC_PP>());
+  if (px == BC_PP && py == BC_NN) return f(std::integral_constant<int, BC_PP>(), std::integral_constant<int, BC_NN>());
+  if (px == BC_NN && py == BC_PP) return f(std::integral_constant<int, BC_NN>(), std::integral_constant<int, BC_PP>());
+  if (px == BC_NN && py == BC_NN) return f(std::integral_constant<int, BC_NN>(), std::integral_constant<int, BC_NN>());
   return cudaErrorInvalidValue;
 }
 
-template <int N, int C, typename Out>
-cudaError_t inv_pairs(const AxisPlan &ax, const AxisPlan &ay, const float *S, const Out &out, const Geo &g,
-                      cudaStream_t st) {
-  using G = FixGeo<float, N, C>;
-  const int px = ax.pair, py = ay.pair;
-#define FG_FIX_INV(PX, PY)                                                                                      \
-  if (px == PX && py == PY)                                                                                     \
-    return cluster_start(k_xyinv_fix<float, N, C, PX, PY, Out>, G::SMEM, g.nz, C, st, ax, ay, S, out, g);
-  FG_FIX_INV(BC_PP, BC_PP)
-  FG_FIX_INV(BC_PP, BC_NN)
-  FG_FIX_INV(BC_NN, BC_PP)
-  FG_FIX_INV(BC_NN, BC_NN)
-#undef FG_FIX_INV
-  return cudaErrorInvalidValue;
+template <int N>
+cudaError_t fwd_n(const AxisPlan &ax, const AxisPlan &ay, const InF32 &in, float *S, const Geo &g, double *nrm,
+                  cudaStream_t st) {
+  using Cf = FixCfg<N>;
+  using G = FixGeo<float, N, Cf::C>;
+  return with_kinds<N>(ax.pair, ay.pair, [&](auto px, auto py) {
+    return cluster_start(k_xyfwd_fix<float, N, Cf::C, Cf::NTH, decltype(px)::value, decltype(py)::value, InF32>,
+                         G::SMEM, g.nz, Cf::C, Cf::NTH, st, ax, ay, in, S, g, nrm);
+  });
 }
 
-template <typename In>
-cudaError_t fwd_dispatch(const AxisPlan &ax, const AxisPlan &ay, const In &in, float *S, const Geo &g, double *nrm,
-                         int C, cudaStream_t st, bool *handled) {
-  *handled = fixed_supported(g.nx, g.ny, C, ax.pair, ay.pair);
-  if (!*handled) return cudaSuccess;
-  return fwd_pairs<256, 8, In>(ax, ay, in, S, g, nrm, st);
+template <int N, typename Out>
+cudaError_t inv_n(const AxisPlan &ax, const AxisPlan &ay, const float *S, const Out &out, const Geo &g,
+                  cudaStream_t st) {
+  using Cf = FixCfg<N>;
+  using G = FixGeo<float, N, Cf::C>;
+  return with_kinds<N>(ax.pair, ay.pair, [&](auto px, auto py) {
+    return cluster_start(k_xyinv_fix<float, N, Cf::C, Cf::NTH, decltype(px)::value, decltype(py)::value, Out>,
+                         G::SMEM, g.nz, Cf::C, Cf::NTH, st, ax, ay, S, out, g);
+  });
 }
 
-template <typename Out>
-cudaError_t inv_dispatch(const AxisPlan &ax, const AxisPlan &ay, const float *S, const Out &out, const Geo &g, int C,
-                         cudaStream_t st, bool *handled) {
-  *handled = fixed_supported(g.nx, g.ny, C, ax.pair, ay.pair);
-  if (!*handled) return cudaSuccess;
-  return inv_pairs<256, 8, Out>(ax, ay, S, out, g, st);
+// Co-resident clusters of the (N, PP, PP) inverse kernel: 0 when a cluster
+// of the required size cannot be placed on this device.
+template <int N> int capacity_n() {
+  using Cf = FixCfg<N>;
+  using G = FixGeo<float, N, Cf::C>;
+  auto kernel = k_xyinv_fix<float, N, Cf::C, Cf::NTH, BC_PP, BC_PP, OutHalo>;
+  if (prepare((const void *)kernel, G::SMEM, Cf::C)) return 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)Cf::C);
+  cfg.blockDim = dim3((unsigned)Cf::NTH);
+  cfg.dynamicSmemBytes = G::SMEM;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)Cf::C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kernel, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
 }
 
 }  // namespace
@@ -263,32 +278,34 @@ bool fixed_supported(int nx, int ny, int C, int px, int py) {
   if (const char *e = getenv("FLUTAS_GB300_FIXED")) {  // 0 disables the fixed-size kernels (A/B timing)
     if (atoi(e) == 0) return false;
   }
-  return nx == 256 && ny == 256 && C == 8 && kind_ok(px) && kind_ok(py);
+  if (nx != ny || !kind_ok(px) || !kind_ok(py)) return false;
+  return (nx == 256 && C == FixCfg<256>::C) || (nx == 512 && C == FixCfg<512>::C);
 }
 
-cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InKeep<InFillps> &in, float *S, const Geo &g,
-                        double *nrm, int C, cudaStream_t st, bool *handled) {
-  return fwd_dispatch(ax, ay, in, S, g, nrm, C, st, handled);
+int fixed_cluster_size(int nx, int ny, int px, int py) {
+  if (nx != ny || !kind_ok(px) || !kind_ok(py)) return 0;
+  if (nx == 256) return capacity_n<256>() > 0 ? FixCfg<256>::C : 0;
+  if (nx == 512) return capacity_n<512>() > 0 ? FixCfg<512>::C : 0;
+  return 0;
 }
-cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InKeep<InHalo> &in, float *S, const Geo &g,
-                        double *nrm, int C, cudaStream_t st, bool *handled) {
-  return fwd_dispatch(ax, ay, in, S, g, nrm, C, st, handled);
-}
-cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InResidual &in, float *S, const Geo &g,
-                        double *nrm, int C, cudaStream_t st, bool *handled) {
-  return fwd_dispatch(ax, ay, in, S, g, nrm, C, st, handled);
-}
+
 cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InF32 &in, float *S, const Geo &g,
                         double *nrm, int C, cudaStream_t st, bool *handled) {
-  return fwd_dispatch(ax, ay, in, S, g, nrm, C, st, handled);
+  *handled = fixed_supported(g.nx, g.ny, C, ax.pair, ay.pair);
+  if (!*handled) return cudaSuccess;
+  return g.nx == 256 ? fwd_n<256>(ax, ay, in, S, g, nrm, st) : fwd_n<512>(ax, ay, in, S, g, nrm, st);
 }
 cudaError_t xyinv_fixed(const AxisPlan &ax, const AxisPlan &ay, const float *S, const OutHalo &out, const Geo &g,
                         int C, cudaStream_t st, bool *handled) {
-  return inv_dispatch(ax, ay, S, out, g, C, st, handled);
+  *handled = fixed_supported(g.nx, g.ny, C, ax.pair, ay.pair);
+  if (!*handled) return cudaSuccess;
+  return g.nx == 256 ? inv_n<256>(ax, ay, S, out, g, st) : inv_n<512>(ax, ay, S, out, g, st);
 }
 cudaError_t xyinv_fixed(const AxisPlan &ax, const AxisPlan &ay, const float *S, const OutHaloAdd &out, const Geo &g,
                         int C, cudaStream_t st, bool *handled) {
-  return inv_dispatch(ax, ay, S, out, g, C, st, handled);
+  *handled = fixed_supported(g.nx, g.ny, C, ax.pair, ay.pair);
+  if (!*handled) return cudaSuccess;
+  return g.nx == 256 ? inv_n<256>(ax, ay, S, out, g, st) : inv_n<512>(ax, ay, S, out, g, st);
 }
 
 }  // namespace fg

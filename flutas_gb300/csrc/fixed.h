@@ -8,9 +8,13 @@
 
 namespace fg {
 
-// Built variants: FP32, square planes N x N with N = 256 and clusters of 8
-// CTAs, x and y transforms of kind PP or NN.
+// Built variants: FP32, square planes N x N with N = 256 (clusters of 8 CTAs,
+// two per SM) or N = 512 (clusters of 16, one per SM), x and y transforms of
+// kind PP or NN, input already evaluated in FP32 (k_stencil_pass).
 bool fixed_supported(int nx, int ny, int C, int px, int py);
+// Cluster size of the built variant for this plane, 0 when none is built or
+// this device cannot place its cluster.
+int fixed_cluster_size(int nx, int ny, int px, int py);
 
 template <typename T, typename In>
 cudaError_t xyfwd_fixed(const AxisPlan &, const AxisPlan &, const In &, T *, const Geo &, double *, int,
@@ -18,12 +22,6 @@ cudaError_t xyfwd_fixed(const AxisPlan &, const AxisPlan &, const In &, T *, con
   *handled = false;
   return cudaSuccess;
 }
-cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InKeep<InFillps> &in, float *S, const Geo &g,
-                        double *nrm, int C, cudaStream_t st, bool *handled);
-cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InKeep<InHalo> &in, float *S, const Geo &g,
-                        double *nrm, int C, cudaStream_t st, bool *handled);
-cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InResidual &in, float *S, const Geo &g,
-                        double *nrm, int C, cudaStream_t st, bool *handled);
 cudaError_t xyfwd_fixed(const AxisPlan &ax, const AxisPlan &ay, const InF32 &in, float *S, const Geo &g,
                         double *nrm, int C, cudaStream_t st, bool *handled);
 

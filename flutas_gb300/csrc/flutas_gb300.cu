@@ -868,6 +868,13 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
   if (!pl->path32 && (pl->clus32 = cluster_size_for<float>(nx, ny, smax)) &&
       cluster_capacity(k_xyinv_cluster<float, OutHalo>, cluster_plane_smem(nx, ny, pl->clus32, 4), pl->clus32) > 0)
     pl->path32 = 2;
+  if (!pl->path32) {  // planes whose only cluster split is a compile-time-sized variant (512^2: 16 CTAs)
+    const int cf = fixed_cluster_size(nx, ny, px, py);
+    if (cf) {
+      pl->path32 = 2;
+      pl->clus32 = cf;
+    }
+  }
   if (const char *e = getenv("FLUTAS_GB300_XY_PATH")) {  // 0 forces separate passes (A/B timing)
     if (atoi(e) == 0) pl->path64 = pl->path32 = 0;
   }

@@ -317,11 +317,11 @@ def test_gpu_mixed_reported_residual(lib, oracle, n, cbc):
         assert relres <= max(tol, 1e-11)
 
 
-@pytest.mark.parametrize("cbc", ["PPPPNN", "NNPPDD", "PPNNNN", "NNNNPP"])
-def test_gpu_fixed_size_cluster_kernels(lib, oracle, cbc, monkeypatch):
-    """256^2 planes run the compile-time-sized cluster kernels in the mixed path;
-    the result matches the oracle and the run-time-sized kernels."""
-    n = (256, 256, 5)
+@pytest.mark.parametrize("n,cbc", [((256, 256, 5), "PPPPNN"), ((256, 256, 5), "NNPPDD"), ((256, 256, 5), "PPNNNN"),
+                                   ((256, 256, 5), "NNNNPP"), ((512, 512, 3), "NNPPND"), ((512, 512, 3), "PPPPNN")])
+def test_gpu_fixed_size_cluster_kernels(lib, oracle, n, cbc, monkeypatch):
+    """256^2 and 512^2 planes run the compile-time-sized cluster kernels in the
+    mixed path; the result matches the oracle and the run-time-sized kernels."""
     rng = np.random.default_rng(3)
     P, dzci, dzfi, dzc, dzf, dli = plan_for(lib, n, cbc, 0.5)
     f = compatible_rhs(rng, n, cbc, dzf)

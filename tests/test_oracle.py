@@ -145,3 +145,14 @@ def test_oracle_projection_is_divergence_free(oracle, cbc, nh_u):
     velocity_ghosts(u, v, w, n, cbc, nh_u)
     tot, mx = O.chkdiv(n, dxi, dyi, 1.0, nh_u, nh_u, dzfi, u, v, w)
     assert mx <= 1e-11 * 1.0 * dxi
+
+
+@pytest.mark.parametrize("gr", [0.0, 1.0, 2.0])
+def test_bench_grid_matches_initgrid(oracle, gr):
+    """bench.py's stretched z grid (configuration C3) is initgrid's (src/initgrid.f90)."""
+    import bench
+    n = 64
+    dzci, dzfi = bench.zgrid_stretched(n, gr)
+    dzc, dzf, zc, zf = oracle.initgrid(n, gr, 1.0, 1)
+    # equal up to the last bits of libm tanh (numpy vs C)
+    assert np.allclose(1.0 / dzci, dzc, rtol=1e-12, atol=0) and np.allclose(1.0 / dzfi, dzf, rtol=1e-12, atol=0)
