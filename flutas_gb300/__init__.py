@@ -46,6 +46,7 @@ EXPORTED = [
     "flutas_gb300_batch_destroy", "flutas_gb300_batch_set", "flutas_gb300_batch_get",
     "flutas_gb300_server_create", "flutas_gb300_server_submit", "flutas_gb300_server_wait",
     "flutas_gb300_server_stats", "flutas_gb300_server_reset_stats", "flutas_gb300_server_destroy",
+    "flutas_gb300_load", "flutas_gb300_load_scalar", "flutas_gb300_load_ns",
 ]
 
 
@@ -116,6 +117,9 @@ def load(path: str | None = None):
     L.flutas_gb300_last_solve.argtypes = [vp, vp, vp]
     L.flutas_gb300_profile.argtypes = [ip]
     L.flutas_gb300_profile_report.argtypes = [C.c_char_p, ip, ip]
+    L.flutas_gb300_load.argtypes = [C.c_char, C.c_char_p, vp, ip, vp]
+    L.flutas_gb300_load_scalar.argtypes = [C.c_char, C.c_char_p, vp, vp, vp]
+    L.flutas_gb300_load_ns.argtypes = [C.c_char, C.c_char_p, vp, ip, vp, vp, vp, vp, vp, vp]
     for name in EXPORTED:
         getattr(L, name).restype = C.c_int
     _lib = L
@@ -338,6 +342,30 @@ def chkdiv_noalloc(n, dxi, dyi, dzi, nh_d, nh_u, dzfi, u, v, w):
                                               float(dzi), int(nh_d), int(nh_u), _ptr(dzfi), _ptr(u), _ptr(v),
                                               _ptr(w), C.addressof(tot), C.addressof(mx)))
     return tot.value, mx.value
+
+
+def load_field(io, filename, n, fld, nh=1):
+    """load (src/load.f90:21-89): io 'r' reads the raw FP64 interior of `filename`
+    into fld (halo nh; host array or CUDA tensor), io 'w' writes it."""
+    _check(load().flutas_gb300_load(io.encode()[:1], str(filename).encode(), C.cast(_i3(n), C.c_void_p), int(nh),
+                                    _ptr(fld)))
+
+
+def load_scalar(io, filename, time=0.0, istep=0, dto=0.0):
+    """load_scalar (src/load.f90:91-128); returns (time, istep, dto)."""
+    t, it, d = C.c_double(time), C.c_int(istep), C.c_double(dto)
+    _check(load().flutas_gb300_load_scalar(io.encode()[:1], str(filename).encode(), C.addressof(t), C.addressof(it),
+                                           C.addressof(d)))
+    return t.value, it.value, d.value
+
+
+def load_ns(io, filename, n, u, v, w, p, time=0.0, istep=0.0, nh=1):
+    """load_ns (src/load.f90:130-214); returns (time, istep)."""
+    t, it = C.c_double(time), C.c_double(istep)
+    _check(load().flutas_gb300_load_ns(io.encode()[:1], str(filename).encode(), C.cast(_i3(n), C.c_void_p),
+                                       int(nh), _ptr(u), _ptr(v), _ptr(w), _ptr(p), C.addressof(t),
+                                       C.addressof(it)))
+    return t.value, it.value
 
 
 def pres_tw_src(n, dxi, dyi, dzi, nh_d, nh_u, dzci, rho0i, f_t12, f_t12_o, p, pold, rho, u, v, w):

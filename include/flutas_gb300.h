@@ -247,6 +247,25 @@ FLUTAS_API int flutas_gb300_server_reset_stats(void *server);
 /* Waits for every queued request, then stops the workers and frees the plans. */
 FLUTAS_API int flutas_gb300_server_destroy(void *server);
 
+/* ---------------------------------------------------------------------------
+ * Restart-file I/O (src/load.f90).  Fields are raw FP64 files of the global
+ * interior, x fastest, no header, exactly 8*n[0]*n[1]*n[2] bytes.
+ * ------------------------------------------------------------------------- */
+/* load (src/load.f90:21-89): io = 'r' reads `filename` into the interior of
+ * fld, io = 'w' writes the interior of fld to it (created or truncated).  fld
+ * has nh halo cells on every side (nh = 0: fld is the contiguous interior, as
+ * the Fortran explicit-shape dummy argument) and is host or device memory.
+ * Reading a missing file or a file of another size returns FLUTAS_EINVAL with
+ * the reference's message (where it stops the run). */
+FLUTAS_API int flutas_gb300_load(char io, const char *filename, const int n[3], int nh, double *fld);
+/* load_scalar (src/load.f90:91-128): time, dto and istep as text; written
+ * with the format (2E15.7, 1I9.8), read list-directed. */
+FLUTAS_API int flutas_gb300_load_scalar(char io, const char *filename, double *time, int *istep, double *dto);
+/* load_ns (src/load.f90:130-214): u, v, w, p and then (time, istep) as two
+ * FP64 values in one file (the CaNS restart layout); fields as in load. */
+FLUTAS_API int flutas_gb300_load_ns(char io, const char *filename, const int n[3], int nh, double *u, double *v,
+                                    double *w, double *p, double *time, double *istep);
+
 /* Number of kernels this library has launched in the process (all plans). */
 FLUTAS_API int flutas_gb300_launch_count(unsigned long long *count);
 
