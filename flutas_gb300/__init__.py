@@ -46,7 +46,7 @@ EXPORTED = [
     "flutas_gb300_batch_destroy", "flutas_gb300_batch_set", "flutas_gb300_batch_get",
     "flutas_gb300_server_create", "flutas_gb300_server_submit", "flutas_gb300_server_wait",
     "flutas_gb300_server_stats", "flutas_gb300_server_reset_stats", "flutas_gb300_server_destroy",
-    "flutas_gb300_load", "flutas_gb300_load_scalar", "flutas_gb300_load_ns",
+    "flutas_gb300_load", "flutas_gb300_load_scalar", "flutas_gb300_load_ns", "flutas_gb300_update_property",
 ]
 
 
@@ -118,6 +118,7 @@ def load(path: str | None = None):
     L.flutas_gb300_profile.argtypes = [ip]
     L.flutas_gb300_profile_report.argtypes = [C.c_char_p, ip, ip]
     L.flutas_gb300_load.argtypes = [C.c_char, C.c_char_p, vp, ip, vp]
+    L.flutas_gb300_update_property.argtypes = [vp, vp, vp, vp]
     L.flutas_gb300_load_scalar.argtypes = [C.c_char, C.c_char_p, vp, vp, vp]
     L.flutas_gb300_load_ns.argtypes = [C.c_char, C.c_char_p, vp, ip, vp, vp, vp, vp, vp, vp]
     for name in EXPORTED:
@@ -342,6 +343,13 @@ def chkdiv_noalloc(n, dxi, dyi, dzi, nh_d, nh_u, dzfi, u, v, w):
                                               float(dzi), int(nh_d), int(nh_u), _ptr(dzfi), _ptr(u), _ptr(v),
                                               _ptr(w), C.addressof(tot), C.addressof(mx)))
     return tot.value, mx.value
+
+
+def update_property(n, prop12, vof, prop):
+    """update_property (src/vof.f90:240-271): interior of prop from vof."""
+    _check(load().flutas_gb300_update_property(C.cast(_i3(n), C.c_void_p),
+                                               C.cast((C.c_double * 2)(*[float(x) for x in prop12]), C.c_void_p),
+                                               _ptr(vof), _ptr(prop)))
 
 
 def load_field(io, filename, n, fld, nh=1):

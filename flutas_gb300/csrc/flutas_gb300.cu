@@ -1028,6 +1028,25 @@ int flutas_gb300_fillps(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, 
   return FLUTAS_OK;
 }
 
+int flutas_gb300_update_property(const int n[3], const double prop12[2], const double *vof, double *prop) {
+  // src/vof.f90:240-271
+  if (!n || !prop12 || !vof || !prop) return fail(FLUTAS_EINVAL, "update_property: null argument");
+  if (n[0] < 1 || n[1] < 1 || n[2] < 1) return fail(FLUTAS_EINVAL, "update_property: bad sizes");
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  g_ctx_mir.reset();
+  cudaStream_t st = 0;
+  const size_t pb = sizeof(double) * (size_t)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+  Staged sv, sp;
+  TRY(stage_in(g_ctx_mir, vof, pb, true, false, st, &sv));
+  TRY(stage_in(g_ctx_mir, prop, pb, true, true, st, &sp));  // the halo comes back as it went in
+  const Geo g{n[0], n[1], n[2], 1};
+  TRY(launch("k_update_property", st,
+             [&] { k_update_property<<<grid_cells(g), 256, 0, st>>>(sv.d, sp.d, prop12[0], prop12[1], g); }));
+  TRY(stage_out(sp, st));
+  CK(cudaStreamSynchronize(st));
+  return FLUTAS_OK;
+}
+
 int flutas_gb300_correc(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, double dyi, double dzi,
                         const double *dzci, double dt, double rho0, const double *p, double *u, double *v,
                         double *w, const double *rho) {

@@ -944,6 +944,19 @@ __global__ void k_pres_tw_src(PresTwArgs a) {
 }
 #endif
 
+// update_property (src/vof.f90:240-271): prop = vof*prop12(1) + (1-vof)*prop12(2)
+// on the interior of halo-1 arrays, rounded as written (no contraction into an
+// FMA), so the result is bit-identical to the reference expression.
+#ifndef FG_NO_PLAIN_KERNELS
+__global__ void k_update_property(const double *vof, double *prop, double p1, double p2, Geo g) {
+  for_cells(g, [&](int i0, int j0, int k0) {
+    const long c = g.pidx(i0 + 1, j0 + 1, k0 + 1);
+    const double f = vof[c];
+    prop[c] = __dadd_rn(__dmul_rn(f, p1), __dmul_rn(__dsub_rn(1.0, f), p2));
+  });
+}
+#endif
+
 // correc with the pressure increment phi, fused with p = p + phi
 // (src/correc.f90:57-60 and the update of src/apps/two_phase_inc_isot/main__two_phase_inc_isot.f90:698-714).
 struct CorrecAddArgs {

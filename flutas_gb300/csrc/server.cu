@@ -48,6 +48,7 @@ struct PlanEntry {
   Sig sig;
   void *arr[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<double> lam, a, b, c, rx, ry, rz;
+  double normfft = 0.0;
   size_t bytes = 0;   // device bytes held (updated after use)
   bool busy = false;
   Clock::time_point last;
@@ -141,6 +142,7 @@ PlanEntry *acquire_plan(flutas_server *s, const Sig &sig, const flutas_request &
     flutas_gb300_last_error(buf, sizeof buf);
     *err = buf;
   }
+  raw->normfft = nf;
   lk.lock();
   if (*rc) {
     s->plans.remove_if([&](const std::unique_ptr<PlanEntry> &p) { return p.get() == raw; });
@@ -189,7 +191,14 @@ int run_request(flutas_server *s, Request *q, PlanEntry *pe, cudaStream_t st) {
     if ((rc = dmalloc(pb, &x))) return rc;
     bufs.push_back(x);
     cudaMemcpyAsync(x, r.rhs, pb, cudaMemcpyDefault, st);
-    rc = flutas_gb300_solve_mixed(plan, x, r.tol, r.max_iter, &q->relres, &q->iters);
+    if (r.tol > 0.0) {
+      rc = flutas_gb300_solve_mixed(plan, x, r.tol, r.max_iter, &q->relres, &q->iters);
+    } else {  // tol = 0: the plain FP64 solver call (the drop-in form)
+      rc = flutas_gb300_solver(r.n, pe->arr, pe->normfft, pe->lam.data(), pe->a.data(), pe->b.data(), pe->c.data(),
+                               r.cbc + 4, "ccc", x);
+      q->relres = 0.0;
+      q->iters = 0;
+    }
     if (rc == 0 || rc == FLUTAS_EITER) cudaMemcpyAsync(r.p, x, pb, cudaMemcpyDefault, st);
   } else {
     const size_t ub = sizeof(double) * cells_halo(r.n, r.nh_u);
@@ -343,10 +352,16 @@ int flutas_gb300_server_create(size_t hbm_budget, int slots, void **srv) {
 int flutas_gb300_server_submit(void *srv, const flutas_request *r, long long *ticket) {
   flutas_server *s = (flutas_server *)srv;
   if (!s || s->magic != flutas_server::MAGIC || !r || !ticket) return sfail("server_submit: bad arguments");
-  if (r->kind != 0 && r->kind != 1) return FLUTAS_EINVAL;
-  if (r->kind == 0 && (!r->rhs || !r->p || !(r->tol > 0.0))) return FLUTAS_EINVAL;
-  if (r->kind == 1 && (!r->u || !r->v || !r->w || !r->p || r->nh_u < 1 || (r->rho && !r->pold))) return FLUTAS_EINVAL;
-  if (r->n[0] < 2 || r->n[1] < 2 || r->n[2] < 3 || r->nh_d < 1 || !r->dzci || !r->dzfi) return FLUTAS_EINVAL;
+  auto bad = [](const char *why) {
+    fg_set_error_text(why);
+    return FLUTAS_EINVAL;
+  };
+  if (r->kind != 0 && r->kind != 1) return bad("server_submit: kind must be 0 (solve) or 1 (projection)");
+  if (r->kind == 0 && (!r->rhs || !r->p || !(r->tol >= 0.0))) return bad("server_submit: solve needs rhs, p, tol >= 0");
+  if (r->kind == 1 && (!r->u || !r->v || !r->w || !r->p || r->nh_u < 1 || (r->rho && !r->pold)))
+    return bad("server_submit: projection needs u, v, w, p, nh_u >= 1 (and pold with rho)");
+  if (r->n[0] < 2 || r->n[1] < 2 || r->n[2] < 3 || r->nh_d < 1 || !r->dzci || !r->dzfi)
+    return bad("server_submit: bad sizes or missing dzci/dzfi");
   auto q = std::make_unique<Request>();
   q->r = *r;
   memcpy(q->sig.n, r->n, sizeof q->sig.n);

@@ -224,7 +224,7 @@ typedef struct {
   const double *dzci, *dzfi;   /* (1-nh_d:nz+nh_d), host memory */
   char cbc[6];
   const double *bcpre;         /* nullable: homogeneous BC values */
-  double tol;                  /* kind 0: > 0 (mixed precision); kind 1: > 0 mixed, 0 FP64 */
+  double tol;                  /* > 0: mixed precision refined to tol; 0: the plain FP64 path */
   int max_iter;
   const double *rhs;           /* kind 0: RHS, halo-1 array */
   double *p;                   /* kind 0: solution out; kind 1: pressure in/out (p^n -> p^n + phi) */
@@ -246,6 +246,13 @@ FLUTAS_API int flutas_gb300_server_stats(void *server, char *buf, int len);
 FLUTAS_API int flutas_gb300_server_reset_stats(void *server);
 /* Waits for every queued request, then stops the workers and frees the plans. */
 FLUTAS_API int flutas_gb300_server_destroy(void *server);
+
+/* update_property (src/vof.f90:240-271): prop = vof*prop12[0] + (1-vof)*prop12[1]
+ * on the interior of the halo-1 arrays vof and prop (0:n+1 per axis; the halo
+ * of prop is left for boundp, as in the apps: main__two_phase_inc_isot.f90:461-462).
+ * Rounded as the Fortran expression (bit-identical). */
+FLUTAS_API int flutas_gb300_update_property(const int n[3], const double prop12[2], const double *vof,
+                                            double *prop);
 
 /* ---------------------------------------------------------------------------
  * Restart-file I/O (src/load.f90).  Fields are raw FP64 files of the global

@@ -703,9 +703,16 @@ void or_initgrid(int two_end, int n, double gr, double lz, int nh_d, double *dzc
 }
 
 void or_update_property(int nx, int ny, int nz, double rho1, double rho2, const double *psi, double *rho) {
-  const long tot = (long)(nx + 2) * (ny + 2) * (nz + 2);
+  /* src/vof.f90:240-271: prop = vof*prop12(1) + (1-vof)*prop12(2) on the interior (halo-1 arrays); the
+     halo is left to the caller's boundary routine */
+  const long NX = nx + 2, NY = ny + 2;
 #pragma omp parallel for num_threads(NT) schedule(static)
-  for (long t = 0; t < tot; t++) rho[t] = psi[t] * rho1 + (1.0 - psi[t]) * rho2;
+  for (int k = 1; k <= nz; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        const long t = i + NX * (j + NY * (long)k);
+        rho[t] = psi[t] * rho1 + (1.0 - psi[t]) * rho2;
+      }
 }
 
 static inline double ghost_lo(char bc, double p1, double pn) { return bc == 'P' ? pn : (bc == 'N' ? p1 : -p1); }

@@ -91,7 +91,7 @@ void or_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, double dzi, 
 /* initgrid.f90:17-97 with gridpoint_cluster_two_end (102-118) or one_end (120-136). */
 void or_initgrid(int two_end, int n, double gr, double lz, int nh_d, double *dzc,
                  double *dzf, double *zc, double *zf);
-/* vof.f90 update_property: rho = psi*rho1 + (1-psi)*rho2 over the full halo box. */
+/* vof.f90:240-271 update_property: rho = psi*rho1 + (1-psi)*rho2 on the interior of halo-1 arrays. */
 void or_update_property(int nx, int ny, int nz, double rho1, double rho2,
                         const double *psi, double *rho);
 /* Residual of the discrete operator the solver inverts: r = f - A p, with the

@@ -194,8 +194,9 @@ def initgrid(n, gr, lz, nh_d=1, two_end=True):
     return tuple(arrs)  # dzc, dzf, zc, zf
 
 
-def update_property(n, rho1, rho2, psi):
-    rho = np.empty_like(psi)
+def update_property(n, rho1, rho2, psi, rho=None):
+    """Interior of rho from psi (src/vof.f90:240-271); the halo is the caller's (boundp)."""
+    rho = np.zeros_like(psi) if rho is None else rho
     lib().or_update_property(n[0], n[1], n[2], rho1, rho2, psi, rho)
     return rho
 

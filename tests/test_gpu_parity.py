@@ -272,6 +272,11 @@ def test_gpu_two_phase_projection_df(lib, oracle, precision):
     oracle.boundp(cbc, n, [0] * 6, 1, [1 / dxi, 1 / dyi, 1.0], dzc, dzf, pold)
     psi = (rng.uniform(0, 1, shp) > 0.7).astype(np.float64)
     rho = oracle.update_property(n, 1000.0, 1.0, psi)
+    oracle.boundp(cbc, n, [0] * 6, 1, [1 / dxi, 1 / dyi, 1.0], dzc, dzf, rho)  # as the app does after it
+    rho_gpu = np.zeros_like(psi)
+    lib.update_property(n, [1000.0, 1.0], psi, rho_gpu)
+    lib.boundp(cbc, n, [0] * 6, 1, [1 / dxi, 1 / dyi, 1.0], dzc, dzf, rho_gpu)
+    assert np.array_equal(rho_gpu, rho)
     dl = [1 / dxi, 1 / dyi, 0.0]
     uo, vo, wo, po = u.copy(), v.copy(), w.copy(), p.copy()
     oracle.pres_tw_src(n, dxi, dyi, 16.0, 1, 1, dzci, 1.0, dt, dt, po, pold, rho, uo, vo, wo)

@@ -97,3 +97,20 @@ def test_serving_two_phase_projection_request(lib):
                     max_iter=8, cbcvel=cbcvel, bcvel=[0.0] * 18)
     for a, b in zip(fields, alone):
         assert rel_l2(a, b) <= 1e-9
+
+
+def test_serving_fp64_requests(lib):
+    """tol = 0 serves the plain FP64 solver: the result equals the drop-in call's."""
+    reqs = _requests(seed=12)[:3]
+    S = lib.Server(hbm_budget_bytes=8 << 30, slots=2)
+    outs = [np.zeros_like(r["rhs"]) for r in reqs]
+    ts = [S.submit_solve(r["n"], r["dli"], r["dzci"], r["dzfi"], r["cbc"], r["rhs"], o, tol=0.0)
+          for r, o in zip(reqs, outs)]
+    res = [S.wait(t) for t in ts]
+    S.close()
+    for r, o, (rc, rr, it, lat) in zip(reqs, outs, res):
+        assert rc == 0 and it == 0
+        P = lib.initsolver(r["n"], r["dli"], 1, r["dzci"], r["dzfi"], r["cbc"], [0.0] * 6, "ccc")
+        alone = r["rhs"].copy()
+        P.solver(alone)
+        assert np.array_equal(o[1:-1, 1:-1, 1:-1], alone[1:-1, 1:-1, 1:-1])
