@@ -165,6 +165,21 @@ template <typename T, int R, bool INV> FG_HD void dftR(C2<T> *a, const C2<T> *W,
   for (int q = 0; q < R; q++) a[q] = o[q];
 }
 
+// The same with the R roots of unity W_R^m (m < R) already in registers:
+// R - 1 table loads per stage instead of R(R-1) per butterfly.
+template <typename T, int R> FG_HD void dftR_w(C2<T> *a, const C2<T> *wr) {
+  C2<T> o[R];
+#pragma unroll
+  for (int q = 0; q < R; q++) {
+    C2<T> acc = a[0];
+#pragma unroll
+    for (int r = 1; r < R; r++) acc = cadd<T>(acc, cmul<T>(a[r], wr[(r * q) % R]));
+    o[q] = acc;
+  }
+#pragma unroll
+  for (int q = 0; q < R; q++) a[q] = o[q];
+}
+
 template <typename T, int R, bool INV> FG_HD void dft_any(C2<T> *a, const C2<T> *W, int N) {
   if constexpr (R == 2) dft2<T, INV>(a[0], a[1]);
   else if constexpr (R == 4) dft4<T, INV>(a[0], a[1], a[2], a[3]);
@@ -185,6 +200,12 @@ FG_HD void stage_pass(const C2<T> *in, C2<T> *out, int N, int B, int ldb, int Ns
   const int total = B * NR;
   const int tws = N / (Ns * R);
   const FastDiv fb(B), fn(Ns);
+  constexpr bool ODD = (R & (R - 1)) != 0;
+  C2<T> wr[ODD ? R : 1];  // odd radices: W_R^m, loaded once per stage
+  if constexpr (ODD) {
+#pragma unroll
+    for (int m = 0; m < R; m++) wr[m] = twid<T>(W, N, m * (N / R), INV);
+  }
   for (int bf = tid; bf < total; bf += nth) {
     const int c = fb.mod(bf), j = fb.div(bf);
     const int kk = fn.mod(j);
@@ -195,7 +216,8 @@ FG_HD void stage_pass(const C2<T> *in, C2<T> *out, int N, int B, int ldb, int Ns
 #pragma unroll
       for (int r = 1; r < R; r++) a[r] = cmul<T>(a[r], twid<T>(W, N, kk * r * tws, INV));
     }
-    dft_any<T, R, INV>(a, W, N);
+    if constexpr (ODD) dftR_w<T, R>(a, wr);
+    else dft_any<T, R, INV>(a, W, N);
     const int idxD = (j - kk) * R + kk;
 #pragma unroll
     for (int r = 0; r < R; r++) out[(idxD + r * Ns) * ldb + c] = a[r];

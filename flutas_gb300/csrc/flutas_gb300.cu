@@ -1739,6 +1739,7 @@ struct flutas_batch {
   DBuf arena;                 // x, f (FP64 halo), S, S2 (FP32) of every grid
   std::vector<double *> x;    // device halo arrays handed to the caller
   DBuf d_grids, d_prefix, d_counters, d_nrm, d_active, d_relres, d_iters;
+  DBuf d_act, d_ids, d_nslots;  // compacted work lists of the grids still refining
   std::vector<BatchGrid> grids;
   size_t smem_x = 0, smem_y = 0, smem_z = 0;
   int grid_x = 0, grid_y = 0, grid_z = 0;
@@ -1881,7 +1882,7 @@ void batch_free(flutas_batch *bt) {
     if (p) flutas_gb300_fftend(arr);
   }
   DBuf *bufs[] = {&bt->arena, &bt->d_grids, &bt->d_prefix, &bt->d_counters, &bt->d_nrm, &bt->d_active,
-                  &bt->d_relres, &bt->d_iters};
+                  &bt->d_relres, &bt->d_iters, &bt->d_act, &bt->d_ids, &bt->d_nslots};
   for (DBuf *d : bufs) d->release();
   if (bt->stream) cudaStreamDestroy(bt->stream);
   bt->magic = 0;
@@ -1897,7 +1898,10 @@ int batch_capture(flutas_batch *bt, double tol, int max_iter) {
   const int npass = 5 + 5 * max_iter;
   TRY(bt->d_counters.ensure(sizeof(int) * npass));
   BatchGrid *dg = bt->d_grids.as<BatchGrid>();
-  const long *px = bt->d_prefix.as<long>(), *py = px + (ng + 1), *pz = py + (ng + 1);
+  const long *full = bt->d_prefix.as<long>();
+  long *act = bt->d_act.as<long>();
+  const long *px = act, *py = px + (ng + 1), *pz = py + (ng + 1);
+  int *ids = bt->d_ids.as<int>(), *nslots = bt->d_nslots.as<int>();
   int *cnt = bt->d_counters.as<int>();
   double *relres = bt->d_relres.as<double>();
   int *iters = bt->d_iters.as<int>();
@@ -1905,7 +1909,11 @@ int batch_capture(flutas_batch *bt, double tol, int max_iter) {
   cudaGraph_t graph = nullptr;
   int nodes = 0, c = 0;
   CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  auto Q = [&](const long *pre) { return BatchQueue{dg, pre, ng, cnt + (c++)}; };
+  auto Q = [&](const long *pre) { return BatchQueue{dg, pre, ids, nslots, cnt + (c++)}; };
+  auto compact = [&] {
+    kb_compact<<<1, 1024, 0, st>>>(dg, ng, full, act, ids, nslots);
+    nodes++;
+  };
   auto fwd_chain = [&](int xmode, int outmode) {
     kb_xfwd<<<bt->grid_x, 256, bt->smem_x, st>>>(Q(px), xmode);
     nodes++;
@@ -1921,12 +1929,14 @@ int batch_capture(flutas_batch *bt, double tol, int max_iter) {
   cudaMemsetAsync(cnt, 0, sizeof(int) * npass, st);
   kb_reset<<<(ng + 255) / 256, 256, 0, st>>>(dg, ng);
   nodes += 1;
+  compact();
   fwd_chain(0, 0);
   rest_chain(0);
   for (int it = 1; it <= max_iter; it++) {
     fwd_chain(1, 1);
     kb_update<<<(ng + 255) / 256, 256, 0, st>>>(dg, ng, tol, it, max_iter, relres, iters);
     nodes++;
+    if (it < max_iter) compact();
     if (it < max_iter) rest_chain(1);
   }
   cudaError_t e = cudaStreamEndCapture(st, &graph);
@@ -2042,7 +2052,9 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
     pre[(ngrids + 1) + g + 1] = pre[(ngrids + 1) + g] + ty[g];
     pre[2 * (ngrids + 1) + g + 1] = pre[2 * (ngrids + 1) + g] + tz[g];
   }
-  if ((rc = bt->d_prefix.ensure(sizeof(long) * pre.size())) || (rc = bt->d_grids.ensure(sizeof(BatchGrid) * ngrids)))
+  if ((rc = bt->d_prefix.ensure(sizeof(long) * pre.size())) || (rc = bt->d_grids.ensure(sizeof(BatchGrid) * ngrids)) ||
+      (rc = bt->d_act.ensure(sizeof(long) * pre.size())) || (rc = bt->d_ids.ensure(sizeof(int) * ngrids)) ||
+      (rc = bt->d_nslots.ensure(sizeof(int))))
     return bail(rc);
   if (cudaMemcpy(bt->d_prefix.p, pre.data(), sizeof(long) * pre.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(bt->d_grids.p, bt->grids.data(), sizeof(BatchGrid) * ngrids, cudaMemcpyHostToDevice) != cudaSuccess)

@@ -1239,10 +1239,15 @@ struct BatchGrid {
   int *active;           // 1 while the grid still refines
 };
 
+// Work queue of one pass over the grids that still refine: slot s of the
+// compacted list is grid ids[s]; prefix[s] is the running total of tiles of
+// slots < s (nslots + 1 entries).  kb_compact rebuilds the list after every
+// convergence update, so a pass over converged grids has no items at all.
 struct BatchQueue {
   const BatchGrid *grids;
-  const long *prefix;    // ngrids+1 running totals of tiles for this pass
-  int ngrids;
+  const long *prefix;
+  const int *ids;
+  const int *nslots;
   int *counter;          // work counter of this pass (zeroed before the pass)
 };
 
@@ -1268,12 +1273,13 @@ __device__ __forceinline__ long batch_next(int *counter) {
 #ifndef FG_NO_PLAIN_KERNELS
 __global__ void __launch_bounds__(256) kb_xfwd(BatchQueue q, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const long total = q.prefix[q.ngrids];
+  const int ns = *q.nslots;
+  const long total = q.prefix[ns];
   for (long item = batch_next(q.counter); item < total; item = batch_next(q.counter)) {
-    const int gi = batch_find(q.prefix, q.ngrids, item);
-    const BatchGrid &G = q.grids[gi];
+    const int slot = batch_find(q.prefix, ns, item);
+    const BatchGrid &G = q.grids[q.ids[slot]];
     if (!*G.active) continue;
-    const long row0 = (item - q.prefix[gi]) * G.M;
+    const long row0 = (item - q.prefix[slot]) * G.M;
     float ss = 0.0f;
     if (mode == 0) {
       InKeep<InHalo> in{InHalo{G.x, G.g}, G.f, G.g};
@@ -1293,12 +1299,13 @@ __global__ void __launch_bounds__(256) kb_xfwd(BatchQueue q, int mode) {
 template <bool BACKWARD>
 __global__ void __launch_bounds__(256) kb_ypass(BatchQueue q) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const long total = q.prefix[q.ngrids];
+  const int ns = *q.nslots;
+  const long total = q.prefix[ns];
   for (long item = batch_next(q.counter); item < total; item = batch_next(q.counter)) {
-    const int gi = batch_find(q.prefix, q.ngrids, item);
-    const BatchGrid &G = q.grids[gi];
+    const int slot = batch_find(q.prefix, ns, item);
+    const BatchGrid &G = q.grids[q.ids[slot]];
     if (!*G.active) continue;
-    ypass_tile<float, BACKWARD>(G.ay, G.S, G.g, G.W, item - q.prefix[gi], smem_raw);
+    ypass_tile<float, BACKWARD>(G.ay, G.S, G.g, G.W, item - q.prefix[slot], smem_raw);
   }
 }
 
@@ -1306,12 +1313,13 @@ __global__ void __launch_bounds__(256) kb_ypass(BatchQueue q) {
 #ifndef FG_NO_PLAIN_KERNELS
 __global__ void __launch_bounds__(256) kb_xinv(BatchQueue q, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const long total = q.prefix[q.ngrids];
+  const int ns = *q.nslots;
+  const long total = q.prefix[ns];
   for (long item = batch_next(q.counter); item < total; item = batch_next(q.counter)) {
-    const int gi = batch_find(q.prefix, q.ngrids, item);
-    const BatchGrid &G = q.grids[gi];
+    const int slot = batch_find(q.prefix, ns, item);
+    const BatchGrid &G = q.grids[q.ids[slot]];
     if (!*G.active) continue;
-    const long row0 = (item - q.prefix[gi]) * G.M;
+    const long row0 = (item - q.prefix[slot]) * G.M;
     if (mode == 0) xinv_tile<float, OutHalo>(G.ax, G.S, OutHalo{G.x, G.normfft, G.g}, G.g, G.M, row0, smem_raw);
     else xinv_tile<float, OutHaloAdd>(G.ax, G.S, OutHaloAdd{G.x, G.normfft, G.g}, G.g, G.M, row0, smem_raw);
   }
@@ -1426,12 +1434,13 @@ static __device__ void zcol_f32(const ZArgs &za, float *S, float *S2, long q, bo
 __global__ void __launch_bounds__(128) kb_z(BatchQueue q) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float *chk = (float *)smem_raw;
-  const long total = q.prefix[q.ngrids];
+  const int ns = *q.nslots;
+  const long total = q.prefix[ns];
   for (long item = batch_next(q.counter); item < total; item = batch_next(q.counter)) {
-    const int gi = batch_find(q.prefix, q.ngrids, item);
-    const BatchGrid &G = q.grids[gi];
+    const int slot = batch_find(q.prefix, ns, item);
+    const BatchGrid &G = q.grids[q.ids[slot]];
     if (!*G.active) continue;
-    const long qcol = (item - q.prefix[gi]) * blockDim.x + threadIdx.x;
+    const long qcol = (item - q.prefix[slot]) * blockDim.x + threadIdx.x;
     zcol_f32<16>(G.za, G.S, G.S2, qcol, qcol < G.za.nq, chk);
   }
 }
@@ -1459,6 +1468,66 @@ __global__ void kb_reset(BatchGrid *grids, int ng) {
     *grids[g].active = 1;
     grids[g].nrm[0] = 0.0;
     grids[g].nrm[1] = 0.0;
+  }
+}
+
+// Compacted work lists (one block): the grids still active, in grid order,
+// and for each of the three passes the running totals of their tiles.  full
+// holds the per-grid running totals of the passes (3 x (ng+1)), act receives
+// the compacted ones (3 x (ng+1)), ids the slot -> grid map, nslots the count.
+__global__ void __launch_bounds__(1024) kb_compact(const BatchGrid *grids, int ng, const long *full, long *act,
+                                                   int *ids, int *nslots) {
+  __shared__ long wsum[4][32];
+  const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, wid = t >> 5;
+  const int chunk = (ng + nt - 1) / nt, g0 = t * chunk, g1 = min(ng, g0 + chunk);
+  const long L = ng + 1;
+  long c[4] = {0, 0, 0, 0};  // active grids, x tiles, y tiles, z tiles of this thread's range
+  for (int g = g0; g < g1; g++)
+    if (*grids[g].active) {
+      c[0]++;
+      for (int p = 0; p < 3; p++) c[p + 1] += full[p * L + g + 1] - full[p * L + g];
+    }
+  long incl[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {  // exclusive scan over the block: warp scan, then over the warp totals
+    long v = c[k];
+    for (int o = 1; o < 32; o <<= 1) {
+      const long u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+    incl[k] = v;
+    if (lane == 31) wsum[k][wid] = v;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      long v = lane < (nt >> 5) ? wsum[k][lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const long u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+      }
+      wsum[k][lane] = v;  // inclusive totals of warps 0..lane
+    }
+  }
+  __syncthreads();
+  long base[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) base[k] = (wid ? wsum[k][wid - 1] : 0) + incl[k] - c[k];
+  int slot = (int)base[0];
+  long pos[3] = {base[1], base[2], base[3]};
+  for (int g = g0; g < g1; g++)
+    if (*grids[g].active) {
+      ids[slot] = g;
+      for (int p = 0; p < 3; p++) {
+        act[p * L + slot] = pos[p];
+        pos[p] += full[p * L + g + 1] - full[p * L + g];
+      }
+      slot++;
+    }
+  if (t == nt - 1) {  // the last thread ends the lists
+    *nslots = slot;
+    for (int p = 0; p < 3; p++) act[p * L + slot] = pos[p];
   }
 }
 #endif
