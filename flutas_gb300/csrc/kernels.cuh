@@ -48,13 +48,20 @@ inline dim3 grid_cells(const Geo &g, int threads = 256) {
 }
 
 // Reciprocal in FP64: FP32 seed refined by two Newton-Raphson steps
-// y <- y (2 - x y); each step squares the relative error (2^-23 -> 2^-46 -> ~1 ulp).
-// Valid for the positive, normal arguments it is used on (densities).
+// y <- y (2 - x y); each step squares the relative error (2^-22 -> 2^-44 -> ~1 ulp).
+// The seed's conversions run on the integer ALUs (bits.cuh), so the FP64 pipe
+// issues only the four Newton instructions.  Valid for arguments whose
+// magnitude lies in FP32's normal range.
 __device__ __forceinline__ double rcp64(double x) {
-  double y = (double)__frcp_rn((float)x);
+  double y = f64_of(__frcp_rn(f32_of(x)));
   y = y * fma(-x, y, 2.0);
   y = y * fma(-x, y, 2.0);
   return y;
+}
+// True when |x| lies in FP32's normal range (exponent bits only: no FP64 instruction).
+__device__ __forceinline__ bool f32_range(double x) {
+  const unsigned e = (hi_word(x) >> 20) & 0x7ffu;
+  return e > 897u && e < 1150u;
 }
 
 // Value of an FP64 RHS in the arithmetic type of a pass, and the FP32 value
@@ -322,15 +329,16 @@ __device__ __forceinline__ void block_sum_add(double v, double *acc) {
   }
 }
 
-// Stencil pass of the mixed solve: evaluates an FP64 RHS functor (fillps,
+// Stencil pass ahead of a transform: evaluates an FP64 RHS functor (fillps,
 // or the residual f - A x) per cell, optionally keeps the FP64 value (halo-1
-// array `keep`) and writes the FP32-truncated value into `s32` (no halo, x
-// fastest: the input of the transform, which may run in place), and adds the
+// array `keep`) and writes the value in the transform's type into `s32` (no
+// halo, x fastest: the input of the transform, which may run in place; FP32
+// values truncated), and adds the
 // FP32 sum of squares of the FP32 values to *nrm (as the fused norms of the
 // transform passes).  With keep = s32 = nullptr it is the norm-only check.
 // Four cells per thread are evaluated before any is stored.
-template <typename In>
-__global__ void __launch_bounds__(256) k_stencil_pass(In in, Geo g, double *keep, float *s32, double *nrm) {
+template <typename In, typename TO>
+__global__ void __launch_bounds__(256) k_stencil_pass(In in, Geo g, double *keep, TO *s32, double *nrm) {
   const int tot = g.nx * g.ny * g.nz;  // < 2^31
   const FastDiv fx(g.nx), fy(g.ny);
   float ss = 0.0f;
@@ -353,7 +361,11 @@ __global__ void __launch_bounds__(256) k_stencil_pass(In in, Geo g, double *keep
       ss = fmaf(f, f, ss);
       if (idx < tot) {
         if (keep) keep[g.pidx(xs[u] + 1, ys[u] + 1, ks[u] + 1)] = v[u];
-        if (s32) s32[idx] = f;
+        if (s32) {
+          TO o;
+          to_pass_into(o, v[u]);  // the FP32 value for FP32 transforms, the FP64 value itself otherwise
+          s32[idx] = o;
+        }
       }
     }
   }
@@ -900,8 +912,8 @@ struct PresTwArgs {
   Geo g;
 };
 __device__ __forceinline__ double rcp64_1(double x) {
-  const double y = (double)__frcp_rn((float)x);  // FP32 seed, error <= 2^-24
-  return y * fma(-x, y, 2.0);                      // one Newton step: error ~2^-48
+  const double y = f64_of(__frcp_rn(f32_of(x)));  // FP32 seed (integer-ALU conversions), error < 2^-22
+  return y * fma(-x, y, 2.0);                       // one Newton step: error < 2^-44
 }
 __device__ __forceinline__ double df_incr(double dp, double dq, double rs, double A, double B, double f2) {
   const double t = dp - dq;
@@ -1053,7 +1065,9 @@ __device__ __forceinline__ T zpivot(T bb, T a, T dprev, bool first) {
 // 1/x: the SFU reciprocal in FP32 (the FP32 solve is refined in FP64), a
 // correctly rounded division in FP64.
 __device__ __forceinline__ float zrcp(float x) { return __fdividef(1.0f, x); }
-__device__ __forceinline__ double zrcp(double x) { return 1.0 / x; }
+// FP64 pivots: Newton-Raphson reciprocal (rcp64) inside FP32's normal range,
+// an IEEE division outside it.
+__device__ __forceinline__ double zrcp(double x) { return f32_range(x) ? rcp64(x) : 1.0 / x; }
 
 template <typename T, int CH>
 __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, long q_begin, long q_end) {
