@@ -763,6 +763,43 @@ def run_serve(args):
 
 
 
+
+def run_solve(args):
+    """Poisson solves alone on one grid (--grid NX NY NZ, --cbc, uniform z), mixed
+    to --tol (0: the FP64 solver), on a device array with a seeded U[-1,1] RHS."""
+    import torch
+    import flutas_gb300 as F
+    nx, ny, nz = args.grid
+    dzci, dzfi = zgrid_stretched(nz, 0.0)
+    P = F.initsolver([nx, ny, nz], [float(nx), float(ny), float(nz)], 1, dzci, dzfi, args.cbc, [0.0] * 6, "ccc")
+    rng = np.random.default_rng(args.seed)
+    f = np.zeros((nz + 2, ny + 2, nx + 2))
+    g = rng.uniform(-1.0, 1.0, (nz, ny, nx))
+    f[1:-1, 1:-1, 1:-1] = g - g.mean()
+    rhs = torch.from_numpy(f).cuda()
+    x = rhs.clone()
+
+    def once():
+        x.copy_(rhs)
+        return P.solve_mixed(x, tol=args.tol, max_iter=10) if args.tol > 0 else (P.solver(x), None)
+
+    for _ in range(args.warmup):
+        once()
+    ts, out = [], None
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        out = once()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    info = P.info()
+    return {"mode": "solve", "grid": [nx, ny, nz], "cbc": args.cbc, "tol": args.tol,
+            "ms_per_solve": round(float(np.median(ts)), 4), "relres_and_fp32_solves": out if args.tol > 0 else None,
+            "xy_path_fp32": info["xy_path_fp32"], "xy_path_fp64": info["xy_path_fp64"],
+            "timing": "CUDA events around each solve (median), including the device copy of the RHS"}
+
 # ------------------------------------------------------------ configs C1, C3
 def zgrid_stretched(n, gr):
     """dzci, dzfi (0:n+1) of src/initgrid.f90 steps 1-5 with two-end tanh
@@ -962,7 +999,7 @@ def main():
                     help="only the headline mode (for profiler captures): W warm-up + K steps, no extra modes, "
                          "no e2e, no CPU baseline")
     ap.add_argument("--precision", type=int, default=1, help="with --single: 1 mixed to 1e-10, 0 FP64")
-    ap.add_argument("--mode", choices=["projection", "batch", "serve", "c1", "c3"], default="projection",
+    ap.add_argument("--mode", choices=["projection", "batch", "serve", "c1", "c3", "solve"], default="projection",
                     help="projection: the headline two-phase step; batch: 512 uneven grids in one graph; "
                          "serve: Poisson request stream through the continuous-batching server")
     ap.add_argument("--grids", type=int, default=512)
@@ -970,6 +1007,9 @@ def main():
     ap.add_argument("--slots", type=int, default=4)
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--rates", type=float, nargs="+", default=[0.5, 0.8, 1.0, 1.2])
+    ap.add_argument("--grid", type=int, nargs=3, default=[256, 256, 32], help="--mode solve: nx ny nz")
+    ap.add_argument("--cbc", default="PPPPNN", help="--mode solve: pressure BCs")
+    ap.add_argument("--tol", type=float, default=1e-10, help="--mode solve: mixed tolerance (0: FP64 solver)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -977,7 +1017,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "ours" and args.mode != "projection":
-        res = {"batch": run_batch, "serve": run_serve, "c1": run_config1, "c3": run_config3}[args.mode](args)
+        res = {"batch": run_batch, "serve": run_serve, "c1": run_config1, "c3": run_config3,
+               "solve": run_solve}[args.mode](args)
     elif args.impl == "reference":
         res = run_reference(args, rank)
     else:
