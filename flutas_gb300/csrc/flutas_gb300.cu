@@ -647,10 +647,13 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
       pl->path32 == 2 && fixed_supported(g.nx, g.ny, pl->clus32, pl->tx32.ap.pair, pl->ty32.ap.pair);
   auto stencil = [&](const auto &in, double *keep, float *s32, double *acc) -> int {
     using In = std::decay_t<decltype(in)>;
-    const int grid = grid_for(k_stencil_pass<In, float>, 256, 0, ((long)g.nx * g.ny * g.nz + 1023) / 1024);
+    const long cells = (long)g.nx * g.ny * g.nz;
+    const int grid = grid_for(k_stencil_pass<In, float>, 256, 0, (cells + 1023) / 1024);
     if (grid < 0) return grid;
     static const std::string name = std::string("k_stencil<") + In::tag + ">";
     const char *nm = (keep || s32) ? name.c_str() : "k_resnorm";
+    if (cells >= (1L << 31) - 4096)  // the int variant also forms indices up to 3 blocks past the end
+      return launch(nm, st, [&] { k_stencil_pass<In, float, long long><<<grid, 256, 0, st>>>(in, g, keep, s32, acc); });
     return launch(nm, st, [&] { k_stencil_pass<In, float><<<grid, 256, 0, st>>>(in, g, keep, s32, acc); });
   };
   auto transform = [&](const InResidual &R, double *acc) -> int {  // residual -> S
@@ -1450,10 +1453,16 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     double *S = pl->S64.as<double>();
     // fillps at full occupancy (the FP64 pipe bounds it), then the transform in place
     const Geo gs{nx, ny, nz, 1};
-    const int grid = grid_for(k_stencil_pass<InFillps, double>, 256, 0, ((long)nx * ny * nz + 1023) / 1024);
+    const long cells = (long)nx * ny * nz;
+    const int grid = grid_for(k_stencil_pass<InFillps, double>, 256, 0, (cells + 1023) / 1024);
     if (grid < 0) return grid;
-    TRY(launch("k_stencil<f64,fillps>", st,
-               [&] { k_stencil_pass<InFillps, double><<<grid, 256, 0, st>>>(in, gs, nullptr, S, nullptr); }));
+    if (cells >= (1L << 31) - 4096)  // the int variant also forms indices up to 3 blocks past the end
+      TRY(launch("k_stencil<f64,fillps>", st, [&] {
+        k_stencil_pass<InFillps, double, long long><<<grid, 256, 0, st>>>(in, gs, nullptr, S, nullptr);
+      }));
+    else
+      TRY(launch("k_stencil<f64,fillps>", st,
+                 [&] { k_stencil_pass<InFillps, double><<<grid, 256, 0, st>>>(in, gs, nullptr, S, nullptr); }));
     TRY(fwd_xy<double>(pl, InPlain{S, gs}, S, pl->tx64, pl->ty64, pl->path64));
     TRY(zsolve<double>(pl, S, pl->lam.as<double>(), pl->a.as<double>(), pl->b.as<double>(), pl->c.as<double>(),
                        pl->pin_zero_mode));

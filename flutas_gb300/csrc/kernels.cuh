@@ -337,26 +337,35 @@ __device__ __forceinline__ void block_sum_add(double v, double *acc) {
 // FP32 sum of squares of the FP32 values to *nrm (as the fused norms of the
 // transform passes).  With keep = s32 = nullptr it is the norm-only check.
 // Four cells per thread are evaluated before any is stored.
-template <typename In, typename TO>
+template <typename In, typename TO, typename IDX = int>
 __global__ void __launch_bounds__(256) k_stencil_pass(In in, Geo g, double *keep, TO *s32, double *nrm) {
-  const int tot = g.nx * g.ny * g.nz;  // < 2^31
+  // IDX = int while nx*ny*nz < 2^31 (shift/multiply divisions), long long beyond
+  const IDX tot = (IDX)g.nx * g.ny * g.nz;
   const FastDiv fx(g.nx), fy(g.ny);
   float ss = 0.0f;
-  for (int b = blockIdx.x * blockDim.x * 4 + threadIdx.x; b < tot; b += gridDim.x * blockDim.x * 4) {
+  for (IDX b = (IDX)blockIdx.x * blockDim.x * 4 + threadIdx.x; b < tot; b += (IDX)gridDim.x * blockDim.x * 4) {
     double v[4];
     int xs[4], ys[4], ks[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      const int idx = b + u * (int)blockDim.x;
-      const int row = fx.div(idx), k = fy.div(row);
-      xs[u] = idx - row * g.nx;
+      const IDX idx = b + (IDX)u * blockDim.x;
+      int row;
+      if constexpr (sizeof(IDX) == 4) {
+        row = fx.div((int)idx);
+        xs[u] = (int)idx - row * g.nx;
+      } else {
+        const IDX r = idx / g.nx;  // rows stay below 2^31 (ny*nz)
+        row = (int)r;
+        xs[u] = (int)(idx - r * g.nx);
+      }
+      const int k = fy.div(row);
       ks[u] = k;
       ys[u] = row - k * g.ny;
       v[u] = idx < tot ? in(xs[u], ys[u], ks[u]) : 0.0;
     }
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      const int idx = b + u * (int)blockDim.x;
+      const IDX idx = b + (IDX)u * blockDim.x;
       const float f = f32_of(v[u]);
       ss = fmaf(f, f, ss);
       if (idx < tot) {
