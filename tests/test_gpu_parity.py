@@ -342,3 +342,30 @@ def test_gpu_fixed_size_cluster_kernels(lib, oracle, n, cbc, monkeypatch):
         assert rel_l2(p[1:-1, 1:-1, 1:-1], ref[1:-1, 1:-1, 1:-1], remove_mean=singular(cbc)) <= 1e-7
         out[fixed] = p
     assert rel_l2(out["1"][1:-1, 1:-1, 1:-1], out["0"][1:-1, 1:-1, 1:-1], remove_mean=singular(cbc)) <= 1e-7
+
+
+# The grid shapes and pressure BCs of the reference's example cases
+# (examples/*/dns.in: itot jtot ktot and cbcpre); droplet_rb's 1024x1024x512 is
+# cut to 4 levels (same 1024^2 planes) so the oracle stays fast.
+EXAMPLES = [("abc_triperiodic", (32, 32, 32), "PPPPPP"), ("coarse_two_layer_rb", (128, 64, 128), "PPNNPP"),
+            ("dhc", (2, 128, 128), "PPNNNN"), ("droplet_rb", (1024, 1024, 4), "PPPPNN"),
+            ("laminar_ldc_2D", (2, 64, 64), "PPNNNN"), ("laminar_channel", (64, 32, 32), "PPPPNN"),
+            ("coarse_turb_channel", (256, 128, 72), "PPPPNN"), ("laminar_ldc", (64, 64, 64), "NNNNNN"),
+            ("rising_bubble_3d", (32, 32, 64), "NNNNNN")]
+
+
+@pytest.mark.parametrize("name,n,cbc", EXAMPLES, ids=[e[0] for e in EXAMPLES])
+def test_gpu_reference_example_grids(lib, oracle, name, n, cbc):
+    rng = np.random.default_rng(len(name))
+    P, dzci, dzfi, dzc, dzf, dli = plan_for(lib, n, cbc, 0.0)
+    S = oracle.SolverSetup(n, dli, 1, dzci, dzfi, cbc, [0] * 6, "ccc")
+    f = compatible_rhs(rng, n, cbc, dzf)
+    ref = f.copy()
+    S.solve(ref)
+    got = f.copy()
+    P.solver(got)
+    assert rel_l2(got[1:-1, 1:-1, 1:-1], ref[1:-1, 1:-1, 1:-1], remove_mean=singular(cbc)) <= 1e-12
+    mixed = f.copy()
+    relres, _ = P.solve_mixed(mixed, tol=1e-10, max_iter=10)
+    r = oracle.residual(n, cbc, dli[0], dli[1], 1, dzci, dzfi, f, mixed)
+    assert relres <= 1e-10 and np.linalg.norm(r) / np.linalg.norm(f[1:-1, 1:-1, 1:-1]) <= 1.01e-10
