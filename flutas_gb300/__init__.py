@@ -311,10 +311,10 @@ def boundp(cbc, n, bc, nh_d, dl, dzc, dzf, p, nh_p=1):
                                       _ptr(dzc), _ptr(dzf), _ptr(p)))
 
 
-def bounduvw(cbcvel, n, bcvel, nh_d, nh_u, dl, dzc, dzf, u, v, w):
-    """bounduvw(cbc,n,bc,nh_d,nh_u,halo,isoutflow,dl,dzc,dzf,u,v,w) without outflow."""
+def bounduvw(cbcvel, n, bcvel, nh_d, nh_u, dl, dzc, dzf, u, v, w, isoutflow=None):
+    """bounduvw(cbc,n,bc,nh_d,nh_u,halo,isoutflow,dl,dzc,dzf,u,v,w); isoutflow: 6 flags (0:1,1:3)."""
     halo = (C.c_int * 3)(1, 1, 1)
-    outf = (C.c_int * 6)()
+    outf = (C.c_int * 6)(*[int(bool(x)) for x in (isoutflow or [0] * 6)])
     _check(load().flutas_gb300_bounduvw(_chars(cbcvel, 18), C.cast(_i3(n), C.c_void_p),
                                         C.cast((C.c_double * 18)(*[float(x) for x in bcvel]), C.c_void_p),
                                         int(nh_d), int(nh_u), C.cast(halo, C.c_void_p), C.cast(outf, C.c_void_p),

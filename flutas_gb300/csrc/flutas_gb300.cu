@@ -1315,10 +1315,12 @@ int set_bc_dev(double *p, int nx, int ny, int nz, int h, char ctype, int ibound,
   return 0;
 }
 
-// bounduvw (src/bound.f90:17-144), single domain, no outflow.  dzc/dzf host
+// bounduvw (src/bound.f90:17-144), single domain, with the outflow faces of
+// src/bound.f90:649-773 when isoutflow is given.  dzc/dzf host
 // values.  One launch per direction (x, then y, then z, as the reference).
 int bounduvw_dev(const char *cbc, const double *bc, int nx, int ny, int nz, int nh_d, int h, const double dl[3],
-                 const double *dzc_h, const double *dzf_h, double *u, double *v, double *w, cudaStream_t st) {
+                 const double *dzc_h, const double *dzf_h, double *u, double *v, double *w, cudaStream_t st,
+                 const int *isoutflow = nullptr, const double *dzf_d = nullptr) {
   if (h < 1 || h > 4) return fail(FLUTAS_EUNSUPPORTED, "bounduvw: halo %d not in 1..4", h);
   auto CB = [&](int ib, int d, int c) { return cbc[ib + 2 * d + 6 * c]; };
   auto BV = [&](int ib, int d, int c) { return bc[ib + 2 * d + 6 * c]; };
@@ -1350,6 +1352,18 @@ int bounduvw_dev(const char *cbc, const double *bc, int nx, int ny, int nz, int 
     const long cnt = (long)(na + 2 * h) * (nb + 2 * h);
     TRY(launch("k_set_bc3", st, [&] { k_set_bc3<<<stream_grid(cnt), 256, 0, st>>>(a); }));
   }
+  if (isoutflow)  // src/bound.f90:130-141: directions in order, low side first
+    for (int q = 1; q <= 3; q++)
+      for (int id = 0; id <= 1; id++) {
+        if (!isoutflow[id + 2 * (q - 1)]) continue;
+        OutflowArgs o;
+        o.u = u; o.v = v; o.w = w;
+        o.dzf = dzf_d;
+        o.dx = dl[0]; o.dy = dl[1]; o.dxi = 1.0 / dl[0]; o.dyi = 1.0 / dl[1];
+        o.nx = nx; o.ny = ny; o.nz = nz; o.h = h; o.idir = id == 0 ? -q : q;
+        const long pts = (long)(q == 1 ? ny : nx) * (q == 3 ? ny : nz) * (h + 1);
+        TRY(launch("k_outflow", st, [&] { k_outflow<<<stream_grid(pts), 256, 0, st>>>(o); }));
+      }
   return 0;
 }
 
@@ -1370,10 +1384,10 @@ int flutas_gb300_bounduvw(const char cbcvel[18], const int n[3], const double bc
   (void)halo;
   if (!cbcvel || !n || !bcvel || !dl || !dzc || !dzf) return fail(FLUTAS_EINVAL, "bounduvw: null argument");
   TRY(check_cbcvel(cbcvel));
-  if (isoutflow)
-    for (int i = 0; i < 6; i++)
-      if (isoutflow[i]) return fail(FLUTAS_EUNSUPPORTED, "bounduvw: outflow boundaries are not implemented");
   if (nh_u < 1 || nh_u > 4 || nh_d < nh_u) return fail(FLUTAS_EINVAL, "bounduvw: bad halo sizes");
+  bool any_outflow = false;
+  if (isoutflow)
+    for (int i = 0; i < 6; i++) any_outflow |= isoutflow[i] != 0;
   const int nx = n[0], ny = n[1], nz = n[2];
   std::vector<double> dzc_h(nz + 2 * nh_d), dzf_h(nz + 2 * nh_d);
   const size_t zb = sizeof(double) * (nz + 2 * nh_d);
@@ -1392,7 +1406,14 @@ int flutas_gb300_bounduvw(const char cbcvel[18], const int n[3], const double bc
   TRY(stage_in(g_ctx_mir, u, ub, true, true, st, &su));
   TRY(stage_in(g_ctx_mir, v, ub, true, true, st, &sv));
   TRY(stage_in(g_ctx_mir, w, ub, true, true, st, &sw));
-  TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dl, dzc_h.data(), dzf_h.data(), su.d, sv.d, sw.d, st));
+  double *dzf_d = nullptr;
+  if (any_outflow) {  // the outflow faces need dzf on the device
+    TRY(g_ctx_small[2].ensure(zb));
+    dzf_d = g_ctx_small[2].as<double>();
+    CK(cudaMemcpyAsync(dzf_d, dzf_h.data(), zb, cudaMemcpyHostToDevice, st));
+  }
+  TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dl, dzc_h.data(), dzf_h.data(), su.d, sv.d, sw.d, st,
+                   any_outflow ? isoutflow : nullptr, dzf_d ? dzf_d + (nh_d - 1) : nullptr));
   TRY(stage_out(su, st));
   TRY(stage_out(sv, st));
   TRY(stage_out(sw, st));

@@ -965,6 +965,52 @@ __global__ void k_pres_tw_src(PresTwArgs a) {
 }
 #endif
 
+// outflow (src/bound.f90:649-773): the velocity normal to an outflow boundary
+// from zero divergence of the adjacent cells.  idir = +-1, +-2, +-3 (sign:
+// high or low side).  One thread per (face point, layer q); the high side starts
+// at the last interior face and runs q = 0..nh_u, the low side writes the
+// ghosts q = 0..nh_u-1, as the reference does.  Rounded as written (no FMA), so
+// the values are bit-identical to the reference expression.
+struct OutflowArgs {
+  double *u, *v, *w;
+  const double *dzf;  // dzf[k], k in 1-nh_d..nz+nh_d
+  double dx, dy, dxi, dyi;
+  int nx, ny, nz, h, idir;
+};
+#ifndef FG_NO_PLAIN_KERNELS
+__global__ void k_outflow(OutflowArgs a) {
+  const int ad = a.idir < 0 ? -a.idir : a.idir;
+  const bool hi = a.idir > 0;
+  const int nq = hi ? a.h + 1 : a.h;  // layers q = 0..qmin+1 (high) or 0..qmin (low), qmin = h - 1
+  const int na = ad == 1 ? a.ny : a.nx, nb = ad == 3 ? a.ny : a.nz;
+  const long tot = (long)na * nb * nq;
+  const long HX = a.nx + 2 * a.h, HY = a.ny + 2 * a.h;
+  auto at = [&](int i, int j, int k) { return (long)(i - 1 + a.h) + HX * ((long)(j - 1 + a.h) + HY * (long)(k - 1 + a.h)); };
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long)gridDim.x * blockDim.x) {
+    const int q = (int)(t % nq), ab = (int)(t / nq), p1 = ab % na + 1, p2 = ab / na + 1;
+    if (ad == 1) {
+      const int j = p1, k = p2, i = hi ? a.nx + q : 1 + q;  // i: the face whose neighbours give the divergence
+      const double s = __dadd_rn(__dmul_rn(__dsub_rn(a.v[at(i, j, k)], a.v[at(i, j - 1, k)]), a.dyi),
+                                 __dmul_rn(__dsub_rn(a.w[at(i, j, k)], a.w[at(i, j, k - 1)]), 1.0 / a.dzf[k]));
+      if (hi) a.u[at(i, j, k)] = __dsub_rn(a.u[at(a.nx - 1 - q, j, k)], __dmul_rn(a.dx, s));
+      else a.u[at(-q, j, k)] = __dadd_rn(a.u[at(1 + q, j, k)], __dmul_rn(a.dx, s));
+    } else if (ad == 2) {
+      const int i = p1, k = p2, j = hi ? a.ny + q : 1 + q;
+      const double s = __dadd_rn(__dmul_rn(__dsub_rn(a.u[at(i, j, k)], a.u[at(i - 1, j, k)]), a.dxi),
+                                 __dmul_rn(__dsub_rn(a.w[at(i, j, k)], a.w[at(i, j, k - 1)]), 1.0 / a.dzf[k]));
+      if (hi) a.v[at(i, j, k)] = __dsub_rn(a.v[at(i, a.ny - 1 - q, k)], __dmul_rn(a.dy, s));
+      else a.v[at(i, -q, k)] = __dadd_rn(a.v[at(i, 1 + q, k)], __dmul_rn(a.dy, s));
+    } else {
+      const int i = p1, j = p2, k = hi ? a.nz + q : 1 + q;
+      const double s = __dadd_rn(__dmul_rn(__dsub_rn(a.u[at(i, j, k)], a.u[at(i - 1, j, k)]), a.dxi),
+                                 __dmul_rn(__dsub_rn(a.v[at(i, j, k)], a.v[at(i, j - 1, k)]), a.dyi));
+      if (hi) a.w[at(i, j, k)] = __dsub_rn(a.w[at(i, j, a.nz - 1 - q)], __dmul_rn(a.dzf[k], s));
+      else a.w[at(i, j, -q)] = __dadd_rn(a.w[at(i, j, 1 + q)], __dmul_rn(a.dzf[-q], s));
+    }
+  }
+}
+#endif
+
 // update_property (src/vof.f90:240-271): prop = vof*prop12(1) + (1-vof)*prop12(2)
 // on the interior of halo-1 arrays, rounded as written (no contraction into an
 // FMA), so the result is bit-identical to the reference expression.

@@ -87,8 +87,10 @@ FLUTAS_API int flutas_gb300_boundp(const char cbc[6], const int n[3], const doub
 
 /* Replaces bounduvw (src/bound.f90:17) for a single domain: velocity ghosts per
  * set_bc (src/bound.f90:227-646), the face-normal component non-centred.
- * cbcvel/bcvel are cbcvel/bcvel(0:1,1:3,1:3) in memory order; outflow
- * boundaries (isoutflow, src/bound.f90:648+) return FLUTAS_EUNSUPPORTED. */
+ * cbcvel/bcvel are cbcvel/bcvel(0:1,1:3,1:3) in memory order; isoutflow
+ * (nullable) is isoutflow(0:1,1:3): flagged faces get the zero-divergence
+ * outflow velocity of src/bound.f90:649-773 after the ghosts, bit-identical to
+ * the reference expression.  The fused projections take no outflow flags. */
 FLUTAS_API int flutas_gb300_bounduvw(const char cbcvel[18], const int n[3], const double bcvel[18],
                                      int nh_d, int nh_u, const int halo[3], const int isoutflow[6],
                                      const double dl[3], const double *dzc, const double *dzf,

@@ -570,9 +570,70 @@ static void set_bc(int nx, int ny, int nz, char ctype, int ibound, int idir, dou
   set_bc_h(nx, ny, nz, 1, ctype, ibound, idir, 1, rvalue, &dr, p);
 }
 
+/* bound.f90:649-773 (outflow): the velocity normal to an outflow boundary from zero divergence; idir =
+   +-1,2,3 (sign: which side).  The right/back/top cases start at the last interior face and run one layer
+   further than the left/front/bottom ones, as the reference does. */
+void or_outflow(int nx, int ny, int nz, int idir, int nh_d, int nh_u, const double dl[3], const double *dzf,
+                double *u, double *v, double *w) {
+  const int h = nh_u, qmin = nh_u - 1;
+  const long HX = nx + 2 * h, HY = ny + 2 * h;
+  const double dx = dl[0], dy = dl[1], dxi = 1.0 / dx, dyi = 1.0 / dy;
+#define U3(a, i, j, k) a[((i) - 1 + h) + HX * (((j) - 1 + h) + HY * (long)((k) - 1 + h))]
+#define DZF(k) dzf[(k) - 1 + nh_d]
+  switch (idir) {
+    case 1: {
+      const int i = nx;
+      for (int k = 1; k <= nz; k++) for (int j = 1; j <= ny; j++) for (int q = 0; q <= qmin + 1; q++) {
+        const double s = (U3(v, i + q, j, k) - U3(v, i + q, j - 1, k)) * dyi + (U3(w, i + q, j, k) - U3(w, i + q, j, k - 1)) * (1.0 / DZF(k));
+        U3(u, i + q, j, k) = U3(u, i - 1 - q, j, k) - dx * s;
+      }
+    } break;
+    case 2: {
+      const int j = ny;
+      for (int k = 1; k <= nz; k++) for (int q = 0; q <= qmin + 1; q++) for (int i = 1; i <= nx; i++) {
+        const double s = (U3(u, i, j + q, k) - U3(u, i - 1, j + q, k)) * dxi + (U3(w, i, j + q, k) - U3(w, i, j + q, k - 1)) * (1.0 / DZF(k));
+        U3(v, i, j + q, k) = U3(v, i, j - 1 - q, k) - dy * s;
+      }
+    } break;
+    case 3: {
+      const int k = nz;
+      for (int q = 0; q <= qmin + 1; q++) for (int j = 1; j <= ny; j++) for (int i = 1; i <= nx; i++) {
+        const double s = (U3(u, i, j, k + q) - U3(u, i - 1, j, k + q)) * dxi + (U3(v, i, j, k + q) - U3(v, i, j - 1, k + q)) * dyi;
+        U3(w, i, j, k + q) = U3(w, i, j, k - 1 - q) - DZF(k + q) * s;
+      }
+    } break;
+    case -1: {
+      const int i = 0;
+      for (int k = 1; k <= nz; k++) for (int j = 1; j <= ny; j++) for (int q = 0; q <= qmin; q++) {
+        const double s = (U3(v, i + 1 + q, j, k) - U3(v, i + 1 + q, j - 1, k)) * dyi + (U3(w, i + 1 + q, j, k) - U3(w, i + 1 + q, j, k - 1)) * (1.0 / DZF(k));
+        U3(u, i - q, j, k) = U3(u, i + 1 + q, j, k) + dx * s;
+      }
+    } break;
+    case -2: {
+      const int j = 0;
+      for (int k = 1; k <= nz; k++) for (int q = 0; q <= qmin; q++) for (int i = 1; i <= nx; i++) {
+        const double s = (U3(u, i, j + 1 + q, k) - U3(u, i - 1, j + 1 + q, k)) * dxi + (U3(w, i, j + 1 + q, k) - U3(w, i, j + 1 + q, k - 1)) * (1.0 / DZF(k));
+        U3(v, i, j - q, k) = U3(v, i, j + 1 + q, k) + dy * s;
+      }
+    } break;
+    case -3: {
+      const int k = 0;
+      for (int q = 0; q <= qmin; q++) for (int j = 1; j <= ny; j++) for (int i = 1; i <= nx; i++) {
+        const double s = (U3(u, i, j, k + 1 + q) - U3(u, i - 1, j, k + 1 + q)) * dxi + (U3(v, i, j, k + 1 + q) - U3(v, i, j - 1, k + 1 + q)) * dyi;
+        U3(w, i, j, k - q) = U3(w, i, j, k + 1 + q) + DZF(k - q) * s;
+      }
+    } break;
+    default: break;
+  }
+#undef U3
+#undef DZF
+}
+
 void or_bounduvw(const char cbc[18], const int n[3], const double bc[18], int nh_d, int nh_u,
-                 const double dl[3], const double *dzc, const double *dzf, double *u, double *v, double *w) {
-  /* bound.f90:17-144 (single domain, no outflow); cbc/bc are (0:1,3,3): [ib + 2*dir + 6*comp] */
+                 const double dl[3], const double *dzc, const double *dzf, double *u, double *v, double *w,
+                 const int *isoutflow) {
+  /* bound.f90:17-144 (single domain); cbc/bc are (0:1,3,3): [ib + 2*dir + 6*comp]; isoutflow (0:1,3):
+     [idir + 2*dir], nullable */
   const int nx = n[0], ny = n[1], nz = n[2], h = nh_u;
   double *f[3] = {u, v, w};
   double dr[8];
@@ -592,6 +653,10 @@ void or_bounduvw(const char cbc[18], const int n[3], const double bc[18], int nh
   for (int c = 0; c < 2; c++) set_bc_h(nx, ny, nz, h, CB(1, 2, c), 1, 3, 1, BV(1, 2, c), dr, f[c]);
   for (int q = 0; q < h; q++) dr[q] = dzf[nz + q - 1 + nh_d];
   set_bc_h(nx, ny, nz, h, CB(1, 2, 2), 1, 3, 0, BV(1, 2, 2), dr, w);
+  if (isoutflow)  /* bound.f90:130-141, directions in order, low side first */
+    for (int q = 1; q <= 3; q++)
+      for (int id = 0; id <= 1; id++)
+        if (isoutflow[id + 2 * (q - 1)]) or_outflow(nx, ny, nz, id == 0 ? -q : q, nh_d, nh_u, dl, dzf, u, v, w);
 #undef CB
 #undef BV
 }

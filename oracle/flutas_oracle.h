@@ -75,7 +75,8 @@ void or_boundp(const char cbc[6], const int n[3], const double bc[6], int nh_d,
 /* bound.f90:17-144 bounduvw, single domain, no outflow.  cbc, bc are the
  * Fortran cbcvel/bcvel(0:1,1:3,1:3) in memory order. */
 void or_bounduvw(const char cbc[18], const int n[3], const double bc[18], int nh_d, int nh_u,
-                 const double dl[3], const double *dzc, const double *dzf, double *u, double *v, double *w);
+                 const double dl[3], const double *dzc, const double *dzf, double *u, double *v, double *w,
+                 const int *isoutflow);
 /* bound.f90:829-944 */
 void or_updt_rhs_b(int nx, int ny, int nz, const char c_or_f[3], const char cbc[6],
                    const double *rhsbx, const double *rhsby, const double *rhsbz, double *p);

@@ -66,7 +66,7 @@ def lib():
         L.or_boundp.argtypes = [C.c_char_p, C.c_int * 3, C.c_double * 6, C.c_int, C.c_double * 3,
                                 _dp, _dp, _dp]
         L.or_bounduvw.argtypes = [C.c_char_p, C.c_int * 3, C.c_double * 18, C.c_int, C.c_int,
-                                  C.c_double * 3, _dp, _dp, _dp, _dp, _dp]
+                                  C.c_double * 3, _dp, _dp, _dp, _dp, _dp, C.c_void_p]
         L.or_updt_rhs_b.argtypes = [C.c_int] * 3 + [C.c_char_p, C.c_char_p, _dp, _dp, _dp, _dp]
         L.or_chkdiv.argtypes = [C.c_int] * 3 + [C.c_double] * 3 + [C.c_int] * 2 + [
             _dp, _dp, _dp, _dp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -166,10 +166,11 @@ def boundp(cbc, n, bc, nh_d, dl, dzc, dzf, p):
                     (C.c_double * 3)(*dl), dzc, dzf, p)
 
 
-def bounduvw(cbcvel, n, bcvel, nh_d, nh_u, dl, dzc, dzf, u, v, w):
-    """cbcvel: 18 characters in Fortran (0:1,1:3,1:3) memory order."""
+def bounduvw(cbcvel, n, bcvel, nh_d, nh_u, dl, dzc, dzf, u, v, w, isoutflow=None):
+    """cbcvel: 18 characters in Fortran (0:1,1:3,1:3) memory order; isoutflow: 6 flags (0:1,1:3)."""
+    outf = (C.c_int * 6)(*[int(bool(x)) for x in isoutflow]) if isoutflow is not None else None
     lib().or_bounduvw(_b(cbcvel), (C.c_int * 3)(*n), (C.c_double * 18)(*bcvel), nh_d, nh_u,
-                      (C.c_double * 3)(*dl), dzc, dzf, u, v, w)
+                      (C.c_double * 3)(*dl), dzc, dzf, u, v, w, outf)
 
 
 def updt_rhs_b(n, c_or_f, cbc, rhsbx, rhsby, rhsbz, p):

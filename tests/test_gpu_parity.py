@@ -369,3 +369,21 @@ def test_gpu_reference_example_grids(lib, oracle, name, n, cbc):
     relres, _ = P.solve_mixed(mixed, tol=1e-10, max_iter=10)
     r = oracle.residual(n, cbc, dli[0], dli[1], 1, dzci, dzfi, f, mixed)
     assert relres <= 1e-10 and np.linalg.norm(r) / np.linalg.norm(f[1:-1, 1:-1, 1:-1]) <= 1.01e-10
+
+
+@pytest.mark.parametrize("flags", [[1, 0, 0, 0, 0, 0], [0, 1, 0, 0, 0, 0], [0, 0, 1, 0, 0, 0], [0, 0, 0, 1, 0, 0],
+                                   [0, 0, 0, 0, 1, 0], [0, 0, 0, 0, 0, 1], [1] * 6],
+                         ids=["x-", "x+", "y-", "y+", "z-", "z+", "all"])
+@pytest.mark.parametrize("nh_u", [1, 2])
+def test_gpu_bounduvw_outflow(lib, oracle, flags, nh_u):
+    """bounduvw with outflow faces (src/bound.f90:649-773): bit-identical to the oracle."""
+    n = [14, 10, 8]
+    rng = np.random.default_rng(sum(flags) + 10 * nh_u)
+    dzci, dzfi, dzc, dzf = zgrid(n[2], 1.5, nh_d=nh_u)
+    u, v, w = random_velocity(rng, n, nh_u)
+    uo, vo, wo = u.copy(), v.copy(), w.copy()
+    dl = [1 / 14, 1 / 10, 0.0]
+    oracle.bounduvw("NNDDDD" * 3, n, [0.0] * 18, nh_u, nh_u, dl, dzc, dzf, uo, vo, wo, isoutflow=flags)
+    lib.bounduvw("NNDDDD" * 3, n, [0.0] * 18, nh_u, nh_u, dl, dzc, dzf, u, v, w, isoutflow=flags)
+    for a, b in ((u, uo), (v, vo), (w, wo)):
+        assert np.array_equal(a, b)

@@ -156,3 +156,20 @@ def test_bench_grid_matches_initgrid(oracle, gr):
     dzc, dzf, zc, zf = oracle.initgrid(n, gr, 1.0, 1)
     # equal up to the last bits of libm tanh (numpy vs C)
     assert np.allclose(1.0 / dzci, dzc, rtol=1e-12, atol=0) and np.allclose(1.0 / dzfi, dzf, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("side", range(6))
+def test_oracle_outflow_zero_divergence(oracle, side):
+    """outflow (src/bound.f90:649-773) makes the cells next to an outflow face divergence-free."""
+    n = [10, 8, 6]
+    rng = np.random.default_rng(side)
+    dzci, dzfi, dzc, dzf = zgrid(n[2], 1.0)
+    u, v, w = random_velocity(rng, n, 1)
+    flags = [0] * 6
+    flags[side] = 1
+    oracle.bounduvw("PPPPDD" * 3, n, [0.0] * 18, 1, 1, [1 / 10, 1 / 8, 1.0], dzc, dzf, u, v, w, isoutflow=flags)
+    # divergence of the interior cells; arrays are [k, j, i] with one halo layer
+    div = ((u[1:-1, 1:-1, 1:-1] - u[1:-1, 1:-1, :-2]) * 10 + (v[1:-1, 1:-1, 1:-1] - v[1:-1, :-2, 1:-1]) * 8
+           + (w[1:-1, 1:-1, 1:-1] - w[:-2, 1:-1, 1:-1]) * dzfi[1:-1, None, None])
+    face = [div[:, :, 0], div[:, :, -1], div[:, 0, :], div[:, -1, :], div[0], div[-1]][side]
+    assert np.abs(face).max() <= 1e-12 * np.abs(div).max()
