@@ -64,8 +64,8 @@ FG_HD unsigned bits_of_float(float x) {
 #endif
 }
 
-FG_HD float f32_of(double x) {
-  const unsigned hi = hi_word(x), lo = lo_word(x);
+// General form: every exponent (subnormal results flushed, overflow to inf, NaN kept).
+FG_HD float f32_of_any(unsigned hi, unsigned lo) {
   const unsigned sign = hi & 0x80000000u, ex = (hi >> 20) & 0x7ffu;
   const int e = (int)ex - 896;  // FP32 biased exponent
   unsigned f = sign | ((unsigned)e << 23) | (((hi << 3) | (lo >> 29)) & 0x7fffffu);
@@ -74,8 +74,24 @@ FG_HD float f32_of(double x) {
   return float_of_bits(f);
 }
 
+// For |x| in FP32's normal range (double exponent 897..1150) the FP32 bit
+// pattern is the double's top 32 bits shifted left by 3 (exponent field and
+// the top 23 mantissa bits), with the FP32 exponent = double exponent - 896:
+// in that range the low 8 bits of the double exponent are the FP32 exponent
+// with bit 7 flipped, so one XOR rebiases.  Four integer instructions; other
+// values take the general form above.
+FG_HD float f32_of(double x) {
+  const unsigned hi = hi_word(x), lo = lo_word(x);
+  if ((hi & 0x7fffffffu) - 0x38100000u < 0x47f00000u - 0x38100000u)
+    return float_of_bits(((((hi << 3) | (lo >> 29)) & 0x7fffffffu) ^ 0x40000000u) | (hi & 0x80000000u));
+  return f32_of_any(hi, lo);
+}
+
 FG_HD double f64_of(float x) {
-  const unsigned f = bits_of_float(x), e = (f >> 23) & 0xffu;
+  const unsigned f = bits_of_float(x);
+  if ((f & 0x7fffffffu) - 0x00800000u < 0x7f000000u)  // normal: rebias the exponent by +896, spread the mantissa
+    return from_words((((f & 0x7fffffffu) >> 3) + 0x38000000u) | (f & 0x80000000u), f << 29);
+  const unsigned e = (f >> 23) & 0xffu;
   unsigned hi = (f & 0x80000000u) | ((e + 896u) << 20) | ((f >> 3) & 0xfffffu), lo = f << 29;
   if (e == 0) {
     hi = f & 0x80000000u;

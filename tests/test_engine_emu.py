@@ -73,12 +73,15 @@ def test_bit_conversions(emu):
     emu.fg_emu_f32_of.argtypes = [dp, fp, C.c_long]
     emu.fg_emu_f64_of.argtypes = [fp, dp, C.c_long]
     rng = np.random.default_rng(5)
+    edges = [2.0 ** -126, np.nextafter(2.0 ** -126, 0.0), np.nextafter(2.0 ** -126, 1.0), 2.0 ** 127,
+             np.nextafter(2.0 ** 128, 0.0), 2.0 ** 128, np.nextafter(2.0 ** -125, 0.0)]  # ends of the fast path
     x = np.concatenate([rng.standard_normal(4000) * 10.0 ** rng.integers(-30, 30, 4000),
-                        np.array([0.0, -0.0, 1.0, -1.0, 3.0e38, -3.0e38, 1.5e-38, 2.0 ** -126, 2.0 ** -127])])
+                        np.array([0.0, -0.0, 1.0, -1.0, 3.0e38, -3.0e38, 1.5e-38, 2.0 ** -126, 2.0 ** -127]),
+                        np.array(edges), -np.array(edges)])
     y = np.empty(len(x), np.float32)
     emu.fg_emu_f32_of(x, y, len(x))
     assert np.array_equal(y.view(np.uint32), _trunc_f32(x).view(np.uint32))
-    nrm = np.abs(x) >= 2.0 ** -126
+    nrm = (np.abs(x) >= 2.0 ** -126) & (np.abs(x) < np.float64(np.finfo(np.float32).max))
     assert np.all(np.abs(y[nrm] - x[nrm]) <= np.abs(x[nrm]) * 2.0 ** -23)
     # out of range: below 2^-126 -> signed zero, above FP32 max -> inf, NaN stays NaN
     z = np.array([1e-40, -1e-300, 1e39, -1e300, np.inf, -np.inf, np.nan])
@@ -86,7 +89,9 @@ def test_bit_conversions(emu):
     emu.fg_emu_f32_of(z, w, len(z))
     assert w[0] == 0.0 and np.signbit(w[1]) and w[1] == 0.0
     assert w[2] == np.inf and w[3] == -np.inf and w[4] == np.inf and w[5] == -np.inf and np.isnan(w[6])
-    f = np.concatenate([y[np.isfinite(y)], np.array([np.inf, -np.inf, np.nan], np.float32)])
+    tiny = np.array([np.finfo(np.float32).tiny, np.nextafter(np.float32(np.finfo(np.float32).tiny), np.float32(0)),
+                     np.finfo(np.float32).max, -np.finfo(np.float32).max], np.float32)
+    f = np.concatenate([y[np.isfinite(y)], tiny, np.array([np.inf, -np.inf, np.nan], np.float32)])
     d = np.empty(len(f), np.float64)
     emu.fg_emu_f64_of(np.ascontiguousarray(f), d, len(f))
     normal = (np.abs(f) >= 2.0 ** -126) | (f == 0) | ~np.isfinite(f)
