@@ -83,6 +83,8 @@ BYTES_PER_CELL = {
     "k_stencil<fillps>": 36,        # R u,v,w (24) W f-copy FP64 (8) W S FP32 (4)
     "k_stencil<residual>": 20,      # R f, x (16) W S (4)
     "k_resnorm": 16,                # R f, x
+    "k_resnorm_correc": 88,         # R f, x ; RW u,v,w ; RW p
+    "k_sub": 24,                    # R x, s ; W d (halo-1 array)
     # cluster plane kernels (run-time sized, and compile-time sized for 256^2)
     "k_xyfwd_cluster<f32,keep-fillps>": 36,
     "k_xyfwd_cluster<f32,keep-halo>": 20,
@@ -104,7 +106,7 @@ BYTES_PER_CELL = {
 # not HBM, bounds them): DF increments 3x(2 sub + 1 add), fillps 3 sub + 1 mul
 # + 2 fma, residual 2 add + 5 fma, correc 3x(sub + fma) + 1 add.
 FP64_PER_CELL = {"k_pres_tw_src": 9, "k_stencil<fillps>": 6, "k_stencil<residual>": 7, "k_resnorm": 7,
-                 "k_correc_padd": 7}
+                 "k_correc_padd": 7, "k_resnorm_correc": 14}
 FP64_PEAK_TOPS = 0.60   # FP64 FMA instructions/s measured on this part (1.20 TFLOP/s counting an FMA as 2)
 
 

@@ -11,6 +11,7 @@
 #include "fixed.h"
 #include "fft_fixed.cuh"
 
+#include <cstdint>
 #include <cstdlib>
 #include <type_traits>
 #include <mutex>
@@ -31,6 +32,25 @@ template <typename T, int N, int C> struct FixGeo {
 struct Barrier {
   __device__ void operator()() const { __syncthreads(); }
 };
+
+// Asynchronous global -> shared copies (no register staging: every copy of a
+// thread is in flight at once) and an L2 prefetch of a contiguous span.
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+               "l"(__cvta_generic_to_global(src))
+               : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+               "l"(__cvta_generic_to_global(src))
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// bytes: a multiple of 16 from a 16-byte aligned address (the caller checks)
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(__cvta_generic_to_global(p)), "r"(bytes)
+               : "memory");
+}
 
 // Columns [r*COLS, (r+1)*COLS) of every CTA's x-spectrum rows (pitch P) into
 // this CTA's column block (N x COLS, row-major).
@@ -102,20 +122,30 @@ __global__ void __launch_bounds__(FIX_NTH, 512 / FIX_NTH) k_xyfwd_fix(AxisPlan a
   const int y0 = r * G::ROWS;
   float ss = 0.0f;
   for (int k = blockIdx.x / C; k < g.nz; k += gridDim.x / C) {
-    load_cells<T>(
-        in, G::ROWS * N,
-        [&](int idx, int &x, int &y, int &kk) -> bool {
-          const unsigned u = idx;
-          x = (int)(u % N);
-          y = y0 + (int)(u / N);
-          kk = k;
-          return true;
-        },
-        [&](int idx, T t) {
-          const unsigned u = idx;
-          B0[u + u / N] = t;  // row ly = u / N at pitch P = N + 1
-        },
-        ss);
+    bool copied = false;
+    if constexpr (std::is_same_v<In, InF32> && std::is_same_v<T, float>) {
+      if (!nrm) {  // this CTA's rows of plane k, copied into the pitched slab (no norm to take on the way)
+        const float *src = in.f + ((long)k * N + y0) * N;
+        for (int u = tid; u < G::ROWS * N; u += FIX_NTH) cp_async4(B0 + u + u / N, src + u);
+        cp_async_wait_all();
+        copied = true;
+      }
+    }
+    if (!copied)
+      load_cells<T>(
+          in, G::ROWS * N,
+          [&](int idx, int &x, int &y, int &kk) -> bool {
+            const unsigned u = idx;
+            x = (int)(u % N);
+            y = y0 + (int)(u / N);
+            kk = k;
+            return true;
+          },
+          [&](int idx, T t) {
+            const unsigned u = idx;
+            B0[u + u / N] = t;  // row ly = u / N at pitch P = N + 1
+          },
+          ss);
     __syncthreads();
     // x: rows in B0 -> stages in B1/B2 -> split into the x-spectrum rows, B0
     fix::forward<T, N, PX, G::BX, FIX_NTH>(B0, G::P, 1, (C2<T> *)B1, (C2<T> *)B2, Wt, Qx,
@@ -143,10 +173,25 @@ __global__ void __launch_bounds__(FIX_NTH, 512 / FIX_NTH) k_xyinv_fix(AxisPlan a
   const Barrier bar;
   const int y0 = r * G::ROWS;
   for (int k = blockIdx.x / C; k < g.nz; k += gridDim.x / C) {
+    if constexpr (std::is_same_v<Out, OutHaloAdd>) {  // the rows this CTA adds to, on their way to L2
+      const double *span = out.p + out.g.pidx(0, y0 + 1, k + 1);
+      const unsigned bytes = (unsigned)(sizeof(double) * G::ROWS * (N + 2)) & ~15u;
+      if (tid == 0 && ((uintptr_t)span & 15) == 0) prefetch_l2(span, bytes);
+    }
     const T *Sp = S + (long)k * N * N + r * G::COLS;
-    for (int i = tid; i < N * G::COLS; i += FIX_NTH) {
-      const unsigned u = i;
-      B0[i] = Sp[(u / G::COLS) * N + u % G::COLS];
+    if constexpr (std::is_same_v<T, float>) {  // the column block: 16-byte copies, all in flight together
+      static_assert(G::COLS % 4 == 0, "column block rows must be whole 16-byte chunks");
+      constexpr int Q = G::COLS / 4;
+      for (int i = tid; i < N * Q; i += FIX_NTH) {
+        const unsigned rw = i / Q, c = i % Q;
+        cp_async16(B0 + rw * G::COLS + 4 * c, Sp + (long)rw * N + 4 * c);
+      }
+      cp_async_wait_all();
+    } else {
+      for (int i = tid; i < N * G::COLS; i += FIX_NTH) {
+        const unsigned u = i;
+        B0[i] = Sp[(u / G::COLS) * N + u % G::COLS];
+      }
     }
     __syncthreads();
     // y^-1: columns in B0 -> stages in B1/B0 -> columns in B2

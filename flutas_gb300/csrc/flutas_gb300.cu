@@ -11,6 +11,8 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -326,7 +328,7 @@ struct flutas_plan {
   DBuf czc;            // folded correc factors dt*dzci(k)/rho0
   DBuf zdf;            // per-level factors of the Dodd-Ferrante term
   AxisTables tx64, ty64, tx32, ty32;
-  DBuf S64, S32, fbuf, phi, nrm;
+  DBuf S64, S32, fbuf, phi, phi2, nrm;
   Mirrors mir;
   cudaStream_t stream = 0;
   bool sync = true;
@@ -336,7 +338,8 @@ struct flutas_plan {
   bool rhsb_zero = false;      // every boundary-RHS value is 0 (homogeneous BCs): updt_rhs_b adds nothing
   double last_relres = 0.0;    // relative residual / FP32 solves of the last mixed solve
   int last_iters = 0;
-  double contraction = 1e-3;   // residual reduction of one FP32 solve, last measured
+  double contraction = 1e-3;   // residual reduction of one FP32 solve, last measured (initial value:
+                               // FLUTAS_GB300_CONTRACTION when set, for tests of the misprediction paths)
 };
 
 namespace {
@@ -630,9 +633,22 @@ int solve_fp64_dev(flutas_plan *pl, double *p, const double *lam, const double *
 // With the fixed-size cluster kernels, the FP64 RHS (fillps, residual) is
 // evaluated by a stencil pass at full occupancy and the transform reads its
 // FP32 values in place; the other paths evaluate it in the transform's loads.
+// The correction a mixed projection applies after its solve (correc with
+// phi = x, p = p + x), fused into the solve's last convergence check when the
+// measured contraction predicts it (k_resnorm_correc).  If that check does not
+// end the solve after all, the solve keeps a copy of the x it applied and the
+// caller adds the correction of the difference (correc and the p update are
+// linear in phi).
+struct FinalCorrec {
+  CorrecAddArgs ca;
+  std::function<int()> boundp_phi;  // ghosts of phi, read by the correction
+  double *snapshot = nullptr;       // x as applied, when the solve went on
+  bool applied = false, continued = false;
+};
+
 template <typename First>
 int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, int max_iter, double *relres,
-                    int *iters) {
+                    int *iters, FinalCorrec *fc = nullptr) {
   Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
   const size_t halo_bytes = sizeof(double) * (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
   TRY(pl->S32.ensure(sizeof(float) * (size_t)g.nx * g.ny * g.nz));
@@ -682,8 +698,21 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
   for (;;) {
     const bool norm_only = it >= max_iter || before * pl->contraction <= 0.5 * tol;
     CK(cudaMemsetAsync(nrm + 1, 0, sizeof(double), st));
-    if (norm_only) TRY(stencil(R, nullptr, nullptr, nrm + 1));
-    else TRY(transform(R, nrm + 1));
+    if (norm_only && fc && !fc->applied) {
+      TRY(fc->boundp_phi());
+      const long cells = (long)g.nx * g.ny * g.nz;
+      const int grid = grid_for(k_resnorm_correc<int>, 256, 0, (cells + 511) / 512);
+      if (grid < 0) return grid;
+      if (cells >= (1L << 31) - 4096)
+        TRY(launch("k_resnorm_correc", st, [&] { k_resnorm_correc<long long><<<grid, 256, 0, st>>>(R, fc->ca, nrm + 1); }));
+      else
+        TRY(launch("k_resnorm_correc", st, [&] { k_resnorm_correc<int><<<grid, 256, 0, st>>>(R, fc->ca, nrm + 1); }));
+      fc->applied = true;
+    } else if (norm_only) {
+      TRY(stencil(R, nullptr, nullptr, nrm + 1));
+    } else {
+      TRY(transform(R, nrm + 1));
+    }
     double h[2];
     CK(cudaMemcpyAsync(h, nrm, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -692,6 +721,12 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
     rel = h[0] > 0 ? std::sqrt(h[1] / h[0]) : std::sqrt(h[1]);
     if (before > 0.0) pl->contraction = std::min(1.0, std::max(rel / before, 1e-12));
     if (rel <= tol || it >= max_iter) break;
+    if (fc && fc->applied && !fc->continued) {  // the fused check did not end the solve: keep the applied x
+      fc->continued = true;
+      TRY(pl->phi2.ensure(halo_bytes));
+      fc->snapshot = pl->phi2.as<double>();
+      CK(cudaMemcpyAsync(fc->snapshot, x, halo_bytes, cudaMemcpyDeviceToDevice, st));
+    }
     if (norm_only) TRY(transform(R, nullptr));  // prediction missed
     // correction of this pass: e = A^-1 r in FP32, x += e in FP64
     TRY(zsolve<float>(pl, S, lam, a, b, c, true));
@@ -881,6 +916,10 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
   if (const char *e = getenv("FLUTAS_GB300_XY_PATH")) {  // 0 forces separate passes (A/B timing)
     if (atoi(e) == 0) pl->path64 = pl->path32 = 0;
   }
+  if (const char *e = getenv("FLUTAS_GB300_CONTRACTION")) {  // initial predicted contraction (tests)
+    const double c = atof(e);
+    if (c > 0.0 && c <= 1.0) pl->contraction = c;
+  }
   arrplan[0] = pl;
   arrplan[1] = arrplan[2] = arrplan[3] = nullptr;
   return FLUTAS_OK;
@@ -893,7 +932,7 @@ int flutas_gb300_fftend(void **arrplan) {
   cudaStreamSynchronize(pl->stream);
   DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->czc, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
                   &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W, &pl->tx32.Q, &pl->ty32.W,
-                  &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->nrm};
+                  &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm};
   for (DBuf *d : bufs) d->release();
   pl->mir.release();
   pl->magic = 0;
@@ -917,7 +956,7 @@ int flutas_gb300_plan_info(void *plan, size_t *device_bytes, int *xy_path_fp64, 
     size_t s = 0;
     const DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->czc, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1],
                           &pl->rhsb[2], &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W,
-                          &pl->tx32.Q, &pl->ty32.W, &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->nrm};
+                          &pl->tx32.Q, &pl->ty32.W, &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm};
     for (const DBuf *d : bufs) s += d->bytes;
     for (const DBuf &d : pl->mir.bufs) s += d.bytes;
     *device_bytes = s;
@@ -1488,13 +1527,9 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     TRY(zsolve<double>(pl, S, pl->lam.as<double>(), pl->a.as<double>(), pl->b.as<double>(), pl->c.as<double>(),
                        pl->pin_zero_mode));
     TRY(inv_xy<double>(pl, S, OutHalo{phi, pl->normfft, gp}, pl->tx64, pl->ty64, pl->path64));
-  } else {
-    rc = solve_mixed_dev(pl, in, phi, tol, max_iter, &pl->last_relres, &pl->last_iters);
-    if (rc != 0 && rc != FLUTAS_EITER) return rc;
   }
   const double dl[3] = {1.0 / dxi, 1.0 / dyi, 0.0};
   const double dzc0 = 1.0 / pl->dzci_h[0 - 1 + nh_d], dzcn = 1.0 / pl->dzci_h[nz - 1 + nh_d];
-  TRY(boundp_dev(phi, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
   CorrecAddArgs ca;
   const double rho0i = 1.0 / rho0;
   TRY(pl->czc.ensure(sizeof(double) * (nz + 2 * nh_d)));
@@ -1505,7 +1540,25 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   ca.u = u; ca.v = v; ca.w = w; ca.p = p;
   ca.cx = (dt * dxi) * rho0i; ca.cy = (dt * dyi) * rho0i;
   ca.g = g;
-  TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<grid_cells(ca.g), 256, 0, st>>>(ca); }));
+  FinalCorrec fc;
+  if (precision != 0) {
+    fc.ca = ca;
+    fc.boundp_phi = [&] { return boundp_dev(phi, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st); };
+    rc = solve_mixed_dev(pl, in, phi, tol, max_iter, &pl->last_relres, &pl->last_iters, &fc);
+    if (rc != 0 && rc != FLUTAS_EITER) return rc;
+  }
+  if (!fc.applied) {
+    TRY(boundp_dev(phi, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
+    TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<grid_cells(ca.g), 256, 0, st>>>(ca); }));
+  } else if (fc.continued) {  // the correction of x - (x as applied)
+    double *d = fc.snapshot;
+    const long n = (long)(nx + 2) * (ny + 2) * (nz + 2);
+    TRY(launch("k_sub", st, [&] { k_sub<<<stream_grid(n), 256, 0, st>>>(phi, d, d, n); }));
+    TRY(boundp_dev(d, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
+    CorrecAddArgs cd = ca;
+    cd.phi = d;
+    TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<grid_cells(cd.g), 256, 0, st>>>(cd); }));
+  }
   if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
   TRY(boundp_dev(p, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
   return rc;

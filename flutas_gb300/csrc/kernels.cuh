@@ -1049,6 +1049,67 @@ __global__ void k_correc_padd(CorrecAddArgs a) {
 }
 #endif
 
+// The last convergence check of a mixed projection fused with the correction
+// it leads to: ||f - A x||^2 (as k_stencil_pass) and, in the same pass,
+// correc with phi = x and p = p + x (k_correc_padd's arithmetic).  Both halves
+// are bound by the FP64 pipe and read the same x; one pass saves the other's
+// memory traffic and launch.  The caller applies it when the measured
+// contraction predicts convergence and tops the correction up if the check
+// fails after all (correc and the p update are linear in phi).
+template <typename IDX = int>
+__global__ void __launch_bounds__(256) k_resnorm_correc(InResidual R, CorrecAddArgs a, double *nrm) {
+  const Geo &g = a.g;  // velocity halo h; R.g: halo-1 geometry of x and f
+  const IDX tot = (IDX)g.nx * g.ny * g.nz;
+  const FastDiv fx(g.nx), fy(g.ny);
+  const long plane = (long)(g.nx + 2) * (g.ny + 2);
+  float ss = 0.0f;
+  for (IDX b = (IDX)blockIdx.x * blockDim.x * 2 + threadIdx.x; b < tot; b += (IDX)gridDim.x * blockDim.x * 2) {
+    double v[2];
+    int xs[2], ys[2], ks[2];
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      const IDX idx = b + (IDX)u * blockDim.x;
+      int row;
+      if constexpr (sizeof(IDX) == 4) {
+        row = fx.div((int)idx);
+        xs[u] = (int)idx - row * g.nx;
+      } else {
+        const IDX r = idx / g.nx;
+        row = (int)r;
+        xs[u] = (int)(idx - r * g.nx);
+      }
+      ks[u] = fy.div(row);
+      ys[u] = row - ks[u] * g.ny;
+      v[u] = idx < tot ? R(xs[u], ys[u], ks[u]) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      const IDX idx = b + (IDX)u * blockDim.x;
+      const float f = f32_of(v[u]);
+      ss = fmaf(f, f, ss);
+      if (idx < tot) {
+        const int i = xs[u] + 1, j = ys[u] + 1, k = ks[u] + 1;
+        const long pc = g.pidx(i, j, k), ui = g.uidx(i, j, k);
+        const double ph = a.phi[pc];
+        a.u[ui] = fma(-a.cx, a.phi[pc + 1] - ph, a.u[ui]);
+        a.v[ui] = fma(-a.cy, a.phi[pc + (g.nx + 2)] - ph, a.v[ui]);
+        a.w[ui] = fma(-a.cz[k], a.phi[pc + plane] - ph, a.w[ui]);
+        a.p[pc] = a.p[pc] + ph;
+      }
+    }
+  }
+  block_sum_add((double)ss, nrm);
+}
+
+// d = x - s on a whole halo-1 array (the correction still to apply after a
+// fused check that did not end the solve).
+#ifndef FG_NO_PLAIN_KERNELS
+__global__ void k_sub(const double *x, const double *s, double *d, long n) {
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) d[t] = x[t] - s[t];
+}
+#endif
+
+
 }  // namespace fg
 
 namespace fg {

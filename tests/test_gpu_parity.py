@@ -259,6 +259,22 @@ def test_gpu_bounduvw_matches_oracle(lib, oracle, cbcvel, nh_u):
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
 def test_gpu_two_phase_projection_df(lib, oracle, precision):
     """pres_tw_src + bounduvw + projection of a two-phase field == the oracle sequence."""
+    two_phase_case(lib, oracle, precision)
+
+
+@pytest.mark.parametrize("contraction", ["1e-30", "1.0"], ids=["fused-check-missed", "late-prediction"])
+def test_gpu_mixed_projection_final_check(lib, oracle, contraction, monkeypatch):
+    """The mixed projection applies correc + p update inside its last check when
+    the predicted contraction says the solve has converged.  A prediction of
+    1e-30 makes the first check the fused one although it cannot pass: the
+    solve goes on and the projection adds the correction of the rest.  A
+    prediction of 1 delays the fused check to a later iteration.  Both must
+    give the oracle's fields."""
+    monkeypatch.setenv("FLUTAS_GB300_CONTRACTION", contraction)
+    two_phase_case(lib, oracle, 1)
+
+
+def two_phase_case(lib, oracle, precision):
     n, cbc, cbcvel = [32, 24, 16], "PPPPNN", "PPPPDD" * 3
     rng = np.random.default_rng(51)
     dzci, dzfi, dzc, dzf = zgrid(n[2], 0.0)
