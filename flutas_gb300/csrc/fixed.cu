@@ -33,25 +33,6 @@ struct Barrier {
   __device__ void operator()() const { __syncthreads(); }
 };
 
-// Asynchronous global -> shared copies (no register staging: every copy of a
-// thread is in flight at once) and an L2 prefetch of a contiguous span.
-__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
-               "l"(__cvta_generic_to_global(src))
-               : "memory");
-}
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
-               "l"(__cvta_generic_to_global(src))
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-// bytes: a multiple of 16 from a 16-byte aligned address (the caller checks)
-__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(__cvta_generic_to_global(p)), "r"(bytes)
-               : "memory");
-}
-
 // Columns [r*COLS, (r+1)*COLS) of every CTA's x-spectrum rows (pitch P) into
 // this CTA's column block (N x COLS, row-major).
 template <typename T, int N, int C, int FIX_NTH>

@@ -552,8 +552,7 @@ int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const doub
   if (!za.periodic) {
     constexpr int CH = 16;
     const int nt = 128;
-    const int nch = (za.nn + CH - 1) / CH;
-    const size_t sm = sizeof(T) * (size_t)nch * nt;
+    const size_t sm = zstream_smem<T, CH>(za.nn, nt);
     if ((int)sm > max_smem_optin()) return fail(FLUTAS_EUNSUPPORTED, "nz=%d too large for the z kernel", za.nz);
     TRY(allow_smem(k_zstream<T, CH>));
     // launch in column batches whose eliminated values (one column of T per

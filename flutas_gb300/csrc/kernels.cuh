@@ -1174,10 +1174,6 @@ namespace fg {
 // the elimination factors d_k are not stored: the backward sweep recomputes
 // them chunk by chunk from d at the chunk start, kept in shared memory.
 // ===========================================================================
-template <typename T>
-__device__ __forceinline__ T zpivot(T bb, T a, T dprev, bool first) {
-  return first ? bb : fma(-a, dprev, bb);
-}
 // 1/x: the SFU reciprocal in FP32 (the FP32 solve is refined in FP64), a
 // correctly rounded division in FP64.
 __device__ __forceinline__ float zrcp(float x) { return __fdividef(1.0f, x); }
@@ -1185,53 +1181,106 @@ __device__ __forceinline__ float zrcp(float x) { return __fdividef(1.0f, x); }
 // an IEEE division outside it.
 __device__ __forceinline__ double zrcp(double x) { return f32_range(x) ? rcp64(x) : 1.0 / x; }
 
+// Asynchronous global -> shared copies (no register staging: every copy a
+// thread has issued is in flight at once) and an L2 prefetch of a contiguous
+// span.  Copies of 4 and 8 bytes go through L1 (.ca), 16-byte ones bypass it.
+template <int B> __device__ __forceinline__ void cp_async(void *dst, const void *src) {
+  static_assert(B == 4 || B == 8 || B == 16, "cp.async copies 4, 8 or 16 bytes");
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const size_t g = __cvta_generic_to_global(src);
+  if constexpr (B == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(g) : "memory");
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(g), "n"(B) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) { cp_async<4>(dst, src); }
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) { cp_async<16>(dst, src); }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// bytes: a multiple of 16 from a 16-byte aligned address (the caller checks)
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(__cvta_generic_to_global(p)), "r"(bytes)
+               : "memory");
+}
+
+// Coefficients of one z level, staged in shared memory once per CTA so that a
+// level costs one 16- (FP32) or 32-byte (FP64) broadcast load.
+template <typename T> struct alignas(4 * sizeof(T)) ZCoef {
+  T a, b, c, pad;
+};
+template <typename T, int CH> FG_HD size_t zstream_smem(int nn, int nt) {
+  return sizeof(ZCoef<T>) * (size_t)nn + sizeof(T) * (size_t)nt * (size_t)((nn + CH - 1) / CH);
+}
+
+// Chunks whose levels all lie below n - 1 (every chunk but the last) run
+// without per-level predicates; the last one takes the general path (the last
+// level divides, and a pinned singular column ends in zero).  Level 0 needs no
+// case of its own: its pivot b + lam - a*0 is b + lam exactly (a is finite).
 template <typename T, int CH>
 __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, long q_begin, long q_end) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *chk = (T *)smem_raw;  // [nchunks][blockDim.x]: d_{k0-1} of each chunk
   const int tid = threadIdx.x, nt = blockDim.x;
-  const long q = q_begin + (long)blockIdx.x * nt + tid;
-  const bool act = q < q_end;
   const int n = za.nn;
+  ZCoef<T> *co = (ZCoef<T> *)smem_raw;  // [n]
+  T *chk = (T *)(co + n);               // [nch][nt]: d_{k0-1} of each chunk
+  for (int k = tid; k < n; k += nt)
+    co[k] = ZCoef<T>{((const T *)za.at)[k], ((const T *)za.bt)[k], ((const T *)za.ct)[k], (T)0};
+  __syncthreads();
+  const long q = q_begin + (long)blockIdx.x * nt + tid;
+  if (q >= q_end) return;  // no block-wide barrier below
   const long plane = za.nq;
-  const double lam64 = act ? za.lam[q] : 1.0;
+  const double lam64 = za.lam[q];
   const bool pin = za.pin && lam64 == 0.0;
   const T lam = (T)lam64;
-  const T *__restrict__ ca = (const T *)za.at, *__restrict__ cb = (const T *)za.bt, *__restrict__ cc = (const T *)za.ct;
-  T *col = S + (act ? q : 0);
+  T *col = S + q;
   const int nch = (n + CH - 1) / CH;
   // ---- forward elimination
   T r[CH], rn[CH];
 #pragma unroll
-  for (int i = 0; i < CH; i++) r[i] = (act && i < n) ? col[(long)i * plane] : (T)0;
+  for (int i = 0; i < CH; i++) r[i] = i < n ? col[(long)i * plane] : (T)0;
   T dprev = (T)0, yprev = (T)0;
   for (int m = 0; m < nch; m++) {
     const int k0 = m * CH;
+    T *p = col + (long)k0 * plane;
+    {
+      const T *pn = p + (long)CH * plane;
 #pragma unroll
-    for (int i = 0; i < CH; i++) {
-      const int k = k0 + CH + i;
-      rn[i] = (act && k < n) ? col[(long)k * plane] : (T)0;
+      for (int i = 0; i < CH; i++) rn[i] = k0 + CH + i < n ? pn[(long)i * plane] : (T)0;
     }
     chk[m * nt + tid] = dprev;
+    if (k0 + CH < n) {
 #pragma unroll
-    for (int i = 0; i < CH; i++) {
-      const int k = k0 + i;
-      if (k < n) {
-        const T bb = cb[k] + lam;
-        const T ak = ca[k];
-        T y, d;
-        if (k < n - 1) {
-          const T z = zrcp(zpivot<T>(bb, ak, dprev, k == 0));
-          d = cc[k] * z;
-          y = (k == 0 ? r[i] : fma(-ak, yprev, r[i])) * z;
-        } else {
-          const T zl = zpivot<T>(bb, ak, dprev, k == 0);
-          y = (zl != (T)0 && !pin) ? fma(-ak, yprev, r[i]) / zl : (T)0;
-          d = (T)0;
-        }
-        if (act) col[(long)k * plane] = y;
-        dprev = d;
+      for (int i = 0; i < CH; i++) {
+        const ZCoef<T> cf = co[k0 + i];
+        const T z = zrcp(fma(-cf.a, dprev, cf.b + lam));
+        const T y = fma(-cf.a, yprev, r[i]) * z;
+        dprev = cf.c * z;
+        *p = y;
+        p += plane;
         yprev = y;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < CH; i++) {
+        const int k = k0 + i;
+        if (k < n) {
+          const ZCoef<T> cf = co[k];
+          const T piv = fma(-cf.a, dprev, cf.b + lam);
+          T y, d;
+          if (k < n - 1) {
+            const T z = zrcp(piv);
+            d = cf.c * z;
+            y = fma(-cf.a, yprev, r[i]) * z;
+          } else {
+            y = (piv != (T)0 && !pin) ? fma(-cf.a, yprev, r[i]) / piv : (T)0;
+            d = (T)0;
+          }
+          *p = y;
+          p += plane;
+          dprev = d;
+          yprev = y;
+        }
       }
     }
 #pragma unroll
@@ -1242,36 +1291,54 @@ __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, lo
   {
     const int k0 = (nch - 1) * CH;
 #pragma unroll
-    for (int i = 0; i < CH; i++) r[i] = (act && k0 + i < n) ? col[(long)(k0 + i) * plane] : (T)0;
+    for (int i = 0; i < CH; i++) r[i] = k0 + i < n ? col[(long)(k0 + i) * plane] : (T)0;
   }
   for (int m = nch - 1; m >= 0; m--) {
     const int k0 = m * CH;
+    if (m > 0) {
+      const T *pp = col + (long)(k0 - CH) * plane;
 #pragma unroll
-    for (int i = 0; i < CH; i++) {
-      const int k = k0 - CH + i;
-      rn[i] = (act && m > 0 && k >= 0) ? col[(long)k * plane] : (T)0;
+      for (int i = 0; i < CH; i++) rn[i] = pp[(long)i * plane];
     }
     T dd[CH];
     T dp = chk[m * nt + tid];
+    if (k0 + CH < n) {
 #pragma unroll
-    for (int i = 0; i < CH; i++) {
-      const int k = k0 + i;
-      if (k < n - 1) {
-        const T bb = cb[k] + lam;
-        const T z = zrcp(zpivot<T>(bb, ca[k], dp, k == 0));
-        dd[i] = cc[k] * z;
+      for (int i = 0; i < CH; i++) {
+        const ZCoef<T> cf = co[k0 + i];
+        const T z = zrcp(fma(-cf.a, dp, cf.b + lam));
+        dd[i] = cf.c * z;
         dp = dd[i];
-      } else {
-        dd[i] = (T)0;
       }
-    }
+      T *p = col + (long)(k0 + CH - 1) * plane;
 #pragma unroll
-    for (int i = CH - 1; i >= 0; i--) {
-      const int k = k0 + i;
-      if (k < n) {
-        const T x = (k == n - 1) ? r[i] : fma(-dd[i], xnext, r[i]);
-        if (act) col[(long)k * plane] = x;
+      for (int i = CH - 1; i >= 0; i--) {
+        const T x = fma(-dd[i], xnext, r[i]);
+        *p = x;
+        p -= plane;
         xnext = x;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < CH; i++) {
+        const int k = k0 + i;
+        if (k < n - 1) {
+          const ZCoef<T> cf = co[k];
+          const T z = zrcp(fma(-cf.a, dp, cf.b + lam));
+          dd[i] = cf.c * z;
+          dp = dd[i];
+        } else {
+          dd[i] = (T)0;
+        }
+      }
+#pragma unroll
+      for (int i = CH - 1; i >= 0; i--) {
+        const int k = k0 + i;
+        if (k < n) {
+          const T x = (k == n - 1) ? r[i] : fma(-dd[i], xnext, r[i]);
+          col[(long)k * plane] = x;
+          xnext = x;
+        }
       }
     }
 #pragma unroll
