@@ -101,4 +101,26 @@ FG_HD double f64_of(float x) {
   return from_words(hi, lo);
 }
 
+// x = h + l with h = f32_of(x) (x truncated to FP32) and l the next 23 bits of
+// x's significand: both are exact FP32 values and |x - h - l| < 2^-46 |x|.
+// Valid for x = +-0 and 2^-103 <= |x| < 2^128 (double exponent 920..1150),
+// which split_ok tells.  l is the difference of two floats of one binade
+// (exact, Sterbenz): the remainder bits under a power of two, minus it.  No
+// FP64 instruction.
+FG_HD bool split_ok(double x) {
+  const unsigned hi = hi_word(x), lo = lo_word(x);
+  return (hi & 0x7fffffffu) - 0x39800000u < 0x47f00000u - 0x39800000u || ((hi << 1) | lo) == 0u;
+}
+FG_HD void split32(double x, float &h, float &l) {
+  const unsigned hi = hi_word(x), lo = lo_word(x), s = hi & 0x80000000u;
+  const unsigned b = ((((hi >> 20) & 0x7ffu) - 919u) << 23) | s;
+  const bool zero = ((hi << 1) | lo) == 0u;
+  h = zero ? float_of_bits(s) : float_of_bits(((((hi << 3) | (lo >> 29)) & 0x7fffffffu) ^ 0x40000000u) | s);
+  l = zero ? float_of_bits(s) : float_of_bits(b | ((lo >> 6) & 0x7fffffu)) - float_of_bits(b);
+}
+// a - b from the splits of a and b: (ha - hb) is exact when ha and hb are
+// within a factor 2 of each other (the cancelling case), so the result is the
+// FP32 rounding of a - b to within 2^-46 (|a| + |b|) and one more rounding.
+FG_HD float diff32(float ha, float la, float hb, float lb) { return (ha - hb) + (la - lb); }
+
 }  // namespace fg

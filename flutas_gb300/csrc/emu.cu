@@ -79,6 +79,22 @@ extern "C" __attribute__((visibility("default"))) void fg_emu_f32_of(const doubl
 extern "C" __attribute__((visibility("default"))) void fg_emu_f64_of(const float *x, double *y, long n) {
   for (long i = 0; i < n; i++) y[i] = f64_of(x[i]);
 }
+extern "C" __attribute__((visibility("default"))) void fg_emu_split32(const double *x, float *h, float *l, int *ok,
+                                                                       long n) {
+  for (long i = 0; i < n; i++) {
+    ok[i] = split_ok(x[i]) ? 1 : 0;
+    split32(x[i], h[i], l[i]);
+  }
+}
+extern "C" __attribute__((visibility("default"))) void fg_emu_diff32(const double *a, const double *b, float *d,
+                                                                      long n) {
+  for (long i = 0; i < n; i++) {
+    float ha, la, hb, lb;
+    split32(a[i], ha, la);
+    split32(b[i], hb, lb);
+    d[i] = diff32(ha, la, hb, lb);
+  }
+}
 
 namespace {
 

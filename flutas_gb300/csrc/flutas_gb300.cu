@@ -1322,7 +1322,7 @@ int flutas_gb300_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, dou
   TRY(presw_consts(&a, sz.d, nh_d, nz, dxi, dyi, rho0i, f_t12, f2, zab, st));
   a.fp32 = 0;
   a.g = Geo{nx, ny, nz, nh_u};
-  TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<grid_cells(a.g), 256, 0, st>>>(a); }));
+  TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<presw_grid(a.g), PRESTW_NT, 0, st>>>(a); }));
   TRY(stage_out(su, st));
   TRY(stage_out(sv, st));
   TRY(stage_out(sw, st));
@@ -1488,7 +1488,7 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     TRY(presw_consts(&a, dzci_d, nh_d, nz, dxi, dyi, 1.0 / rho0, dt, dt / f_t12_o, pl->zdf.as<double>(), st));
     a.fp32 = precision == 1 ? 1 : 0;  // FP32 increment in the mixed path, FP64 in the FP64 path
     a.g = g;
-    TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<grid_cells(a.g), 256, 0, st>>>(a); }));
+    TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<presw_grid(a.g), PRESTW_NT, 0, st>>>(a); }));
   }
   // ghosts of u*,v*,w* as the app leaves them before fillps (bounduvw)
   if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));

@@ -929,39 +929,92 @@ __device__ __forceinline__ double df_incr(double dp, double dq, double rs, doubl
   const double dg = fma(f2, t, dp);
   return fma(A, t, -B * (rcp64_1(rs) * dg));
 }
-// FP32 increment (mixed path): the differences of p and of pold, which cancel,
-// are taken in FP64; the rest of the Dodd-Ferrante increment (relative error
-// ~1e-7 of a term that is itself small against u) in FP32; the update
-// u += delta stays FP64.  Only the differences and the update use the FP64 pipe.
-__device__ __forceinline__ double df_incr32(double dp64, double dq64, float rs, float A, float B, float f2) {
-  const float dp = f32_of(dp64), t = dp - f32_of(dq64);
+// FP32 increment (mixed path) from the differences of p and of pold across a
+// face (dp, dq: FP32 roundings of differences that cancel, formed without
+// rounding the operands first); the rest of the Dodd-Ferrante increment
+// (relative error ~1e-7 of a term that is itself small against u) in FP32;
+// the update u += delta stays FP64.
+__device__ __forceinline__ double df_incr32(float dp, float dq, float rs, float A, float B, float f2) {
+  const float t = dp - dq;
   const float dg = fmaf(f2, t, dp);
   return f64_of(fmaf(A, t, -B * (__frcp_rn(rs) * dg)));
 }
-__device__ __forceinline__ void pres_tw_cell32(const PresTwArgs &a, int i, int j, int k) {
-  const Geo &g = a.g;
-  const long c0 = g.pidx(i, j, k), cx = c0 + 1, cy = c0 + (g.nx + 2), cz = c0 + (long)(g.nx + 2) * (g.ny + 2);
-  const double p0 = a.p[c0], q0 = a.pold[c0];
-  const float r0 = f32_of(a.rho[c0]);
-  const long ui = g.uidx(i, j, k);
-  a.u[ui] += df_incr32(a.p[cx] - p0, a.pold[cx] - q0, f32_of(a.rho[cx]) + r0, a.xA32, a.xB32, a.f2_32);
-  a.v[ui] += df_incr32(a.p[cy] - p0, a.pold[cy] - q0, f32_of(a.rho[cy]) + r0, a.yA32, a.yB32, a.f2_32);
-  a.w[ui] += df_incr32(a.p[cz] - p0, a.pold[cz] - q0, f32_of(a.rho[cz]) + r0, f32_of(a.zA[k]), f32_of(a.zB[k]),
-                       a.f2_32);
+// p, pold and rho at one cell.
+struct DfPoint {
+  double p, q, r;
+};
+// The six differences come from exact FP32 splits of p and pold (split32):
+// only the three updates use the FP64 pipe.  Cells with a value outside the
+// split's range (|v| < 2^-103 but not 0, or |v| >= 2^128) take FP64
+// differences instead.
+__device__ __forceinline__ void df_cell32(const PresTwArgs &a, int k, const DfPoint &c, const DfPoint &x,
+                                          const DfPoint &y, const DfPoint &z, double &u, double &v, double &w) {
+  const float r0 = f32_of(c.r);
+  const float rx = f32_of(x.r) + r0, ry = f32_of(y.r) + r0, rz = f32_of(z.r) + r0;
+  float dpx, dpy, dpz, dqx, dqy, dqz;
+  if (split_ok(c.p) & split_ok(c.q) & split_ok(x.p) & split_ok(y.p) & split_ok(z.p) & split_ok(x.q) &
+      split_ok(y.q) & split_ok(z.q)) {
+    float h0, l0, h, l;
+    split32(c.p, h0, l0);
+    split32(x.p, h, l); dpx = diff32(h, l, h0, l0);
+    split32(y.p, h, l); dpy = diff32(h, l, h0, l0);
+    split32(z.p, h, l); dpz = diff32(h, l, h0, l0);
+    split32(c.q, h0, l0);
+    split32(x.q, h, l); dqx = diff32(h, l, h0, l0);
+    split32(y.q, h, l); dqy = diff32(h, l, h0, l0);
+    split32(z.q, h, l); dqz = diff32(h, l, h0, l0);
+  } else {
+    dpx = f32_of(x.p - c.p); dpy = f32_of(y.p - c.p); dpz = f32_of(z.p - c.p);
+    dqx = f32_of(x.q - c.q); dqy = f32_of(y.q - c.q); dqz = f32_of(z.q - c.q);
+  }
+  u += df_incr32(dpx, dqx, rx, a.xA32, a.xB32, a.f2_32);
+  v += df_incr32(dpy, dqy, ry, a.yA32, a.yB32, a.f2_32);
+  w += df_incr32(dpz, dqz, rz, f32_of(a.zA[k]), f32_of(a.zB[k]), a.f2_32);
 }
-__device__ __forceinline__ void pres_tw_cell(const PresTwArgs &a, int i, int j, int k) {
-  const Geo &g = a.g;
-  const long c0 = g.pidx(i, j, k), cx = c0 + 1, cy = c0 + (g.nx + 2), cz = c0 + (long)(g.nx + 2) * (g.ny + 2);
-  const double p0 = a.p[c0], q0 = a.pold[c0], r0 = a.rho[c0];
-  const long ui = g.uidx(i, j, k);
-  a.u[ui] += df_incr(a.p[cx] - p0, a.pold[cx] - q0, a.rho[cx] + r0, a.xA, a.xB, a.f2);
-  a.v[ui] += df_incr(a.p[cy] - p0, a.pold[cy] - q0, a.rho[cy] + r0, a.yA, a.yB, a.f2);
-  a.w[ui] += df_incr(a.p[cz] - p0, a.pold[cz] - q0, a.rho[cz] + r0, a.zA[k], a.zB[k], a.f2);
+// FP64 increments, rounded as the reference expression is.
+__device__ __forceinline__ void df_cell64(const PresTwArgs &a, int k, const DfPoint &c, const DfPoint &x,
+                                          const DfPoint &y, const DfPoint &z, double &u, double &v, double &w) {
+  u += df_incr(x.p - c.p, x.q - c.q, x.r + c.r, a.xA, a.xB, a.f2);
+  v += df_incr(y.p - c.p, y.q - c.q, y.r + c.r, a.yA, a.yB, a.f2);
+  w += df_incr(z.p - c.p, z.q - c.q, z.r + c.r, a.zA[k], a.zB[k], a.f2);
+}
+
+// One thread per (i, j) column and PRESTW_KZ consecutive levels: the z
+// neighbour of a level is the centre of the next (12 loads a cell, not 17),
+// and the next level's loads are issued before this level's stores.
+constexpr int PRESTW_KZ = 16, PRESTW_NT = 128;
+inline dim3 presw_grid(const Geo &g) {
+  return dim3((g.nx + PRESTW_NT - 1) / PRESTW_NT, g.ny < 65535 ? g.ny : 65535, (g.nz + PRESTW_KZ - 1) / PRESTW_KZ);
 }
 #ifndef FG_NO_PLAIN_KERNELS
-__global__ void k_pres_tw_src(PresTwArgs a) {
-  if (a.fp32) for_cells(a.g, [&](int i0, int j0, int k0) { pres_tw_cell32(a, i0 + 1, j0 + 1, k0 + 1); });
-  else for_cells(a.g, [&](int i0, int j0, int k0) { pres_tw_cell(a, i0 + 1, j0 + 1, k0 + 1); });
+__global__ void __launch_bounds__(PRESTW_NT) k_pres_tw_src(PresTwArgs a) {
+  const Geo &g = a.g;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (i > g.nx) return;
+  const int kb = blockIdx.z * PRESTW_KZ + 1, ke = min(kb + PRESTW_KZ - 1, g.nz);
+  const long sy = g.nx + 2, sz = sy * (g.ny + 2), usz = (long)(g.nx + 2 * g.h) * (g.ny + 2 * g.h);
+  const double *__restrict__ P = a.p, *__restrict__ Q = a.pold, *__restrict__ R = a.rho;
+  double *__restrict__ U = a.u, *__restrict__ V = a.v, *__restrict__ W = a.w;
+  auto at = [&](long o) { return DfPoint{P[o], Q[o], R[o]}; };
+  for (int j = blockIdx.y + 1; j <= g.ny; j += gridDim.y) {
+    long c = g.pidx(i, j, kb), ui = g.uidx(i, j, kb);
+    DfPoint cen = at(c), x = at(c + 1), y = at(c + sy), z = at(c + sz);
+    double u = U[ui], v = V[ui], w = W[ui];
+    for (int k = kb; k <= ke; k++) {
+      DfPoint xn = x, yn = y, zn = z;
+      double un = u, vn = v, wn = w;
+      if (k < ke) {
+        xn = at(c + sz + 1); yn = at(c + sz + sy); zn = at(c + 2 * sz);
+        un = U[ui + usz]; vn = V[ui + usz]; wn = W[ui + usz];
+      }
+      if (a.fp32) df_cell32(a, k, cen, x, y, z, u, v, w);
+      else df_cell64(a, k, cen, x, y, z, u, v, w);
+      U[ui] = u; V[ui] = v; W[ui] = w;
+      cen = z; x = xn; y = yn; z = zn;
+      u = un; v = vn; w = wn;
+      c += sz; ui += usz;
+    }
+  }
 }
 #endif
 

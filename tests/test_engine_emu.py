@@ -99,6 +99,47 @@ def test_bit_conversions(emu):
     assert np.all(ok[normal])
 
 
+def test_split32_and_diff32(emu):
+    """split32: x = h + l exactly in FP32 pieces, |x - h - l| < 2^-46 |x|, h = f32_of(x),
+    inside 2^-103 <= |x| < 2^128 and for +-0 (split_ok); diff32: a - b of nearly
+    equal values (the cancelling case) to FP32 accuracy, without FP64 arithmetic."""
+    dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+    fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+    ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+    emu.fg_emu_split32.argtypes = [dp, fp, fp, ip, C.c_long]
+    emu.fg_emu_diff32.argtypes = [dp, dp, fp, C.c_long]
+    emu.fg_emu_f32_of.argtypes = [dp, fp, C.c_long]
+    rng = np.random.default_rng(17)
+    lo_edge, hi_edge = 2.0 ** -103, 2.0 ** 128
+    edges = np.array([lo_edge, np.nextafter(lo_edge, 0.0), np.nextafter(hi_edge, 0.0), hi_edge, 0.0, -0.0,
+                      5e-324, np.inf, np.nan, 1.0, np.nextafter(1.0, 2.0), np.nextafter(1.0, 0.0)])
+    x = np.concatenate([rng.standard_normal(6000) * 10.0 ** rng.integers(-32, 38, 6000), edges, -edges])
+    n = len(x)
+    h, l, ok = np.empty(n, np.float32), np.empty(n, np.float32), np.empty(n, np.int32)
+    emu.fg_emu_split32(x, h, l, ok, n)
+    ax = np.abs(x)
+    want_ok = ((ax >= lo_edge) & (ax < hi_edge)) | (x == 0)
+    assert np.array_equal(ok.astype(bool), want_ok)
+    t = np.empty(n, np.float32)
+    emu.fg_emu_f32_of(x, t, n)
+    m = ok.astype(bool) & (x != 0)
+    assert np.array_equal(h[m].view(np.uint32), t[m].view(np.uint32))
+    s = h.astype(np.float64) + l.astype(np.float64)  # exact: 24 + 23 significant bits
+    assert np.all(np.abs(x[m] - s[m]) < ax[m] * 2.0 ** -46)
+    z = x == 0
+    assert np.all(h[z] == 0) and np.all(l[z] == 0)
+    assert np.array_equal(np.signbit(h[z]), np.signbit(x[z]))
+    # diff32 on nearby values: error within 2 FP32 roundings of the exact difference
+    a = rng.standard_normal(8000) * 10.0 ** rng.integers(-20, 20, 8000)
+    rel = 10.0 ** rng.uniform(-12, 0, 8000) * rng.choice([-1.0, 1.0], 8000)
+    b = a * (1.0 + rel)
+    d = np.empty(len(a), np.float32)
+    emu.fg_emu_diff32(a, b, d, len(a))
+    exact = a - b  # within 1 FP64 rounding
+    err = np.abs(d.astype(np.float64) - exact)
+    assert np.all(err <= np.abs(exact) * 2.0 ** -22 + (np.abs(a) + np.abs(b)) * 2.0 ** -45)
+
+
 @pytest.mark.parametrize("dbl", [0, 1], ids=["f32", "f64"])
 @pytest.mark.parametrize("n", [32, 64, 256, 512])
 def test_fixed_size_passes_match_engine(emu, dbl, n):
