@@ -249,12 +249,6 @@ int build_axis(int n, int pair, AxisTables *t) {
   return 0;
 }
 
-// ----------------------------------------------------- block reduction helper
-__device__ __forceinline__ void block_add(double v, double *acc) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(acc, v);
-}
-
 // ------------------------------------------------------ launches + profiling
 std::atomic<unsigned long long> g_launches{0};
 
@@ -579,19 +573,6 @@ int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const doub
 }
 
 // In-functors with side effects / norms for the mixed path ------------------
-struct InHaloCopyNorm {  // value = p interior; also fbuf = value
-  static constexpr const char *tag = "halocopy";
-  const double *p;
-  double *fbuf;
-  Geo g;
-  __device__ double operator()(int i0, int j0, int k0) const {
-    const long id = g.pidx(i0 + 1, j0 + 1, k0 + 1);
-    const double v = p[id];
-    fbuf[id] = v;
-    return v;
-  }
-};
-
 }  // namespace
 
 namespace {
@@ -1032,6 +1013,8 @@ namespace {
 std::mutex g_ctx_mu;
 Mirrors g_ctx_mir;
 DBuf g_ctx_small[4];
+int boundp_dev(double *p, const int n[3], const char cbc[6], const double bc[6], const double dl[3], double dzc0,
+               double dzcn, cudaStream_t st);
 }  // namespace
 
 extern "C" {
@@ -1145,24 +1128,7 @@ int flutas_gb300_boundp(const char cbc[6], const int n[3], const double bc[6], i
     dzc0 = dzc[0 - 1 + nh_d];
     dzcn = dzc[nz - 1 + nh_d];
   }
-  const double dr[3][2] = {{dl[0], dl[0]}, {dl[1], dl[1]}, {dzc0, dzcn}};
-  for (int d = 0; d < 3; d++) {
-    BoundArgs ba;
-    ba.p = sp.d;
-    ba.g = Geo{nx, ny, nz, 1};
-    ba.idir = d + 1;
-    ba.ctype0 = cbc[2 * d];
-    ba.ctype1 = cbc[2 * d + 1];
-    auto fs = [&](char ct, int ib, double rv, double drv, double *f, double *s) {
-      if (ct == 'D') { *f = 2.0 * rv; *s = -1.0; }
-      else if (ct == 'N') { *f = ib == 0 ? -drv * rv : drv * rv; *s = 1.0; }
-      else { *f = 0.0; *s = 0.0; }
-    };
-    fs(ba.ctype0, 0, bc[2 * d], dr[d][0], &ba.f0, &ba.s0);
-    fs(ba.ctype1, 1, bc[2 * d + 1], dr[d][1], &ba.f1, &ba.s1);
-    long cnt = d == 0 ? (long)(ny + 2) * (nz + 2) : (d == 1 ? (long)(nx + 2) * (nz + 2) : (long)(nx + 2) * (ny + 2));
-    TRY(launch("k_boundp_dir", st, [&] { k_boundp_dir<<<stream_grid(cnt), 256, 0, st>>>(ba); }));
-  }
+  TRY(boundp_dev(sp.d, n, cbc, bc, dl, dzc0, dzcn, st));
   TRY(stage_out(sp, st));
   CK(cudaStreamSynchronize(st));
   return FLUTAS_OK;
@@ -1211,11 +1177,113 @@ int flutas_gb300_chkdiv(int nx, int ny, int nz, double dxi, double dyi, double d
 
 namespace {
 
+// ---- ghost cells in one launch (k_ghosts): the maps of set_bc's passes
+int gm_slot(int t, int n, int h) { return t <= 0 ? -t : h + t - n; }
+void gm_set(GMap *m, int n, int h, int t, int kind, int src, double F = 0.0, double S = 0.0) {
+  m[gm_slot(t, n, h)] = GMap{F, S, src, kind};
+}
+void gm_clear(GMap *m) {
+  for (int s = 0; s < GM_SLOTS; s++) m[s] = GMap{0.0, 0.0, 0, GM_KEEP};
+}
+// True when no map of the line reads a position the line writes (the maps
+// then compose; grids too small for it keep the pass-by-pass kernels).
+bool gm_closed(const GMap *m, int n, int h) {
+  for (int s = 0; s < 2 * h + 1; s++) {
+    if (m[s].kind != GM_COPY && m[s].kind != GM_AFF) continue;
+    const int t = m[s].src;
+    if (t < 1 || t > n || (t == n && m[h].kind != GM_KEEP)) return false;
+  }
+  return true;
+}
+// Completes a (hi), checks that the maps compose and launches k_ghosts;
+// *done = false (nothing launched) when they do not compose.
+template <int NC> int ghosts_launch(GhostArgs<NC> &a, cudaStream_t st, bool *done) {
+  *done = false;
+  for (int d = 0; d < 3; d++) {
+    if (a.n[d] < 2 * a.h + 1) return 0;
+    a.hi[d] = a.n[d];
+    for (int c = 0; c < NC; c++) {
+      if (!gm_closed(a.m[c][d], a.n[d], a.h)) return 0;
+      if (a.m[c][d][a.h].kind != GM_KEEP) a.hi[d] = a.n[d] - 1;
+    }
+  }
+  long E[3], w[3];
+  for (int d = 0; d < 3; d++) {
+    E[d] = a.n[d] + 2 * a.h;
+    w[d] = E[d] - a.hi[d];
+  }
+  const long tot = w[0] * E[1] * E[2] + (long)a.hi[0] * w[1] * E[2] + (long)a.hi[0] * a.hi[1] * w[2];
+  TRY(launch(NC == 1 ? "k_ghosts<1>" : "k_ghosts<3>", st, [&] { k_ghosts<NC><<<stream_grid(tot), 256, 0, st>>>(a); }));
+  *done = true;
+  return 0;
+}
+// boundp's maps (src/bound.f90:146-225 with set_bc's centred forms, nh_p = 1):
+// periodic copies, and ghost = f + s * inner (D: f = 2 bc, s = -1; N: f = -+dr bc, s = 1).
+void boundp_maps(GhostArgs<1> &a, const int n[3], const char cbc[6], const double bc[6], const double dr[3][2]) {
+  auto fs = [&](char ct, int ib, double rv, double drv, double *f, double *sc) {
+    if (ct == 'D') { *f = 2.0 * rv; *sc = -1.0; }
+    else if (ct == 'N') { *f = ib == 0 ? -drv * rv : drv * rv; *sc = 1.0; }
+    else { *f = 0.0; *sc = 0.0; }
+  };
+  a.h = 1;
+  for (int d = 0; d < 3; d++) {
+    a.n[d] = n[d];
+    GMap *m = a.m[0][d];
+    gm_clear(m);
+    double f, sc;
+    if (cbc[2 * d] == 'P') gm_set(m, n[d], 1, 0, GM_COPY, n[d]);
+    else { fs(cbc[2 * d], 0, bc[2 * d], dr[d][0], &f, &sc); gm_set(m, n[d], 1, 0, GM_AFF, 1, f, sc); }
+    if (cbc[2 * d + 1] == 'P') gm_set(m, n[d], 1, n[d] + 1, GM_COPY, 1);
+    else { fs(cbc[2 * d + 1], 1, bc[2 * d + 1], dr[d][1], &f, &sc); gm_set(m, n[d], 1, n[d] + 1, GM_AFF, n[d], f, sc); }
+  }
+}
+
+// The maps of one direction and component of bounduvw's set_bc pass
+// (k_set_bc3: both ends, layers in order, the last write of a cell wins).
+void setbc_maps(GMap *m, const BcSide side[2], int n, int h) {
+  gm_clear(m);
+  for (int ib = 0; ib < 2; ib++) {
+    const BcSide &sd = side[ib];
+    for (int q = 0; q < h; q++) {
+      const double f = sd.factor[q];
+      if (sd.ctype == 'P') {
+        gm_set(m, n, h, 0 - q, GM_COPY, n - q);
+        gm_set(m, n, h, n + 1 + q, GM_COPY, 1 + q);
+      } else if (sd.centered) {
+        if (ib == 0) gm_set(m, n, h, 0 - q, GM_AFF, 1 + q, f, sd.sgn);
+        else gm_set(m, n, h, n + 1 + q, GM_AFF, n - q, f, sd.sgn);
+      } else if (sd.ctype == 'D') {
+        if (ib == 0) {
+          gm_set(m, n, h, 0 - q, GM_CONST, 0, f);
+        } else {
+          gm_set(m, n, h, n + q, GM_CONST, 0, f);
+          gm_set(m, n, h, n + 1 + q, GM_COPY, n - 1 - q);
+        }
+      } else {
+        if (ib == 0) {
+          gm_set(m, n, h, 0 - q, GM_AFF, 1 + q, 1.0 * f, 1.0);
+        } else {
+          gm_set(m, n, h, n + q, GM_AFF, n - 1 - q, 1.0 * f, 1.0);
+          gm_set(m, n, h, n + 1 + q, GM_AFF, n - 1 - q, 2.0 * f, 1.0);
+        }
+      }
+    }
+  }
+}
+
 // boundp on a device halo array with the plan-less BoundArgs kernel
 int boundp_dev(double *p, const int n[3], const char cbc[6], const double bc[6], const double dl[3], double dzc0,
                double dzcn, cudaStream_t st) {
   const int nx = n[0], ny = n[1], nz = n[2];
   const double dr[3][2] = {{dl[0], dl[0]}, {dl[1], dl[1]}, {dzc0, dzcn}};
+  {
+    GhostArgs<1> ga;
+    ga.f[0] = p;
+    boundp_maps(ga, n, cbc, bc, dr);
+    bool done;
+    TRY(ghosts_launch(ga, st, &done));
+    if (done) return 0;
+  }
   for (int d = 0; d < 3; d++) {
     BoundArgs ba;
     ba.p = p;
@@ -1334,36 +1402,19 @@ int flutas_gb300_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, dou
 
 namespace {
 
-int set_bc_dev(double *p, int nx, int ny, int nz, int h, char ctype, int ibound, int idir, int centered,
-               double rvalue, const double *dr, cudaStream_t st) {
-  if (h < 1 || h > 4) return fail(FLUTAS_EUNSUPPORTED, "set_bc: halo %d not in 1..4", h);
-  SetBcArgs a;
-  a.p = p; a.nx = nx; a.ny = ny; a.nz = nz; a.h = h;
-  a.idir = idir; a.ibound = ibound; a.centered = centered; a.ctype = ctype;
-  a.sgn = 0.0;
-  for (int q = 0; q < h; q++) a.factor[q] = rvalue;
-  if (ctype == 'D' && centered) { for (int q = 0; q < h; q++) a.factor[q] = 2.0 * a.factor[q]; a.sgn = -1.0; }
-  if (ctype == 'N') {
-    for (int q = 0; q < h; q++) a.factor[q] = ibound == 0 ? -dr[q] * a.factor[q] : dr[q] * a.factor[q];
-    a.sgn = 1.0;
-  }
-  const int na = idir == 1 ? ny : nx, nb = idir == 3 ? ny : nz;
-  const long cnt = (long)(na + 2 * h) * (nb + 2 * h);
-  TRY(launch("k_set_bc", st, [&] { k_set_bc<<<stream_grid(cnt), 256, 0, st>>>(a); }));
-  return 0;
-}
-
 // bounduvw (src/bound.f90:17-144), single domain, with the outflow faces of
 // src/bound.f90:649-773 when isoutflow is given.  dzc/dzf host
-// values.  One launch per direction (x, then y, then z, as the reference).
+// values.  One k_ghosts launch for the three set_bc passes (the pass-by-pass
+// kernel, x then y then z as the reference, where the maps do not compose).
 int bounduvw_dev(const char *cbc, const double *bc, int nx, int ny, int nz, int nh_d, int h, const double dl[3],
                  const double *dzc_h, const double *dzf_h, double *u, double *v, double *w, cudaStream_t st,
                  const int *isoutflow = nullptr, const double *dzf_d = nullptr) {
   if (h < 1 || h > 4) return fail(FLUTAS_EUNSUPPORTED, "bounduvw: halo %d not in 1..4", h);
   auto CB = [&](int ib, int d, int c) { return cbc[ib + 2 * d + 6 * c]; };
   auto BV = [&](int ib, int d, int c) { return bc[ib + 2 * d + 6 * c]; };
+  SetBc3Args passes[3];
   for (int d = 0; d < 3; d++) {
-    SetBc3Args a;
+    SetBc3Args &a = passes[d];
     a.f[0] = u; a.f[1] = v; a.f[2] = w;
     a.nx = nx; a.ny = ny; a.nz = nz; a.h = h; a.idir = d + 1;
     for (int c = 0; c < 3; c++)
@@ -1386,6 +1437,16 @@ int bounduvw_dev(const char *cbc, const double *bc, int nx, int ny, int nz, int 
           sd.sgn = 1.0;
         }
       }
+  }
+  GhostArgs<3> ga;
+  ga.f[0] = u; ga.f[1] = v; ga.f[2] = w;
+  ga.n[0] = nx; ga.n[1] = ny; ga.n[2] = nz; ga.h = h;
+  for (int d = 0; d < 3; d++)
+    for (int c = 0; c < 3; c++) setbc_maps(ga.m[c][d], passes[d].side[c], ga.n[d], h);
+  bool done;
+  TRY(ghosts_launch(ga, st, &done));
+  for (int d = 0; d < 3 && !done; d++) {  // grids too small for the maps to compose: pass by pass
+    const SetBc3Args &a = passes[d];
     const int na = d == 0 ? ny : nx, nb = d == 2 ? ny : nz;
     const long cnt = (long)(na + 2 * h) * (nb + 2 * h);
     TRY(launch("k_set_bc3", st, [&] { k_set_bc3<<<stream_grid(cnt), 256, 0, st>>>(a); }));

@@ -1167,52 +1167,6 @@ __global__ void k_sub(const double *x, const double *s, double *d, long n) {
 
 namespace fg {
 
-// set_bc (src/bound.f90:227-646) for any halo h, centred or not.  One thread per
-// point of the face (halo range of the two other axes); the ghost layers
-// q = 0..h-1 are written in order by that thread, as the reference loops.
-struct SetBcArgs {
-  double *p;
-  int nx, ny, nz, h;
-  int idir, ibound, centered;
-  char ctype;
-  double factor[4];
-  double sgn;
-};
-#ifndef FG_NO_PLAIN_KERNELS
-__global__ void k_set_bc(SetBcArgs s) {
-  const int n = s.idir == 1 ? s.nx : (s.idir == 2 ? s.ny : s.nz);
-  const int na = s.idir == 1 ? s.ny : s.nx, nb = s.idir == 3 ? s.ny : s.nz;
-  const long HX = s.nx + 2 * s.h, HY = s.ny + 2 * s.h;
-  const long wa = na + 2 * s.h, wb = nb + 2 * s.h;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < wa * wb; t += (long)gridDim.x * blockDim.x) {
-    const int a = (int)(t % wa) + 1 - s.h, b = (int)(t / wa) + 1 - s.h;
-    auto at = [&](int tt) -> long {
-      int i, j, k;
-      if (s.idir == 1) { i = tt; j = a; k = b; }
-      else if (s.idir == 2) { i = a; j = tt; k = b; }
-      else { i = a; j = b; k = tt; }
-      return (long)(i - 1 + s.h) + HX * ((long)(j - 1 + s.h) + HY * (long)(k - 1 + s.h));
-    };
-    double *p = s.p;
-    for (int q = 0; q < s.h; q++) {
-      const double f = s.factor[q];
-      if (s.ctype == 'P') {
-        p[at(0 - q)] = p[at(n - q)];
-        p[at(n + 1 + q)] = p[at(1 + q)];
-      } else if (s.centered) {
-        if (s.ibound == 0) p[at(0 - q)] = f + s.sgn * p[at(1 + q)];
-        else p[at(n + 1 + q)] = f + s.sgn * p[at(n - q)];
-      } else if (s.ctype == 'D') {
-        if (s.ibound == 0) p[at(0 - q)] = f;
-        else { p[at(n + q)] = f; p[at(n + 1 + q)] = p[at(n - 1 - q)]; }
-      } else {
-        if (s.ibound == 0) p[at(0 - q)] = 1.0 * f + p[at(1 + q)];
-        else { p[at(n + q)] = 1.0 * f + p[at(n - 1 - q)]; p[at(n + 1 + q)] = 2.0 * f + p[at(n - 1 - q)]; }
-      }
-    }
-  }
-}
-#endif
 
 }  // namespace fg
 
@@ -1456,6 +1410,100 @@ __global__ void k_set_bc3(SetBc3Args s) {
 }
 #endif
 
+}  // namespace fg
+
+namespace fg {
+
+// ---------------------------------------------------------------------------
+// Ghost cells in one launch.  set_bc runs three passes over the whole
+// extended faces, x then y then z (src/bound.f90:17-225); every pass reads
+// only cells that no pass writes (interior cells next to the boundary), so
+// the final value of a written cell is a composition of at most three maps,
+// one per direction, each acting on one cell of its line: unchanged, a copy,
+// F + S*v or a constant F.  GhostArgs holds the map of every written position
+// t of every direction and component (slot -t for t <= 0, h + t - n for
+// t >= n); k_ghosts evaluates the composition for each written cell, x map
+// first, with the arithmetic of the passes (F + S*v, S in {-1, 0, 1}, exact
+// product), so the values are bit-identical to the three passes.
+// ---------------------------------------------------------------------------
+enum : int { GM_KEEP = 0, GM_COPY = 1, GM_AFF = 2, GM_CONST = 3 };
+struct GMap {
+  double F, S;
+  int src, kind;
+};
+constexpr int GM_SLOTS = 9;  // 2h + 1, h <= 4
+template <int NC> struct GhostArgs {
+  double *f[NC];
+  int n[3], h;
+  int hi[3];  // positions 1..hi[d] are never written (hi = n or n - 1)
+  GMap m[NC][3][GM_SLOTS];
+};
+#ifndef FG_NO_PLAIN_KERNELS
+template <int NC> __global__ void k_ghosts(const __grid_constant__ GhostArgs<NC> a) {  // maps read in place
+  const int h = a.h;
+  const long E0 = a.n[0] + 2 * h, E1 = a.n[1] + 2 * h, E2 = a.n[2] + 2 * h;
+  const long w0 = E0 - a.hi[0], w1 = E1 - a.hi[1], w2 = E2 - a.hi[2];
+  const long c0 = a.hi[0], c1 = a.hi[1];
+  const long T0 = w0 * E1 * E2, T1 = c0 * w1 * E2, T2 = c0 * c1 * w2;
+  auto wpos = [&](int d, long s) -> int { return s < h ? (int)s + 1 - h : a.hi[d] + 1 + (int)(s - h); };
+  auto slot = [&](int d, int t) -> int { return t <= 0 ? -t : h + t - a.n[d]; };
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < T0 + T1 + T2; t += (long)gridDim.x * blockDim.x) {
+    int ip[3];
+    if (t < T0) {
+      ip[0] = wpos(0, t % w0);
+      const long r = t / w0;
+      ip[1] = (int)(r % E1) + 1 - h;
+      ip[2] = (int)(r / E1) + 1 - h;
+    } else if (t < T0 + T1) {
+      const long u = t - T0;
+      ip[0] = (int)(u % c0) + 1;
+      const long r = u / c0;
+      ip[1] = wpos(1, r % w1);
+      ip[2] = (int)(r / w1) + 1 - h;
+    } else {
+      const long u = t - T0 - T1;
+      ip[0] = (int)(u % c0) + 1;
+      const long r = u / c0;
+      ip[1] = (int)(r % c1) + 1;
+      ip[2] = wpos(2, r / c1);
+    }
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+      const GMap *mp[3];
+      bool any = false;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const int tt = ip[d];
+        mp[d] = (tt <= 0 || tt > a.hi[d]) ? &a.m[c][d][slot(d, tt)] : nullptr;
+        if (mp[d] && mp[d]->kind == GM_KEEP) mp[d] = nullptr;
+        any |= mp[d] != nullptr;
+      }
+      if (!any) continue;
+      // sources, z map first; a constant ends the chain
+      int sp[3] = {ip[0], ip[1], ip[2]};
+      int top = -1;  // the direction whose constant starts the chain (-1: a cell of f)
+      for (int d = 2; d >= 0; d--) {
+        if (!mp[d]) continue;
+        if (mp[d]->kind == GM_CONST) { top = d; break; }
+        sp[d] = mp[d]->src;
+      }
+      double v;
+      int from;
+      if (top >= 0) {
+        v = mp[top]->F;
+        from = top + 1;
+      } else {
+        const double *f = a.f[c];
+        v = f[(long)(sp[0] - 1 + h) + E0 * ((long)(sp[1] - 1 + h) + E1 * (long)(sp[2] - 1 + h))];
+        from = 0;
+      }
+      for (int d = from; d < 3; d++)
+        if (mp[d] && mp[d]->kind == GM_AFF) v = mp[d]->F + mp[d]->S * v;
+      a.f[c][(long)(ip[0] - 1 + h) + E0 * ((long)(ip[1] - 1 + h) + E1 * (long)(ip[2] - 1 + h))] = v;
+    }
+  }
+}
+#endif
 }  // namespace fg
 
 namespace fg {
