@@ -585,6 +585,16 @@ int stream_grid(long n, int threads = 256) {
   return (int)g;
 }
 
+int scale_jobs(const ScaleJobs &j, cudaStream_t st) {
+  if (j.count == 0) return 0;
+  return launch("k_scale_vecs", st, [&] { k_scale_vecs<<<j.count, 256, 0, st>>>(j); });
+}
+int scale_vecs(const double *in, double s, double *out, int n, cudaStream_t st) {
+  ScaleJobs j;
+  j.add(in, s, out, n);
+  return scale_jobs(j, st);
+}
+
 int finish(flutas_plan *pl) {
   if (pl->sync) CK(cudaStreamSynchronize(pl->stream));
   return 0;
@@ -633,7 +643,8 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
   const size_t halo_bytes = sizeof(double) * (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
   TRY(pl->S32.ensure(sizeof(float) * (size_t)g.nx * g.ny * g.nz));
   TRY(pl->fbuf.ensure(halo_bytes));
-  TRY(pl->nrm.ensure(sizeof(double) * 4));
+  if (max_iter < 1) max_iter = 1;
+  TRY(pl->nrm.ensure(sizeof(double) * (max_iter + 2)));  // [0]: |f|^2, [it]: |r|^2 after solve it
   float *S = pl->S32.as<float>();
   double *f = pl->fbuf.as<double>();
   double *nrm = pl->nrm.as<double>();
@@ -657,7 +668,7 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
     TRY(stencil(R, nullptr, S, acc));
     return fwd_xy<float>(pl, InF32{S, g}, S, pl->tx32, pl->ty32, pl->path32);
   };
-  CK(cudaMemsetAsync(nrm, 0, sizeof(double) * 2, st));
+  CK(cudaMemsetAsync(nrm, 0, sizeof(double) * (max_iter + 2), st));
   if (split) {
     TRY(stencil(first, f, S, nrm + 0));
     TRY(fwd_xy<float>(pl, InF32{S, g}, S, pl->tx32, pl->ty32, pl->path32));
@@ -675,32 +686,47 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
   R.g = g;
   int it = 1;
   double rel = 0.0, before = 1.0;  // relative residual before the latest FP32 solve
+  bool measured = true;            // before was read back (not predicted)
+  std::vector<double> h(max_iter + 2);
   for (;;) {
-    const bool norm_only = it >= max_iter || before * pl->contraction <= 0.5 * tol;
-    CK(cudaMemsetAsync(nrm + 1, 0, sizeof(double), st));
+    const double predicted = before * pl->contraction;
+    const bool norm_only = it >= max_iter || predicted <= 0.5 * tol;
+    double *acc = nrm + it;
     if (norm_only && fc && !fc->applied) {
       TRY(fc->boundp_phi());
       const long cells = (long)g.nx * g.ny * g.nz;
       const int grid = grid_for(k_resnorm_correc<int>, 256, 0, (cells + 511) / 512);
       if (grid < 0) return grid;
       if (cells >= (1L << 31) - 4096)
-        TRY(launch("k_resnorm_correc", st, [&] { k_resnorm_correc<long long><<<grid, 256, 0, st>>>(R, fc->ca, nrm + 1); }));
+        TRY(launch("k_resnorm_correc", st, [&] { k_resnorm_correc<long long><<<grid, 256, 0, st>>>(R, fc->ca, acc); }));
       else
-        TRY(launch("k_resnorm_correc", st, [&] { k_resnorm_correc<int><<<grid, 256, 0, st>>>(R, fc->ca, nrm + 1); }));
+        TRY(launch("k_resnorm_correc", st, [&] { k_resnorm_correc<int><<<grid, 256, 0, st>>>(R, fc->ca, acc); }));
       fc->applied = true;
     } else if (norm_only) {
-      TRY(stencil(R, nullptr, nullptr, nrm + 1));
+      TRY(stencil(R, nullptr, nullptr, acc));
     } else {
-      TRY(transform(R, nrm + 1));
+      TRY(transform(R, acc));
     }
-    double h[2];
-    CK(cudaMemcpyAsync(h, nrm, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (!std::isfinite(h[1]) || !std::isfinite(h[0]))
-      return fail(FLUTAS_ENONFINITE, "non-finite residual in mixed solve");
-    rel = h[0] > 0 ? std::sqrt(h[1] / h[0]) : std::sqrt(h[1]);
-    if (before > 0.0) pl->contraction = std::min(1.0, std::max(rel / before, 1e-12));
-    if (rel <= tol || it >= max_iter) break;
+    if (!norm_only && measured && predicted > 1e3 * tol) {
+      // the residual is predicted three orders of magnitude above tol: the next
+      // solve is queued behind this check without a wait, and its norm is read
+      // with the next check, which waits (were it converged after all, one more
+      // solve changes nothing)
+      before = predicted;
+      measured = false;
+    } else {
+      CK(cudaMemcpyAsync(h.data(), nrm, sizeof(double) * (it + 1), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      for (int j = 0; j <= it; j++)
+        if (!std::isfinite(h[j])) return fail(FLUTAS_ENONFINITE, "non-finite residual in mixed solve");
+      auto relof = [&](int j) { return h[0] > 0 ? std::sqrt(h[j] / h[0]) : std::sqrt(h[j]); };
+      rel = relof(it);
+      const double prev = it > 1 ? relof(it - 1) : 1.0;
+      if (prev > 0.0) pl->contraction = std::min(1.0, std::max(rel / prev, 1e-12));
+      if (rel <= tol || it >= max_iter) break;
+      before = rel;
+      measured = true;
+    }
     if (fc && fc->applied && !fc->continued) {  // the fused check did not end the solve: keep the applied x
       fc->continued = true;
       TRY(pl->phi2.ensure(halo_bytes));
@@ -712,7 +738,6 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
     TRY(zsolve<float>(pl, S, lam, a, b, c, true));
     TRY(inv_xy<float>(pl, S, OutHaloAdd{x, pl->normfft, g}, pl->tx32, pl->ty32, pl->path32));
     it++;
-    before = rel;
   }
   if (relres) *relres = rel;
   if (iters) *iters = it;
@@ -1038,7 +1063,7 @@ int flutas_gb300_fillps(int nx, int ny, int nz, int nh_d, int nh_u, double dxi, 
   TRY(stage_in(g_ctx_mir, p, pb, true, true, st, &sp));
   TRY(g_ctx_small[1].ensure(sizeof(double) * (nz + 2 * nh_d)));
   double *cz = g_ctx_small[1].as<double>();
-  TRY(launch("k_scale_vec", st, [&] { k_scale_vec<<<1, 256, 0, st>>>(sz.d, dti * rho0, cz, nz + 2 * nh_d); }));
+  TRY(scale_vecs(sz.d, dti * rho0, cz, nz + 2 * nh_d, st));
   InFillps in;
   in.u = su.d; in.v = sv.d; in.w = sw.d;
   in.cz = cz + (nh_d - 1);
@@ -1308,7 +1333,7 @@ int boundp_dev(double *p, const int n[3], const char cbc[6], const double bc[6],
 // the per-level z factors zA = f_t12*f2/rho0*dzci(k), zB = 2*f_t12*dzci(k)
 // computed on the device into zab (2*(nz+2nh_d) doubles); dzci_d is (1-nh_d:).
 int presw_consts(PresTwArgs *a, const double *dzci_d, int nh_d, int nz, double dxi, double dyi, double rho0i,
-                 double f_t12, double f2, double *zab, cudaStream_t st) {
+                 double f_t12, double f2, double *zab, ScaleJobs &jobs) {
   const int len = nz + 2 * nh_d;
   a->f2 = f2;
   a->xA = f_t12 * dxi * f2 * rho0i;
@@ -1317,8 +1342,8 @@ int presw_consts(PresTwArgs *a, const double *dzci_d, int nh_d, int nz, double d
   a->yB = 2.0 * f_t12 * dyi;
   a->xA32 = (float)a->xA; a->xB32 = (float)a->xB; a->yA32 = (float)a->yA; a->yB32 = (float)a->yB;
   a->f2_32 = (float)f2;
-  TRY(launch("k_scale_vec", st, [&] { k_scale_vec<<<1, 256, 0, st>>>(dzci_d, f_t12 * f2 * rho0i, zab, len); }));
-  TRY(launch("k_scale_vec", st, [&] { k_scale_vec<<<1, 256, 0, st>>>(dzci_d, 2.0 * f_t12, zab + len, len); }));
+  jobs.add(dzci_d, f_t12 * f2 * rho0i, zab, len);
+  jobs.add(dzci_d, 2.0 * f_t12, zab + len, len);
   a->zA = zab + (nh_d - 1);
   a->zB = zab + len + (nh_d - 1);
   return 0;
@@ -1387,7 +1412,9 @@ int flutas_gb300_pres_tw_src(int nx, int ny, int nz, double dxi, double dyi, dou
   PresTwArgs a;
   a.p = sp.d; a.pold = so.d; a.rho = sr.d;
   a.u = su.d; a.v = sv.d; a.w = sw.d;
-  TRY(presw_consts(&a, sz.d, nh_d, nz, dxi, dyi, rho0i, f_t12, f2, zab, st));
+  ScaleJobs jobs;
+  TRY(presw_consts(&a, sz.d, nh_d, nz, dxi, dyi, rho0i, f_t12, f2, zab, jobs));
+  TRY(scale_jobs(jobs, st));
   a.fp32 = 0;
   a.g = Geo{nx, ny, nz, nh_u};
   TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<presw_grid(a.g), PRESTW_NT, 0, st>>>(a); }));
@@ -1541,12 +1568,22 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   const double dlv[3] = {1.0 / dxi, 1.0 / dyi, 0.0};
   cudaStream_t st = pl->stream;
   const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+  // every folded z factor of the step in one launch: Dodd-Ferrante, fillps, correc
+  const double dti = 1.0 / dt, rho0i = 1.0 / rho0;
+  ScaleJobs jobs;
+  PresTwArgs a;
   if (rho) {
     TRY(pl->zdf.ensure(sizeof(double) * 2 * (nz + 2 * nh_d)));
-    PresTwArgs a;
+    TRY(presw_consts(&a, dzci_d, nh_d, nz, dxi, dyi, rho0i, dt, dt / f_t12_o, pl->zdf.as<double>(), jobs));
+  }
+  TRY(pl->czf.ensure(sizeof(double) * (nz + 2 * nh_d)));
+  TRY(pl->czc.ensure(sizeof(double) * (nz + 2 * nh_d)));
+  jobs.add(dzfi_d, dti * rho0, pl->czf.as<double>(), nz + 2 * nh_d);
+  jobs.add(dzci_d, dt * rho0i, pl->czc.as<double>(), nz + 2 * nh_d);
+  TRY(scale_jobs(jobs, st));
+  if (rho) {
     a.p = p; a.pold = pold; a.rho = rho;
     a.u = u; a.v = v; a.w = w;
-    TRY(presw_consts(&a, dzci_d, nh_d, nz, dxi, dyi, 1.0 / rho0, dt, dt / f_t12_o, pl->zdf.as<double>(), st));
     a.fp32 = precision == 1 ? 1 : 0;  // FP32 increment in the mixed path, FP64 in the FP64 path
     a.g = g;
     TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<presw_grid(a.g), PRESTW_NT, 0, st>>>(a); }));
@@ -1555,9 +1592,6 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
   TRY(pl->phi.ensure(pb));
   double *phi = pl->phi.as<double>();
-  TRY(pl->czf.ensure(sizeof(double) * (nz + 2 * nh_d)));
-  const double dti = 1.0 / dt;
-  TRY(launch("k_scale_vec", st, [&] { k_scale_vec<<<1, 256, 0, st>>>(dzfi_d, dti * rho0, pl->czf.as<double>(), nz + 2 * nh_d); }));
   InFillps in;
   in.u = u; in.v = v; in.w = w;
   in.cz = pl->czf.as<double>() + (nh_d - 1);
@@ -1591,11 +1625,6 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   const double dl[3] = {1.0 / dxi, 1.0 / dyi, 0.0};
   const double dzc0 = 1.0 / pl->dzci_h[0 - 1 + nh_d], dzcn = 1.0 / pl->dzci_h[nz - 1 + nh_d];
   CorrecAddArgs ca;
-  const double rho0i = 1.0 / rho0;
-  TRY(pl->czc.ensure(sizeof(double) * (nz + 2 * nh_d)));
-  TRY(launch("k_scale_vec", st, [&] {
-    k_scale_vec<<<1, 256, 0, st>>>(dzci_d, dt * rho0i, pl->czc.as<double>(), nz + 2 * nh_d);
-  }));
   ca.phi = phi; ca.cz = pl->czc.as<double>() + (nh_d - 1);
   ca.u = u; ca.v = v; ca.w = w; ca.p = p;
   ca.cx = (dt * dxi) * rho0i; ca.cy = (dt * dyi) * rho0i;

@@ -1507,10 +1507,23 @@ template <int NC> __global__ void k_ghosts(const __grid_constant__ GhostArgs<NC>
 }  // namespace fg
 
 namespace fg {
-// out[k] = s * in[k] for k in [0, n): folded z factors (e.g. dti*rho0*dzfi(k))
+// out[k] = s * in[k] for k in [0, n): folded z factors (e.g. dti*rho0*dzfi(k)),
+// up to four vectors in one launch (one block each).
+struct ScaleJobs {
+  const double *in[4];
+  double s[4];
+  double *out[4];
+  int n[4];
+  int count = 0;
+  void add(const double *i, double sc, double *o, int len) {
+    in[count] = i; s[count] = sc; out[count] = o; n[count] = len;
+    count++;
+  }
+};
 #ifndef FG_NO_PLAIN_KERNELS
-__global__ void k_scale_vec(const double *in, double s, double *out, int n) {
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) out[k] = s * in[k];
+__global__ void k_scale_vecs(ScaleJobs j) {
+  const int b = blockIdx.x;
+  for (int k = threadIdx.x; k < j.n[b]; k += blockDim.x) j.out[b][k] = j.s[b] * j.in[b][k];
 }
 #endif
 }  // namespace fg
