@@ -118,6 +118,19 @@ FG_HD void split32(double x, float &h, float &l) {
   h = zero ? float_of_bits(s) : float_of_bits(((((hi << 3) | (lo >> 29)) & 0x7fffffffu) ^ 0x40000000u) | s);
   l = zero ? float_of_bits(s) : float_of_bits(b | ((lo >> 6) & 0x7fffffu)) - float_of_bits(b);
 }
+// The forms for values already known to be nonzero and inside split32's range
+// (split_range: three integer instructions), without the zero case.
+FG_HD bool split_range(double x) { return (hi_word(x) & 0x7fffffffu) - 0x39800000u < 0x47f00000u - 0x39800000u; }
+FG_HD void split32_in(double x, float &h, float &l) {
+  const unsigned hi = hi_word(x), lo = lo_word(x), s = hi & 0x80000000u;
+  const unsigned b = ((((hi >> 20) & 0x7ffu) - 919u) << 23) | s;
+  h = float_of_bits(((((hi << 3) | (lo >> 29)) & 0x7fffffffu) ^ 0x40000000u) | s);
+  l = float_of_bits(b | ((lo >> 6) & 0x7fffffu)) - float_of_bits(b);
+}
+FG_HD float f32_in(double x) {  // f32_of's fast path (split_range lies inside it)
+  const unsigned hi = hi_word(x), lo = lo_word(x);
+  return float_of_bits(((((hi << 3) | (lo >> 29)) & 0x7fffffffu) ^ 0x40000000u) | (hi & 0x80000000u));
+}
 // a - b from the splits of a and b: (ha - hb) is exact when ha and hb are
 // within a factor 2 of each other (the cancelling case), so the result is the
 // FP32 rounding of a - b to within 2^-46 (|a| + |b|) and one more rounding.

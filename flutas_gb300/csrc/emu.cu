@@ -84,6 +84,15 @@ extern "C" __attribute__((visibility("default"))) void fg_emu_split32(const doub
   for (long i = 0; i < n; i++) {
     ok[i] = split_ok(x[i]) ? 1 : 0;
     split32(x[i], h[i], l[i]);
+    if (split_range(x[i])) {  // the in-range forms agree with the general ones
+      float h2, l2;
+      split32_in(x[i], h2, l2);
+      const float f = f32_in(x[i]);
+      ok[i] |= (bits_of_float(h2) == bits_of_float(h[i]) && bits_of_float(l2) == bits_of_float(l[i]) &&
+                bits_of_float(f) == bits_of_float(f32_of(x[i])))
+                   ? 2
+                   : 4;
+    }
   }
 }
 extern "C" __attribute__((visibility("default"))) void fg_emu_diff32(const double *a, const double *b, float *d,

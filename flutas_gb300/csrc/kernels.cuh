@@ -937,39 +937,43 @@ __device__ __forceinline__ double df_incr(double dp, double dq, double rs, doubl
 __device__ __forceinline__ double df_incr32(float dp, float dq, float rs, float A, float B, float f2) {
   const float t = dp - dq;
   const float dg = fmaf(f2, t, dp);
-  return f64_of(fmaf(A, t, -B * (__frcp_rn(rs) * dg)));
+  return f64_of(fmaf(A, t, -B * (__fdividef(1.0f, rs) * dg)));  // SFU reciprocal (rs: a sum of densities)
 }
 // p, pold and rho at one cell.
 struct DfPoint {
   double p, q, r;
 };
 // The six differences come from exact FP32 splits of p and pold (split32):
-// only the three updates use the FP64 pipe.  Cells with a value outside the
-// split's range (|v| < 2^-103 but not 0, or |v| >= 2^128) take FP64
-// differences instead.
-__device__ __forceinline__ void df_cell32(const PresTwArgs &a, int k, const DfPoint &c, const DfPoint &x,
+// only the three updates use the FP64 pipe.  A cell whose twelve values are not
+// all nonzero and inside the split's range (2^-103 <= |v| < 2^128) takes FP64
+// differences and the general conversions instead.  zA, zB: the level's z
+// factors in FP32.
+__device__ __forceinline__ void df_cell32(const PresTwArgs &a, float zA, float zB, const DfPoint &c, const DfPoint &x,
                                           const DfPoint &y, const DfPoint &z, double &u, double &v, double &w) {
-  const float r0 = f32_of(c.r);
-  const float rx = f32_of(x.r) + r0, ry = f32_of(y.r) + r0, rz = f32_of(z.r) + r0;
-  float dpx, dpy, dpz, dqx, dqy, dqz;
-  if (split_ok(c.p) & split_ok(c.q) & split_ok(x.p) & split_ok(y.p) & split_ok(z.p) & split_ok(x.q) &
-      split_ok(y.q) & split_ok(z.q)) {
+  float r0, rx, ry, rz, dpx, dpy, dpz, dqx, dqy, dqz;
+  if (split_range(c.p) & split_range(c.q) & split_range(c.r) & split_range(x.p) & split_range(x.q) &
+      split_range(x.r) & split_range(y.p) & split_range(y.q) & split_range(y.r) & split_range(z.p) &
+      split_range(z.q) & split_range(z.r)) {
+    r0 = f32_in(c.r);
+    rx = f32_in(x.r) + r0; ry = f32_in(y.r) + r0; rz = f32_in(z.r) + r0;
     float h0, l0, h, l;
-    split32(c.p, h0, l0);
-    split32(x.p, h, l); dpx = diff32(h, l, h0, l0);
-    split32(y.p, h, l); dpy = diff32(h, l, h0, l0);
-    split32(z.p, h, l); dpz = diff32(h, l, h0, l0);
-    split32(c.q, h0, l0);
-    split32(x.q, h, l); dqx = diff32(h, l, h0, l0);
-    split32(y.q, h, l); dqy = diff32(h, l, h0, l0);
-    split32(z.q, h, l); dqz = diff32(h, l, h0, l0);
+    split32_in(c.p, h0, l0);
+    split32_in(x.p, h, l); dpx = diff32(h, l, h0, l0);
+    split32_in(y.p, h, l); dpy = diff32(h, l, h0, l0);
+    split32_in(z.p, h, l); dpz = diff32(h, l, h0, l0);
+    split32_in(c.q, h0, l0);
+    split32_in(x.q, h, l); dqx = diff32(h, l, h0, l0);
+    split32_in(y.q, h, l); dqy = diff32(h, l, h0, l0);
+    split32_in(z.q, h, l); dqz = diff32(h, l, h0, l0);
   } else {
+    r0 = f32_of(c.r);
+    rx = f32_of(x.r) + r0; ry = f32_of(y.r) + r0; rz = f32_of(z.r) + r0;
     dpx = f32_of(x.p - c.p); dpy = f32_of(y.p - c.p); dpz = f32_of(z.p - c.p);
     dqx = f32_of(x.q - c.q); dqy = f32_of(y.q - c.q); dqz = f32_of(z.q - c.q);
   }
   u += df_incr32(dpx, dqx, rx, a.xA32, a.xB32, a.f2_32);
   v += df_incr32(dpy, dqy, ry, a.yA32, a.yB32, a.f2_32);
-  w += df_incr32(dpz, dqz, rz, f32_of(a.zA[k]), f32_of(a.zB[k]), a.f2_32);
+  w += df_incr32(dpz, dqz, rz, zA, zB, a.f2_32);
 }
 // FP64 increments, rounded as the reference expression is.
 __device__ __forceinline__ void df_cell64(const PresTwArgs &a, int k, const DfPoint &c, const DfPoint &x,
@@ -990,8 +994,15 @@ inline dim3 presw_grid(const Geo &g) {
 __global__ void __launch_bounds__(PRESTW_NT) k_pres_tw_src(PresTwArgs a) {
   const Geo &g = a.g;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (i > g.nx) return;
   const int kb = blockIdx.z * PRESTW_KZ + 1, ke = min(kb + PRESTW_KZ - 1, g.nz);
+  __shared__ float zab[2][PRESTW_KZ];  // the block's z factors in FP32 (mixed path)
+  static_assert(PRESTW_NT >= 2 * PRESTW_KZ, "one thread per z factor");
+  if (a.fp32 && threadIdx.x < 2 * PRESTW_KZ) {
+    const int q = threadIdx.x % PRESTW_KZ, half = threadIdx.x / PRESTW_KZ;
+    if (kb + q <= g.nz) zab[half][q] = f32_of((half ? a.zB : a.zA)[kb + q]);
+  }
+  __syncthreads();
+  if (i > g.nx) return;
   const long sy = g.nx + 2, sz = sy * (g.ny + 2), usz = (long)(g.nx + 2 * g.h) * (g.ny + 2 * g.h);
   const double *__restrict__ P = a.p, *__restrict__ Q = a.pold, *__restrict__ R = a.rho;
   double *__restrict__ U = a.u, *__restrict__ V = a.v, *__restrict__ W = a.w;
@@ -1007,7 +1018,7 @@ __global__ void __launch_bounds__(PRESTW_NT) k_pres_tw_src(PresTwArgs a) {
         xn = at(c + sz + 1); yn = at(c + sz + sy); zn = at(c + 2 * sz);
         un = U[ui + usz]; vn = V[ui + usz]; wn = W[ui + usz];
       }
-      if (a.fp32) df_cell32(a, k, cen, x, y, z, u, v, w);
+      if (a.fp32) df_cell32(a, zab[0][k - kb], zab[1][k - kb], cen, x, y, z, u, v, w);
       else df_cell64(a, k, cen, x, y, z, u, v, w);
       U[ui] = u; V[ui] = v; W[ui] = w;
       cen = z; x = xn; y = yn; z = zn;

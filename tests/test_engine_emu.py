@@ -119,7 +119,10 @@ def test_split32_and_diff32(emu):
     emu.fg_emu_split32(x, h, l, ok, n)
     ax = np.abs(x)
     want_ok = ((ax >= lo_edge) & (ax < hi_edge)) | (x == 0)
-    assert np.array_equal(ok.astype(bool), want_ok)
+    assert np.array_equal((ok & 1).astype(bool), want_ok)
+    # split_range: the same range without zero; there split32_in / f32_in == split32 / f32_of
+    in_range = (ax >= lo_edge) & (ax < hi_edge)
+    assert np.array_equal((ok & 6) == 2, in_range) and not np.any(ok & 4)
     t = np.empty(n, np.float32)
     emu.fg_emu_f32_of(x, t, n)
     m = ok.astype(bool) & (x != 0)
