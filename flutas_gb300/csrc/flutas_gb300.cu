@@ -545,7 +545,7 @@ int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const doub
   za.pin = (pin && zsing) ? 1 : 0;
   if (!za.periodic) {
     constexpr int CH = 16;
-    const int nt = 128;
+    static const int nt = getenv("FG_Z_NT") ? atoi(getenv("FG_Z_NT")) : 64;
     const size_t sm = zstream_smem<T, CH>(za.nn, nt);
     if ((int)sm > max_smem_optin()) return fail(FLUTAS_EUNSUPPORTED, "nz=%d too large for the z kernel", za.nz);
     TRY(allow_smem(k_zstream<T, CH>));
@@ -1556,7 +1556,7 @@ namespace {
 // (src/source.f90:247-309) are added to u*,v*,w* first.
 int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const double *dzci_d, const double *dzfi_d,
                    double dt, double rho0, double *u, double *v, double *w, double *p, int precision, double tol,
-                   int max_iter, const double *rho, const double *pold, double f_t12_o, const char *cbcvel,
+                   int max_iter, const double *rho, double *pold, double f_t12_o, const char *cbcvel,
                    const double *bcvel) {
   const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2], nh_d = pl->nh_d;
   Geo g{nx, ny, nz, nh_u};
@@ -1627,6 +1627,7 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   CorrecAddArgs ca;
   ca.phi = phi; ca.cz = pl->czc.as<double>() + (nh_d - 1);
   ca.u = u; ca.v = v; ca.w = w; ca.p = p;
+  ca.pold = pold;  // two-phase step: pold = p^n (main__two_phase_inc_isot.f90:655-674) in the same pass
   ca.cx = (dt * dxi) * rho0i; ca.cy = (dt * dyi) * rho0i;
   ca.g = g;
   FinalCorrec fc;
@@ -1646,16 +1647,18 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     TRY(boundp_dev(d, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
     CorrecAddArgs cd = ca;
     cd.phi = d;
+    cd.pold = nullptr;  // written by the first application
     TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<grid_cells(cd.g), 256, 0, st>>>(cd); }));
   }
   if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
+  if (pold) TRY(boundp_dev(pold, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
   TRY(boundp_dev(p, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
   return rc;
 }
 
 int projection_entry(void *plan, int nh_u, double dxi, double dyi, const double *dzci, const double *dzfi,
                      const double bcpre[6], double dt, double rho0, double *u, double *v, double *w, double *p,
-                     int precision, double tol, int max_iter, const double *rho, const double *pold,
+                     int precision, double tol, int max_iter, const double *rho, double *pold,
                      double f_t12_o, const char *cbcvel, const double *bcvel) {
   flutas_plan *pl;
   TRY(check_plan(plan, &pl));
@@ -1683,7 +1686,7 @@ int projection_entry(void *plan, int nh_u, double dxi, double dyi, const double 
   TRY(stage_in(pl->mir, dzfi, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sfi));
   if (rho) {
     TRY(stage_in(pl->mir, rho, pb, true, false, st, &sr));
-    TRY(stage_in(pl->mir, pold, pb, true, false, st, &so));
+    TRY(stage_in(pl->mir, pold, pb, true, true, st, &so));  // in: p^(n-1); out: p^n
   }
   int rc = projection_dev(pl, nh_u, dxi, dyi, sci.d, sfi.d, dt, rho0, su.d, sv.d, sw.d, sp.d, precision, tol,
                           max_iter, rho ? sr.d : nullptr, rho ? so.d : nullptr, f_t12_o, cbcvel, bcvel);
@@ -1692,7 +1695,8 @@ int projection_entry(void *plan, int nh_u, double dxi, double dyi, const double 
   TRY(stage_out(sv, st));
   TRY(stage_out(sw, st));
   TRY(stage_out(sp, st));
-  if (su.host || sp.host) CK(cudaStreamSynchronize(st));
+  if (rho) TRY(stage_out(so, st));
+  if (su.host || sp.host || (rho && so.host)) CK(cudaStreamSynchronize(st));
   TRY(finish(pl));
   return rc;
 }
@@ -1713,7 +1717,7 @@ int flutas_gb300_projection(void *plan, int nh_u, double dxi, double dyi, const 
 int flutas_gb300_projection_df(void *plan, int nh_u, double dxi, double dyi, const double *dzci,
                                const double *dzfi, const double bcpre[6], const char *cbcvel,
                                const double *bcvel, double f_t12, double f_t12_o,
-                               double rho0, const double *rho, const double *pold, double *u, double *v,
+                               double rho0, const double *rho, double *pold, double *u, double *v,
                                double *w, double *p, int precision, double tol, int max_iter) {
   // pres_tw_src (src/source.f90:247-309) then the projection of
   // src/apps/two_phase_inc_isot/main__two_phase_inc_isot.f90:624,655-716

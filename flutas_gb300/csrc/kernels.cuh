@@ -1094,6 +1094,7 @@ struct CorrecAddArgs {
   const double *phi;
   const double *cz;  // cz[k] = dt*rho0i*dzci(k) (index k)
   double *u, *v, *w, *p;
+  double *pold;      // non-null: pold = p before the update (the app's `pold = p`, interior cells)
   double cx, cy;     // dt*dxi*rho0i, dt*dyi*rho0i
   Geo g;
 };
@@ -1108,7 +1109,9 @@ __global__ void k_correc_padd(CorrecAddArgs a) {
     a.u[ui] = fma(-a.cx, a.phi[pc + 1] - ph, a.u[ui]);
     a.v[ui] = fma(-a.cy, a.phi[pc + (g.nx + 2)] - ph, a.v[ui]);
     a.w[ui] = fma(-a.cz[k], a.phi[pc + (long)(g.nx + 2) * (g.ny + 2)] - ph, a.w[ui]);
-    a.p[pc] = a.p[pc] + ph;
+    const double p0 = a.p[pc];
+    if (a.pold) a.pold[pc] = p0;
+    a.p[pc] = p0 + ph;
   });
 }
 #endif
@@ -1158,7 +1161,9 @@ __global__ void __launch_bounds__(256) k_resnorm_correc(InResidual R, CorrecAddA
         a.u[ui] = fma(-a.cx, a.phi[pc + 1] - ph, a.u[ui]);
         a.v[ui] = fma(-a.cy, a.phi[pc + (g.nx + 2)] - ph, a.v[ui]);
         a.w[ui] = fma(-a.cz[k], a.phi[pc + plane] - ph, a.w[ui]);
-        a.p[pc] = a.p[pc] + ph;
+        const double p0 = a.p[pc];
+        if (a.pold) a.pold[pc] = p0;
+        a.p[pc] = p0 + ph;
       }
     }
   }

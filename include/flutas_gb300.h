@@ -153,12 +153,15 @@ FLUTAS_API int flutas_gb300_projection(void *plan, int nh_u, double dxi, double 
  * Dodd-Ferrante constant-coefficient split: explicit (1/rho - 1/rho0) terms
  * built from p and pold) applied to u*,v*,w*, bounduvw (when cbcvel is
  * given), then the projection above with dt = f_t12.  rho, pold: (0:n+1) halo-1 arrays; p holds p^n on entry and
- * p^n + phi on exit (src/apps/two_phase_inc_isot/main__two_phase_inc_isot.f90:624-716). */
+ * p^n + phi on exit; pold holds p^(n-1) on entry (read by pres_tw_src) and p^n on exit, interior copy
+ * then boundp, as the app does between pres_tw_src and fillps
+ * (src/apps/two_phase_inc_isot/main__two_phase_inc_isot.f90:624-716, pold = p at 655-674): repeated
+ * calls are the app's time steps. */
 FLUTAS_API int flutas_gb300_projection_df(void *plan, int nh_u, double dxi, double dyi,
                                           const double *dzci, const double *dzfi,
                                           const double bcpre[6], const char *cbcvel,
                                           const double *bcvel, double f_t12, double f_t12_o,
-                                          double rho0, const double *rho, const double *pold,
+                                          double rho0, const double *rho, double *pold,
                                           double *u, double *v, double *w, double *p, int precision,
                                           double tol, int max_iter);
 
