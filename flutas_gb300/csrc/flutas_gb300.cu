@@ -545,7 +545,7 @@ int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const doub
   za.pin = (pin && zsing) ? 1 : 0;
   if (!za.periodic) {
     constexpr int CH = 16;
-    static const int nt = getenv("FG_Z_NT") ? atoi(getenv("FG_Z_NT")) : 64;
+    const int nt = 128;
     const size_t sm = zstream_smem<T, CH>(za.nn, nt);
     if ((int)sm > max_smem_optin()) return fail(FLUTAS_EUNSUPPORTED, "nz=%d too large for the z kernel", za.nz);
     TRY(allow_smem(k_zstream<T, CH>));
