@@ -20,13 +20,25 @@
 namespace fg {
 namespace {
 
+// Built variants: (N, C, threads) = (256, 8, 256) with three CTAs per SM and
+// (512, 16, 512) with one (non-portable cluster size).  NBUF: plane buffers
+// per CTA.  With two Stockham stages (N = 256) two buffers suffice: every pass
+// writes the buffer its first stage has finished reading (see the kernels),
+// which brings a CTA to 72 KB of shared memory and three CTAs to an SM (at
+// most 80 registers a thread, no spills); N = 512 (three stages) keeps three.
+template <int N> struct FixCfg;
+template <> struct FixCfg<256> { static constexpr int C = 8, NTH = 256, NBUF = 2, MINB = 3; };
+template <> struct FixCfg<512> { static constexpr int C = 16, NTH = 512, NBUF = 3, MINB = 1; };
+
 template <typename T, int N, int C> struct FixGeo {
   static constexpr int ROWS = N / C, COLS = N / C, P = N + 1, BX = ROWS / 2, BY = COLS / 2;
   static constexpr size_t A = (size_t)ROWS * P, BN = (size_t)N * COLS;
   static constexpr size_t BUF = ((sizeof(T) * (A > BN ? A : BN)) + 255) & ~(size_t)255;
   static constexpr size_t TAB = sizeof(C2<T>) * N;
-  static constexpr size_t SMEM = 3 * BUF + 3 * TAB;
+  static constexpr int NBUF = FixCfg<N>::NBUF;
+  static constexpr size_t SMEM = NBUF * BUF + 3 * TAB;
   static_assert(N % C == 0 && ROWS % 2 == 0, "plane must split into an even number of rows per CTA");
+  static_assert(NBUF == 3 || fix::Plan<N>::NST == 2, "two buffers need exactly two stages per transform");
 };
 
 struct Barrier {
@@ -91,13 +103,14 @@ __device__ __forceinline__ void load_tables(const AxisPlan &ax, const AxisPlan &
 }
 
 template <typename T, int N, int C, int FIX_NTH, int PX, int PY, typename In>
-__global__ void __launch_bounds__(FIX_NTH, 512 / FIX_NTH) k_xyfwd_fix(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
+__global__ void __launch_bounds__(FIX_NTH, FixCfg<N>::MINB) k_xyfwd_fix(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
   using G = FixGeo<T, N, C>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
   const int r = (int)cluster.block_rank(), tid = threadIdx.x;
-  T *B0 = (T *)smem_raw, *B1 = (T *)(smem_raw + G::BUF), *B2 = (T *)(smem_raw + 2 * G::BUF);
-  C2<T> *Wt = (C2<T> *)(smem_raw + 3 * G::BUF), *Qx = Wt + N, *Qy = Qx + N;
+  constexpr bool TWO = G::NBUF == 2;
+  T *B0 = (T *)smem_raw, *B1 = (T *)(smem_raw + G::BUF), *B2 = (T *)(smem_raw + (G::NBUF - 1) * G::BUF);
+  C2<T> *Wt = (C2<T> *)(smem_raw + G::NBUF * G::BUF), *Qx = Wt + N, *Qy = Qx + N;
   load_tables<T, N, PX, PY, FIX_NTH>(ax, ay, Wt, Qx, Qy);
   const Barrier bar;
   const int y0 = r * G::ROWS;
@@ -128,31 +141,46 @@ __global__ void __launch_bounds__(FIX_NTH, 512 / FIX_NTH) k_xyfwd_fix(AxisPlan a
           },
           ss);
     __syncthreads();
-    // x: rows in B0 -> stages in B1/B2 -> split into the x-spectrum rows, B0
-    fix::forward<T, N, PX, G::BX, FIX_NTH>(B0, G::P, 1, (C2<T> *)B1, (C2<T> *)B2, Wt, Qx,
-                                            StorePlaneReal<T>{B0, G::P, 0}, tid, bar);
-    cluster.sync();  // every CTA's x-spectrum rows are complete
-    gather_cols<T, N, C, FIX_NTH>(cluster, B0, B1, r);
-    cluster.sync();  // every CTA has read the rows
-    // y: columns in B1 -> stages in B2/B0 -> split into S
-    fix::forward<T, N, PY, G::BY, FIX_NTH>(B1, 1, G::COLS, (C2<T> *)B2, (C2<T> *)B0, Wt, Qy,
-                                            StoreColsS<T>{S, (long)k * N * N, N, r * G::COLS, G::COLS}, tid, bar);
+    if constexpr (TWO) {
+      // x: rows in B0 -> stage B1 -> stage B0 (read after the first stage) -> split
+      // into the x-spectrum rows, B1; gathered into the column block, B0
+      fix::forward<T, N, PX, G::BX, FIX_NTH>(B0, G::P, 1, (C2<T> *)B1, (C2<T> *)B0, Wt, Qx,
+                                              StorePlaneReal<T>{B1, G::P, 0}, tid, bar);
+      cluster.sync();  // every CTA's x-spectrum rows are complete
+      gather_cols<T, N, C, FIX_NTH>(cluster, B1, B0, r);
+      cluster.sync();  // every CTA has read the rows
+      // y: columns in B0 -> stage B1 -> stage B0 -> split into S
+      fix::forward<T, N, PY, G::BY, FIX_NTH>(B0, 1, G::COLS, (C2<T> *)B1, (C2<T> *)B0, Wt, Qy,
+                                              StoreColsS<T>{S, (long)k * N * N, N, r * G::COLS, G::COLS}, tid, bar);
+    } else {
+      // x: rows in B0 -> stages in B1/B2 -> split into the x-spectrum rows, B0
+      fix::forward<T, N, PX, G::BX, FIX_NTH>(B0, G::P, 1, (C2<T> *)B1, (C2<T> *)B2, Wt, Qx,
+                                              StorePlaneReal<T>{B0, G::P, 0}, tid, bar);
+      cluster.sync();  // every CTA's x-spectrum rows are complete
+      gather_cols<T, N, C, FIX_NTH>(cluster, B0, B1, r);
+      cluster.sync();  // every CTA has read the rows
+      // y: columns in B1 -> stages in B2/B0 -> split into S
+      fix::forward<T, N, PY, G::BY, FIX_NTH>(B1, 1, G::COLS, (C2<T> *)B2, (C2<T> *)B0, Wt, Qy,
+                                              StoreColsS<T>{S, (long)k * N * N, N, r * G::COLS, G::COLS}, tid, bar);
+    }
     __syncthreads();
   }
   if (nrm) block_sum_add((double)ss, nrm);
 }
 
 template <typename T, int N, int C, int FIX_NTH, int PX, int PY, typename Out>
-__global__ void __launch_bounds__(FIX_NTH, 512 / FIX_NTH) k_xyinv_fix(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
+__global__ void __launch_bounds__(FIX_NTH, FixCfg<N>::MINB) k_xyinv_fix(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
   using G = FixGeo<T, N, C>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
   const int r = (int)cluster.block_rank(), tid = threadIdx.x;
-  T *B0 = (T *)smem_raw, *B1 = (T *)(smem_raw + G::BUF), *B2 = (T *)(smem_raw + 2 * G::BUF);
-  C2<T> *Wt = (C2<T> *)(smem_raw + 3 * G::BUF), *Qx = Wt + N, *Qy = Qx + N;
+  constexpr bool TWO = G::NBUF == 2;
+  T *B0 = (T *)smem_raw, *B1 = (T *)(smem_raw + G::BUF), *B2 = (T *)(smem_raw + (G::NBUF - 1) * G::BUF);
+  C2<T> *Wt = (C2<T> *)(smem_raw + G::NBUF * G::BUF), *Qx = Wt + N, *Qy = Qx + N;
   load_tables<T, N, PX, PY, FIX_NTH>(ax, ay, Wt, Qx, Qy);
   const Barrier bar;
   const int y0 = r * G::ROWS;
+  T *const rows = TWO ? B1 : B2;  // the x^-1 output rows that store_cells reads
   for (int k = blockIdx.x / C; k < g.nz; k += gridDim.x / C) {
     if constexpr (std::is_same_v<Out, OutHaloAdd>) {  // the rows this CTA adds to, on their way to L2
       const double *span = out.p + out.g.pidx(0, y0 + 1, k + 1);
@@ -175,14 +203,25 @@ __global__ void __launch_bounds__(FIX_NTH, 512 / FIX_NTH) k_xyinv_fix(AxisPlan a
       }
     }
     __syncthreads();
-    // y^-1: columns in B0 -> stages in B1/B0 -> columns in B2
-    fix::inverse<T, N, PY, G::BY, FIX_NTH>(B0, 1, G::COLS, B2, 1, G::COLS, (C2<T> *)B1, (C2<T> *)B0, Wt, Qy, tid,
-                                            bar);
-    cluster.sync();  // every CTA's column block is complete
-    gather_rows<T, N, C, FIX_NTH>(cluster, B2, B0, r);
-    cluster.sync();  // every CTA has read the blocks
-    // x^-1: rows in B0 -> stages in B1/B0 -> rows in B2 (pitch P)
-    fix::inverse<T, N, PX, G::BX, FIX_NTH>(B0, G::P, 1, B2, G::P, 1, (C2<T> *)B1, (C2<T> *)B0, Wt, Qx, tid, bar);
+    if constexpr (TWO) {
+      // y^-1: columns in B0 -> stage B1 -> columns back in B0 (read by the first stage)
+      fix::inverse<T, N, PY, G::BY, FIX_NTH>(B0, 1, G::COLS, B0, 1, G::COLS, (C2<T> *)B1, (C2<T> *)B0, Wt, Qy,
+                                              tid, bar);
+      cluster.sync();  // every CTA's column block is complete
+      gather_rows<T, N, C, FIX_NTH>(cluster, B0, B1, r);
+      cluster.sync();  // every CTA has read the blocks
+      // x^-1: rows in B1 (pitch P) -> stage B0 -> rows back in B1
+      fix::inverse<T, N, PX, G::BX, FIX_NTH>(B1, G::P, 1, B1, G::P, 1, (C2<T> *)B0, (C2<T> *)B1, Wt, Qx, tid, bar);
+    } else {
+      // y^-1: columns in B0 -> stages in B1/B0 -> columns in B2
+      fix::inverse<T, N, PY, G::BY, FIX_NTH>(B0, 1, G::COLS, B2, 1, G::COLS, (C2<T> *)B1, (C2<T> *)B0, Wt, Qy,
+                                              tid, bar);
+      cluster.sync();  // every CTA's column block is complete
+      gather_rows<T, N, C, FIX_NTH>(cluster, B2, B0, r);
+      cluster.sync();  // every CTA has read the blocks
+      // x^-1: rows in B0 -> stages in B1/B0 -> rows in B2 (pitch P)
+      fix::inverse<T, N, PX, G::BX, FIX_NTH>(B0, G::P, 1, B2, G::P, 1, (C2<T> *)B1, (C2<T> *)B0, Wt, Qx, tid, bar);
+    }
     __syncthreads();
     store_cells<T>(
         out, G::ROWS * N,
@@ -195,7 +234,7 @@ __global__ void __launch_bounds__(FIX_NTH, 512 / FIX_NTH) k_xyinv_fix(AxisPlan a
         },
         [&](int idx) {
           const unsigned u = idx;
-          return B2[u + u / N];
+          return rows[u + u / N];
         });
     __syncthreads();
   }
@@ -236,11 +275,6 @@ cudaError_t cluster_start(K kernel, size_t smem, int clusters, int C, int nth, c
 
 bool kind_ok(int p) { return p == BC_PP || p == BC_NN; }
 
-// Built variants: (N, C, threads) = (256, 8, 256) with two CTAs per SM and
-// (512, 16, 512) with one (non-portable cluster size).
-template <int N> struct FixCfg;
-template <> struct FixCfg<256> { static constexpr int C = 8, NTH = 256; };
-template <> struct FixCfg<512> { static constexpr int C = 16, NTH = 512; };
 
 template <int N, typename F> cudaError_t with_kinds(int px, int py, F &&f) {
   if (px == BC_PP && py == BC_PP) return f(std::integral_constant<int, BC_PP>(), std::integral_constant<int, BC_PP>());
