@@ -1039,7 +1039,7 @@ std::mutex g_ctx_mu;
 Mirrors g_ctx_mir;
 DBuf g_ctx_small[4];
 int boundp_dev(double *p, const int n[3], const char cbc[6], const double bc[6], const double dl[3], double dzc0,
-               double dzcn, cudaStream_t st);
+               double dzcn, cudaStream_t st, double *p2 = nullptr);
 }  // namespace
 
 extern "C" {
@@ -1238,13 +1238,15 @@ template <int NC> int ghosts_launch(GhostArgs<NC> &a, cudaStream_t st, bool *don
     w[d] = E[d] - a.hi[d];
   }
   const long tot = w[0] * E[1] * E[2] + (long)a.hi[0] * w[1] * E[2] + (long)a.hi[0] * a.hi[1] * w[2];
-  TRY(launch(NC == 1 ? "k_ghosts<1>" : "k_ghosts<3>", st, [&] { k_ghosts<NC><<<stream_grid(tot), 256, 0, st>>>(a); }));
+  static const char *const names[] = {"", "k_ghosts<1>", "k_ghosts<2>", "k_ghosts<3>"};
+  TRY(launch(names[NC], st, [&] { k_ghosts<NC><<<stream_grid(tot), 256, 0, st>>>(a); }));
   *done = true;
   return 0;
 }
 // boundp's maps (src/bound.f90:146-225 with set_bc's centred forms, nh_p = 1):
 // periodic copies, and ghost = f + s * inner (D: f = 2 bc, s = -1; N: f = -+dr bc, s = 1).
-void boundp_maps(GhostArgs<1> &a, const int n[3], const char cbc[6], const double bc[6], const double dr[3][2]) {
+template <int NC>
+void boundp_maps(GhostArgs<NC> &a, const int n[3], const char cbc[6], const double bc[6], const double dr[3][2]) {
   auto fs = [&](char ct, int ib, double rv, double drv, double *f, double *sc) {
     if (ct == 'D') { *f = 2.0 * rv; *sc = -1.0; }
     else if (ct == 'N') { *f = ib == 0 ? -drv * rv : drv * rv; *sc = 1.0; }
@@ -1260,6 +1262,8 @@ void boundp_maps(GhostArgs<1> &a, const int n[3], const char cbc[6], const doubl
     else { fs(cbc[2 * d], 0, bc[2 * d], dr[d][0], &f, &sc); gm_set(m, n[d], 1, 0, GM_AFF, 1, f, sc); }
     if (cbc[2 * d + 1] == 'P') gm_set(m, n[d], 1, n[d] + 1, GM_COPY, 1);
     else { fs(cbc[2 * d + 1], 1, bc[2 * d + 1], dr[d][1], &f, &sc); gm_set(m, n[d], 1, n[d] + 1, GM_AFF, n[d], f, sc); }
+    for (int c = 1; c < NC; c++)  // further fields of the same BCs
+      for (int sl = 0; sl < GM_SLOTS; sl++) a.m[c][d][sl] = m[sl];
   }
 }
 
@@ -1298,14 +1302,22 @@ void setbc_maps(GMap *m, const BcSide side[2], int n, int h) {
 
 // boundp on a device halo array with the plan-less BoundArgs kernel
 int boundp_dev(double *p, const int n[3], const char cbc[6], const double bc[6], const double dl[3], double dzc0,
-               double dzcn, cudaStream_t st) {
+               double dzcn, cudaStream_t st, double *p2) {
   const int nx = n[0], ny = n[1], nz = n[2];
   const double dr[3][2] = {{dl[0], dl[0]}, {dl[1], dl[1]}, {dzc0, dzcn}};
-  {
+  bool done;
+  if (p2) {  // two fields of the same BCs in one launch
+    GhostArgs<2> ga;
+    ga.f[0] = p;
+    ga.f[1] = p2;
+    boundp_maps(ga, n, cbc, bc, dr);
+    TRY(ghosts_launch(ga, st, &done));
+    if (done) return 0;
+    TRY(boundp_dev(p2, n, cbc, bc, dl, dzc0, dzcn, st, nullptr));
+  } else {
     GhostArgs<1> ga;
     ga.f[0] = p;
     boundp_maps(ga, n, cbc, bc, dr);
-    bool done;
     TRY(ghosts_launch(ga, st, &done));
     if (done) return 0;
   }
@@ -1651,8 +1663,7 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<grid_cells(cd.g), 256, 0, st>>>(cd); }));
   }
   if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
-  if (pold) TRY(boundp_dev(pold, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
-  TRY(boundp_dev(p, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
+  TRY(boundp_dev(p, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st, pold));  // and pold (the app's boundp(pold))
   return rc;
 }
 
