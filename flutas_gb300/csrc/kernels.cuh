@@ -47,6 +47,29 @@ inline dim3 grid_cells(const Geo &g, int threads = 256) {
   return dim3(gx, g.ny < 65535 ? g.ny : 65535, g.nz < 65535 ? g.nz : 65535);
 }
 
+// Asynchronous global -> shared copies (no register staging: every copy a
+// thread has issued is in flight at once) and an L2 prefetch of a contiguous
+// span.  Copies of 4 and 8 bytes go through L1 (.ca), 16-byte ones bypass it.
+template <int B> __device__ __forceinline__ void cp_async(void *dst, const void *src) {
+  static_assert(B == 4 || B == 8 || B == 16, "cp.async copies 4, 8 or 16 bytes");
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const size_t g = __cvta_generic_to_global(src);
+  if constexpr (B == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(g) : "memory");
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(g), "n"(B) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) { cp_async<4>(dst, src); }
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) { cp_async<16>(dst, src); }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// bytes: a multiple of 16 from a 16-byte aligned address (the caller checks)
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(__cvta_generic_to_global(p)), "r"(bytes)
+               : "memory");
+}
+
 // Reciprocal in FP64: FP32 seed refined by two Newton-Raphson steps
 // y <- y (2 - x y); each step squares the relative error (2^-22 -> 2^-44 -> ~1 ulp).
 // The seed's conversions run on the integer ALUs (bits.cuh), so the FP64 pipe
@@ -1203,29 +1226,6 @@ __device__ __forceinline__ float zrcp(float x) { return __fdividef(1.0f, x); }
 // FP64 pivots: Newton-Raphson reciprocal (rcp64) inside FP32's normal range,
 // an IEEE division outside it.
 __device__ __forceinline__ double zrcp(double x) { return f32_range(x) ? rcp64(x) : 1.0 / x; }
-
-// Asynchronous global -> shared copies (no register staging: every copy a
-// thread has issued is in flight at once) and an L2 prefetch of a contiguous
-// span.  Copies of 4 and 8 bytes go through L1 (.ca), 16-byte ones bypass it.
-template <int B> __device__ __forceinline__ void cp_async(void *dst, const void *src) {
-  static_assert(B == 4 || B == 8 || B == 16, "cp.async copies 4, 8 or 16 bytes");
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  const size_t g = __cvta_generic_to_global(src);
-  if constexpr (B == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(g) : "memory");
-  else asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(g), "n"(B) : "memory");
-}
-__device__ __forceinline__ void cp_async4(void *dst, const void *src) { cp_async<4>(dst, src); }
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) { cp_async<16>(dst, src); }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int PENDING> __device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-// bytes: a multiple of 16 from a 16-byte aligned address (the caller checks)
-__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(__cvta_generic_to_global(p)), "r"(bytes)
-               : "memory");
-}
 
 // Coefficients of one z level, staged in shared memory once per CTA so that a
 // level costs one 16- (FP32) or 32-byte (FP64) broadcast load.
