@@ -102,6 +102,17 @@ struct DBuf {
   template <typename T> T *as() const { return (T *)p; }
 };
 
+// Page-locked host memory (an asynchronous copy to it does not block the host).
+bool is_pinned_host(const void *ptr) {
+  if (!ptr) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
 bool is_device_ptr(const void *ptr) {
   if (!ptr) return false;
   cudaPointerAttributes at;
@@ -325,6 +336,8 @@ struct flutas_plan {
   DBuf S64, S32, fbuf, phi, phi2, nrm;
   Mirrors mir;
   cudaStream_t stream = 0;
+  cudaStream_t copy_stream = nullptr;  // device -> host copies that overlap the plan stream's kernels
+  cudaEvent_t ev_ready = nullptr, ev_copied = nullptr;
   bool sync = true;
   int path64 = 0, path32 = 0;  // 0 separate passes, 1 fused plane kernel, 2 cluster plane kernel
   int clus64 = 0, clus32 = 0;  // cluster size of path 2
@@ -935,6 +948,12 @@ int flutas_gb300_fftend(void **arrplan) {
   flutas_plan *pl;
   TRY(check_plan(arrplan[0], &pl));
   cudaStreamSynchronize(pl->stream);
+  if (pl->copy_stream) {
+    cudaStreamSynchronize(pl->copy_stream);
+    cudaStreamDestroy(pl->copy_stream);
+    cudaEventDestroy(pl->ev_ready);
+    cudaEventDestroy(pl->ev_copied);
+  }
   DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->czc, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
                   &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W, &pl->tx32.Q, &pl->ty32.W,
                   &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm};
@@ -1569,7 +1588,7 @@ namespace {
 int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const double *dzci_d, const double *dzfi_d,
                    double dt, double rho0, double *u, double *v, double *w, double *p, int precision, double tol,
                    int max_iter, const double *rho, double *pold, double f_t12_o, const char *cbcvel,
-                   const double *bcvel) {
+                   const double *bcvel, Staged *pold_host = nullptr) {
   const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2], nh_d = pl->nh_d;
   Geo g{nx, ny, nz, nh_u};
   std::vector<double> dzc_h(nz + 2 * nh_d), dzf_h(nz + 2 * nh_d);
@@ -1580,6 +1599,9 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   const double dlv[3] = {1.0 / dxi, 1.0 / dyi, 0.0};
   cudaStream_t st = pl->stream;
   const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+  const double dl[3] = {1.0 / dxi, 1.0 / dyi, 0.0};
+  const double dzc0 = 1.0 / pl->dzci_h[0 - 1 + nh_d], dzcn = 1.0 / pl->dzci_h[nz - 1 + nh_d];
+  bool pold_early = false;  // pold = p done right after pres_tw_src, its host copy overlapping the solve
   // every folded z factor of the step in one launch: Dodd-Ferrante, fillps, correc
   const double dti = 1.0 / dt, rho0i = 1.0 / rho0;
   ScaleJobs jobs;
@@ -1599,6 +1621,24 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     a.fp32 = precision == 1 ? 1 : 0;  // FP32 increment in the mixed path, FP64 in the FP64 path
     a.g = g;
     TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<presw_grid(a.g), PRESTW_NT, 0, st>>>(a); }));
+    if (pold_host && pold_host->host && pold_host->out && is_pinned_host(pold_host->host)) {
+      // pres_tw_src has read pold: pold = p now (whole array, then boundp: the same values as the
+      // correction pass would write), and its copy to the page-locked host array runs on the
+      // plan's copy stream while the solve runs on this one
+      CK(cudaMemcpyAsync(pold, p, pb, cudaMemcpyDeviceToDevice, st));
+      TRY(boundp_dev(pold, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
+      if (!pl->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&pl->ev_ready, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&pl->ev_copied, cudaEventDisableTiming));
+      }
+      CK(cudaEventRecord(pl->ev_ready, st));
+      CK(cudaStreamWaitEvent(pl->copy_stream, pl->ev_ready, 0));
+      CK(cudaMemcpyAsync((void *)pold_host->host, pold, pb, cudaMemcpyDeviceToHost, pl->copy_stream));
+      CK(cudaEventRecord(pl->ev_copied, pl->copy_stream));
+      pold_host->out = false;  // copied: the caller's stage_out skips it
+      pold_early = true;
+    }
   }
   // ghosts of u*,v*,w* as the app leaves them before fillps (bounduvw)
   if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
@@ -1634,12 +1674,10 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
                        pl->pin_zero_mode));
     TRY(inv_xy<double>(pl, S, OutHalo{phi, pl->normfft, gp}, pl->tx64, pl->ty64, pl->path64));
   }
-  const double dl[3] = {1.0 / dxi, 1.0 / dyi, 0.0};
-  const double dzc0 = 1.0 / pl->dzci_h[0 - 1 + nh_d], dzcn = 1.0 / pl->dzci_h[nz - 1 + nh_d];
   CorrecAddArgs ca;
   ca.phi = phi; ca.cz = pl->czc.as<double>() + (nh_d - 1);
   ca.u = u; ca.v = v; ca.w = w; ca.p = p;
-  ca.pold = pold;  // two-phase step: pold = p^n (main__two_phase_inc_isot.f90:655-674) in the same pass
+  ca.pold = pold_early ? nullptr : pold;  // two-phase step: pold = p^n (main__two_phase_inc_isot.f90:655-674)
   ca.cx = (dt * dxi) * rho0i; ca.cy = (dt * dyi) * rho0i;
   ca.g = g;
   FinalCorrec fc;
@@ -1663,7 +1701,8 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<grid_cells(cd.g), 256, 0, st>>>(cd); }));
   }
   if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
-  TRY(boundp_dev(p, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st, pold));  // and pold (the app's boundp(pold))
+  TRY(boundp_dev(p, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st, pold_early ? nullptr : pold));  // and pold
+  if (pold_early) CK(cudaStreamWaitEvent(st, pl->ev_copied, 0));  // the stream's end covers the copy
   return rc;
 }
 
@@ -1700,8 +1739,12 @@ int projection_entry(void *plan, int nh_u, double dxi, double dyi, const double 
     TRY(stage_in(pl->mir, pold, pb, true, true, st, &so));  // in: p^(n-1); out: p^n
   }
   int rc = projection_dev(pl, nh_u, dxi, dyi, sci.d, sfi.d, dt, rho0, su.d, sv.d, sw.d, sp.d, precision, tol,
-                          max_iter, rho ? sr.d : nullptr, rho ? so.d : nullptr, f_t12_o, cbcvel, bcvel);
-  if (rc != 0 && rc != FLUTAS_EITER) return rc;
+                          max_iter, rho ? sr.d : nullptr, rho ? so.d : nullptr, f_t12_o, cbcvel, bcvel,
+                          rho ? &so : nullptr);
+  if (rc != 0 && rc != FLUTAS_EITER) {
+    if (pl->copy_stream) cudaStreamSynchronize(pl->copy_stream);  // no copy into the caller's array after return
+    return rc;
+  }
   TRY(stage_out(su, st));
   TRY(stage_out(sv, st));
   TRY(stage_out(sw, st));
