@@ -57,7 +57,7 @@ METRIC = "Poisson solves/s at <=1e-6 & <=1e-10 rel. residual, mixed vs FP64; p50
 BYTES_PER_CELL = {
     "k_pres_tw_src": 72,            # R p,pold,rho,u,v,w ; W u,v,w
     "k_fillps": 32,                 # R u,v,w ; W rhs
-    "k_correc_padd": 72,            # R phi ; RW u,v,w ; RW p
+    "k_correc_padd": 80,            # R phi ; RW u,v,w ; RW p ; W pold (the two-phase step's pold = p)
     "k_xfwd<f32,keep-fillps>": 36,  # R u,v,w (24) W f-copy (8) W S (4)
     "k_xfwd<f32,keep-halo>": 20,    # R f (8) W f-copy (8) W S (4)
     "k_xfwd<f32,residual>": 20,     # R f, x (16) W S (4)
@@ -84,7 +84,7 @@ BYTES_PER_CELL = {
     "k_stencil<fillps>": 36,        # R u,v,w (24) W f-copy FP64 (8) W S FP32 (4)
     "k_stencil<residual>": 20,      # R f, x (16) W S (4)
     "k_resnorm": 16,                # R f, x
-    "k_resnorm_correc": 88,         # R f, x ; RW u,v,w ; RW p
+    "k_resnorm_correc": 96,         # R f, x ; RW u,v,w ; RW p ; W pold
     "k_sub": 24,                    # R x, s ; W d (halo-1 array)
     # cluster plane kernels (run-time sized, and compile-time sized for 256^2)
     "k_xyfwd_cluster<f32,keep-fillps>": 36,
