@@ -70,7 +70,8 @@ EMU_LIB = os.path.join(HERE, "libflutas_emu.so")
 def build_emu(verbose: bool = False) -> str:
     """Host-only build of the transform passes (CPU emulator used by the tests)."""
     src = os.path.join(CSRC, "emu.cu")
-    deps = [src] + [os.path.join(CSRC, f) for f in ("fft_engine.cuh", "axis_tables.cuh")]
+    deps = [src] + [os.path.join(CSRC, f) for f in ("fft_engine.cuh", "axis_tables.cuh", "fft_fixed.cuh", "bits.cuh",
+                                                   "ghosts.cuh")]
     if _stale(EMU_LIB, deps):
         cmd = [nvcc(), "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "--expt-relaxed-constexpr",
                "-o", EMU_LIB, src]

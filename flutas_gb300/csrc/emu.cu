@@ -11,6 +11,7 @@
 #include "bits.cuh"
 #include "fft_engine.cuh"
 #include "fft_fixed.cuh"
+#include "ghosts.cuh"
 
 using namespace fg;
 
@@ -94,6 +95,45 @@ extern "C" __attribute__((visibility("default"))) void fg_emu_split32(const doub
                    : 4;
     }
   }
+}
+// Ghost cells through the composed maps of ghosts.cuh (what k_ghosts runs);
+// 1 when the maps do not compose (the library then runs the pass-by-pass kernels).
+template <int NC> static int emu_ghosts(GhostArgs<NC> &a) {
+  long count = 0;
+  if (!ghosts_ready(a, &count)) return 1;
+  for (long t = 0; t < count; t++) {  // a cell read is never a cell written: in place is exact
+    int ip[3];
+    ghost_cell(a, t, ip);
+    const long o = ghost_index(a, ip);
+    for (int c = 0; c < NC; c++) {
+      double v;
+      if (ghost_value(a, c, ip, &v)) a.f[c][o] = v;
+    }
+  }
+  return 0;
+}
+extern "C" __attribute__((visibility("default"))) int fg_emu_boundp(const char *cbc, const int *n, const double *bc,
+                                                                     const double *dl, double dzc0, double dzcn,
+                                                                     double *p) {
+  GhostArgs<1> a;
+  a.f[0] = p;
+  const double dr[3][2] = {{dl[0], dl[0]}, {dl[1], dl[1]}, {dzc0, dzcn}};
+  boundp_maps(a, n, cbc, bc, dr);
+  return emu_ghosts(a);
+}
+extern "C" __attribute__((visibility("default"))) int fg_emu_bounduvw(const char *cbc, const int *n, const double *bc,
+                                                                       int nh_d, int h, const double *dl,
+                                                                       const double *dzc, const double *dzf, double *u,
+                                                                       double *v, double *w) {
+  if (h < 1 || h > 4) return 2;
+  BcSide sides[3][3][2];
+  setbc_sides(cbc, bc, n[2], nh_d, h, dl, dzc, dzf, sides);
+  GhostArgs<3> a;
+  a.f[0] = u; a.f[1] = v; a.f[2] = w;
+  a.n[0] = n[0]; a.n[1] = n[1]; a.n[2] = n[2]; a.h = h;
+  for (int d = 0; d < 3; d++)
+    for (int c = 0; c < 3; c++) setbc_maps(a.m[c][d], sides[d][c], n[d], h);
+  return emu_ghosts(a);
 }
 extern "C" __attribute__((visibility("default"))) void fg_emu_diff32(const double *a, const double *b, float *d,
                                                                       long n) {

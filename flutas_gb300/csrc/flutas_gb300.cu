@@ -1221,104 +1221,17 @@ int flutas_gb300_chkdiv(int nx, int ny, int nz, double dxi, double dyi, double d
 
 namespace {
 
-// ---- ghost cells in one launch (k_ghosts): the maps of set_bc's passes
-int gm_slot(int t, int n, int h) { return t <= 0 ? -t : h + t - n; }
-void gm_set(GMap *m, int n, int h, int t, int kind, int src, double F = 0.0, double S = 0.0) {
-  m[gm_slot(t, n, h)] = GMap{F, S, src, kind};
-}
-void gm_clear(GMap *m) {
-  for (int s = 0; s < GM_SLOTS; s++) m[s] = GMap{0.0, 0.0, 0, GM_KEEP};
-}
-// True when no map of the line reads a position the line writes (the maps
-// then compose; grids too small for it keep the pass-by-pass kernels).
-bool gm_closed(const GMap *m, int n, int h) {
-  for (int s = 0; s < 2 * h + 1; s++) {
-    if (m[s].kind != GM_COPY && m[s].kind != GM_AFF) continue;
-    const int t = m[s].src;
-    if (t < 1 || t > n || (t == n && m[h].kind != GM_KEEP)) return false;
-  }
-  return true;
-}
-// Completes a (hi), checks that the maps compose and launches k_ghosts;
-// *done = false (nothing launched) when they do not compose.
+// ---- ghost cells in one launch (k_ghosts; maps and their composition: ghosts.cuh).
+// Completes a, checks that the maps compose and launches k_ghosts; *done =
+// false (nothing launched) when they do not compose.
 template <int NC> int ghosts_launch(GhostArgs<NC> &a, cudaStream_t st, bool *done) {
-  *done = false;
-  for (int d = 0; d < 3; d++) {
-    if (a.n[d] < 2 * a.h + 1) return 0;
-    a.hi[d] = a.n[d];
-    for (int c = 0; c < NC; c++) {
-      if (!gm_closed(a.m[c][d], a.n[d], a.h)) return 0;
-      if (a.m[c][d][a.h].kind != GM_KEEP) a.hi[d] = a.n[d] - 1;
-    }
-  }
-  long E[3], w[3];
-  for (int d = 0; d < 3; d++) {
-    E[d] = a.n[d] + 2 * a.h;
-    w[d] = E[d] - a.hi[d];
-  }
-  const long tot = w[0] * E[1] * E[2] + (long)a.hi[0] * w[1] * E[2] + (long)a.hi[0] * a.hi[1] * w[2];
+  long tot = 0;
+  *done = ghosts_ready(a, &tot);
+  if (!*done) return 0;
   static const char *const names[] = {"", "k_ghosts<1>", "k_ghosts<2>", "k_ghosts<3>"};
-  TRY(launch(names[NC], st, [&] { k_ghosts<NC><<<stream_grid(tot), 256, 0, st>>>(a); }));
-  *done = true;
+  TRY(launch(names[NC], st, [&] { k_ghosts<NC><<<stream_grid(tot), 256, 0, st>>>(a, tot); }));
   return 0;
 }
-// boundp's maps (src/bound.f90:146-225 with set_bc's centred forms, nh_p = 1):
-// periodic copies, and ghost = f + s * inner (D: f = 2 bc, s = -1; N: f = -+dr bc, s = 1).
-template <int NC>
-void boundp_maps(GhostArgs<NC> &a, const int n[3], const char cbc[6], const double bc[6], const double dr[3][2]) {
-  auto fs = [&](char ct, int ib, double rv, double drv, double *f, double *sc) {
-    if (ct == 'D') { *f = 2.0 * rv; *sc = -1.0; }
-    else if (ct == 'N') { *f = ib == 0 ? -drv * rv : drv * rv; *sc = 1.0; }
-    else { *f = 0.0; *sc = 0.0; }
-  };
-  a.h = 1;
-  for (int d = 0; d < 3; d++) {
-    a.n[d] = n[d];
-    GMap *m = a.m[0][d];
-    gm_clear(m);
-    double f, sc;
-    if (cbc[2 * d] == 'P') gm_set(m, n[d], 1, 0, GM_COPY, n[d]);
-    else { fs(cbc[2 * d], 0, bc[2 * d], dr[d][0], &f, &sc); gm_set(m, n[d], 1, 0, GM_AFF, 1, f, sc); }
-    if (cbc[2 * d + 1] == 'P') gm_set(m, n[d], 1, n[d] + 1, GM_COPY, 1);
-    else { fs(cbc[2 * d + 1], 1, bc[2 * d + 1], dr[d][1], &f, &sc); gm_set(m, n[d], 1, n[d] + 1, GM_AFF, n[d], f, sc); }
-    for (int c = 1; c < NC; c++)  // further fields of the same BCs
-      for (int sl = 0; sl < GM_SLOTS; sl++) a.m[c][d][sl] = m[sl];
-  }
-}
-
-// The maps of one direction and component of bounduvw's set_bc pass
-// (k_set_bc3: both ends, layers in order, the last write of a cell wins).
-void setbc_maps(GMap *m, const BcSide side[2], int n, int h) {
-  gm_clear(m);
-  for (int ib = 0; ib < 2; ib++) {
-    const BcSide &sd = side[ib];
-    for (int q = 0; q < h; q++) {
-      const double f = sd.factor[q];
-      if (sd.ctype == 'P') {
-        gm_set(m, n, h, 0 - q, GM_COPY, n - q);
-        gm_set(m, n, h, n + 1 + q, GM_COPY, 1 + q);
-      } else if (sd.centered) {
-        if (ib == 0) gm_set(m, n, h, 0 - q, GM_AFF, 1 + q, f, sd.sgn);
-        else gm_set(m, n, h, n + 1 + q, GM_AFF, n - q, f, sd.sgn);
-      } else if (sd.ctype == 'D') {
-        if (ib == 0) {
-          gm_set(m, n, h, 0 - q, GM_CONST, 0, f);
-        } else {
-          gm_set(m, n, h, n + q, GM_CONST, 0, f);
-          gm_set(m, n, h, n + 1 + q, GM_COPY, n - 1 - q);
-        }
-      } else {
-        if (ib == 0) {
-          gm_set(m, n, h, 0 - q, GM_AFF, 1 + q, 1.0 * f, 1.0);
-        } else {
-          gm_set(m, n, h, n + q, GM_AFF, n - 1 - q, 1.0 * f, 1.0);
-          gm_set(m, n, h, n + 1 + q, GM_AFF, n - 1 - q, 2.0 * f, 1.0);
-        }
-      }
-    }
-  }
-}
-
 // boundp on a device halo array with the plan-less BoundArgs kernel
 int boundp_dev(double *p, const int n[3], const char cbc[6], const double bc[6], const double dl[3], double dzc0,
                double dzcn, cudaStream_t st, double *p2) {
@@ -1468,39 +1381,21 @@ int bounduvw_dev(const char *cbc, const double *bc, int nx, int ny, int nz, int 
                  const double *dzc_h, const double *dzf_h, double *u, double *v, double *w, cudaStream_t st,
                  const int *isoutflow = nullptr, const double *dzf_d = nullptr) {
   if (h < 1 || h > 4) return fail(FLUTAS_EUNSUPPORTED, "bounduvw: halo %d not in 1..4", h);
-  auto CB = [&](int ib, int d, int c) { return cbc[ib + 2 * d + 6 * c]; };
-  auto BV = [&](int ib, int d, int c) { return bc[ib + 2 * d + 6 * c]; };
+  BcSide sides[3][3][2];
+  setbc_sides(cbc, bc, nz, nh_d, h, dl, dzc_h, dzf_h, sides);
   SetBc3Args passes[3];
   for (int d = 0; d < 3; d++) {
     SetBc3Args &a = passes[d];
     a.f[0] = u; a.f[1] = v; a.f[2] = w;
     a.nx = nx; a.ny = ny; a.nz = nz; a.h = h; a.idir = d + 1;
     for (int c = 0; c < 3; c++)
-      for (int ib = 0; ib < 2; ib++) {
-        BcSide &sd = a.side[c][ib];
-        sd.ctype = CB(ib, d, c);
-        sd.centered = (c != d) ? 1 : 0;  // the face-normal component is not centred
-        double dr[4];
-        for (int q = 0; q < h; q++) {
-          if (d < 2) dr[q] = dl[d];
-          else if (c < 2) dr[q] = ib == 0 ? dzc_h[-q - 1 + nh_d] : dzc_h[nz + q - 1 + nh_d];
-          else dr[q] = ib == 0 ? dzf_h[-q - 1 + nh_d] : dzf_h[nz + q - 1 + nh_d];
-        }
-        const double rv = BV(ib, d, c);
-        sd.sgn = 0.0;
-        for (int q = 0; q < h; q++) sd.factor[q] = rv;
-        if (sd.ctype == 'D' && sd.centered) { for (int q = 0; q < h; q++) sd.factor[q] = 2.0 * rv; sd.sgn = -1.0; }
-        if (sd.ctype == 'N') {
-          for (int q = 0; q < h; q++) sd.factor[q] = ib == 0 ? -dr[q] * rv : dr[q] * rv;
-          sd.sgn = 1.0;
-        }
-      }
+      for (int ib = 0; ib < 2; ib++) a.side[c][ib] = sides[d][c][ib];
   }
   GhostArgs<3> ga;
   ga.f[0] = u; ga.f[1] = v; ga.f[2] = w;
   ga.n[0] = nx; ga.n[1] = ny; ga.n[2] = nz; ga.h = h;
   for (int d = 0; d < 3; d++)
-    for (int c = 0; c < 3; c++) setbc_maps(ga.m[c][d], passes[d].side[c], ga.n[d], h);
+    for (int c = 0; c < 3; c++) setbc_maps(ga.m[c][d], sides[d][c], ga.n[d], h);
   bool done;
   TRY(ghosts_launch(ga, st, &done));
   for (int d = 0; d < 3 && !done; d++) {  // grids too small for the maps to compose: pass by pass

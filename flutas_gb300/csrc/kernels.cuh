@@ -17,6 +17,7 @@
 #pragma once
 #include "fft_engine.cuh"
 #include "bits.cuh"
+#include "ghosts.cuh"
 
 namespace fg {
 
@@ -1375,12 +1376,6 @@ namespace fg {
 
 // One direction of bounduvw (src/bound.f90:17-144): both ends, all three
 // velocity components; one thread per face point, ghost layers in order.
-struct BcSide {
-  char ctype;
-  int centered;
-  double factor[4];
-  double sgn;
-};
 struct SetBc3Args {
   double *f[3];
   int nx, ny, nz, h, idir;
@@ -1430,92 +1425,18 @@ __global__ void k_set_bc3(SetBc3Args s) {
 
 namespace fg {
 
-// ---------------------------------------------------------------------------
-// Ghost cells in one launch.  set_bc runs three passes over the whole
-// extended faces, x then y then z (src/bound.f90:17-225); every pass reads
-// only cells that no pass writes (interior cells next to the boundary), so
-// the final value of a written cell is a composition of at most three maps,
-// one per direction, each acting on one cell of its line: unchanged, a copy,
-// F + S*v or a constant F.  GhostArgs holds the map of every written position
-// t of every direction and component (slot -t for t <= 0, h + t - n for
-// t >= n); k_ghosts evaluates the composition for each written cell, x map
-// first, with the arithmetic of the passes (F + S*v, S in {-1, 0, 1}, exact
-// product), so the values are bit-identical to the three passes.
-// ---------------------------------------------------------------------------
-enum : int { GM_KEEP = 0, GM_COPY = 1, GM_AFF = 2, GM_CONST = 3 };
-struct GMap {
-  double F, S;
-  int src, kind;
-};
-constexpr int GM_SLOTS = 9;  // 2h + 1, h <= 4
-template <int NC> struct GhostArgs {
-  double *f[NC];
-  int n[3], h;
-  int hi[3];  // positions 1..hi[d] are never written (hi = n or n - 1)
-  GMap m[NC][3][GM_SLOTS];
-};
+// Ghost cells of boundp / bounduvw in one launch: one thread per written cell,
+// each field's value from the composition of set_bc's maps (ghosts.cuh).
 #ifndef FG_NO_PLAIN_KERNELS
-template <int NC> __global__ void k_ghosts(const __grid_constant__ GhostArgs<NC> a) {  // maps read in place
-  const int h = a.h;
-  const long E0 = a.n[0] + 2 * h, E1 = a.n[1] + 2 * h, E2 = a.n[2] + 2 * h;
-  const long w0 = E0 - a.hi[0], w1 = E1 - a.hi[1], w2 = E2 - a.hi[2];
-  const long c0 = a.hi[0], c1 = a.hi[1];
-  const long T0 = w0 * E1 * E2, T1 = c0 * w1 * E2, T2 = c0 * c1 * w2;
-  auto wpos = [&](int d, long s) -> int { return s < h ? (int)s + 1 - h : a.hi[d] + 1 + (int)(s - h); };
-  auto slot = [&](int d, int t) -> int { return t <= 0 ? -t : h + t - a.n[d]; };
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < T0 + T1 + T2; t += (long)gridDim.x * blockDim.x) {
+template <int NC> __global__ void k_ghosts(const __grid_constant__ GhostArgs<NC> a, long count) {  // maps read in place
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (long)gridDim.x * blockDim.x) {
     int ip[3];
-    if (t < T0) {
-      ip[0] = wpos(0, t % w0);
-      const long r = t / w0;
-      ip[1] = (int)(r % E1) + 1 - h;
-      ip[2] = (int)(r / E1) + 1 - h;
-    } else if (t < T0 + T1) {
-      const long u = t - T0;
-      ip[0] = (int)(u % c0) + 1;
-      const long r = u / c0;
-      ip[1] = wpos(1, r % w1);
-      ip[2] = (int)(r / w1) + 1 - h;
-    } else {
-      const long u = t - T0 - T1;
-      ip[0] = (int)(u % c0) + 1;
-      const long r = u / c0;
-      ip[1] = (int)(r % c1) + 1;
-      ip[2] = wpos(2, r / c1);
-    }
+    ghost_cell(a, t, ip);
+    const long o = ghost_index(a, ip);
 #pragma unroll
     for (int c = 0; c < NC; c++) {
-      const GMap *mp[3];
-      bool any = false;
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        const int tt = ip[d];
-        mp[d] = (tt <= 0 || tt > a.hi[d]) ? &a.m[c][d][slot(d, tt)] : nullptr;
-        if (mp[d] && mp[d]->kind == GM_KEEP) mp[d] = nullptr;
-        any |= mp[d] != nullptr;
-      }
-      if (!any) continue;
-      // sources, z map first; a constant ends the chain
-      int sp[3] = {ip[0], ip[1], ip[2]};
-      int top = -1;  // the direction whose constant starts the chain (-1: a cell of f)
-      for (int d = 2; d >= 0; d--) {
-        if (!mp[d]) continue;
-        if (mp[d]->kind == GM_CONST) { top = d; break; }
-        sp[d] = mp[d]->src;
-      }
       double v;
-      int from;
-      if (top >= 0) {
-        v = mp[top]->F;
-        from = top + 1;
-      } else {
-        const double *f = a.f[c];
-        v = f[(long)(sp[0] - 1 + h) + E0 * ((long)(sp[1] - 1 + h) + E1 * (long)(sp[2] - 1 + h))];
-        from = 0;
-      }
-      for (int d = from; d < 3; d++)
-        if (mp[d] && mp[d]->kind == GM_AFF) v = mp[d]->F + mp[d]->S * v;
-      a.f[c][(long)(ip[0] - 1 + h) + E0 * ((long)(ip[1] - 1 + h) + E1 * (long)(ip[2] - 1 + h))] = v;
+      if (ghost_value(a, c, ip, &v)) a.f[c][o] = v;
     }
   }
 }
