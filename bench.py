@@ -18,7 +18,9 @@ value        : projections/s with the mixed-precision solve (FP32 bulk, FP64
 e2e          : same through the C ABI with pinned HOST buffers (H2D of
                u,v,w,p,rho,pold and D2H of u,v,w,p,pold inside every step).
 modes        : the same step refined to 1e-6, and the plain FP64 solve.
-roofline     : the kernel with the largest share of the timed region, its
+roofline     : the kernel with the largest share of a profiled timed region
+               (the same step with CUDA events around every launch, run after
+               the headline region so their overhead stays out of it): its
                algorithmic bytes per launch / its mean CUDA-event duration.
 cpu_baseline : the FP64 oracle restatement of solver_cpu (not FFTW) on the
                host cores, a bounded sample of the same projection.

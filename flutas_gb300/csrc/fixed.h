@@ -9,7 +9,7 @@
 namespace fg {
 
 // Built variants: FP32, square planes N x N with N = 256 (clusters of 8 CTAs,
-// two per SM) or N = 512 (clusters of 16, one per SM), x and y transforms of
+// three per SM) or N = 512 (clusters of 16, one per SM), x and y transforms of
 // kind PP or NN, input already evaluated in FP32 (k_stencil_pass).
 bool fixed_supported(int nx, int ny, int C, int px, int py);
 // Cluster size of the built variant for this plane, 0 when none is built or
