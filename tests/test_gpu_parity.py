@@ -50,6 +50,9 @@ CASES = [
     ((128, 128, 12), "PPPPNN", 0.0),   # fused plane path in FP32, cluster path in FP64
     ((256, 64, 6), "NNPPNN", 1.5),     # planes larger than one CTA: cluster path
     ((176, 144, 5), "PPNNDD", 0.0),    # radices 11, 9
+    ((32, 24, 40), "PPPPNN", 1.5),     # z sweeps over full 16-level chunks and a partial last one
+    ((24, 16, 33), "NNNNDN", 0.0),
+    ((32, 24, 16), "PPPPDD", 1.5),     # exactly one chunk
 ]
 
 
@@ -184,7 +187,8 @@ def test_gpu_fused_projection(lib, oracle, precision):
 
 
 @pytest.mark.parametrize("n,cbc,gr", [((64, 64, 32), "PPPPNN", 0.0), ((64, 48, 32), "NNPPND", 2.0),
-                                      ((48, 80, 16), "DDNNDD", 1.0), ((32, 32, 32), "PPPPPP", 0.0)])
+                                      ((48, 80, 16), "DDNNDD", 1.0), ((32, 32, 32), "PPPPPP", 0.0),
+                                      ((40, 24, 37), "PPPPNN", 1.0)])  # partial last z chunk
 @pytest.mark.parametrize("tol", [1e-6, 1e-10])
 def test_gpu_mixed_precision_refinement(lib, oracle, n, cbc, gr, tol):
     rng = np.random.default_rng(41)
