@@ -148,7 +148,7 @@ extern "C" __attribute__((visibility("default"))) void fg_emu_diff32(const doubl
 namespace {
 
 template <typename T, int N, int PAIR, int M>
-int run_fixed(int backward, const double *in, double *out) {
+int run_fixed(int backward, const double *in, double *out, bool alias = false) {
   constexpr int B = M / 2;
   AxisPlan ap;
   std::vector<C2<T>> W, Q;
@@ -157,6 +157,25 @@ int run_fixed(int backward, const double *in, double *out) {
   for (size_t i = 0; i < R.size(); i++) R[i] = (T)in[i];
   std::vector<C2<T>> b0((size_t)B * N), b1((size_t)B * N);
   auto bar = [] {};
+  if (alias) {
+    // the two-buffer rotation of the N = 256 plane kernels (fixed.cu), two stages:
+    // X holds the lines and is the second stage buffer; the forward split goes to Y
+    // (the first stage buffer, read by the second stage), the inverse back into X
+    static_assert(sizeof(C2<T>) * B == sizeof(T) * M, "a buffer holds the lines or the B complex lines");
+    if (fix::Plan<N>::NST != 2) return -2;
+    std::vector<C2<T>> X((size_t)B * N), Y((size_t)B * N);
+    T *x = (T *)X.data(), *y = (T *)Y.data();
+    for (size_t i = 0; i < R.size(); i++) x[i] = R[i];
+    if (backward) {
+      fix::inverse<T, N, PAIR, B, 1>(x, N, 1, x, N, 1, Y.data(), X.data(), W.data(), Q.data(), 0, bar);
+      for (size_t i = 0; i < O.size(); i++) out[i] = (double)x[i];
+    } else {
+      HostStore<T> st{y, N, 1};
+      fix::forward<T, N, PAIR, B, 1>(x, N, 1, Y.data(), X.data(), W.data(), Q.data(), st, 0, bar);
+      for (size_t i = 0; i < O.size(); i++) out[i] = (double)y[i];
+    }
+    return 0;
+  }
   if (backward) {
     fix::inverse<T, N, PAIR, B, 1>(R.data(), N, 1, O.data(), N, 1, b0.data(), b1.data(), W.data(), Q.data(), 0, bar);
   } else {
@@ -168,11 +187,11 @@ int run_fixed(int backward, const double *in, double *out) {
 }
 
 template <typename T, int N>
-int fixed_pairs(int pair, int backward, const double *in, double *out) {
+int fixed_pairs(int pair, int backward, const double *in, double *out, bool alias = false) {
   switch (pair) {
-    case BC_PP: return run_fixed<T, N, BC_PP, 8>(backward, in, out);
-    case BC_NN: return run_fixed<T, N, BC_NN, 8>(backward, in, out);
-    case BC_DD: return run_fixed<T, N, BC_DD, 8>(backward, in, out);
+    case BC_PP: return run_fixed<T, N, BC_PP, 8>(backward, in, out, alias);
+    case BC_NN: return run_fixed<T, N, BC_NN, 8>(backward, in, out, alias);
+    case BC_DD: return run_fixed<T, N, BC_DD, 8>(backward, in, out, alias);
     default: return -1;
   }
 }
@@ -189,6 +208,18 @@ extern "C" __attribute__((visibility("default"))) int fg_emu_fixed(int dbl, int 
   FG_EMU_FIX(64)
   FG_EMU_FIX(256)
   FG_EMU_FIX(512)
+#undef FG_EMU_FIX
+  return -1;
+}
+// The same passes with the two-buffer rotation (n with two Stockham stages: 32, 64, 256).
+extern "C" __attribute__((visibility("default"))) int fg_emu_fixed_alias(int dbl, int pair, int n, int backward,
+                                                                         const double *in, double *out) {
+#define FG_EMU_FIX(NN_)                                                                                  \
+  if (n == NN_) return dbl ? fixed_pairs<double, NN_>(pair, backward, in, out, true)                  \
+                           : fixed_pairs<float, NN_>(pair, backward, in, out, true);
+  FG_EMU_FIX(32)
+  FG_EMU_FIX(64)
+  FG_EMU_FIX(256)
 #undef FG_EMU_FIX
   return -1;
 }
