@@ -12,6 +12,7 @@
 #include "fft_engine.cuh"
 #include "fft_fixed.cuh"
 #include "ghosts.cuh"
+#include "ptrcheck.h"
 
 using namespace fg;
 
@@ -222,4 +223,10 @@ extern "C" __attribute__((visibility("default"))) int fg_emu_fixed_alias(int dbl
   FG_EMU_FIX(256)
 #undef FG_EMU_FIX
   return -1;
+}
+
+// The library's decision on where an array argument lives (ptrcheck.h).
+extern "C" __attribute__((visibility("default"))) int fg_emu_classify_ptr(int attr_ok, int mem_type, int ptr_device,
+                                                                         int cur_device) {
+  return classify_ptr(attr_ok != 0, mem_type, ptr_device, cur_device);
 }

@@ -8,6 +8,7 @@
 #include "axis_tables.cuh"
 #include "kernels.cuh"
 #include "fixed.h"
+#include "ptrcheck.h"
 
 #include <cuda_runtime.h>
 
@@ -102,6 +103,8 @@ struct DBuf {
   template <typename T> T *as() const { return (T *)p; }
 };
 
+int noalloc_prepare();  // set-up of flutas_gb300_chkdiv_noalloc on the current device
+
 // Page-locked host memory (an asynchronous copy to it does not block the host).
 bool is_pinned_host(const void *ptr) {
   if (!ptr) return false;
@@ -113,15 +116,27 @@ bool is_pinned_host(const void *ptr) {
   return at.type == cudaMemoryTypeHost;
 }
 
-bool is_device_ptr(const void *ptr) {
-  if (!ptr) return false;
+// Where an array argument lives (ptrcheck.h): host, device memory usable in
+// place on the current device (or managed), or device memory of another GPU.
+int ptr_kind(const void *ptr, int *ptr_dev = nullptr) {
+  if (!ptr) return PTR_HOST;
   cudaPointerAttributes at;
-  cudaError_t e = cudaPointerGetAttributes(&at, ptr);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  const bool ok = cudaPointerGetAttributes(&at, ptr) == cudaSuccess;
+  if (!ok) cudaGetLastError();
+  int cur = 0;
+  if (cudaGetDevice(&cur) != cudaSuccess) cudaGetLastError();
+  if (ptr_dev) *ptr_dev = ok ? at.device : -1;
+  return classify_ptr(ok, ok ? (int)at.type : 0, ok ? at.device : -1, cur);
+}
+
+// Device memory (of any device): readable with cudaMemcpy.
+bool is_device_ptr(const void *ptr) { return ptr_kind(ptr) != PTR_HOST; }
+
+int reject_other_device(const char *who, const void *ptr) {
+  int dev = -1, cur = -1;
+  ptr_kind(ptr, &dev);
+  cudaGetDevice(&cur);
+  return fail(FLUTAS_EINVAL, "%s: an array lives on device %d, but the current device is %d", who, dev, cur);
 }
 
 // A field argument: device pointers are used in place, host pointers are
@@ -156,7 +171,9 @@ int stage_in(Mirrors &m, const void *user, size_t bytes, bool in, bool out, cuda
   s->bytes = bytes;
   s->out = out;
   if (!user) return fail(FLUTAS_EINVAL, "null array argument");
-  if (is_device_ptr(user)) {
+  const int kind = ptr_kind(user);
+  if (kind == PTR_OTHER_DEVICE) return reject_other_device("array argument", user);
+  if (kind == PTR_DEVICE) {
     s->d = (double *)user;
     return 0;
   }
@@ -334,6 +351,8 @@ struct flutas_plan {
   DBuf zdf;            // per-level factors of the Dodd-Ferrante term
   AxisTables tx64, ty64, tx32, ty32;
   DBuf S64, S32, fbuf, phi, phi2, nrm;
+  DBuf nf_flag;         // set by the FP64 z kernel when a column's solution is not finite
+  bool nf_armed = false;  // an FP64 solve since the flag was last read
   Mirrors mir;
   cudaStream_t stream = 0;
   cudaStream_t copy_stream = nullptr;  // device -> host copies that overlap the plan stream's kernels
@@ -547,6 +566,14 @@ template <typename T>
 int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const double *b, const double *c, bool pin) {
   ZArgs za;
   za.a = a; za.b = b; za.c = c; za.lam = lam;
+  // the FP64 path has no residual norm: its z kernel flags a non-finite solution
+  za.nonfinite = nullptr;
+  if (sizeof(T) == 8) {
+    TRY(pl->nf_flag.ensure(sizeof(int)));
+    za.nonfinite = pl->nf_flag.as<int>();
+    CK(cudaMemsetAsync(za.nonfinite, 0, sizeof(int), pl->stream));
+    pl->nf_armed = true;
+  }
   if (sizeof(T) == 8) { za.at = a; za.bt = b; za.ct = c; }
   else { za.at = pl->a32.p; za.bt = pl->b32.p; za.ct = pl->c32.p; }
   za.nq = pl->n[0] * pl->n[1];
@@ -610,6 +637,18 @@ int scale_vecs(const double *in, double s, double *out, int n, cudaStream_t st) 
 
 int finish(flutas_plan *pl) {
   if (pl->sync) CK(cudaStreamSynchronize(pl->stream));
+  return 0;
+}
+
+// After a synchronised FP64 solve: FLUTAS_ENONFINITE when its solution holds a
+// NaN or Inf (a non-finite right-hand side; the reference would carry it into
+// the fields without a word).  In asynchronous mode nothing is read back.
+int check_nonfinite(flutas_plan *pl, const char *who) {
+  if (!pl->sync || !pl->nf_armed) return 0;
+  pl->nf_armed = false;
+  int h = 0;
+  CK(cudaMemcpy(&h, pl->nf_flag.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) return fail(FLUTAS_ENONFINITE, "%s: the solution is not finite (NaN or Inf in the right-hand side)", who);
   return 0;
 }
 
@@ -938,6 +977,7 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
     const double c = atof(e);
     if (c > 0.0 && c <= 1.0) pl->contraction = c;
   }
+  if ((rc = noalloc_prepare())) return bail(rc);  // the allocation-free check is ready on this device
   arrplan[0] = pl;
   arrplan[1] = arrplan[2] = arrplan[3] = nullptr;
   return FLUTAS_OK;
@@ -956,7 +996,7 @@ int flutas_gb300_fftend(void **arrplan) {
   }
   DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->czc, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
                   &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W, &pl->tx32.Q, &pl->ty32.W,
-                  &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm};
+                  &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm, &pl->nf_flag};
   for (DBuf *d : bufs) d->release();
   pl->mir.release();
   pl->magic = 0;
@@ -980,7 +1020,7 @@ int flutas_gb300_plan_info(void *plan, size_t *device_bytes, int *xy_path_fp64, 
     size_t s = 0;
     const DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->czc, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1],
                           &pl->rhsb[2], &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W,
-                          &pl->tx32.Q, &pl->ty32.W, &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm};
+                          &pl->tx32.Q, &pl->ty32.W, &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm, &pl->nf_flag};
     for (const DBuf *d : bufs) s += d->bytes;
     for (const DBuf &d : pl->mir.bufs) s += d.bytes;
     *device_bytes = s;
@@ -1008,7 +1048,9 @@ int flutas_gb300_solver(const int n[3], void *const *arrplan, double normfft, co
   // the ones initsolver filled (their device copies live in the plan)
   auto pick = [&](const double *user, const void *hostinit, const DBuf &dev, size_t cnt, const double **out) -> int {
     if (!user || user == hostinit) { *out = dev.as<double>(); return 0; }
-    if (is_device_ptr(user)) { *out = user; return 0; }
+    const int kind = ptr_kind(user);
+    if (kind == PTR_OTHER_DEVICE) return reject_other_device("solver", user);
+    if (kind == PTR_DEVICE) { *out = user; return 0; }
     // a different host array: refresh the plan's device copy
     CK(cudaMemcpyAsync(dev.p, user, sizeof(double) * cnt, cudaMemcpyHostToDevice, pl->stream));
     *out = dev.as<double>();
@@ -1026,7 +1068,8 @@ int flutas_gb300_solver(const int n[3], void *const *arrplan, double normfft, co
   TRY(solve_fp64_dev(pl, sp.d, dl, da, db, dc));
   TRY(stage_out(sp, pl->stream));
   if (sp.host) CK(cudaStreamSynchronize(pl->stream));
-  return finish(pl);
+  TRY(finish(pl));
+  return check_nonfinite(pl, "solver");
 }
 
 int flutas_gb300_solve_mixed(void *plan, double *p, double tol, int max_iter, double *relres, int *iters) {
@@ -1647,6 +1690,7 @@ int projection_entry(void *plan, int nh_u, double dxi, double dyi, const double 
   if (rho) TRY(stage_out(so, st));
   if (su.host || sp.host || (rho && so.host)) CK(cudaStreamSynchronize(st));
   TRY(finish(pl));
+  if (precision == 0) TRY(check_nonfinite(pl, "projection"));
   return rc;
 }
 
@@ -1804,21 +1848,36 @@ __global__ void k_chkdiv_rows_reduce(double *rows, long nrow) {
 }
 
 std::mutex g_noalloc_mu;
-double *g_noalloc_addr[64] = {};
+bool g_noalloc_ready[64] = {};
 
-// Device address of g_noalloc_rows on the current device (looked up on the
-// first call made with that device current, then cached).
-int noalloc_rows(double **out) {
+// Set-up of the allocation-free check on the current device, once per device:
+// loads both kernels (under CUDA's lazy module loading a kernel is otherwise
+// loaded, and its code and the module's device arrays allocated, at its first
+// launch) and checks that the scratch array's address resolves.  initsolver
+// runs it too, so an application that created a plan has it done already.
+int noalloc_prepare() {
   int dev = 0;
   CK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return fail(FLUTAS_EUNSUPPORTED, "chkdiv_noalloc: device index %d above 63", dev);
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
-    void *p = nullptr;
-    CK(cudaGetSymbolAddress(&p, g_noalloc_rows));
-    g_noalloc_addr[dev] = (double *)p;
-  }
-  *out = g_noalloc_addr[dev];
+  if (g_noalloc_ready[dev]) return 0;
+  cudaFuncAttributes fa;
+  CK(cudaFuncGetAttributes(&fa, k_chkdiv_rows));
+  CK(cudaFuncGetAttributes(&fa, k_chkdiv_rows_reduce));
+  void *p = nullptr;
+  CK(cudaGetSymbolAddress(&p, g_noalloc_rows));
+  g_noalloc_ready[dev] = true;
+  return 0;
+}
+
+// Device address of g_noalloc_rows in the current context.  Looked up on
+// every call (a table lookup once the module is loaded), so a context that
+// was torn down and re-created (cudaDeviceReset) never leaves a stale address.
+int noalloc_rows(double **out) {
+  TRY(noalloc_prepare());
+  void *p = nullptr;
+  CK(cudaGetSymbolAddress(&p, g_noalloc_rows));
+  *out = (double *)p;
   return 0;
 }
 
@@ -1835,8 +1894,12 @@ int flutas_gb300_chkdiv_noalloc(int nx, int ny, int nz, double dxi, double dyi, 
   if ((long)ny * nz > FLUTAS_NOALLOC_MAX_ROWS)
     return fail(FLUTAS_EINVAL, "chkdiv_noalloc: ny*nz = %ld exceeds the %d rows of its fixed scratch",
                 (long)ny * nz, FLUTAS_NOALLOC_MAX_ROWS);
-  if (!is_device_ptr(u) || !is_device_ptr(v) || !is_device_ptr(w) || !is_device_ptr(dzfi))
-    return fail(FLUTAS_EINVAL, "chkdiv_noalloc: u, v, w and dzfi must be device (or managed) memory");
+  for (const void *q : {(const void *)u, (const void *)v, (const void *)w, (const void *)dzfi}) {
+    const int kind = ptr_kind(q);
+    if (kind == PTR_OTHER_DEVICE) return reject_other_device("chkdiv_noalloc", q);
+    if (kind != PTR_DEVICE)
+      return fail(FLUTAS_EINVAL, "chkdiv_noalloc: u, v, w and dzfi must be device (or managed) memory");
+  }
   double *rows = nullptr;
   TRY(noalloc_rows(&rows));
   DivArgs da;
@@ -2132,6 +2195,7 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
     rep << "grid " << g << " n=" << nx << "x" << ny << "x" << nz << " cbc=" << std::string(pl->cbc, 6) << " x:maxe=" << vx.maxe
         << ",M=" << vx.tile << " y:maxe=" << vy.maxe << ",W=" << vy.tile << "\n";
     ZArgs za;
+    za.nonfinite = nullptr;  // the per-grid residual norms flag non-finite values
     za.a = pl->a.as<double>(); za.b = pl->b.as<double>(); za.c = pl->c.as<double>();
     za.at = pl->a32.p; za.bt = pl->b32.p; za.ct = pl->c32.p;
     za.lam = pl->lam.as<double>();
@@ -2228,9 +2292,11 @@ int flutas_gb300_batch_solve(void *batch, double tol, int max_iter, double *relr
   for (int g = 0; g < bt->ng; g++) {
     if (relres) relres[g] = rr[g];
     if (iters) iters[g] = it[g];
-    if (!(rr[g] <= tol)) rc = FLUTAS_EITER;
+    if (!std::isfinite(rr[g])) rc = FLUTAS_ENONFINITE;
+    else if (!(rr[g] <= tol) && rc == FLUTAS_OK) rc = FLUTAS_EITER;
   }
-  if (rc) fail(rc, "batch_solve: some grids did not reach tol in %d solves", max_iter);
+  if (rc == FLUTAS_ENONFINITE) fail(rc, "batch_solve: non-finite residual (NaN or Inf in a right-hand side)");
+  else if (rc) fail(rc, "batch_solve: some grids did not reach tol in %d solves", max_iter);
   return rc;
 }
 

@@ -722,7 +722,16 @@ struct ZArgs {
   int nn;                    // nz - q   (solver_cpu.f90:71-72)
   int periodic;              // bcz == 'PP'
   int pin;                   // 1: the singular (lam == 0) column of an N/P z problem is pinned
+  int *nonfinite;            // nullable: set to 1 when a column's solution is not finite
 };
+
+// A non-finite value anywhere in a column (or in the z-plane transforms that
+// fed it) reaches the column's level-0 solution through the forward
+// elimination and the back substitution: checking that one value per column
+// flags a NaN/Inf input of the solve.
+template <typename T> __device__ __forceinline__ void flag_nonfinite(const ZArgs &za, T x0) {
+  if (za.nonfinite && !isfinite((double)x0)) atomicOr(za.nonfinite, 1);
+}
 
 // Thomas on a column in shared memory (stride ts), in place; d scratch (stride ts).
 // T is the arithmetic type.  Follows dgtsv_homebrewed step by step.
@@ -781,6 +790,7 @@ __global__ void __launch_bounds__(128) k_zsolve(ZArgs za, T *S) {
         pc[(n - 1) * TC] = pn;
         for (int k = 0; k < n - 1; k++) pc[k * TC] = (T)pc[k * TC] + (T)p2c[k * TC] * pn;
       }
+      flag_nonfinite(za, (T)pc[0]);
     }
     __syncthreads();
     for (int idx = tid; idx < nz * TC; idx += TC) {
@@ -1368,6 +1378,7 @@ __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, lo
 #pragma unroll
     for (int i = 0; i < CH; i++) r[i] = rn[i];
   }
+  flag_nonfinite(za, xnext);  // level 0
 }
 
 }  // namespace fg

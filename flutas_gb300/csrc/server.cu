@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
@@ -66,6 +67,7 @@ struct Request {
   int rc = 0;
   double relres = 0.0;
   int iters = 0;
+  double t0 = 0.0, t1 = 0.0;  // device span (ms after the server's reference event)
   std::string err;
 };
 
@@ -90,6 +92,10 @@ struct flutas_server {
   std::vector<double> latencies;  // ms, completed requests
   Clock::time_point t_first, t_last;
   long long completed = 0;
+  // device-side span of every completed request (ms after ev_ref): the stream
+  // work of the request from its first copy to its last, from CUDA events
+  cudaEvent_t ev_ref = nullptr;
+  std::vector<std::pair<double, double>> spans;
 };
 
 namespace {
@@ -162,6 +168,19 @@ void evict_for(flutas_server *s, size_t need) {
     flutas_gb300_fftend(victim->arr);
     s->plans.remove_if([&](const std::unique_ptr<PlanEntry> &p) { return p.get() == victim; });
   }
+}
+
+// Largest number of request spans that overlap at one instant.
+int max_overlap(std::vector<std::pair<double, double>> sp) {
+  std::vector<std::pair<double, int>> ev;
+  for (auto &x : sp) {
+    ev.push_back({x.first, 1});
+    ev.push_back({x.second, -1});
+  }
+  std::sort(ev.begin(), ev.end());  // at equal times the end (-1) sorts before the start
+  int cur = 0, best = 0;
+  for (auto &e : ev) best = std::max(best, cur += e.second);
+  return best;
 }
 
 int run_request(flutas_server *s, Request *q, PlanEntry *pe, cudaStream_t st) {
@@ -259,6 +278,9 @@ void worker_main(flutas_server *s) {
   cudaSetDevice(s->device);
   cudaStream_t st = nullptr;
   cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
     // admission: the head of the queue, when the budget covers it
@@ -293,11 +315,22 @@ void worker_main(flutas_server *s) {
     PlanEntry *pe = acquire_plan(s, q->sig, q->r, &rc, &err, lk);
     if (pe) {
       lk.unlock();
+      cudaEventRecord(ev0, st);
       rc = run_request(s, q, pe, st);
+      cudaEventRecord(ev1, st);
+      float t0 = 0.0f, t1 = 0.0f;
+      const bool timed = cudaEventSynchronize(ev1) == cudaSuccess &&
+                         cudaEventElapsedTime(&t0, s->ev_ref, ev0) == cudaSuccess &&
+                         cudaEventElapsedTime(&t1, s->ev_ref, ev1) == cudaSuccess;
+      if (!timed) cudaGetLastError();
       if (rc && rc != FLUTAS_EITER) {
         char buf[512];
         flutas_gb300_last_error(buf, sizeof buf);
         err = buf;
+      }
+      if (timed) {
+        q->t0 = t0;
+        q->t1 = t1;
       }
       size_t pbytes = 0;
       flutas_gb300_plan_info(pe->arr[0], &pbytes, nullptr, nullptr);
@@ -322,10 +355,13 @@ void worker_main(flutas_server *s) {
       s->latencies.push_back(ms);
       s->completed++;
       s->t_last = q->t_done;
+      if (q->t1 > q->t0) s->spans.push_back({q->t0, q->t1});
     }
     s->cv.notify_all();
   }
   lk.unlock();
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
   cudaStreamDestroy(st);
 }
 
@@ -342,6 +378,13 @@ int flutas_gb300_server_create(size_t hbm_budget, int slots, void **srv) {
   if (!srv || slots < 1 || slots > 64 || hbm_budget == 0) return sfail("server_create: bad arguments");
   flutas_server *s = new flutas_server();
   cudaGetDevice(&s->device);
+  if (cudaEventCreate(&s->ev_ref) != cudaSuccess || cudaEventRecord(s->ev_ref, 0) != cudaSuccess ||
+      cudaEventSynchronize(s->ev_ref) != cudaSuccess) {
+    cudaGetLastError();
+    delete s;
+    fg_set_error_text("server_create: CUDA event set-up failed");
+    return FLUTAS_ECUDA;
+  }
   s->budget = hbm_budget;
   s->t_first = Clock::now();
   for (int i = 0; i < slots; i++) s->workers.emplace_back(worker_main, s);
@@ -362,6 +405,30 @@ int flutas_gb300_server_submit(void *srv, const flutas_request *r, long long *ti
     return bad("server_submit: projection needs u, v, w, p, nh_u >= 1 (and pold with rho)");
   if (r->n[0] < 2 || r->n[1] < 2 || r->n[2] < 3 || r->nh_d < 1 || !r->dzci || !r->dzfi)
     return bad("server_submit: bad sizes or missing dzci/dzfi");
+  if (r->n[0] > 65536 || r->n[1] > 65536 || r->n[2] > 65536 || r->nh_d > 8)
+    return bad("server_submit: sizes beyond 65536 cells per axis or nh_d above 8");
+  for (int i = 0; i < 6; i++)
+    if (r->cbc[i] != 'P' && r->cbc[i] != 'N' && r->cbc[i] != 'D')
+      return bad("server_submit: bad pressure BC character (P, N or D)");
+  for (int d = 0; d < 3; d++)
+    if ((r->cbc[2 * d] == 'P') != (r->cbc[2 * d + 1] == 'P'))
+      return bad("server_submit: a periodic BC must be set on both ends of its axis");
+  for (int d = 0; d < 3; d++)
+    if (!(r->dli[d] > 0.0) || !std::isfinite(r->dli[d])) return bad("server_submit: dli must be finite and > 0");
+  if (!std::isfinite(r->tol) || (r->tol > 0.0 && r->max_iter < 1))
+    return bad("server_submit: tol must be finite (0: FP64) and max_iter >= 1");
+  if (r->kind == 1) {
+    if (r->nh_u > 4 || r->nh_u > r->nh_d) return bad("server_submit: nh_u must be <= 4 and <= nh_d");
+    if (!(r->dt != 0.0) || !std::isfinite(r->dt) || !(r->rho0 > 0.0) || !std::isfinite(r->rho0) ||
+        (r->rho && (!(r->dt_old != 0.0) || !std::isfinite(r->dt_old))))
+      return bad("server_submit: dt (and dt_old) must be finite and non-zero, rho0 finite and > 0");
+    if (r->cbcvel) {
+      if (!r->bcvel) return bad("server_submit: cbcvel given without bcvel");
+      for (int i = 0; i < 18; i++)
+        if (r->cbcvel[i] != 'P' && r->cbcvel[i] != 'N' && r->cbcvel[i] != 'D')
+          return bad("server_submit: bad velocity BC character (P, N or D)");
+    }
+  }
   auto q = std::make_unique<Request>();
   q->r = *r;
   memcpy(q->sig.n, r->n, sizeof q->sig.n);
@@ -414,9 +481,10 @@ int flutas_gb300_server_stats(void *srv, char *buf, int len) {
   for (auto &pe : s->plans) resident += pe->bytes;
   snprintf(buf, (size_t)len,
            "{\"completed\": %lld, \"p50_ms\": %.4f, \"p99_ms\": %.4f, \"span_s\": %.4f, \"used_bytes\": %zu, "
-           "\"budget_bytes\": %zu, \"resident_plans\": %zu, \"resident_plan_bytes\": %zu, \"queued\": %zu, \"inflight\": %d}",
+           "\"budget_bytes\": %zu, \"resident_plans\": %zu, \"resident_plan_bytes\": %zu, \"queued\": %zu, \"inflight\": %d, "
+           "\"max_device_overlap\": %d}",
            s->completed, pct(0.5), pct(0.99), span, s->used, s->budget, s->plans.size(), resident, s->queue.size(),
-           s->inflight);
+           s->inflight, max_overlap(s->spans));
   return FLUTAS_OK;
 }
 
@@ -425,6 +493,7 @@ int flutas_gb300_server_reset_stats(void *srv) {
   if (!s || s->magic != flutas_server::MAGIC) return FLUTAS_EINVAL;
   std::lock_guard<std::mutex> lk(s->mu);
   s->latencies.clear();
+  s->spans.clear();
   s->completed = 0;
   s->t_first = s->t_last = Clock::now();
   return FLUTAS_OK;
@@ -441,6 +510,7 @@ int flutas_gb300_server_destroy(void *srv) {
   s->cv.notify_all();
   for (auto &t : s->workers) t.join();
   for (auto &pe : s->plans) flutas_gb300_fftend(pe->arr);
+  if (s->ev_ref) cudaEventDestroy(s->ev_ref);
   s->magic = 0;
   delete s;
   return FLUTAS_OK;

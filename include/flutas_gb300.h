@@ -3,7 +3,7 @@
  *
  * The entry points keep the argument lists of the Fortran routines they
  * replace, so a FluTAS app binds them through iso_c_binding with a one-line
- * `use` swap (see INTEGRATION.md).  Plain pointers and sizes only.
+ * `use` swap.  Plain pointers and sizes only.
  *
  * Conventions
  *  - Arrays are Fortran column-major (x fastest) and are passed as the address
@@ -177,13 +177,21 @@ FLUTAS_API int flutas_gb300_plan_info(void *plan, size_t *device_bytes, int *xy_
  * allocate device memory at the point of the call: an application that gives
  * the whole device to its own memory pool, or a diagnostic run after an
  * out-of-memory error, when a cudaMalloc would fail.  u, v, w and dzfi must
- * be device or managed memory (host arrays would need staging buffers).  Its
- * scratch is a fixed 1 MiB device array inside the library, one (sum, max)
- * pair per (j,k) row of cells, so ny*nz may not exceed 65536 (FLUTAS_EINVAL
- * otherwise).  The first call made on a device looks the array's address up
- * for that device.  All calls share the array: calls that overlap on the GPU
- * (several host threads, or several streams) race and must be serialised by
- * the caller.  Synchronous: returns after the result is on the host. */
+ * be device memory of the current device, or managed memory (host arrays
+ * would need staging buffers; another GPU's arrays are rejected with
+ * FLUTAS_EINVAL).  Its scratch is a fixed 1 MiB device array inside the
+ * library, one (sum, max) pair per (j,k) row of cells, so ny*nz may not
+ * exceed 65536 (FLUTAS_EINVAL otherwise).
+ * Set-up: the first call on a device (or the first flutas_gb300_initsolver on
+ * it, whichever comes first) loads the check's two kernels and resolves the
+ * array's address on that device.  Under CUDA's lazy module loading that
+ * first load may itself allocate device memory, so make one call (or create a
+ * plan) on each device before relying on the guarantee, and before any
+ * stream capture; CUDA_MODULE_LOADING=EAGER loads everything at start-up.
+ * All calls share the array and every call rewrites the rows it reads: calls
+ * that overlap on the GPU (several host threads, or several streams) race and
+ * must be serialised by the caller.  Synchronous: returns after the result is
+ * on the host. */
 FLUTAS_API int flutas_gb300_chkdiv_noalloc(int nx, int ny, int nz, double dxi, double dyi, double dzi,
                                            int nh_d, int nh_u, const double *dzfi, const double *u,
                                            const double *v, const double *w, double *divtot,
@@ -246,7 +254,9 @@ FLUTAS_API int flutas_gb300_server_submit(void *server, const flutas_request *re
 /* Blocks until the request is done; returns its status (FLUTAS_EITER when tol was not reached). */
 FLUTAS_API int flutas_gb300_server_wait(void *server, long long ticket, double *relres, int *iters,
                                         double *latency_ms);
-/* JSON text: completed, p50_ms, p99_ms (submit-to-result latency), span_s, budget use. */
+/* JSON text: completed, p50_ms, p99_ms (submit-to-result latency), span_s, budget use, and
+ * max_device_overlap: the largest number of requests whose work was on the device at one
+ * instant (spans from CUDA events on the workers' streams). */
 FLUTAS_API int flutas_gb300_server_stats(void *server, char *buf, int len);
 FLUTAS_API int flutas_gb300_server_reset_stats(void *server);
 /* Waits for every queued request, then stops the workers and frees the plans. */

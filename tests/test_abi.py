@@ -77,3 +77,21 @@ def test_missing_library_fails_loudly(tmp_path):
             raise AssertionError("load() of a missing library must raise")
     finally:
         F._lib = saved
+
+
+def test_pointer_classification_rejects_another_devices_memory():
+    """Arrays are used in place only when they live on the current device (or are
+    managed); device memory of another GPU is rejected on the host, because a kernel
+    on this device would fault on it.  Checked on the pure decision function the
+    library uses, with the attribute values cudaPointerGetAttributes reports."""
+    from flutas_gb300 import build as B
+    E = C.CDLL(B.build_emu())
+    E.fg_emu_classify_ptr.argtypes = [C.c_int] * 4
+    E.fg_emu_classify_ptr.restype = C.c_int
+    HOST, DEVICE, OTHER = 0, 1, 2
+    # (attr_ok, type, ptr_device, current_device) -> kind; type 0 unregistered, 1 host, 2 device, 3 managed
+    cases = {(0, 0, -1, 0): HOST, (1, 0, -2, 0): HOST, (1, 1, 0, 0): HOST, (1, 1, 1, 0): HOST,
+             (1, 2, 0, 0): DEVICE, (1, 2, 3, 3): DEVICE, (1, 2, 1, 0): OTHER, (1, 2, 0, 1): OTHER,
+             (1, 3, 0, 0): DEVICE, (1, 3, 1, 0): DEVICE}
+    for args, want in cases.items():
+        assert E.fg_emu_classify_ptr(*args) == want, args

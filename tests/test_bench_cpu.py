@@ -56,3 +56,34 @@ def test_repeated_steps_stay_bounded(oracle):
     # no advection: p accumulates the corrections, but sub-exponentially (doubling per step
     # would give a factor 1024 between steps 10 and 20)
     assert peak[19] < 8 * peak[9], peak
+
+
+def test_accuracy_block_states_parity_and_the_div_bound():
+    """The headline's accuracy block says, in so many words, whether each form meets
+    max|div u| <= 1e-11 U/dx and whether the FP64 form is within 1e-12 of the oracle."""
+    sys.path.insert(0, ROOT)
+    import bench
+    vs = {"fp64_vs_oracle_rel_l2_phi": 3e-14, "fp64_vs_oracle_rel_l2_u": 1e-15,
+          "mixed_vs_oracle_rel_l2_phi": 2e-12, "mixed_vs_oracle_rel_l2_u": 4e-9, "oracle_max_div_after": 1e-12}
+    a = bench.accuracy_block(256, 1.5e-12, 2e-12, 4e-9, 5.0e-9, 1.1e-12, vs)
+    assert a["div_bound"] == 256e-11
+    assert a["mixed_meets_div_bound"] is False and a["fp64_meets_div_bound"] is True
+    assert a["fp64_parity_1e-12"] is True and a["oracle_max_div_after"] == 1e-12
+    b = bench.accuracy_block(256, 1e-13, 0, 0, 1e-9, 1e-12, None)
+    assert b["mixed_meets_div_bound"] is True and "fp64_parity_1e-12" not in b
+
+
+def test_cpu_first_step_is_the_oracle_step(oracle):
+    """The oracle step the bench compares the GPU forms with: one cpu_step on the
+    pristine fields, and the max|div u| it leaves within the bound."""
+    sys.path.insert(0, ROOT)
+    import bench
+    n = 16
+    fields = {k: t.numpy() for k, t in bench.make_fields(n, 3, "cpu").items()}
+    st = bench.cpu_first_step(n, fields)
+    O, S, dzci, dzfi, dz = bench.cpu_setup(n)
+    f = {k: a.copy() for k, a in fields.items()}
+    bench.cpu_step(O, S, n, f, dzci, dzfi, dz)
+    for k in ("u", "v", "w", "p", "pold"):
+        assert np.array_equal(st["f"][k], f[k]), k
+    assert st["max_div"] <= 1e-11 * n

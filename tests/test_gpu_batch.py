@@ -73,3 +73,27 @@ def test_batch_second_solve_reuses_graph(lib):
     for g in range(3):
         assert np.array_equal(sol1[g], B.get(g))
     assert np.array_equal(r1, r2)
+
+
+@pytest.mark.parametrize("tol", [1e-6, 1e-10])
+def test_batch_grid_alone_equals_in_batch(lib, tol):
+    """Each grid solved in a batch of one (the same tuned transform plans and tile
+    shapes, cached per process) gives the result it gets among the other grids,
+    within the requested tolerance (in practice bit for bit)."""
+    grids, rhs = _batch_inputs()
+    B = lib.Batch(grids, autotune=True)
+    for g, r in enumerate(rhs):
+        B.set(g, r)
+    B.solve(tol=tol, max_iter=8)
+    mixed = [B.get(g) for g in range(len(grids))]
+    B.destroy()
+    for g, (gd, r) in enumerate(zip(grids, rhs)):
+        A = lib.Batch([gd], autotune=True)
+        A.set(0, r)
+        rr, _ = A.solve(tol=tol, max_iter=8)
+        alone = A.get(0)
+        A.destroy()
+        assert rr[0] <= tol
+        d = rel_l2(mixed[g][1:-1, 1:-1, 1:-1], alone[1:-1, 1:-1, 1:-1], remove_mean=singular(gd["cbc"]))
+        print(f"batch grid {g} in the mix vs alone: {d:.2e}")
+        assert d <= tol, (g, d)

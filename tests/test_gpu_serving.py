@@ -45,6 +45,9 @@ def test_serving_results_match_alone(lib):
         errs.append(lib.last_error() if res[-1][0] else "")
     st = S.stats()
     assert st["completed"] == len(reqs) and st["p99_ms"] >= st["p50_ms"] > 0, [(r[0], e) for r, e in zip(res, errs)]
+    # continuous batching, not a queue: requests were on the device at the same time
+    # (spans from CUDA events recorded on the workers' streams)
+    assert st["max_device_overlap"] >= 2, st
     S.close()
     for r, o, (rc, rr, it, lat) in zip(reqs, outs, res):
         assert rc == 0 and rr <= r["tol"] and it >= 1 and lat > 0
@@ -52,8 +55,11 @@ def test_serving_results_match_alone(lib):
         alone = r["rhs"].copy()
         rr2, _ = P.solve_mixed(alone, tol=r["tol"], max_iter=8)
         assert rr2 <= r["tol"]
+        # the same plan kinds and kernels run alone and in the mix: the results agree
+        # within the request's own tolerance (in practice bit for bit)
         d = rel_l2(o[1:-1, 1:-1, 1:-1], alone[1:-1, 1:-1, 1:-1], remove_mean=singular(r["cbc"]))
-        assert d <= max(1e3 * r["tol"], 1e-12), (r["n"], d)
+        print(f"served vs alone {r['n']} {r['cbc']}: {d:.2e}")
+        assert d <= r["tol"], (r["n"], d)
 
 
 def test_serving_budget_admission(lib):

@@ -30,6 +30,27 @@ def test_chkdiv_noalloc_matches_chkdiv_twice(lib):
         assert tot == pytest.approx(tot_ref, rel=1e-10, abs=1e-9 * abs(mx_ref) * np.prod(n))
 
 
+def test_chkdiv_noalloc_leaves_device_free_memory_unchanged(lib):
+    """The property the entry point exists for: once its kernels are loaded on the
+    device (one warm-up call), further calls take no device memory.  Free device
+    memory (cudaMemGetInfo) is the same before and after several calls."""
+    import torch
+    n = [64, 48, 40]
+    rng = np.random.default_rng(78)
+    dzci, dzfi, dzc, dzf = zgrid(n[2], 1.2)
+    u, v, w = (torch.from_numpy(a).cuda() for a in random_velocity(rng, n, 1))
+    dzfi_d = torch.from_numpy(dzfi).cuda()
+    lib.chkdiv_noalloc(n, 64.0, 48.0, 40.0, 1, 1, dzfi_d, u, v, w)  # warm-up: kernels loaded
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    first = lib.chkdiv_noalloc(n, 64.0, 48.0, 40.0, 1, 1, dzfi_d, u, v, w)
+    for _ in range(4):
+        assert lib.chkdiv_noalloc(n, 64.0, 48.0, 40.0, 1, 1, dzfi_d, u, v, w) == first
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+
+
 def test_chkdiv_noalloc_rejects_oversized_and_host_arrays(lib):
     import torch
     n = [8, 300, 300]  # 90000 rows > 65536
