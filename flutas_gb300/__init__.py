@@ -47,6 +47,7 @@ EXPORTED = [
     "flutas_gb300_server_create", "flutas_gb300_server_submit", "flutas_gb300_server_wait",
     "flutas_gb300_server_stats", "flutas_gb300_server_reset_stats", "flutas_gb300_server_destroy",
     "flutas_gb300_load", "flutas_gb300_load_scalar", "flutas_gb300_load_ns", "flutas_gb300_update_property",
+    "flutas_gb300_initgrid",
 ]
 
 
@@ -121,6 +122,7 @@ def load(path: str | None = None):
     L.flutas_gb300_update_property.argtypes = [vp, vp, vp, vp]
     L.flutas_gb300_load_scalar.argtypes = [C.c_char, C.c_char_p, vp, vp, vp]
     L.flutas_gb300_load_ns.argtypes = [C.c_char, C.c_char_p, vp, ip, vp, vp, vp, vp, vp, vp]
+    L.flutas_gb300_initgrid.argtypes = [C.c_char_p, ip, dp, dp, ip, vp, vp, vp, vp]
     for name in EXPORTED:
         getattr(L, name).restype = C.c_int
     _lib = L
@@ -285,6 +287,15 @@ class Plan:
                 _lib.flutas_gb300_fftend(C.cast(self.arrplan, C.c_void_p))
         except Exception:
             pass
+
+
+def initgrid(inivel, n, gr, lz, nh_d=1):
+    """initgrid(inivel,n,gr,lz,nh_d,dzc,dzf,zc,zf) (src/initgrid.f90:17): returns
+    dzc, dzf, zc, zf, each with n + 2*nh_d entries (index k-1+nh_d is cell k)."""
+    out = [np.empty(int(n) + 2 * int(nh_d)) for _ in range(4)]
+    _check(load().flutas_gb300_initgrid(_chars(inivel, 3), int(n), float(gr), float(lz), int(nh_d),
+                                        *[a.ctypes.data for a in out]))
+    return tuple(out)
 
 
 def initsolver(n, dli, nh_d, dzci, dzfi, cbc, bc, c_or_f="ccc") -> Plan:

@@ -9,7 +9,7 @@
 !                               correc => gb300_correc, boundp => gb300_boundp,                 &
 !                               bounduvw => gb300_bounduvw, updt_rhs_b => gb300_updt_rhs_b,     &
 !                               chkdiv => gb300_chkdiv, pres_tw_src => gb300_pres_tw_src,       &
-!                               fftend => gb300_fftend
+!                               fftend => gb300_fftend, initgrid => gb300_initgrid
 !
 ! Each wrapper calls the C ABI of libflutas_gb300.so (include/flutas_gb300.h)
 ! through iso_c_binding and hands a non-zero status to the app's usual abort
@@ -32,7 +32,7 @@ module mod_solver_gb300
   private
   public :: gb300_initsolver, gb300_solver_cpu, gb300_solver_gpu, gb300_fillps, gb300_correc, &
             gb300_boundp, gb300_bounduvw, gb300_updt_rhs_b, gb300_chkdiv, gb300_pres_tw_src, &
-            gb300_fftend, gb300_update_property, gb300_load, gb300_chkdiv_noalloc
+            gb300_fftend, gb300_update_property, gb300_load, gb300_chkdiv_noalloc, gb300_initgrid
   !
   interface
     ! src/initsolver.f90:21
@@ -172,6 +172,15 @@ module mod_solver_gb300
       integer(c_int), intent(in) :: n(3)
       integer(c_int), value :: nh
       real(c_double) :: fld(*)
+    end function
+    ! src/initgrid.f90:17
+    integer(c_int) function c_initgrid(inivel, n, gr, lz, nh_d, dzc, dzf, zc, zf) bind(C, name='flutas_gb300_initgrid')
+      import
+      character(kind=c_char), intent(in) :: inivel(3)
+      integer(c_int), value :: n
+      real(c_double), value :: gr, lz
+      integer(c_int), value :: nh_d
+      real(c_double) :: dzc(*), dzf(*), zc(*), zf(*)
     end function
     integer(c_int) function c_last_error(buf, len) bind(C, name='flutas_gb300_last_error')
       import
@@ -368,5 +377,14 @@ contains
     real(rp)        , intent(inout), dimension(n(1),n(2),n(3)) :: fld
     call check(c_load(io, trim(filename)//c_null_char, int(n, c_int), 0_c_int, fld), 'load')
   end subroutine gb300_load
+  !
+  subroutine gb300_initgrid(inivel, n, gr, lz, nh_d, dzc, dzf, zc, zf)
+    character(len=3), intent(in )                           :: inivel
+    integer         , intent(in )                           :: n
+    real(rp)        , intent(in )                           :: gr, lz
+    integer         , intent(in )                           :: nh_d
+    real(rp)        , intent(out), dimension(1-nh_d:n+nh_d) :: dzc, dzf, zc, zf
+    call check(c_initgrid(inivel, int(n, c_int), gr, lz, int(nh_d, c_int), dzc, dzf, zc, zf), 'initgrid')
+  end subroutine gb300_initgrid
   !
 end module mod_solver_gb300

@@ -57,6 +57,14 @@ FLUTAS_API int flutas_gb300_initsolver(const int n[3], const double dli[3], int 
                             double *c, void **arrplan, double *normfft, double *rhsbx,
                             double *rhsby, double *rhsbz);
 
+/* Replaces initgrid (src/initgrid.f90:17-97, clustering functions 102-135), on
+ * the host: the z grid dzc, dzf, zc, zf(1-nh_d:n+nh_d) of n cells on [0,lz],
+ * tanh-clustered with factor gr (0: uniform) at both walls, or at the lower
+ * wall when inivel is 'hcl' or 'hcp'.  The apps pass 1/dzc, 1/dzf on as dzci,
+ * dzfi. */
+FLUTAS_API int flutas_gb300_initgrid(const char inivel[3], int n, double gr, double lz, int nh_d, double *dzc,
+                                     double *dzf, double *zc, double *zf);
+
 /* Replaces solver_cpu (src/solver_cpu.f90:20) / solver_gpu (src/solver_gpu.f90:31):
  * FP64 fwd x/y r2r transforms, z tridiagonal solve per (kx,ky), inverse
  * transforms, times normfft.  p(0:n+1,...) in place (interior overwritten).

@@ -95,3 +95,17 @@ def test_pointer_classification_rejects_another_devices_memory():
              (1, 3, 0, 0): DEVICE, (1, 3, 1, 0): DEVICE}
     for args, want in cases.items():
         assert E.fg_emu_classify_ptr(*args) == want, args
+
+
+def test_initgrid_matches_the_oracle(lib, oracle):
+    """flutas_gb300_initgrid (host code, no device work) gives the oracle's restatement
+    of src/initgrid.f90 bit for bit: two-end and one-end clustering, uniform, wider halos."""
+    for inivel, two_end in (("zer", True), ("poi", True), ("hcl", False), ("hcp", False)):
+        for n, gr, nh in ((64, 2.0, 1), (33, 1.3, 2), (16, 0.0, 3), (256, 2.5, 1)):
+            got = lib.initgrid(inivel, n, gr, 1.7, nh)
+            ref = oracle.initgrid(n, gr, 1.7, nh, two_end=two_end)
+            for a, b in zip(got, ref):
+                assert np.array_equal(a, b), (inivel, n, gr, nh)
+    import pytest
+    with pytest.raises(lib.FlutasError):
+        lib.initgrid("zer", 4, 1.0, 1.0, 5)  # halo wider than the grid

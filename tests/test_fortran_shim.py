@@ -18,7 +18,8 @@ HDR = os.path.join(ROOT, "include", "flutas_gb300.h")
 # Dummy-argument lists of the FluTAS routines (the interface the apps call):
 # src/initsolver.f90:21, src/solver_cpu.f90:20, src/solver_gpu.f90:31, src/fillps.f90:16,
 # src/correc.f90:16, src/bound.f90:146, src/bound.f90:17, src/bound.f90:829,
-# src/chkdiv.f90:18, src/source.f90:247, src/fft.f90:159, src/vof.f90:240, src/load.f90:21
+# src/chkdiv.f90:18, src/source.f90:247, src/fft.f90:159, src/vof.f90:240, src/load.f90:21,
+# src/initgrid.f90:17
 REFERENCE_ARGS = {
     "initsolver": "n,dims,dims_z,dli,nh_d,dzci,dzfi,cbc,bc,c_or_f,lambdaxy,a,b,c,arrplan,normfft,rhsbx,rhsby,rhsbz",
     "solver_cpu": "n,arrplan,normfft,lambdaxy,a,b,c,bcz,c_or_f,p",
@@ -33,6 +34,7 @@ REFERENCE_ARGS = {
     "fftend": "arrplan",
     "update_property": "n,prop12,vof,prop",
     "load": "io,filename,n,fld",
+    "initgrid": "inivel,n,gr,lz,nh_d,dzc,dzf,zc,zf",
 }
 
 
