@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "fft_engine.cuh"
+#include "fft_ext.cuh"
 
 namespace fg {
 
@@ -44,6 +45,40 @@ inline int fill_axis_tables(int n, int pair, AxisPlan *ap, std::vector<C2<T>> &W
       const long double a = PI * k / (long double)n;
       Q[h + k] = mk<T>((T)cosl(a), (T)(-sinl(a)));
     }
+  }
+  return 0;
+}
+
+// Tables of an extended-FFT axis (fft_ext.cuh): kinds kf (forward) and kb
+// (backward) on lines of n cells.  Returns -1 if the DFT length has a prime
+// factor above 13.
+template <typename T>
+inline int fill_ext_tables(int n, int kf, int kb, ExtAxis *ea, std::vector<C2<T>> &W, std::vector<C2<T>> &Qa,
+                           std::vector<C2<T>> &Qb) {
+  *ea = ExtAxis{};
+  ea->n = n;
+  ea->kf = kf;
+  ea->kb = kb;
+  ea->L = ext_length(kf, n);
+  if (ext_length(kb, n) != ea->L || ea->L < 2) return -1;
+  const int ns = make_radix_plan(ea->L, ea->radix, sizeof(T) == 8 ? 3 : 4);
+  if (ns < 0) return -1;
+  ea->nst = ns;
+  const long double PI = 3.141592653589793238462643383279502884L;
+  W.assign(ea->L, mk<T>(0, 0));
+  for (int t = 0; t < ea->L; t++) {
+    const long double a = 2.0L * PI * t / ea->L;
+    W[t] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+  }
+  Qa.assign(n + 1, mk<T>(0, 0));
+  for (int m = 0; m <= n; m++) {
+    const long double a = PI * m / (2.0L * n);
+    Qa[m] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+  }
+  Qb.assign(n, mk<T>(0, 0));
+  for (int k = 0; k < n; k++) {
+    const long double a = PI * (2.0L * k + 1.0L) / (4.0L * n);
+    Qb[k] = mk<T>((T)cosl(a), (T)(-sinl(a)));
   }
   return 0;
 }

@@ -230,3 +230,35 @@ extern "C" __attribute__((visibility("default"))) int fg_emu_classify_ptr(int at
                                                                          int cur_device) {
   return classify_ptr(attr_ok != 0, mem_type, ptr_device, cur_device);
 }
+
+// One extended-FFT r2r transform (fft_ext.cuh) of M lines of length n (line l
+// at in[l*n + t]): the pre pass, the Stockham stages and the read-out, as the
+// kernel runs them.  Points the kind does not transform are copied through.
+template <typename T> static int run_ext(int kind, int n, int M, const double *in, double *out) {
+  ExtAxis ea;
+  std::vector<C2<T>> W, Qa, Qb;
+  if (fill_ext_tables<T>(n, kind, kind, &ea, W, Qa, Qb) != 0) return -2;
+  ea.W = W.data();
+  ea.Qa = Qa.data();
+  ea.Qb = Qb.data();
+  std::vector<T> X((size_t)M * n), Y((size_t)M * n);
+  for (long i = 0; i < (long)M * n; i++) X[i] = Y[i] = (T)in[i];
+  std::vector<C2<T>> c1((size_t)M * ea.L), c2((size_t)M * ea.L);
+  ext_pre<T>(ea, kind, X.data(), n, 1, M, c1.data(), 0, 1);
+  C2<T> *cur = c1.data(), *nxt = c2.data();
+  int Ns = 1;
+  for (int s = 0; s < ea.nst; s++) {
+    stage_dispatch<T, false>(ea.radix[s], cur, nxt, ea.L, M, M, Ns, W.data(), 0, 1);
+    Ns *= ea.radix[s];
+    C2<T> *t = cur; cur = nxt; nxt = t;
+  }
+  ext_post<T>(ea, kind, cur, M, Y.data(), n, 1, 0, 1);
+  for (long i = 0; i < (long)M * n; i++) out[i] = (double)Y[i];
+  return 0;
+}
+
+extern "C" __attribute__((visibility("default"))) int fg_emu_ext(int dbl, int kind, int n, int M, const double *in,
+                                                                 double *out) {
+  if (n < 2 || M < 1 || kind < EXT_DCT1 || kind > EXT_DST4) return -1;
+  return dbl ? run_ext<double>(kind, n, M, in, out) : run_ext<float>(kind, n, M, in, out);
+}

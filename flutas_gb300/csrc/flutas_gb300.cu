@@ -277,6 +277,33 @@ int build_axis(int n, int pair, AxisTables *t) {
   return 0;
 }
 
+// Device tables of an extended-FFT axis (FP64: the kinds it serves run on the
+// FP64 path only).
+struct ExtTables {
+  DBuf W, Qa, Qb;
+  ExtAxis ea{};
+  void release() { W.release(); Qa.release(); Qb.release(); }
+};
+
+int build_ext(int n, int kf, int kb, ExtTables *t) {
+  ExtAxis ea{};
+  std::vector<C2<double>> W, Qa, Qb;
+  if (fill_ext_tables<double>(n, kf, kb, &ea, W, Qa, Qb) != 0)
+    return fail(FLUTAS_EUNSUPPORTED, "extended transform length %d (n=%d) has a prime factor above 13",
+                ext_length(kf, n), n);
+  TRY(t->W.ensure(sizeof(C2<double>) * W.size()));
+  TRY(t->Qa.ensure(sizeof(C2<double>) * Qa.size()));
+  TRY(t->Qb.ensure(sizeof(C2<double>) * Qb.size()));
+  CK(cudaMemcpy(t->W.p, W.data(), sizeof(C2<double>) * W.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(t->Qa.p, Qa.data(), sizeof(C2<double>) * Qa.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(t->Qb.p, Qb.data(), sizeof(C2<double>) * Qb.size(), cudaMemcpyHostToDevice));
+  ea.W = t->W.p;
+  ea.Qa = t->Qa.p;
+  ea.Qb = t->Qb.p;
+  t->ea = ea;
+  return 0;
+}
+
 // ------------------------------------------------------ launches + profiling
 std::atomic<unsigned long long> g_launches{0};
 
@@ -351,6 +378,10 @@ struct flutas_plan {
   DBuf zdf;            // per-level factors of the Dodd-Ferrante term
   AxisTables tx64, ty64, tx32, ty32;
   DBuf S64, S32, fbuf, phi, phi2, nrm;
+  bool face = false;      // a face-centred axis (c_or_f = 'f')
+  bool ext[2] = {false, false};  // x / y transform through the extended FFT (fft_ext.cuh)
+  bool fp64_only = false; // face-centred or extended kinds: the FP64 solver only
+  ExtTables ex[2];
   DBuf nf_flag;         // set by the FP64 z kernel when a column's solution is not finite
   bool nf_armed = false;  // an FP64 solve since the flag was last read
   Mirrors mir;
@@ -652,9 +683,106 @@ int check_nonfinite(flutas_plan *pl, const char *who) {
   return 0;
 }
 
+// x/y transforms of a plan with an extended-FFT axis, in place on the FP64
+// spectral array S: per axis k_r2r_ext, or the paired/DCT-IV engine's separate
+// pass (k_xfwd / k_ypass / k_xinv reading and writing S itself).
+int ext_pass(flutas_plan *pl, double *S, int axis, bool backward) {
+  const Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
+  cudaStream_t st = pl->stream;
+  const ExtAxis &ea = pl->ex[axis].ea;
+  const int kind = backward ? ea.kb : ea.kf;
+  const size_t per_line = 2 * sizeof(C2<double>) * (size_t)ea.L + sizeof(double) * (size_t)ea.n;
+  int B = (int)std::min<size_t>(16, (size_t)(144 * 1024) / per_line);
+  if (B < 1) B = 1;
+  const size_t sm = per_line * B;
+  if ((int)sm > max_smem_optin()) return fail(FLUTAS_EUNSUPPORTED, "extended transform of n=%d too long", ea.n);
+  TRY(allow_smem(k_r2r_ext<double>));
+  const long lines = axis == 0 ? (long)g.ny * g.nz : (long)g.nx * g.nz;
+  const int grid = grid_for(k_r2r_ext<double>, 256, sm, (lines + B - 1) / B);
+  if (grid < 0) return grid;
+  return launch(axis == 0 ? "k_r2r_ext<f64,x>" : "k_r2r_ext<f64,y>", st,
+                [&] { k_r2r_ext<double><<<grid, 256, sm, st>>>(ea, kind, S, g, axis, B); });
+}
+
+int xy_ext(flutas_plan *pl, double *S, bool backward) {
+  const Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
+  cudaStream_t st = pl->stream;
+  const int P = xpitch(g.nx);
+  int M = (int)((64 * 1024) / (sizeof(double) * (size_t)(P + g.nx)));
+  M = std::max(2, (M / 2) * 2);
+  const size_t smx = align_up<double>(sizeof(double) * (size_t)M * P) + sizeof(double) * (size_t)M * g.nx;
+  const long rows = (long)g.ny * g.nz;
+  int W = (int)((64 * 1024) / (2 * sizeof(double) * (size_t)g.ny));
+  W = (W / 2) * 2;
+  if (W > g.nx + (g.nx & 1)) W = g.nx + (g.nx & 1);
+  if (W < 2) W = 2;
+  const size_t smy = align_up<double>(sizeof(double) * (size_t)W * g.ny) + sizeof(double) * (size_t)W * g.ny;
+  const long tiles = (long)((g.nx + W - 1) / W) * g.nz;
+  auto xpass = [&]() -> int {
+    if (pl->ext[0]) return ext_pass(pl, S, 0, backward);
+    if (!backward) {
+      const int grid = grid_for(k_xfwd<double, InPlain>, 256, smx, (rows + M - 1) / M);
+      if (grid < 0) return grid;
+      return launch("k_xfwd<f64,plain>", st,
+                    [&] { k_xfwd<double, InPlain><<<grid, 256, smx, st>>>(pl->tx64.ap, InPlain{S, g}, S, g, M, nullptr); });
+    }
+    const int grid = grid_for(k_xinv<double, OutPlain>, 256, smx, (rows + M - 1) / M);
+    if (grid < 0) return grid;
+    return launch("k_xinv<f64,plain>", st,
+                  [&] { k_xinv<double, OutPlain><<<grid, 256, smx, st>>>(pl->tx64.ap, S, OutPlain{S, g}, g, M); });
+  };
+  auto ypass = [&]() -> int {
+    if (pl->ext[1]) return ext_pass(pl, S, 1, backward);
+    if (!backward) {
+      const int grid = grid_for(k_ypass<double, false>, 256, smy, tiles);
+      if (grid < 0) return grid;
+      return launch("k_ypass_fwd<f64>", st, [&] { k_ypass<double, false><<<grid, 256, smy, st>>>(pl->ty64.ap, S, g, W); });
+    }
+    const int grid = grid_for(k_ypass<double, true>, 256, smy, tiles);
+    if (grid < 0) return grid;
+    return launch("k_ypass_inv<f64>", st, [&] { k_ypass<double, true><<<grid, 256, smy, st>>>(pl->ty64.ap, S, g, W); });
+  };
+  if (!backward) {
+    TRY(xpass());
+    return ypass();
+  }
+  TRY(ypass());
+  return xpass();
+}
+
+// The FP64 solve of a plan with an extended-FFT axis: p's interior into S,
+// forward x and y in place, z, inverse y and x in place, S * normfft into p.
+int solve_fp64_ext_spec(flutas_plan *pl, double *S, double *out_halo, const double *lam, const double *a,
+                        const double *b, const double *c) {
+  const Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
+  cudaStream_t st = pl->stream;
+  TRY(xy_ext(pl, S, false));
+  TRY(zsolve<double>(pl, S, lam, a, b, c, pl->pin_zero_mode));
+  TRY(xy_ext(pl, S, true));
+  const long cells = (long)g.nx * g.ny * g.nz;
+  const int grid = (int)std::min<long>((cells + 255) / 256, (long)num_sms() * 8);
+  return launch("k_spec_out", st, [&] { k_spec_out<double><<<grid, 256, 0, st>>>(S, OutHalo{out_halo, pl->normfft, g}, g); });
+}
+
 // FP64 solve on a device halo array (the plan's own stream).
 int solve_fp64_dev(flutas_plan *pl, double *p, const double *lam, const double *a, const double *b, const double *c) {
   Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
+  if (pl->ext[0] || pl->ext[1]) {
+    TRY(pl->S64.ensure(sizeof(double) * (size_t)g.nx * g.ny * g.nz));
+    double *S = pl->S64.as<double>();
+    const long cells = (long)g.nx * g.ny * g.nz;
+    const int grid = grid_for(k_stencil_pass<InHalo, double>, 256, 0, (cells + 1023) / 1024);
+    if (grid < 0) return grid;
+    if (cells >= (1L << 31) - 4096)
+      TRY(launch("k_stencil<f64,halo>", pl->stream, [&] {
+        k_stencil_pass<InHalo, double, long long><<<grid, 256, 0, pl->stream>>>(InHalo{p, g}, g, nullptr, S, nullptr);
+      }));
+    else
+      TRY(launch("k_stencil<f64,halo>", pl->stream, [&] {
+        k_stencil_pass<InHalo, double><<<grid, 256, 0, pl->stream>>>(InHalo{p, g}, g, nullptr, S, nullptr);
+      }));
+    return solve_fp64_ext_spec(pl, S, p, lam, a, b, c);
+  }
   TRY(pl->S64.ensure(sizeof(double) * (size_t)g.nx * g.ny * g.nz));
   double *S = pl->S64.as<double>();
   TRY(fwd_xy<double>(pl, InHalo{p, g}, S, pl->tx64, pl->ty64, pl->path64));
@@ -827,10 +955,33 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
     if ((cbc[2 * d] == 'P') != (cbc[2 * d + 1] == 'P'))
       return fail(FLUTAS_EINVAL, "initsolver: periodic BC must be set on both ends (axis %d)", d + 1);
   }
-  if (c_or_f[0] != 'c' || c_or_f[1] != 'c' || c_or_f[2] != 'c')
-    return fail(FLUTAS_EUNSUPPORTED, "initsolver: only cell-centred ('ccc') pressure is implemented on the GPU");
-  int px = pair_code(cbc[0], cbc[1]), py = pair_code(cbc[2], cbc[3]);
-  if (px < 0 || py < 0) return fail(FLUTAS_EINVAL, "initsolver: bad BC pair");
+  for (int d = 0; d < 3; d++)
+    if (c_or_f[d] != 'c' && c_or_f[d] != 'f')
+      return fail(FLUTAS_EINVAL, "initsolver: c_or_f(%d) must be 'c' or 'f'", d + 1);
+  const int bx = pair_code(cbc[0], cbc[1]), by = pair_code(cbc[2], cbc[3]);
+  if (bx < 0 || by < 0 || pair_code(cbc[4], cbc[5]) < 0) return fail(FLUTAS_EINVAL, "initsolver: bad BC pair");
+  // the transform of each x/y axis (find_fft, src/fft.f90:233-291): a kind of the paired /
+  // DCT-IV engine (pair code), or an extended-FFT kind (fft_ext.cuh) for the face-centred
+  // REDFT00, RODFT00, RODFT01/10 and the odd-length REDFT11 / RODFT11
+  struct AxisKind {
+    int pair, kf, kb;
+  };
+  auto axis_kind = [](int bcpair, char cf, int nn) -> AxisKind {
+    if (cf == 'c') {
+      if (bcpair == BC_ND && nn % 2) return {bcpair, EXT_DCT4, EXT_DCT4};
+      if (bcpair == BC_DN && nn % 2) return {bcpair, EXT_DST4, EXT_DST4};
+      return {bcpair, EXT_NONE, EXT_NONE};
+    }
+    switch (bcpair) {
+      case BC_PP: return {BC_PP, EXT_NONE, EXT_NONE};           // R2HC / HC2R
+      case BC_NN: return {BC_NN, EXT_DCT1, EXT_DCT1};           // REDFT00 / REDFT00
+      case BC_DD: return {BC_DD, EXT_DST1, EXT_DST1};           // RODFT00 / RODFT00 on n-1 points
+      case BC_ND: return {BC_NN, EXT_NONE, EXT_NONE};           // REDFT10 / REDFT01
+      default: return {BC_DD, EXT_DST3, EXT_DST2};              // DN: RODFT01 / RODFT10
+    }
+  };
+  const AxisKind kx = axis_kind(bx, c_or_f[0], nx), ky = axis_kind(by, c_or_f[1], ny);
+  const int px = kx.pair, py = ky.pair;
   flutas_plan *pl = new flutas_plan();
   int rc = 0;
   auto bail = [&](int r) { pl->magic = 0; delete pl; return r; };
@@ -841,46 +992,60 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
   memcpy(pl->dli, dli, sizeof(double) * 3);
   memcpy(pl->bc, bc, sizeof(double) * 6);
   pl->nh_d = nh_d;
-  // eigenvalues (initsolver.f90:122-186), CPU natural order, times dli^2 (61-64)
+  pl->face = c_or_f[0] == 'f' || c_or_f[1] == 'f' || c_or_f[2] == 'f';
+  pl->ext[0] = kx.kf != EXT_NONE;
+  pl->ext[1] = ky.kf != EXT_NONE;
+  pl->fp64_only = pl->face || pl->ext[0] || pl->ext[1];
+  // eigenvalues (initsolver.f90:122-186), CPU natural order, times dli^2 (61-64).  The
+  // face-centred NN pair keeps the cell-centred formula (the reference writes 2(n-1+1));
+  // the face-centred DD pair transforms n-1 points and leaves lambda(n) unset (its point is
+  // a boundary, not transformed): 0 here, as in the oracle.
   const double pi = 3.141592653589793238462643383279502884;
-  auto eig = [&](int nn, int pair, double *lam) {
+  auto eig = [&](int nn, int bcpair, char cf, double *lam) {
     for (int l = 1; l <= nn; l++) {
       double s;
-      switch (pair) {
+      switch (bcpair) {
         case BC_PP: s = std::sin((1.0 * (l - 1)) * pi / (1.0 * nn)); break;
         case BC_NN: s = std::sin((1.0 * (l - 1)) * pi / (2.0 * nn)); break;
         case BC_DD: s = std::sin((1.0 * (l - 0)) * pi / (2.0 * nn)); break;
         default: s = std::sin((1.0 * (2 * l - 1)) * pi / (4.0 * nn)); break;
       }
-      lam[l - 1] = -4.0 * s * s;
+      lam[l - 1] = (bcpair == BC_DD && cf == 'f' && l == nn) ? 0.0 : -4.0 * s * s;
     }
   };
   std::vector<double> lx(nx), ly(ny);
-  eig(nx, px, lx.data());
-  eig(ny, py, ly.data());
+  eig(nx, bx, c_or_f[0], lx.data());
+  eig(ny, by, c_or_f[1], ly.data());
   for (int i = 0; i < nx; i++) lx[i] = lx[i] * (dli[0] * dli[0]);
   for (int j = 0; j < ny; j++) ly[j] = ly[j] * (dli[1] * dli[1]);
   for (int j = 0; j < ny; j++)
     for (int i = 0; i < nx; i++) lambdaxy[i + (long)nx * j] = lx[i] + ly[j];
-  // tridmatrix (initsolver.f90:188-246), cell-centred
+  // tridmatrix (initsolver.f90:188-246), cell- or face-centred in z
   auto DZCI = [&](int k) { return dzci[k - 1 + nh_d]; };
   auto DZFI = [&](int k) { return dzfi[k - 1 + nh_d]; };
+  const bool zface = c_or_f[2] == 'f';
   for (int k = 1; k <= nz; k++) {
-    a[k - 1] = DZFI(k) * DZCI(k - 1);
-    c[k - 1] = DZFI(k) * DZCI(k);
+    a[k - 1] = zface ? DZFI(k) * DZCI(k) : DZFI(k) * DZCI(k - 1);
+    c[k - 1] = zface ? DZFI(k + 1) * DZCI(k) : DZFI(k) * DZCI(k);
   }
   for (int k = 0; k < nz; k++) b[k] = -(a[k] + c[k]);
   auto fac = [](char ch) { return ch == 'D' ? -1.0 : (ch == 'N' ? 1.0 : 0.0); };
-  b[0] = b[0] + fac(cbc[4]) * a[0];
-  b[nz - 1] = b[nz - 1] + fac(cbc[5]) * c[nz - 1];
-  // bc_rhs (initsolver.f90:248-298), cell-centred
-  auto bc_rhs = [&](const char *cb, int n1, int n2, const double *bv, const double dlc[2], const double dlf[2], double *rhs) {
+  if (!zface) {
+    b[0] = b[0] + fac(cbc[4]) * a[0];
+    b[nz - 1] = b[nz - 1] + fac(cbc[5]) * c[nz - 1];
+  } else {
+    if (cbc[4] == 'N') b[0] = b[0] + fac(cbc[4]) * a[0];
+    if (cbc[5] == 'N') b[nz - 1] = b[nz - 1] + fac(cbc[5]) * c[nz - 1];
+  }
+  // bc_rhs (initsolver.f90:248-298)
+  auto bc_rhs = [&](const char *cb, int n1, int n2, const double *bv, const double dlc[2], const double dlf[2],
+                    char cf, double *rhs) {
     double factor[2];
     for (int ib = 0; ib < 2; ib++) {
       double sgn = ib == 0 ? 1.0 : -1.0;
       if (cb[ib] == 'P') factor[ib] = 0.0;
-      else if (cb[ib] == 'D') factor[ib] = -2.0 * bv[ib];
-      else factor[ib] = sgn * dlc[ib] * bv[ib];
+      else if (cb[ib] == 'D') factor[ib] = cf == 'c' ? -2.0 * bv[ib] : -bv[ib];
+      else factor[ib] = sgn * (cf == 'c' ? dlc[ib] : dlf[ib]) * bv[ib];
     }
     for (int ib = 0; ib < 2; ib++) {
       double v = factor[ib] / dlc[ib] / dlf[ib];
@@ -889,18 +1054,22 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
   };
   {
     double dl0[2] = {1.0 / dli[0], 1.0 / dli[0]}, dl1[2] = {1.0 / dli[1], 1.0 / dli[1]};
-    double dlc[2] = {1.0 / DZCI(0), 1.0 / DZCI(nz)}, dlf[2] = {1.0 / DZFI(1), 1.0 / DZFI(nz)};
-    bc_rhs(cbc + 0, ny, nz, bc + 0, dl0, dl0, rhsbx);
-    bc_rhs(cbc + 2, nx, nz, bc + 2, dl1, dl1, rhsby);
-    bc_rhs(cbc + 4, nx, ny, bc + 4, dlc, dlf, rhsbz);
+    double dlc[2] = {1.0 / DZCI(zface ? 1 : 0), 1.0 / DZCI(zface ? nz - 1 : nz)};
+    double dlf[2] = {1.0 / DZFI(1), 1.0 / DZFI(nz)};
+    bc_rhs(cbc + 0, ny, nz, bc + 0, dl0, dl0, c_or_f[0], rhsbx);
+    bc_rhs(cbc + 2, nx, nz, bc + 2, dl1, dl1, c_or_f[1], rhsby);
+    bc_rhs(cbc + 4, nx, ny, bc + 4, dlc, dlf, c_or_f[2], rhsbz);
   }
-  // fftini normalisation (fft.f90:71-150)
-  double nf = 1.0;
-  nf *= (px == BC_PP ? 1.0 : 2.0) * nx;
-  nf *= (py == BC_PP ? 1.0 : 2.0) * ny;
-  pl->normfft = 1.0 / nf;
+  // fftini normalisation (fft.f90:71-150): norm(1)*(n + norm(2) - ix), the face-centred NN
+  // pair 2(n-1), the face-centred DD pair 2(n+1-1)
+  auto normf = [](int bcpair, char cf, int nn) {
+    if (bcpair == BC_PP) return 1.0 * nn;
+    if (cf == 'f' && bcpair == BC_NN) return 2.0 * (nn - 1);
+    return 2.0 * nn;
+  };
+  pl->normfft = 1.0 / (normf(bx, c_or_f[0], nx) * normf(by, c_or_f[1], ny));
   *normfft = pl->normfft;
-  pl->nn = nz;  // cell-centred: q = 0 (solver_cpu.f90:71-72)
+  pl->nn = nz - ((zface && cbc[5] == 'D') ? 1 : 0);  // solver_cpu.f90:71-72
   pl->pin_zero_mode = false;  // FP64 path follows dgtsv_homebrewed's z == 0 test
   // host copies + device copies
   pl->lam_h.assign(lambdaxy, lambdaxy + (long)nx * ny);
@@ -951,8 +1120,11 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
   if ((rc = up(pl->rhsb[0], rhsbx, 2 * (size_t)ny * nz)) || (rc = up(pl->rhsb[1], rhsby, 2 * (size_t)nx * nz)) ||
       (rc = up(pl->rhsb[2], rhsbz, 2 * (size_t)nx * ny)))
     return bail(rc);
-  if ((rc = build_axis<double>(nx, px, &pl->tx64)) || (rc = build_axis<double>(ny, py, &pl->ty64)) ||
-      (rc = build_axis<float>(nx, px, &pl->tx32)) || (rc = build_axis<float>(ny, py, &pl->ty32)))
+  if ((rc = pl->ext[0] ? build_ext(nx, kx.kf, kx.kb, &pl->ex[0]) : build_axis<double>(nx, px, &pl->tx64)) ||
+      (rc = pl->ext[1] ? build_ext(ny, ky.kf, ky.kb, &pl->ex[1]) : build_axis<double>(ny, py, &pl->ty64)))
+    return bail(rc);
+  if (!pl->fp64_only &&
+      ((rc = build_axis<float>(nx, px, &pl->tx32)) || (rc = build_axis<float>(ny, py, &pl->ty32))))
     return bail(rc);
   const int smax = max_smem_optin();
   pl->path64 = (nx % 2 == 0 && ny % 2 == 0 && (int)plane_smem<double>(nx, ny) <= smax) ? 1 : 0;
@@ -973,6 +1145,7 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
   if (const char *e = getenv("FLUTAS_GB300_XY_PATH")) {  // 0 forces separate passes (A/B timing)
     if (atoi(e) == 0) pl->path64 = pl->path32 = 0;
   }
+  if (pl->ext[0] || pl->ext[1]) pl->path64 = pl->path32 = 0;  // one pass per axis (k_r2r_ext or k_xfwd/k_ypass)
   if (const char *e = getenv("FLUTAS_GB300_CONTRACTION")) {  // initial predicted contraction (tests)
     const double c = atof(e);
     if (c > 0.0 && c <= 1.0) pl->contraction = c;
@@ -998,6 +1171,8 @@ int flutas_gb300_fftend(void **arrplan) {
                   &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W, &pl->tx32.Q, &pl->ty32.W,
                   &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm, &pl->nf_flag};
   for (DBuf *d : bufs) d->release();
+  pl->ex[0].release();
+  pl->ex[1].release();
   pl->mir.release();
   pl->magic = 0;
   delete pl;
@@ -1041,8 +1216,8 @@ int flutas_gb300_solver(const int n[3], void *const *arrplan, double normfft, co
     return fail(FLUTAS_EINVAL, "solver: n=(%d,%d,%d) differs from the plan's (%d,%d,%d)", n[0], n[1], n[2], pl->n[0], pl->n[1], pl->n[2]);
   if (bcz[0] != pl->cbc[4] || bcz[1] != pl->cbc[5])
     return fail(FLUTAS_EINVAL, "solver: bcz differs from the plan's z BCs");
-  if (c_or_f[0] != 'c' || c_or_f[1] != 'c' || c_or_f[2] != 'c')
-    return fail(FLUTAS_EUNSUPPORTED, "solver: only cell-centred ('ccc') is implemented on the GPU");
+  if (c_or_f[0] != pl->c_or_f[0] || c_or_f[1] != pl->c_or_f[1] || c_or_f[2] != pl->c_or_f[2])
+    return fail(FLUTAS_EINVAL, "solver: c_or_f differs from the plan's");
   (void)normfft;  // the plan's normfft (identical to initsolver's output) is used
   // coefficient arrays: device pointers are used as given; host arrays must be
   // the ones initsolver filled (their device copies live in the plan)
@@ -1077,6 +1252,8 @@ int flutas_gb300_solve_mixed(void *plan, double *p, double tol, int max_iter, do
   TRY(check_plan(plan, &pl));
   if (!p) return fail(FLUTAS_EINVAL, "solve_mixed: null p");
   if (!(tol > 0.0) || max_iter < 1) return fail(FLUTAS_EINVAL, "solve_mixed: need tol > 0 and max_iter >= 1");
+  if (pl->fp64_only)
+    return fail(FLUTAS_EUNSUPPORTED, "solve_mixed: face-centred and odd-length ND/DN plans have the FP64 solver only");
   pl->mir.reset();
   Staged sp;
   const size_t pbytes = sizeof(double) * (size_t)(pl->n[0] + 2) * (pl->n[1] + 2) * (pl->n[2] + 2);
@@ -1607,10 +1784,15 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     else
       TRY(launch("k_stencil<f64,fillps>", st,
                  [&] { k_stencil_pass<InFillps, double><<<grid, 256, 0, st>>>(in, gs, nullptr, S, nullptr); }));
-    TRY(fwd_xy<double>(pl, InPlain{S, gs}, S, pl->tx64, pl->ty64, pl->path64));
-    TRY(zsolve<double>(pl, S, pl->lam.as<double>(), pl->a.as<double>(), pl->b.as<double>(), pl->c.as<double>(),
-                       pl->pin_zero_mode));
-    TRY(inv_xy<double>(pl, S, OutHalo{phi, pl->normfft, gp}, pl->tx64, pl->ty64, pl->path64));
+    if (pl->ext[0] || pl->ext[1]) {  // odd-length ND/DN: extended-FFT passes
+      TRY(solve_fp64_ext_spec(pl, S, phi, pl->lam.as<double>(), pl->a.as<double>(), pl->b.as<double>(),
+                              pl->c.as<double>()));
+    } else {
+      TRY(fwd_xy<double>(pl, InPlain{S, gs}, S, pl->tx64, pl->ty64, pl->path64));
+      TRY(zsolve<double>(pl, S, pl->lam.as<double>(), pl->a.as<double>(), pl->b.as<double>(), pl->c.as<double>(),
+                         pl->pin_zero_mode));
+      TRY(inv_xy<double>(pl, S, OutHalo{phi, pl->normfft, gp}, pl->tx64, pl->ty64, pl->path64));
+    }
   }
   CorrecAddArgs ca;
   ca.phi = phi; ca.cz = pl->czc.as<double>() + (nh_d - 1);
@@ -1653,6 +1835,9 @@ int projection_entry(void *plan, int nh_u, double dxi, double dyi, const double 
   if (!dzci || !dzfi || !bcpre || !u || !v || !w || !p) return fail(FLUTAS_EINVAL, "projection: null argument");
   if (nh_u < 1 || dt == 0.0 || rho0 == 0.0) return fail(FLUTAS_EINVAL, "projection: bad nh_u/dt/rho0");
   if (precision == 1 && (!(tol > 0.0) || max_iter < 1)) return fail(FLUTAS_EINVAL, "projection: need tol > 0, max_iter >= 1");
+  if (pl->face) return fail(FLUTAS_EUNSUPPORTED, "projection: the fused projection is cell-centred (c_or_f = 'ccc')");
+  if (precision == 1 && pl->fp64_only)
+    return fail(FLUTAS_EUNSUPPORTED, "projection: odd-length ND/DN plans project in FP64 only (precision 0)");
   for (int i = 0; i < 6; i++)
     if (bcpre[i] != pl->bc[i]) return fail(FLUTAS_EINVAL, "projection: bcpre differs from initsolver's bc");
   if (cbcvel) {
@@ -2178,6 +2363,8 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
       return bail(rc);
     bt->plans[g] = arr[0];
     flutas_plan *pl = (flutas_plan *)arr[0];
+    if (pl->fp64_only) return bail(fail(FLUTAS_EUNSUPPORTED, "batch_create: grid %d has an odd-length ND/DN axis "
+                                                             "(the batched solve is mixed precision)", g));
     BatchGrid &G = bt->grids[g];
     G.g = Geo{nx, ny, nz, 1};
     // tuned transform plans and tiles

@@ -9,6 +9,7 @@
 //   updt_rhs_b               : src/bound.f90:829-944
 //   chkdiv                   : src/chkdiv.f90:37-63
 //   pres_tw_src              : src/source.f90:247-309 (constant-coefficient branch)
+//   face-centred / odd DCT-IV: src/fft.f90:233-291 (extended-FFT kinds, fft_ext.cuh)
 //
 // Layouts (Fortran column-major, x fastest):
 //   p-like fields  (0:nx+1, 0:ny+1, 0:nz+1)        double
@@ -16,6 +17,7 @@
 //   spectral S     (nx, ny, nz) no halo             T (double or float)
 #pragma once
 #include "fft_engine.cuh"
+#include "fft_ext.cuh"
 #include "bits.cuh"
 #include "ghosts.cuh"
 
@@ -221,6 +223,14 @@ struct OutHalo {  // p(i,j,k) = v * scale   (scale applied in the arithmetic typ
   __device__ double pre(int, int, int) const { return 0.0; }
   __device__ void put(int i0, int j0, int k0, double, double v) const { (*this)(i0, j0, k0, v); }
   __device__ void put(int i0, int j0, int k0, double, float v) const { (*this)(i0, j0, k0, v); }
+};
+struct OutPlain {  // the contiguous (nx,ny,nz) spectral array itself (an in-place inverse pass)
+  static constexpr const char *tag = "plain";
+  double *s;
+  Geo g;
+  __device__ void operator()(int i0, int j0, int k0, double v) const { s[g.sidx(i0, j0, k0)] = v; }
+  __device__ double pre(int, int, int) const { return 0.0; }
+  __device__ void put(int i0, int j0, int k0, double, double v) const { (*this)(i0, j0, k0, v); }
 };
 struct OutHaloAdd {  // p(i,j,k) += v * scale  (iterative-refinement update, accumulated in FP64)
   static constexpr const char *tag = "haloadd";
@@ -2003,6 +2013,72 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xyinv_cluster(A
         },
         [&](int idx) { return B2[idx + fnx.div(idx)]; });
     __syncthreads();
+  }
+}
+
+
+// ===========================================================================
+// Extended-FFT r2r pass (fft_ext.cuh): the face-centred kinds and the
+// odd-length DCT-IV / DST-IV, in place on the spectral array S (nx, ny, nz),
+// along x (axis 0: line = row j + ny*k) or y (axis 1: line = i + nx*k).  A tile
+// of B lines: points staged in shared memory X (line-major), the complex DFT
+// of length L in two ping-pong buffers, the read-out back into X (points the
+// kind does not transform keep their value) and stored.  Global accesses are
+// coalesced: x lines are read point-fastest, y lines line-fastest.
+// ===========================================================================
+template <typename T>
+__global__ void __launch_bounds__(256) k_r2r_ext(ExtAxis ea, int kind, T *S, Geo g, int axis, int B) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = ea.n, L = ea.L;
+  C2<T> *c1 = (C2<T> *)smem_raw, *c2 = c1 + (size_t)L * B;
+  T *X = (T *)(c2 + (size_t)L * B);
+  const long lines = axis == 0 ? (long)g.ny * g.nz : (long)g.nx * g.nz;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  auto at = [&](long l, int j) -> long {  // S index of point j of line l
+    if (axis == 0) return l * g.nx + j;
+    const long k = l / g.nx, i = l - k * g.nx;
+    return i + (long)g.nx * (j + (long)g.ny * k);
+  };
+  for (long l0 = (long)blockIdx.x * B; l0 < lines; l0 += (long)gridDim.x * B) {
+    const int nb = (int)min((long)B, lines - l0);
+    for (int idx = tid; idx < B * n; idx += nth) {
+      int c, j;
+      if (axis == 0) { c = idx / n; j = idx - c * n; }
+      else { j = idx / B; c = idx - j * B; }
+      X[c * n + j] = c < nb ? S[at(l0 + c, j)] : (T)0;
+    }
+    __syncthreads();
+    ext_pre<T>(ea, kind, X, n, 1, B, c1, tid, nth);
+    __syncthreads();
+    C2<T> *cur = c1, *nxt = c2;
+    int Ns = 1;
+    for (int s = 0; s < ea.nst; s++) {
+      stage_dispatch<T, false>(ea.radix[s], cur, nxt, L, B, B, Ns, (const C2<T> *)ea.W, tid, nth);
+      Ns *= ea.radix[s];
+      C2<T> *t = cur; cur = nxt; nxt = t;
+      __syncthreads();
+    }
+    ext_post<T>(ea, kind, cur, B, X, n, 1, tid, nth);
+    __syncthreads();
+    for (int idx = tid; idx < B * n; idx += nth) {
+      int c, j;
+      if (axis == 0) { c = idx / n; j = idx - c * n; }
+      else { j = idx / B; c = idx - j * B; }
+      if (c < nb) S[at(l0 + c, j)] = X[c * n + j];
+    }
+    __syncthreads();
+  }
+}
+
+// The spectral array written back into the interior of a halo array, times
+// normfft (the last step of solver_cpu, src/solver_cpu.f90:93).
+template <typename T>
+__global__ void k_spec_out(const T *S, OutHalo out, Geo g) {
+  const long tot = (long)g.nx * g.ny * g.nz;
+  for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < tot; c += (long)gridDim.x * blockDim.x) {
+    const long row = c / g.nx, k = row / g.ny;
+    const int i0 = (int)(c - row * g.nx), j0 = (int)(row - k * g.ny);
+    out(i0, j0, (int)k, S[c]);
   }
 }
 

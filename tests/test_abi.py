@@ -46,13 +46,13 @@ def test_initsolver_rejects_bad_bc_without_touching_the_device(lib):
                                        rh[1].ctypes.data, rh[2].ctypes.data)
         assert rc == code
         assert lib.last_error()
-    # face-centred pressure is not implemented on the GPU: a clear error, not a fallback
+    # c_or_f is 'c' (cell-centred) or 'f' (face-centred) per axis; anything else is refused
     rc = L.flutas_gb300_initsolver(C.cast(n, C.c_void_p), C.cast(dli, C.c_void_p), 1, dz.ctypes.data,
-                                   dz.ctypes.data, b"PPPPNN", C.cast(bc, C.c_void_p), b"ccf",
+                                   dz.ctypes.data, b"PPPPNN", C.cast(bc, C.c_void_p), b"ccx",
                                    lam.ctypes.data, abc[0].ctypes.data, abc[1].ctypes.data,
                                    abc[2].ctypes.data, C.cast(arr, C.c_void_p), C.addressof(nf),
                                    rh[0].ctypes.data, rh[1].ctypes.data, rh[2].ctypes.data)
-    assert rc == lib.FLUTAS_EUNSUPPORTED
+    assert rc == lib.FLUTAS_EINVAL and "c_or_f" in lib.last_error()
 
 
 def test_invalid_plan_handles_are_rejected(lib):

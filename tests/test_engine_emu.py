@@ -180,3 +180,40 @@ def test_fixed_passes_two_buffer_rotation(emu, dbl, n):
             assert emu.fg_emu_fixed(dbl, pair, n, bwd, x, ref) == 0
             assert emu.fg_emu_fixed_alias(dbl, pair, n, bwd, x, got) == 0
             assert np.array_equal(got, ref), (pair, bwd)
+
+
+EXT_KINDS = {1: "REDFT00", 2: "RODFT00", 3: "RODFT10", 4: "RODFT01", 5: "REDFT11", 6: "RODFT11"}
+
+
+@pytest.mark.parametrize("kind", sorted(EXT_KINDS), ids=lambda k: EXT_KINDS[k])
+@pytest.mark.parametrize("n", [5, 9, 12, 17, 33, 64, 65, 75, 96])
+@pytest.mark.parametrize("dbl", [1, 0], ids=["f64", "f32"])
+def test_extended_fft_kinds_match_the_oracle(oracle, kind, n, dbl):
+    """The face-centred kinds (REDFT00, RODFT00, RODFT10/01 swapped for DN) and the
+    odd-length DCT-IV/DST-IV run as one complex DFT of a symmetric extension
+    (fft_ext.cuh); executed on the CPU exactly as the kernel runs them, they give
+    FFTW's definitions (the oracle's r2r) to rounding.  RODFT00 transforms the first
+    n-1 points of a line of n cells and leaves the last one."""
+    from flutas_gb300 import build as B
+    E = C.CDLL(B.build_emu())
+    E.fg_emu_ext.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    E.fg_emu_ext.restype = C.c_int
+    rng = np.random.default_rng(n * 10 + kind)
+    M = 3
+    x = rng.standard_normal((M, n))
+    y = np.empty_like(x)
+    L = 2 * (n - 1) if kind == 1 else 2 * n
+    rc = E.fg_emu_ext(dbl, kind, n, M, x.ctypes.data, y.ctypes.data)
+    radix = np.zeros(12, dtype=np.int32)
+    if E.fg_emu_radix_plan(L, radix.ctypes.data) < 0:
+        assert rc == -2  # a prime factor above 13: refused, not computed
+        return
+    assert rc == 0
+    okind = getattr(oracle, EXT_KINDS[kind])
+    for m in range(M):
+        if kind == 2:
+            ref = np.append(oracle.r2r(okind, x[m, :n - 1]), x[m, n - 1])
+        else:
+            ref = oracle.r2r(okind, x[m])
+        err = np.abs(y[m] - ref).max() / np.abs(ref).max()
+        assert err <= (1e-13 if dbl else 2e-6), (n, err)
