@@ -47,7 +47,7 @@ EXPORTED = [
     "flutas_gb300_server_create", "flutas_gb300_server_submit", "flutas_gb300_server_wait",
     "flutas_gb300_server_stats", "flutas_gb300_server_reset_stats", "flutas_gb300_server_destroy",
     "flutas_gb300_load", "flutas_gb300_load_scalar", "flutas_gb300_load_ns", "flutas_gb300_update_property",
-    "flutas_gb300_initgrid",
+    "flutas_gb300_initgrid", "flutas_gb300_rk", "flutas_gb300_rk_sp", "flutas_gb300_cmpt_time_factors",
 ]
 
 
@@ -123,6 +123,9 @@ def load(path: str | None = None):
     L.flutas_gb300_load_scalar.argtypes = [C.c_char, C.c_char_p, vp, vp, vp]
     L.flutas_gb300_load_ns.argtypes = [C.c_char, C.c_char_p, vp, ip, vp, vp, vp, vp, vp, vp]
     L.flutas_gb300_initgrid.argtypes = [C.c_char_p, ip, dp, dp, ip, vp, vp, vp, vp]
+    L.flutas_gb300_rk.argtypes = [C.c_char_p, dp, dp] + [ip] * 3 + [dp] * 3 + [ip] * 2 + [vp] * 10
+    L.flutas_gb300_rk_sp.argtypes = [dp, dp] + [ip] * 3 + [dp] * 3 + [ip] * 2 + [vp, vp, dp] + [vp] * 6
+    L.flutas_gb300_cmpt_time_factors.argtypes = [C.c_char_p, ip, ip, ip, vp, dp, dp, vp, vp, vp]
     for name in EXPORTED:
         getattr(L, name).restype = C.c_int
     _lib = L
@@ -287,6 +290,34 @@ class Plan:
                 _lib.flutas_gb300_fftend(C.cast(self.arrplan, C.c_void_p))
         except Exception:
             pass
+
+
+def rk(space_scheme_mom, f_t1, f_t2, n, dxi, dyi, dzi, nh_d, nh_u, dzci, dzfi, u, v, w, mu, rho,
+       dudtrko, dvdtrko, dwdtrko):
+    """rk(space_scheme_mom,f_t1,f_t2,nx,ny,nz,dxi,dyi,dzi,nh_d,nh_u,dzci,dzfi,u,v,w,mu,rho,
+    dudtrko,dvdtrko,dwdtrko) (src/rk.f90:26), two-phase right-hand sides; in place."""
+    _check(load().flutas_gb300_rk(_chars(space_scheme_mom, 3), float(f_t1), float(f_t2), int(n[0]), int(n[1]),
+                                  int(n[2]), float(dxi), float(dyi), float(dzi), int(nh_d), int(nh_u), _ptr(dzci),
+                                  _ptr(dzfi), _ptr(u), _ptr(v), _ptr(w), _ptr(mu), _ptr(rho), _ptr(dudtrko),
+                                  _ptr(dvdtrko), _ptr(dwdtrko)))
+
+
+def rk_sp(f_t1, f_t2, n, dxi, dyi, dzi, nh_d, nh_u, dzci, dzfi, visc_sp, u, v, w, dudtrko, dvdtrko, dwdtrko):
+    """rk of the single-phase build (momad_xyz_sp, visc_sp = mu_sp/rho_sp); in place."""
+    _check(load().flutas_gb300_rk_sp(float(f_t1), float(f_t2), int(n[0]), int(n[1]), int(n[2]), float(dxi),
+                                     float(dyi), float(dzi), int(nh_d), int(nh_u), _ptr(dzci), _ptr(dzfi),
+                                     float(visc_sp), _ptr(u), _ptr(v), _ptr(w), _ptr(dudtrko), _ptr(dvdtrko),
+                                     _ptr(dwdtrko)))
+
+
+def cmpt_time_factors(time_scheme, restart, istep, irk_ss, rkcoeff, dt, dto):
+    """cmpt_time_factors (src/rk.f90:104): returns f_t1, f_t2, f_t12."""
+    rc = np.ascontiguousarray(np.asarray(rkcoeff, dtype=np.float64).ravel(order="F"))
+    f = [C.c_double() for _ in range(3)]
+    _check(load().flutas_gb300_cmpt_time_factors(_chars(time_scheme, 3), int(bool(restart)), int(istep), int(irk_ss),
+                                                 rc.ctypes.data, float(dt), float(dto),
+                                                 *[C.addressof(x) for x in f]))
+    return tuple(x.value for x in f)
 
 
 def initgrid(inivel, n, gr, lz, nh_d=1):

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libflutas_gb300.so")
 BUILD_DIR = os.path.join(HERE, "_build")
 
-SOURCES = ["flutas_gb300.cu", "server.cu", "fixed.cu", "io.cu", "grid.cu"]
+SOURCES = ["flutas_gb300.cu", "server.cu", "fixed.cu", "io.cu", "grid.cu", "mom.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",

@@ -307,6 +307,14 @@ int build_ext(int n, int kf, int kb, ExtTables *t) {
 // ------------------------------------------------------ launches + profiling
 std::atomic<unsigned long long> g_launches{0};
 
+}  // namespace
+
+// Kernel launches made by the library's other translation units (momentum
+// predictor, restart I/O) are counted here too.  Library-internal.
+void fg_note_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+namespace {
+
 struct ProfRec {
   const char *name;
   cudaEvent_t a, b;

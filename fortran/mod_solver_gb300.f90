@@ -9,7 +9,12 @@
 !                               correc => gb300_correc, boundp => gb300_boundp,                 &
 !                               bounduvw => gb300_bounduvw, updt_rhs_b => gb300_updt_rhs_b,     &
 !                               chkdiv => gb300_chkdiv, pres_tw_src => gb300_pres_tw_src,       &
-!                               fftend => gb300_fftend, initgrid => gb300_initgrid
+!                               fftend => gb300_fftend, initgrid => gb300_initgrid,             &
+!                               rk => gb300_rk, cmpt_time_factors => gb300_cmpt_time_factors
+!
+! (gb300_rk follows the app's build: the two-phase right-hand sides with _USE_VOF,
+! momad_xyz_sp with mu_sp/rho_sp of mod_param otherwise; the file is preprocessed
+! like the reference's own sources.)
 !
 ! Each wrapper calls the C ABI of libflutas_gb300.so (include/flutas_gb300.h)
 ! through iso_c_binding and hands a non-zero status to the app's usual abort
@@ -32,7 +37,8 @@ module mod_solver_gb300
   private
   public :: gb300_initsolver, gb300_solver_cpu, gb300_solver_gpu, gb300_fillps, gb300_correc, &
             gb300_boundp, gb300_bounduvw, gb300_updt_rhs_b, gb300_chkdiv, gb300_pres_tw_src, &
-            gb300_fftend, gb300_update_property, gb300_load, gb300_chkdiv_noalloc, gb300_initgrid
+            gb300_fftend, gb300_update_property, gb300_load, gb300_chkdiv_noalloc, gb300_initgrid, &
+            gb300_rk, gb300_cmpt_time_factors
   !
   interface
     ! src/initsolver.f90:21
@@ -181,6 +187,43 @@ module mod_solver_gb300
       real(c_double), value :: gr, lz
       integer(c_int), value :: nh_d
       real(c_double) :: dzc(*), dzf(*), zc(*), zf(*)
+    end function
+    ! src/rk.f90:26 (two-phase right-hand sides)
+    integer(c_int) function c_rk(space_scheme_mom, f_t1, f_t2, nx, ny, nz, dxi, dyi, dzi, nh_d, nh_u, dzci, dzfi, &
+                                 u, v, w, mu, rho, dudtrko, dvdtrko, dwdtrko) bind(C, name='flutas_gb300_rk')
+      import
+      character(kind=c_char), intent(in) :: space_scheme_mom(3)
+      real(c_double), value :: f_t1, f_t2
+      integer(c_int), value :: nx, ny, nz
+      real(c_double), value :: dxi, dyi, dzi
+      integer(c_int), value :: nh_d, nh_u
+      real(c_double), intent(in) :: dzci(*), dzfi(*)
+      real(c_double) :: u(*), v(*), w(*)
+      real(c_double), intent(in) :: mu(*), rho(*)
+      real(c_double) :: dudtrko(*), dvdtrko(*), dwdtrko(*)
+    end function
+    ! src/rk.f90:26 (single-phase right-hand sides)
+    integer(c_int) function c_rk_sp(f_t1, f_t2, nx, ny, nz, dxi, dyi, dzi, nh_d, nh_u, dzci, dzfi, visc_sp, &
+                                    u, v, w, dudtrko, dvdtrko, dwdtrko) bind(C, name='flutas_gb300_rk_sp')
+      import
+      real(c_double), value :: f_t1, f_t2
+      integer(c_int), value :: nx, ny, nz
+      real(c_double), value :: dxi, dyi, dzi
+      integer(c_int), value :: nh_d, nh_u
+      real(c_double), intent(in) :: dzci(*), dzfi(*)
+      real(c_double), value :: visc_sp
+      real(c_double) :: u(*), v(*), w(*)
+      real(c_double) :: dudtrko(*), dvdtrko(*), dwdtrko(*)
+    end function
+    ! src/rk.f90:104
+    integer(c_int) function c_cmpt_time_factors(time_scheme, restart, istep, irk_ss, rkcoeff, dt, dto, &
+                                                 f_t1, f_t2, f_t12) bind(C, name='flutas_gb300_cmpt_time_factors')
+      import
+      character(kind=c_char), intent(in) :: time_scheme(3)
+      integer(c_int), value :: restart, istep, irk_ss
+      real(c_double), intent(in) :: rkcoeff(6)
+      real(c_double), value :: dt, dto
+      real(c_double) :: f_t1, f_t2, f_t12
     end function
     integer(c_int) function c_last_error(buf, len) bind(C, name='flutas_gb300_last_error')
       import
@@ -377,6 +420,40 @@ contains
     real(rp)        , intent(inout), dimension(n(1),n(2),n(3)) :: fld
     call check(c_load(io, trim(filename)//c_null_char, int(n, c_int), 0_c_int, fld), 'load')
   end subroutine gb300_load
+  !
+  subroutine gb300_rk(space_scheme_mom, f_t1, f_t2, nx, ny, nz, dxi, dyi, dzi, nh_d, nh_u, dzci, dzfi, u, v, w, &
+                      mu, rho, dudtrko, dvdtrko, dwdtrko)
+#if !defined(_USE_VOF)
+    use mod_param, only: mu_sp, rho_sp
+#endif
+    character(len=3), intent(in   )                        :: space_scheme_mom
+    real(rp)        , intent(in   )                        :: f_t1, f_t2
+    integer         , intent(in   )                        :: nx, ny, nz
+    real(rp)        , intent(in   )                        :: dxi, dyi, dzi
+    integer         , intent(in   )                        :: nh_d, nh_u
+    real(rp)        , intent(in   ), dimension(1-nh_d:)    :: dzci, dzfi
+    real(rp)        , intent(inout), dimension(1-nh_u:,1-nh_u:,1-nh_u:), contiguous :: u, v, w
+    real(rp)        , intent(in   ), dimension(0:,0:,0:), contiguous                :: mu, rho
+    real(rp)        , intent(inout), dimension(:,:,:), contiguous                   :: dudtrko, dvdtrko, dwdtrko
+#if defined(_USE_VOF)
+    call check(c_rk(space_scheme_mom, f_t1, f_t2, int(nx, c_int), int(ny, c_int), int(nz, c_int), dxi, dyi, dzi, &
+                    int(nh_d, c_int), int(nh_u, c_int), dzci, dzfi, u, v, w, mu, rho, dudtrko, dvdtrko, dwdtrko), 'rk')
+#else
+    call check(c_rk_sp(f_t1, f_t2, int(nx, c_int), int(ny, c_int), int(nz, c_int), dxi, dyi, dzi, int(nh_d, c_int), &
+                       int(nh_u, c_int), dzci, dzfi, mu_sp/rho_sp, u, v, w, dudtrko, dvdtrko, dwdtrko), 'rk')
+#endif
+  end subroutine gb300_rk
+  !
+  subroutine gb300_cmpt_time_factors(time_scheme, restart, istep, irk_ss, rkcoeff, dt, dto, f_t1, f_t2, f_t12)
+    character(len=3), intent(in )                 :: time_scheme
+    logical         , intent(in )                 :: restart
+    integer         , intent(in )                 :: istep, irk_ss
+    real(rp)        , intent(in ), dimension(2,3) :: rkcoeff
+    real(rp)        , intent(in )                 :: dt, dto
+    real(rp)        , intent(out)                 :: f_t1, f_t2, f_t12
+    call check(c_cmpt_time_factors(time_scheme, merge(1_c_int, 0_c_int, restart), int(istep, c_int), &
+                                   int(irk_ss, c_int), rkcoeff, dt, dto, f_t1, f_t2, f_t12), 'cmpt_time_factors')
+  end subroutine gb300_cmpt_time_factors
   !
   subroutine gb300_initgrid(inivel, n, gr, lz, nh_d, dzc, dzf, zc, zf)
     character(len=3), intent(in )                           :: inivel

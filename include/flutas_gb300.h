@@ -122,6 +122,32 @@ FLUTAS_API int flutas_gb300_pres_tw_src(int nx, int ny, int nz, double dxi, doub
                              double f_t12_o, const double *p, const double *pold,
                              const double *rho, double *u, double *v, double *w);
 
+/* Replaces rk (src/rk.f90:26-102) of the two-phase apps: the momentum
+ * right-hand sides of momad_xyz_tw_cen (space_scheme_mom "cen",
+ * src/mom.f90:21-197) or momad_xyz_tw_fll ("fll", src/mom.f90:199-386; needs
+ * nh_u >= 2) from the old u,v,w, mu, rho (halo-1 arrays), then
+ * u = u + f_t1*dudt + f_t2*dudtrko and dudtrko = dudt on the interior (the
+ * halo is left for bounduvw).  dudtrko, dvdtrko, dwdtrko are (nx,ny,nz).
+ * FP64, 3-D (the reference's _TWOD build is not covered). */
+FLUTAS_API int flutas_gb300_rk(const char space_scheme_mom[3], double f_t1, double f_t2, int nx, int ny, int nz,
+                               double dxi, double dyi, double dzi, int nh_d, int nh_u, const double *dzci,
+                               const double *dzfi, double *u, double *v, double *w, const double *mu,
+                               const double *rho, double *dudtrko, double *dvdtrko, double *dwdtrko);
+
+/* rk of the single-phase build (src/rk.f90:26-102 with momad_xyz_sp,
+ * src/mom.f90:388-575): visc_sp = mu_sp/rho_sp of the app's parameters. */
+FLUTAS_API int flutas_gb300_rk_sp(double f_t1, double f_t2, int nx, int ny, int nz, double dxi, double dyi,
+                                  double dzi, int nh_d, int nh_u, const double *dzci, const double *dzfi,
+                                  double visc_sp, double *u, double *v, double *w, double *dudtrko,
+                                  double *dvdtrko, double *dwdtrko);
+
+/* Replaces cmpt_time_factors (src/rk.f90:104-135), on the host: f_t1, f_t2,
+ * f_t12 of AB2 ("ab2", first-order Euler at istep 1) or of RK3 substep irk_ss
+ * ("rk3", rkcoeff(2,3) in memory order). */
+FLUTAS_API int flutas_gb300_cmpt_time_factors(const char time_scheme[3], int restart, int istep, int irk_ss,
+                                              const double rkcoeff[6], double dt, double dto, double *f_t1,
+                                              double *f_t2, double *f_t12);
+
 /* Replaces fftend (src/fft.f90:159-179): frees the plan in arrplan(1,1). */
 FLUTAS_API int flutas_gb300_fftend(void **arrplan);
 

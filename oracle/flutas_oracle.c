@@ -804,3 +804,212 @@ void or_residual(const int n[3], const char cbc[6], double dxi, double dyi, int 
         r[PIDX(i, j, k)] = f[PIDX(i, j, k)] - (ax + ay + az);
       }
 }
+
+/* ------------------------------------------------------------------------- */
+/* Momentum predictor: momad_xyz_tw_cen (src/mom.f90:21-197), momad_xyz_tw_fll */
+/* (src/mom.f90:199-386), momad_xyz_sp (src/mom.f90:388-575) and rk            */
+/* (src/rk.f90:26-102); the 3-D branches (no _TWOD).  Velocities have halo h,   */
+/* mu and rho halo 1, dudt/dvdt/dwdt are (nx,ny,nz) without halo.               */
+/* ------------------------------------------------------------------------- */
+#define DT3(a, i, j, k) a[((i) - 1) + (long)nx * (((j) - 1) + (long)ny * ((k) - 1))]
+
+static void mom_cell(int variant, int nx, int ny, int nz, double dxi, double dyi, double dzi, int nh_d, int h,
+                     const double *dzci, const double *dzfi, const double *u, const double *v, const double *w,
+                     const double *mu, const double *rho, double visc_sp, int i, int j, int k, double *du,
+                     double *dv, double *dw) {
+  const long NX = nx + 2, NY = ny + 2, UX = nx + 2 * h, UY = ny + 2 * h;
+  (void)nz;
+#define U(a, b, c) u[UIDX(a, b, c)]
+#define V(a, b, c) v[UIDX(a, b, c)]
+#define W(a, b, c) w[UIDX(a, b, c)]
+#define MU(a, b, c) mu[PIDX(a, b, c)]
+#define RHO(a, b, c) rho[PIDX(a, b, c)]
+#define ZCI(q) dzci[(q) - 1 + nh_d]
+#define ZFI(q) dzfi[(q) - 1 + nh_d]
+  const int ip = i + 1, im = i - 1, jp = j + 1, jm = j - 1, kp = k + 1, km = k - 1;
+  double dudxp, dudxm, dudyp, dudym, dudzp, dudzm, dvdxp, dvdxm, dvdyp, dvdym, dvdzp, dvdzm, dwdxp, dwdxm, dwdyp,
+      dwdym, dwdzp, dwdzm;
+  double muxm, muxp, muym, muyp, muzm, muzp, rhox, rhoy, rhoz;
+  /* advection: centred fluxes in divergence form (cen, sp), or the fourth-order
+     gradient form with an upwind-biased fourth difference (fll) */
+  double adv_u, adv_v, adv_w;
+  if (variant != 1) {
+    const double uuip = 0.25 * (U(ip, j, k) + U(i, j, k)) * (U(ip, j, k) + U(i, j, k));
+    const double uuim = 0.25 * (U(im, j, k) + U(i, j, k)) * (U(im, j, k) + U(i, j, k));
+    const double uvjp = 0.25 * (U(i, jp, k) + U(i, j, k)) * (V(ip, j, k) + V(i, j, k));
+    const double uvjm = 0.25 * (U(i, jm, k) + U(i, j, k)) * (V(ip, jm, k) + V(i, jm, k));
+    const double uwkp = 0.25 * (U(i, j, kp) + U(i, j, k)) * (W(ip, j, k) + W(i, j, k));
+    const double uwkm = 0.25 * (U(i, j, km) + U(i, j, k)) * (W(ip, j, km) + W(i, j, km));
+    adv_u = dxi * (-uuip + uuim) + dyi * (-uvjp + uvjm) + ZFI(k) * (-uwkp + uwkm);
+    const double uvip = 0.25 * (U(i, j, k) + U(i, jp, k)) * (V(i, j, k) + V(ip, j, k));
+    const double uvim = 0.25 * (U(im, j, k) + U(im, jp, k)) * (V(i, j, k) + V(im, j, k));
+    const double vvjp = 0.25 * (V(i, j, k) + V(i, jp, k)) * (V(i, j, k) + V(i, jp, k));
+    const double vvjm = 0.25 * (V(i, j, k) + V(i, jm, k)) * (V(i, j, k) + V(i, jm, k));
+    const double wvkp = 0.25 * (W(i, j, k) + W(i, jp, k)) * (V(i, j, kp) + V(i, j, k));
+    const double wvkm = 0.25 * (W(i, j, km) + W(i, jp, km)) * (V(i, j, km) + V(i, j, k));
+    adv_v = dxi * (-uvip + uvim) + dyi * (-vvjp + vvjm) + ZFI(k) * (-wvkp + wvkm);
+    const double uwip = 0.25 * (W(i, j, k) + W(ip, j, k)) * (U(i, j, k) + U(i, j, kp));
+    const double uwim = 0.25 * (W(i, j, k) + W(im, j, k)) * (U(im, j, k) + U(im, j, kp));
+    const double vwjp = 0.25 * (W(i, j, k) + W(i, jp, k)) * (V(i, j, k) + V(i, j, kp));
+    const double vwjm = 0.25 * (W(i, j, k) + W(i, jm, k)) * (V(i, jm, k) + V(i, jm, kp));
+    const double wwkp = 0.25 * (W(i, j, k) + W(i, j, kp)) * (W(i, j, k) + W(i, j, kp));
+    const double wwkm = 0.25 * (W(i, j, k) + W(i, j, km)) * (W(i, j, k) + W(i, j, km));
+    adv_w = dxi * (-uwip + uwim) + dyi * (-vwjp + vwjm) + ZCI(k) * (-wwkp + wwkm);
+  } else {
+#define G4(f1, f2, f3, f4, f5, c, dl) \
+  ((c) * ((f1) - 8.0 * (f2) + 8.0 * (f4) - (f5)) * (1.0 / 12.0) * (dl) + \
+   3.0 * fabs(c) * ((f1) - 4.0 * (f2) + 6.0 * (f3) - 4.0 * (f4) + (f5)) * (1.0 / 12.0) * (dl))
+    double uc = U(i, j, k);
+    double vc = 0.25 * (V(i, j, k) + V(ip, j, k) + V(i, jm, k) + V(ip, jm, k));
+    double wc = 0.25 * (W(i, j, k) + W(ip, j, k) + W(i, j, km) + W(ip, j, km));
+    adv_u = -(G4(U(i - 2, j, k), U(i - 1, j, k), U(i, j, k), U(i + 1, j, k), U(i + 2, j, k), uc, dxi) +
+              G4(U(i, j - 2, k), U(i, j - 1, k), U(i, j, k), U(i, j + 1, k), U(i, j + 2, k), vc, dyi) +
+              G4(U(i, j, k - 2), U(i, j, k - 1), U(i, j, k), U(i, j, k + 1), U(i, j, k + 2), wc, dzi));
+    uc = 0.25 * (U(i, j, k) + U(i, jp, k) + U(im, j, k) + U(im, jp, k));
+    vc = V(i, j, k);
+    wc = 0.25 * (W(i, j, k) + W(i, jp, k) + W(i, j, km) + W(i, jp, km));
+    adv_v = -(G4(V(i - 2, j, k), V(i - 1, j, k), V(i, j, k), V(i + 1, j, k), V(i + 2, j, k), uc, dxi) +
+              G4(V(i, j - 2, k), V(i, j - 1, k), V(i, j, k), V(i, j + 1, k), V(i, j + 2, k), vc, dyi) +
+              G4(V(i, j, k - 2), V(i, j, k - 1), V(i, j, k), V(i, j, k + 1), V(i, j, k + 2), wc, dzi));
+    uc = 0.25 * (U(i, j, k) + U(i, j, kp) + U(im, j, k) + U(im, j, kp));
+    vc = 0.25 * (V(i, j, k) + V(i, j, kp) + V(i, jm, k) + V(i, jm, kp));
+    wc = W(i, j, k);
+    adv_w = -(G4(W(i - 2, j, k), W(i - 1, j, k), W(i, j, k), W(i + 1, j, k), W(i + 2, j, k), uc, dxi) +
+              G4(W(i, j - 2, k), W(i, j - 1, k), W(i, j, k), W(i, j + 1, k), W(i, j + 2, k), vc, dyi) +
+              G4(W(i, j, k - 2), W(i, j, k - 1), W(i, j, k), W(i, j, k + 1), W(i, j, k + 2), wc, dzi));
+#undef G4
+  }
+  /* x-momentum diffusion */
+  dudxp = (U(ip, j, k) - U(i, j, k)) * dxi;
+  dudxm = (U(i, j, k) - U(im, j, k)) * dxi;
+  dudyp = (U(i, jp, k) - U(i, j, k)) * dyi;
+  dudym = (U(i, j, k) - U(i, jm, k)) * dyi;
+  dudzp = (U(i, j, kp) - U(i, j, k)) * ZCI(k);
+  dudzm = (U(i, j, k) - U(i, j, km)) * ZCI(km);
+  if (variant == 2) {
+    *du = adv_u + (dxi * (dudxp - dudxm) + dyi * (dudyp - dudym) + ZFI(k) * (dudzp - dudzm)) * visc_sp;
+  } else {
+    dvdxp = (V(ip, j, k) - V(i, j, k)) * dxi;
+    dvdxm = (V(ip, jm, k) - V(i, jm, k)) * dxi;
+    dwdxp = (W(ip, j, k) - W(i, j, k)) * dxi;
+    dwdxm = (W(ip, j, km) - W(i, j, km)) * dxi;
+    muxp = MU(ip, j, k);
+    muxm = MU(i, j, k);
+    muyp = 0.25 * (MU(i, j, k) + MU(i, jp, k) + MU(ip, jp, k) + MU(ip, j, k));
+    muym = 0.25 * (MU(i, j, k) + MU(i, jm, k) + MU(ip, jm, k) + MU(ip, j, k));
+    muzp = 0.25 * (MU(i, j, k) + MU(i, j, kp) + MU(ip, j, kp) + MU(ip, j, k));
+    muzm = 0.25 * (MU(i, j, k) + MU(i, j, km) + MU(ip, j, km) + MU(ip, j, k));
+    rhox = 0.5 * (RHO(ip, j, k) + RHO(i, j, k));
+    *du = adv_u + (dxi * ((dudxp + dudxp) * muxp - (dudxm + dudxm) * muxm) +
+                   dyi * ((dudyp + dvdxp) * muyp - (dudym + dvdxm) * muym) +
+                   ZFI(k) * ((dudzp + dwdxp) * muzp - (dudzm + dwdxm) * muzm)) / rhox;
+  }
+  /* y-momentum diffusion */
+  dvdxp = (V(ip, j, k) - V(i, j, k)) * dxi;
+  dvdxm = (V(i, j, k) - V(im, j, k)) * dxi;
+  dvdyp = (V(i, jp, k) - V(i, j, k)) * dyi;
+  dvdym = (V(i, j, k) - V(i, jm, k)) * dyi;
+  dvdzp = (V(i, j, kp) - V(i, j, k)) * ZCI(k);
+  dvdzm = (V(i, j, k) - V(i, j, km)) * ZCI(km);
+  if (variant == 2) {
+    *dv = adv_v + (dxi * (dvdxp - dvdxm) + dyi * (dvdyp - dvdym) + ZFI(k) * (dvdzp - dvdzm)) * visc_sp;
+  } else {
+    dudyp = (U(i, jp, k) - U(i, j, k)) * dyi;
+    dudym = (U(im, jp, k) - U(im, j, k)) * dyi;
+    dwdyp = (W(i, jp, k) - W(i, j, k)) * dyi;
+    dwdym = (W(i, jp, km) - W(i, j, km)) * dyi;
+    muxp = 0.25 * (MU(i, j, k) + MU(ip, j, k) + MU(ip, jp, k) + MU(i, jp, k));
+    muxm = 0.25 * (MU(i, j, k) + MU(im, j, k) + MU(im, jp, k) + MU(i, jp, k));
+    muyp = MU(i, jp, k);
+    muym = MU(i, j, k);
+    muzp = 0.25 * (MU(i, j, k) + MU(i, jp, k) + MU(i, jp, kp) + MU(i, j, kp));
+    muzm = 0.25 * (MU(i, j, k) + MU(i, jp, k) + MU(i, jp, km) + MU(i, j, km));
+    rhoy = 0.5 * (RHO(i, jp, k) + RHO(i, j, k));
+    *dv = adv_v + (dxi * ((dvdxp + dudyp) * muxp - (dvdxm + dudym) * muxm) +
+                   dyi * ((dvdyp + dvdyp) * muyp - (dvdym + dvdym) * muym) +
+                   ZFI(k) * ((dvdzp + dwdyp) * muzp - (dvdzm + dwdym) * muzm)) / rhoy;
+  }
+  /* z-momentum diffusion */
+  dwdxp = (W(ip, j, k) - W(i, j, k)) * dxi;
+  dwdxm = (W(i, j, k) - W(im, j, k)) * dxi;
+  dwdyp = (W(i, jp, k) - W(i, j, k)) * dyi;
+  dwdym = (W(i, j, k) - W(i, jm, k)) * dyi;
+  dwdzp = (W(i, j, kp) - W(i, j, k)) * ZFI(kp);
+  dwdzm = (W(i, j, k) - W(i, j, km)) * ZFI(k);
+  if (variant == 2) {
+    *dw = adv_w + (dxi * (dwdxp - dwdxm) + dyi * (dwdyp - dwdym) + ZCI(k) * (dwdzp - dwdzm)) * visc_sp;
+  } else {
+    dudzp = (U(i, j, kp) - U(i, j, k)) * ZCI(k);
+    dudzm = (U(im, j, kp) - U(im, j, k)) * ZCI(k);
+    dvdzp = (V(i, j, kp) - V(i, j, k)) * ZCI(k);
+    dvdzm = (V(i, jm, kp) - V(i, jm, k)) * ZCI(k);
+    muxp = 0.25 * (MU(i, j, k) + MU(i, j, kp) + MU(ip, j, kp) + MU(ip, j, k));
+    muxm = 0.25 * (MU(i, j, k) + MU(i, j, kp) + MU(im, j, kp) + MU(im, j, k));
+    muyp = 0.25 * (MU(i, j, k) + MU(i, j, kp) + MU(i, jp, kp) + MU(i, jp, k));
+    muym = 0.25 * (MU(i, j, k) + MU(i, j, kp) + MU(i, jm, kp) + MU(i, jm, k));
+    muzp = MU(i, j, kp);
+    muzm = MU(i, j, k);
+    rhoz = 0.5 * (RHO(i, j, kp) + RHO(i, j, k));
+    *dw = adv_w + (dxi * ((dwdxp + dudzp) * muxp - (dwdxm + dudzm) * muxm) +
+                   dyi * ((dwdyp + dvdzp) * muyp - (dwdym + dvdzm) * muym) +
+                   ZCI(k) * ((dwdzp + dwdzp) * muzp - (dwdzm + dwdzm) * muzm)) / rhoz;
+  }
+#undef U
+#undef V
+#undef W
+#undef MU
+#undef RHO
+#undef ZCI
+#undef ZFI
+}
+
+void or_momad(int variant, int nx, int ny, int nz, double dxi, double dyi, double dzi, int nh_d, int nh_u,
+              const double *dzci, const double *dzfi, const double *u, const double *v, const double *w,
+              const double *mu, const double *rho, double visc_sp, double *dudt, double *dvdt, double *dwdt) {
+#pragma omp parallel for num_threads(NT) schedule(static)
+  for (int k = 1; k <= nz; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++)
+        mom_cell(variant, nx, ny, nz, dxi, dyi, dzi, nh_d, nh_u, dzci, dzfi, u, v, w, mu, rho, visc_sp, i, j, k,
+                 &DT3(dudt, i, j, k), &DT3(dvdt, i, j, k), &DT3(dwdt, i, j, k));
+}
+
+void or_rk(int variant, double f_t1, double f_t2, int nx, int ny, int nz, double dxi, double dyi, double dzi,
+           int nh_d, int nh_u, const double *dzci, const double *dzfi, double *u, double *v, double *w,
+           const double *mu, const double *rho, double visc_sp, double *dudtrko, double *dvdtrko,
+           double *dwdtrko) {
+  /* rk.f90:54-97: the right-hand sides from the old velocities first, then the update */
+  const long N = (long)nx * ny * nz, h = nh_u, UX = nx + 2 * h, UY = ny + 2 * h;
+  double *d = (double *)malloc(sizeof(double) * 3 * (size_t)N);
+  double *du = d, *dv = d + N, *dw = d + 2 * N;
+  or_momad(variant, nx, ny, nz, dxi, dyi, dzi, nh_d, nh_u, dzci, dzfi, u, v, w, mu, rho, visc_sp, du, dv, dw);
+#pragma omp parallel for num_threads(NT) schedule(static)
+  for (int k = 1; k <= nz; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        const long t = (i - 1) + (long)nx * ((j - 1) + (long)ny * (k - 1));
+        u[UIDX(i, j, k)] = u[UIDX(i, j, k)] + f_t1 * du[t] + f_t2 * dudtrko[t];
+        v[UIDX(i, j, k)] = v[UIDX(i, j, k)] + f_t1 * dv[t] + f_t2 * dvdtrko[t];
+        w[UIDX(i, j, k)] = w[UIDX(i, j, k)] + f_t1 * dw[t] + f_t2 * dwdtrko[t];
+        dudtrko[t] = du[t];
+        dvdtrko[t] = dv[t];
+        dwdtrko[t] = dw[t];
+      }
+  free(d);
+}
+
+int or_cmpt_time_factors(const char *time_scheme, int istep, int irk_ss, const double *rkcoeff, double dt,
+                         double dto, double *f) {
+  /* rk.f90:104-135; rkcoeff(2,3) in memory order; f = f_t1, f_t2, f_t12 */
+  if (!strncmp(time_scheme, "ab2", 3)) {
+    if (istep == 1) { f[0] = 1.0 * dt; f[1] = 0.0 * dt; }
+    else { f[0] = (1.0 + 0.5 * (dt / dto)) * dt; f[1] = (-0.5 * (dt / dto)) * dt; }
+  } else if (!strncmp(time_scheme, "rk3", 3)) {
+    if (irk_ss < 1 || irk_ss > 3) return -1;
+    f[0] = rkcoeff[0 + 2 * (irk_ss - 1)] * dt;
+    f[1] = rkcoeff[1 + 2 * (irk_ss - 1)] * dt;
+  } else return -1;
+  f[2] = f[0] + f[1];
+  return 0;
+}
+#undef DT3

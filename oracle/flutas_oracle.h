@@ -103,6 +103,17 @@ void or_residual(const int n[3], const char cbc[6], double dxi, double dyi, int 
                  const double *p, double *r);
 
 /* OpenMP threads used by the parallel loops (0 = library default). */
+/* momentum predictor (src/mom.f90, src/rk.f90): variant 0 momad_xyz_tw_cen, 1 momad_xyz_tw_fll,
+ * 2 momad_xyz_sp (visc_sp = mu_sp/rho_sp; mu, rho unused) */
+void or_momad(int variant, int nx, int ny, int nz, double dxi, double dyi, double dzi, int nh_d, int nh_u,
+              const double *dzci, const double *dzfi, const double *u, const double *v, const double *w,
+              const double *mu, const double *rho, double visc_sp, double *dudt, double *dvdt, double *dwdt);
+void or_rk(int variant, double f_t1, double f_t2, int nx, int ny, int nz, double dxi, double dyi, double dzi,
+           int nh_d, int nh_u, const double *dzci, const double *dzfi, double *u, double *v, double *w,
+           const double *mu, const double *rho, double visc_sp, double *dudtrko, double *dvdtrko,
+           double *dwdtrko);
+int  or_cmpt_time_factors(const char *time_scheme, int istep, int irk_ss, const double *rkcoeff, double dt,
+                          double dto, double *f);
 void or_set_threads(int nthreads);
 int  or_get_threads(void);
 

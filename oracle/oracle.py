@@ -77,6 +77,10 @@ def lib():
         L.or_update_property.argtypes = [C.c_int] * 3 + [C.c_double] * 2 + [_dp, _dp]
         L.or_residual.argtypes = [C.c_int * 3, C.c_char_p, C.c_double, C.c_double, C.c_int, _dp,
                                   _dp, _dp, _dp, _dp]
+        L.or_momad.argtypes = [C.c_int] * 4 + [C.c_double] * 3 + [C.c_int] * 2 + [_dp] * 7 + [C.c_double] + [_dp] * 3
+        L.or_rk.argtypes = [C.c_int, C.c_double, C.c_double] + [C.c_int] * 3 + [C.c_double] * 3 + [C.c_int] * 2 + \
+            [_dp] * 7 + [C.c_double] + [_dp] * 3
+        L.or_cmpt_time_factors.argtypes = [C.c_char_p, C.c_int, C.c_int, _dp, C.c_double, C.c_double, _dp]
         L.or_set_threads.argtypes = [C.c_int]
         L.or_get_threads.restype = C.c_int
         _lib = L
@@ -206,3 +210,37 @@ def residual(n, cbc, dxi, dyi, nh_d, dzci, dzfi, f, p):
     r = np.zeros_like(f)
     lib().or_residual((C.c_int * 3)(*n), _b(cbc), dxi, dyi, nh_d, dzci, dzfi, f, p, r)
     return r
+
+
+MOM_VARIANTS = {"cen": 0, "fll": 1, "sp": 2}
+
+
+def momad(variant, n, dxi, dyi, dzi, nh_d, nh_u, dzci, dzfi, u, v, w, mu=None, rho=None, visc_sp=0.0):
+    """momad_xyz_tw_cen / _tw_fll / _sp (src/mom.f90): returns dudt, dvdt, dwdt, shape (nz, ny, nx)."""
+    nx, ny, nz = [int(x) for x in n]
+    out = [np.empty((nz, ny, nx)) for _ in range(3)]
+    dummy = np.zeros((nz + 2, ny + 2, nx + 2))
+    lib().or_momad(MOM_VARIANTS[variant], nx, ny, nz, dxi, dyi, dzi, nh_d, nh_u, dzci, dzfi, u, v, w,
+                   dummy if mu is None else mu, dummy if rho is None else rho, float(visc_sp), *out)
+    return out
+
+
+def rk(variant, f_t1, f_t2, n, dxi, dyi, dzi, nh_d, nh_u, dzci, dzfi, u, v, w, mu, rho, dudtrko, dvdtrko,
+       dwdtrko, visc_sp=0.0):
+    """rk (src/rk.f90:26-102), in place on u, v, w and the previous right-hand sides."""
+    nx, ny, nz = [int(x) for x in n]
+    dummy = np.zeros((nz + 2, ny + 2, nx + 2))
+    lib().or_rk(MOM_VARIANTS[variant], f_t1, f_t2, nx, ny, nz, dxi, dyi, dzi, nh_d, nh_u, dzci, dzfi, u, v, w,
+                dummy if mu is None else mu, dummy if rho is None else rho, float(visc_sp), dudtrko, dvdtrko,
+                dwdtrko)
+
+
+def cmpt_time_factors(time_scheme, istep, irk_ss, rkcoeff, dt, dto):
+    """cmpt_time_factors (src/rk.f90:104-135): f_t1, f_t2, f_t12."""
+    f = np.zeros(3)
+    rc = lib().or_cmpt_time_factors(_b(time_scheme), int(istep), int(irk_ss),
+                                    np.ascontiguousarray(rkcoeff, dtype=np.float64).ravel(order="F"),
+                                    float(dt), float(dto), f)
+    if rc != 0:
+        raise ValueError("cmpt_time_factors: bad time scheme")
+    return tuple(f)

@@ -109,3 +109,17 @@ def test_initgrid_matches_the_oracle(lib, oracle):
     import pytest
     with pytest.raises(lib.FlutasError):
         lib.initgrid("zer", 4, 1.0, 1.0, 5)  # halo wider than the grid
+
+
+def test_cmpt_time_factors_matches_the_oracle(lib, oracle):
+    """cmpt_time_factors (src/rk.f90:104-135): AB2 (Euler at the first step) and the
+    three RK3 substeps with the apps' rkcoeff, bit for bit; a bad scheme is refused."""
+    import pytest
+    rkcoeff = np.array([[32 / 60, 0.0], [25 / 60, -17 / 60], [45 / 60, -25 / 60]]).T  # rkcoeff(2,3)
+    for ts, istep, irk in (("ab2", 1, 1), ("ab2", 7, 1), ("rk3", 3, 1), ("rk3", 3, 2), ("rk3", 3, 3)):
+        got = lib.cmpt_time_factors(ts, False, istep, irk, rkcoeff, 1.3e-3, 1.1e-3)
+        ref = oracle.cmpt_time_factors(ts, istep, irk, rkcoeff, 1.3e-3, 1.1e-3)
+        assert got == tuple(float(x) for x in ref), (ts, istep, irk)
+    with pytest.raises(lib.FlutasError) as e:
+        lib.cmpt_time_factors("ab3", False, 1, 1, rkcoeff, 1e-3, 1e-3)
+    assert e.value.code == lib.FLUTAS_EINVAL

@@ -19,7 +19,7 @@ HDR = os.path.join(ROOT, "include", "flutas_gb300.h")
 # src/initsolver.f90:21, src/solver_cpu.f90:20, src/solver_gpu.f90:31, src/fillps.f90:16,
 # src/correc.f90:16, src/bound.f90:146, src/bound.f90:17, src/bound.f90:829,
 # src/chkdiv.f90:18, src/source.f90:247, src/fft.f90:159, src/vof.f90:240, src/load.f90:21,
-# src/initgrid.f90:17
+# src/initgrid.f90:17, src/rk.f90:26, src/rk.f90:104
 REFERENCE_ARGS = {
     "initsolver": "n,dims,dims_z,dli,nh_d,dzci,dzfi,cbc,bc,c_or_f,lambdaxy,a,b,c,arrplan,normfft,rhsbx,rhsby,rhsbz",
     "solver_cpu": "n,arrplan,normfft,lambdaxy,a,b,c,bcz,c_or_f,p",
@@ -35,11 +35,14 @@ REFERENCE_ARGS = {
     "update_property": "n,prop12,vof,prop",
     "load": "io,filename,n,fld",
     "initgrid": "inivel,n,gr,lz,nh_d,dzc,dzf,zc,zf",
+    "rk": "space_scheme_mom,f_t1,f_t2,nx,ny,nz,dxi,dyi,dzi,nh_d,nh_u,dzci,dzfi,u,v,w,mu,rho,dudtrko,dvdtrko,dwdtrko",
+    "cmpt_time_factors": "time_scheme,restart,istep,irk_ss,rkcoeff,dt,dto,f_t1,f_t2,f_t12",
 }
 
 
 def _strip_comments(src):
-    return "\n".join(line.split("!")[0] for line in src.splitlines())
+    # comments and preprocessor lines (the module is preprocessed like the reference's sources)
+    return "\n".join(line.split("!")[0] for line in src.splitlines() if not line.lstrip().startswith("#"))
 
 
 def _join_continuations(src):
