@@ -9,6 +9,7 @@
 // requests of the same grid signature and are evicted least-recently-used when
 // the budget needs room.  Built only on the public C ABI of this library.
 #include "../../include/flutas_gb300.h"
+#include "ptrcheck.h"
 
 #include <cuda_runtime.h>
 
@@ -100,8 +101,30 @@ struct flutas_server {
 
 namespace {
 
-// Device bytes a request needs besides its plan: its fields.
+// Device memory of the current device (or managed): such arrays are used in place.
+bool resident(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  const bool ok = cudaPointerGetAttributes(&at, p) == cudaSuccess;
+  if (!ok) cudaGetLastError();
+  int cur = 0;
+  cudaGetDevice(&cur);
+  return fg::classify_ptr(ok, ok ? (int)at.type : 0, ok ? at.device : -1, cur) == fg::PTR_DEVICE;
+}
+
+// Every field of the request already lives on the device: the request is
+// solved in place, with no staging copies and no field memory of its own.
+// (A two-phase projection takes the staged path: its pold is an input of the
+// request, which the in-place call would overwrite with p^n.)
+bool fields_resident(const flutas_request &r) {
+  if (r.kind == 0) return resident(r.rhs) && resident(r.p);
+  return !r.rho && resident(r.u) && resident(r.v) && resident(r.w) && resident(r.p);
+}
+
+// Device bytes a request needs besides its plan: its fields (none when they
+// are resident already).
 size_t field_bytes(const flutas_request &r) {
+  if (fields_resident(r)) return 0;
   const size_t p = sizeof(double) * cells_halo(r.n, 1);
   if (r.kind == 0) return p;
   const size_t uvw = 3 * sizeof(double) * cells_halo(r.n, r.nh_u);
@@ -205,11 +228,17 @@ int run_request(flutas_server *s, Request *q, PlanEntry *pe, cudaStream_t st) {
     for (double *b : bufs) cudaFreeAsync(b, st);
     cudaStreamSynchronize(st);
   };
+  const bool in_place = fields_resident(r);
   if (r.kind == 0) {
     double *x = nullptr;
-    if ((rc = dmalloc(pb, &x))) return rc;
-    bufs.push_back(x);
-    cudaMemcpyAsync(x, r.rhs, pb, cudaMemcpyDefault, st);
+    if (in_place) {  // the solution array itself holds the RHS during the solve
+      x = r.p;
+      if ((const double *)x != r.rhs) cudaMemcpyAsync(x, r.rhs, pb, cudaMemcpyDeviceToDevice, st);
+    } else {
+      if ((rc = dmalloc(pb, &x))) return rc;
+      bufs.push_back(x);
+      cudaMemcpyAsync(x, r.rhs, pb, cudaMemcpyDefault, st);
+    }
     if (r.tol > 0.0) {
       rc = flutas_gb300_solve_mixed(plan, x, r.tol, r.max_iter, &q->relres, &q->iters);
     } else {  // tol = 0: the plain FP64 solver call (the drop-in form)
@@ -218,7 +247,17 @@ int run_request(flutas_server *s, Request *q, PlanEntry *pe, cudaStream_t st) {
       q->relres = 0.0;
       q->iters = 0;
     }
-    if (rc == 0 || rc == FLUTAS_EITER) cudaMemcpyAsync(r.p, x, pb, cudaMemcpyDefault, st);
+    if (!in_place && (rc == 0 || rc == FLUTAS_EITER)) cudaMemcpyAsync(r.p, x, pb, cudaMemcpyDefault, st);
+  } else if (in_place) {
+    const double bc6[6] = {0, 0, 0, 0, 0, 0};
+    const double *bcp = r.bcpre ? r.bcpre : bc6;
+    const char *cv = q->cbcvel.empty() ? nullptr : q->cbcvel.c_str();
+    const double *bv = q->bcvel.empty() ? nullptr : q->bcvel.data();
+    const int prec = r.tol > 0.0 ? 1 : 0;
+    // dzci / dzfi are host arrays of the request: the projection stages them
+    rc = flutas_gb300_projection(plan, r.nh_u, r.dli[0], r.dli[1], q->sig.dzci.data(), q->sig.dzfi.data(), bcp, cv,
+                                 bv, r.dt, r.rho0, r.u, r.v, r.w, r.p, prec, r.tol, r.max_iter);
+    if (prec) flutas_gb300_last_solve(plan, &q->relres, &q->iters);
   } else {
     const size_t ub = sizeof(double) * cells_halo(r.n, r.nh_u);
     double *u, *v, *w, *p, *rho = nullptr, *pold = nullptr;

@@ -262,6 +262,11 @@ FLUTAS_API int flutas_gb300_batch_destroy(void *batch);
  * requests overlap on the device.  Plans stay resident between requests of
  * the same grid and are evicted least-recently-used when the budget needs
  * room.  The caller's arrays must stay valid until server_wait returns.
+ * Fields that already live on the device (device memory of the current
+ * device, or managed) are solved in place, with no staging copy and no field
+ * memory charged to the budget (a two-phase projection's fields are always
+ * staged: its pold is an input the in-place call would overwrite).  Host
+ * fields are copied to server-owned device buffers and back.
  * ------------------------------------------------------------------------- */
 typedef struct {
   int kind;                    /* 0: Poisson solve rhs -> p; 1: projection of u,v,w,p */

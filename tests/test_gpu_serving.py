@@ -120,3 +120,24 @@ def test_serving_fp64_requests(lib):
         alone = r["rhs"].copy()
         P.solver(alone)
         assert np.array_equal(o[1:-1, 1:-1, 1:-1], alone[1:-1, 1:-1, 1:-1])
+
+
+def test_serving_device_resident_fields(lib):
+    """Requests whose arrays live on the device are solved in place (no staging
+    copies, no field memory charged to the budget): the same result as the host-array
+    request, bit for bit, and the RHS array is left as it was."""
+    import torch
+    reqs = _requests(seed=21)[:4]
+    S = lib.Server(hbm_budget_bytes=8 << 30, slots=2)
+    host_out = [np.zeros_like(r["rhs"]) for r in reqs]
+    dev_rhs = [torch.from_numpy(r["rhs"]).cuda() for r in reqs]
+    dev_out = [torch.zeros_like(t) for t in dev_rhs]
+    th = [S.submit_solve(r["n"], r["dli"], r["dzci"], r["dzfi"], r["cbc"], r["rhs"], o, tol=r["tol"])
+          for r, o in zip(reqs, host_out)]
+    td = [S.submit_solve(r["n"], r["dli"], r["dzci"], r["dzfi"], r["cbc"], x, o, tol=r["tol"])
+          for r, x, o in zip(reqs, dev_rhs, dev_out)]
+    assert all(S.wait(t)[0] == 0 for t in th + td)
+    S.close()
+    for a, b in zip(host_out, dev_out):
+        assert np.array_equal(a, b.cpu().numpy())
+    assert all(np.array_equal(r["rhs"], x.cpu().numpy()) for r, x in zip(reqs, dev_rhs))
