@@ -95,6 +95,9 @@ BYTES_PER_CELL = {
     "k_xyinv_cluster<f32,halo>": 12,
     "k_xyinv_cluster<f32,haloadd>": 20,
     "k_xyfwd_cluster<f64,fillps>": 32,
+    "k_xyfwd_cluster<f64,plain>": 16,   # R S W S (FP64, in place)
+    "k_xyfwd_plane<f64,plain>": 16,
+    "k_stencil<f64,fillps>": 32,        # R u,v,w (24) W S FP64 (8)
     "k_xyfwd_cluster<f64,halo>": 16,
     "k_xyinv_cluster<f64,halo>": 16,
     "k_xyfwd_fix<f32,f32>": 8,      # R S W S (in place)
@@ -108,7 +111,7 @@ BYTES_PER_CELL = {
 # FP64 instructions per cell of the FP64-bound kernels (the part's FP64 rate,
 # not HBM, bounds them): DF increments 3x(2 sub + 1 add), fillps 3 sub + 1 mul
 # + 2 fma, residual 2 add + 5 fma, correc 3x(sub + fma) + 1 add.
-FP64_PER_CELL = {"k_pres_tw_src": 9, "k_stencil<fillps>": 6, "k_stencil<residual>": 7, "k_resnorm": 7,
+FP64_PER_CELL = {"k_stencil<f64,fillps>": 6, "k_pres_tw_src": 9, "k_stencil<fillps>": 6, "k_stencil<residual>": 7, "k_resnorm": 7,
                  "k_correc_padd": 7, "k_resnorm_correc": 14}
 FP64_PEAK_TOPS = 0.60   # FP64 FMA instructions/s measured on this part (1.20 TFLOP/s counting an FMA as 2)
 
@@ -333,6 +336,7 @@ def run_ours(args, rank, world, local_rank):
     # timed region of its own: the events add host and device work, kept out of the headline
     prof_steps = max(5, args.steps // 2)
     t_prof, _, _, _, rep, _ = timed(1, 1e-10, prof_steps, 1, profile=True)
+    _, _, _, _, rep64, _ = timed(0, 0.0, 3, 1, profile=True)  # the FP64 form's kernel split
     clocks = clk.stop()
 
     # accuracy of one mixed step against one FP64 step on the same input
@@ -447,7 +451,9 @@ def run_ours(args, rank, world, local_rank):
                 "fp64": {"solves_per_s": round(world * len(lat_64) / (t_64 / 1e3), 3),
                          "ms_per_step": round(t_64 / len(lat_64), 4),
                          "p50_ms": round(float(np.percentile(lat_64, 50)), 4),
-                         "p99_ms": round(float(np.percentile(lat_64, 99)), 4)},
+                         "p99_ms": round(float(np.percentile(lat_64, 99)), 4),
+                         "roofline": roofline_of(rep64, ncell, n)[0],
+                         "kernels": roofline_of(rep64, ncell, n)[1]},
             },
             "accuracy": accuracy_block(n, relres_mix, err_p, err_u, divmax, divmax64, vs_oracle),
             "e2e": {"value": round(world * e2e_steps / (t_e2e / 1e3), 3), "unit": "projections/s",
@@ -462,6 +468,15 @@ def run_ours(args, rank, world, local_rank):
         }
         if not args.no_cpu_baseline:
             res["cpu_baseline"] = cpu_baseline(n, pristine, budget_s=args.cpu_budget, state=cpu_state)
+    if rank == 0 and not args.no_extras:
+        del pristine, fa, fb, f_mix, f_64, host, hnp
+        torch.cuda.empty_cache()
+        import copy
+        res["batch"] = batch_summary(args)
+        torch.cuda.empty_cache()
+        sa = copy.copy(args)
+        sa.requests, sa.rates = args.serve_requests, [0.5, 0.8, 1.1]
+        res["serving"] = run_serve(sa)
     return res
 
 
@@ -481,6 +496,33 @@ def accuracy_block(n, relres_mix, err_p, err_u, divmax, divmax64, vs_oracle):
         acc["fp64_parity_1e-12"] = bool(vs_oracle["fp64_vs_oracle_rel_l2_phi"] <= 1e-12 and
                                         vs_oracle["fp64_vs_oracle_rel_l2_u"] <= 1e-12)
     return acc
+
+
+def roofline_of(rep, ncell, n):
+    """Roofline entry of the kernel with the largest total time in a profiled region:
+    algorithmic bytes per launch / its mean CUDA-event duration, against the measured
+    HBM peak; for the FP64-bound kernels also the FP64 instruction rate."""
+    if not rep:
+        return None, {}
+    hbm, src = peaks()
+    tot = sum(v[1] for v in rep.values())
+    shares = {k: {"launches": v[0], "ms": round(v[1], 4), "share": round(v[1] / tot, 4)}
+              for k, v in sorted(rep.items(), key=lambda kv: -kv[1][1])}
+    name, (cnt, ms) = max(rep.items(), key=lambda kv: kv[1][1])
+    bpc = BYTES_PER_CELL.get(name)
+    if not bpc:
+        return {"kernel": name, "note": "no byte model for this kernel"}, shares
+    achieved = bpc * ncell / (ms / cnt / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "peak_source": src, "bytes_per_launch": bpc * ncell,
+            "traffic": ncu_traffic(name, n)}
+    f64 = FP64_PER_CELL.get(name)
+    if f64:
+        ops = f64 * ncell / (ms / cnt / 1e3) / 1e12
+        roof["fp64"] = {"instr_per_cell": f64, "achieved_tinstr_s": round(ops, 4), "peak_tinstr_s": FP64_PEAK_TOPS,
+                        "frac": round(ops / FP64_PEAK_TOPS, 4),
+                        "note": "FP64 FMA/add instructions; the binding roof of this kernel"}
+    return roof, shares
 
 
 def ncu_traffic(kernel, n):
@@ -610,7 +652,7 @@ def batch_grids(count, seed):
     return grids
 
 
-def run_batch(args):
+def run_batch(args, keep=False):
     import torch
     import flutas_gb300 as F
     F.load()
@@ -675,7 +717,7 @@ def run_batch(args):
         P.fftend()
     ms = float(np.median(times))
     scale = len(grids) / len(sample)
-    return {"mode": "batch", "metric": "grids solved/s (mixed precision to 1e-10)", "grids": len(grids),
+    out = {"mode": "batch", "metric": "grids solved/s (mixed precision to 1e-10)", "grids": len(grids),
             "cells": cells, "value": round(len(grids) / (ms / 1e3), 2), "unit": "grids/s",
             "ms_per_batch": round(ms, 3), "cells_per_s": round(cells / (ms / 1e3), 1),
             "max_relres": float(np.max(rels)), "fp32_solves_per_grid": {
@@ -687,6 +729,11 @@ def run_batch(args):
                                            round(t_seq_mixed * scale * 1e3, 2)},
             "steps": args.steps, "warmup": args.warmup,
             "timing": "CUDA events around each batch solve; RHS reloaded (device copies) between solves, untimed"}
+    if keep:
+        out.update({"_batch": B, "_grids": grids, "_rhs": rhs, "_iters": iters[-1]})
+    else:
+        B.destroy()
+    return out
 
 
 # ----------------------------------------------------------------- serving mode
@@ -703,55 +750,71 @@ def serve_sizes(rng, count):
     return out
 
 
-def run_serve(args):
+def run_serve(args, classes_n=32, fp64_sample=400):
+    """C5 stream: Poisson requests of log-uniform volume (64^3..384^3, aspect <= 4:1)
+    drawn from `classes_n` grid shapes, 30% with a two-phase (density-jump) RHS,
+    tolerance 1e-6 or 1e-10 (50/50), fields resident on the device (the server solves
+    them in place), admission under the HBM budget, Poisson arrivals at fractions of
+    the measured capacity; the same stream in FP64 through the server, and the plain
+    FP64 drop-in solver on a sample of it."""
     import torch
     import flutas_gb300 as F
     F.load()
     rng = np.random.default_rng(args.seed)
-    # 16 grid shapes drawn log-uniformly in volume (64^3..384^3, aspect <= 4:1);
-    # requests pick a shape uniformly, so their volumes stay log-uniform
-    classes = sorted({tuple(s) for s in serve_sizes(rng, 16)})
+    classes = []
+    while len(classes) < classes_n:
+        for c in serve_sizes(rng, classes_n):
+            if tuple(c) not in classes and len(classes) < classes_n:
+                classes.append(tuple(c))
+    classes.sort()
     sizes = [classes[i] for i in rng.integers(0, len(classes), args.requests)]
-    # one single-phase and one two-phase RHS per size class (pinned host memory)
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev).manual_seed(args.seed)
     rhs = {}
     for c in classes:
         nx, ny, nz = c
         for kind in ("1p", "2p"):
-            f = torch.empty((nz + 2, ny + 2, nx + 2), dtype=torch.float64).pin_memory()
-            g = rng.uniform(-1, 1, (nz, ny, nx))
-            if kind == "2p":  # density-jump structure of a two-phase RHS: large values inside drops
-                zz, yy, xx = np.meshgrid(*(np.linspace(0, 1, m) for m in (nz, ny, nx)), indexing="ij")
+            f = torch.zeros((nz + 2, ny + 2, nx + 2), dtype=torch.float64, device=dev)
+            v = 2.0 * torch.rand((nz, ny, nx), generator=g, dtype=torch.float64, device=dev) - 1.0
+            if kind == "2p":  # density-jump structure of a two-phase RHS: large values inside a drop
+                zz, yy, xx = torch.meshgrid(*(torch.linspace(0, 1, m, device=dev, dtype=torch.float64)
+                                              for m in (nz, ny, nx)), indexing="ij")
                 drop = ((xx - 0.5) ** 2 + (yy - 0.5) ** 2 + (zz - 0.5) ** 2) < 0.04
-                g = g * np.where(drop, float(np.exp(rng.uniform(np.log(10), np.log(1000)))), 1.0)
-            g -= g.mean()
-            f.zero_()
-            f[1:-1, 1:-1, 1:-1] = torch.from_numpy(g)
+                v = v * torch.where(drop, float(np.exp(rng.uniform(np.log(10), np.log(1000)))), 1.0)
+                del zz, yy, xx, drop
+            v -= v.mean()  # compatible with the singular (periodic x, y, Neumann z) problem
+            f[1:-1, 1:-1, 1:-1] = v
             rhs[(c, kind)] = f
-    outs = {c: [torch.empty((c[2] + 2, c[1] + 2, c[0] + 2), dtype=torch.float64).pin_memory() for _ in range(4)]
-            for c in classes}
+    nout = 6
+    outs = {c: [torch.empty_like(rhs[(c, "1p")]) for _ in range(nout)] for c in classes}
+    torch.cuda.synchronize()
     dz = {c: np.full(c[2] + 2, float(c[2])) for c in classes}
     reqs = []
-    for i, s in enumerate(sizes):
+    for s in sizes:
         kind = "2p" if rng.uniform() < 0.3 else "1p"
         tol = 1e-6 if rng.uniform() < 0.5 else 1e-10
         reqs.append((tuple(s), kind, tol))
+    occ = {}
+    slot = []
+    for c, _, _ in reqs:  # the k-th request of a class writes output k mod nout
+        slot.append(occ.get(c, 0) % nout)
+        occ[c] = occ.get(c, 0) + 1
     S = F.Server(hbm_budget_bytes=int(args.budget_gb * (1 << 30)), slots=args.slots)
 
-    def submit(c, kind, tol, k):
-        return S.submit_solve(c, [float(c[0]), float(c[1]), float(c[2])], dz[c], dz[c], "PPPPNN",
-                              rhs[(c, kind)].numpy(), outs[c][k % 4].numpy(), tol=tol, max_iter=8)
+    def submit(i, tol=None):
+        c, kind, t = reqs[i]
+        return S.submit_solve(c, [float(c[0]), float(c[1]), float(c[2])], dz[c], dz[c], "PPPPNN", rhs[(c, kind)],
+                              outs[c][slot[i]], tol=t if tol is None else tol, max_iter=8)
 
-    # warm: one request per class (plans become resident)
-    for j, c in enumerate(classes):
-        S.wait(submit(c, "1p", 1e-6, j))
-    # capacity: everything submitted at once
+    for j, c in enumerate(classes):  # warm: plans become resident
+        S.wait(S.submit_solve(c, [float(c[0]), float(c[1]), float(c[2])], dz[c], dz[c], "PPPPNN", rhs[(c, "1p")],
+                              outs[c][0], tol=1e-6, max_iter=8))
     S.reset_stats()
     t0 = time.perf_counter()
-    ts = [submit(c, kind, tol, i) for i, (c, kind, tol) in enumerate(reqs)]
-    for t in ts:
-        S.wait(t)
-    cap_span = time.perf_counter() - t0
-    capacity = len(reqs) / cap_span
+    ts = [submit(i) for i in range(len(reqs))]
+    cap_stat = [S.wait(t) for t in ts]
+    capacity = len(reqs) / (time.perf_counter() - t0)
+    overlap = S.stats().get("max_device_overlap")
     sweep = []
     for frac in args.rates:
         rate = frac * capacity
@@ -760,63 +823,98 @@ def run_serve(args):
         t0 = time.perf_counter()
         tick = t0
         ts = []
-        for i, (c, kind, tol) in enumerate(reqs):
+        for i in range(len(reqs)):
             tick += gaps[i]
             dt_ = tick - time.perf_counter()
             if dt_ > 0:
                 time.sleep(dt_)
-            ts.append(submit(c, kind, tol, i))
+            ts.append(submit(i))
         stat = [S.wait(t) for t in ts]
         span = time.perf_counter() - t0
         st = S.stats()
-        codes = {}
-        worst = {}
+        codes, worst = {}, {}
         for (c, kind, tol), x in zip(reqs, stat):
             if x[0] != 0:
                 codes[str(x[0])] = codes.get(str(x[0]), 0) + 1
             key = f"{kind}@{tol:g}"
             worst[key] = max(worst.get(key, 0.0), x[1])
-        sweep.append({"offered_per_s": round(rate, 2), "solves_per_s": round(len(reqs) / span, 2),
-                      "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+        sweep.append({"offered_fraction": frac, "offered_per_s": round(rate, 2),
+                      "solves_per_s": round(len(reqs) / span, 2), "p50_ms": round(st["p50_ms"], 3),
+                      "p99_ms": round(st["p99_ms"], 3), "max_device_overlap": st.get("max_device_overlap"),
                       "nonzero_status": codes, "worst_relres": worst})
-    # the same request stream in FP64 through the same server (tol = 0 selects the FP64 path)
+    # the same stream in FP64 through the same server (tol = 0 selects the drop-in solver)
     S.reset_stats()
     t0 = time.perf_counter()
-    ts = [submit(c, kind, 0.0, i) for i, (c, kind, tol) in enumerate(reqs)]
+    ts = [submit(i, tol=0.0) for i in range(len(reqs))]
     for t in ts:
         S.wait(t)
     cap64 = len(reqs) / (time.perf_counter() - t0)
     S.close()
-    # the plain FP64 drop-in solver call with host arrays, as a FluTAS app makes
-    # it, one request after another over the same stream (solver call timed)
-    plans = {}
-    t_fp64 = 0.0
-    lat64 = []
-    for c, kind, tol in reqs:
-        x = outs[c][0].numpy()
+    # the plain FP64 drop-in solver call on device arrays, one request after another (a sample)
+    plans, lat64 = {}, []
+    sample = reqs[:fp64_sample]
+    for c, kind, tol in sample:
+        x = outs[c][0]
         if c not in plans:
             plans[c] = F.initsolver(c, [float(c[0]), float(c[1]), float(c[2])], 1, dz[c], dz[c], "PPPPNN", [0.0] * 6)
-            np.copyto(x, rhs[(c, kind)].numpy())
+            x.copy_(rhs[(c, kind)])
             plans[c].solver(x)
-        np.copyto(x, rhs[(c, kind)].numpy())
+        x.copy_(rhs[(c, kind)])
+        torch.cuda.synchronize()
         t1 = time.perf_counter()
         plans[c].solver(x)
-        dt_ = time.perf_counter() - t1
-        t_fp64 += dt_
-        lat64.append(dt_ * 1e3)
+        lat64.append((time.perf_counter() - t1) * 1e3)
+    for P in plans.values():
+        P.fftend()
+    vols = [int(np.prod(c)) for c, _, _ in reqs]
     return {"mode": "serve", "metric": "projection solves/s and p50/p99 latency under a mixed-size stream",
-            "requests": len(reqs), "size_classes": len(classes), "two_phase_frac": 0.3,
-            "tolerances": "1e-6 / 1e-10 (50/50)", "budget_gb": args.budget_gb, "slots": args.slots,
-            "capacity_solves_per_s": round(capacity, 2), "sweep": sweep,
+            "requests": len(reqs), "size_classes": len(classes),
+            "volume_cells": {"min": min(vols), "median": int(np.median(vols)), "max": max(vols)},
+            "two_phase_frac": 0.3, "tolerances": "1e-6 / 1e-10 (50/50)", "budget_gb": args.budget_gb,
+            "slots": args.slots, "fields": "device-resident (solved in place by the server)",
+            "capacity_solves_per_s": round(capacity, 2), "capacity_max_device_overlap": overlap,
+            "capacity_nonzero_status": sum(1 for x in cap_stat if x[0] != 0), "sweep": sweep,
             "fp64_served_capacity_solves_per_s": round(cap64, 2),
-            "fp64_drop_in_sequential": {"solves_per_s": round(len(reqs) / t_fp64, 2),
+            "fp64_drop_in_sequential": {"solves_per_s": round(len(lat64) / (sum(lat64) / 1e3), 2),
                                         "p50_ms": round(float(np.percentile(lat64, 50)), 3),
                                         "p99_ms": round(float(np.percentile(lat64, 99)), 3),
-                                        "note": "solver() with pinned host arrays, one at a time, same requests"},
-            "timing": "host clock; latency = submit to result on host (includes H2D of the RHS and D2H of the "
-                      "solution); Poisson arrivals"}
+                                        "requests": len(lat64),
+                                        "note": "solver() on device arrays, one at a time, the stream's first "
+                                                "requests"},
+            "timing": "host clock; latency = submit to result (device-resident fields); Poisson arrivals"}
 
 
+def batch_summary(args):
+    """C4 inside the headline line: run_batch with a short timed region, its HBM
+    fraction on the mixed-precision byte model (32 B/cell for the first FP32 solve,
+    48 B/cell for each further one), and the residual of a sample of grids
+    recomputed by the FP64 oracle."""
+    import copy
+    a = copy.copy(args)
+    a.steps, a.warmup = 3, 1
+    res = run_batch(a, keep=True)
+    B, grids, rhs, it = res.pop("_batch"), res.pop("_grids"), res.pop("_rhs"), res.pop("_iters")
+    byts = sum(int(np.prod(g["n"])) * (32 + 48 * (int(k) - 1)) for g, k in zip(grids, it))
+    hbm, src = peaks()
+    gbs = byts / (res["ms_per_batch"] / 1e3) / 1e9
+    res["hbm"] = {"bytes_per_batch": byts, "achieved_gbs": round(gbs, 1), "peak_gbs": hbm,
+                  "frac": round(gbs / hbm, 4), "peak_source": src,
+                  "model": "per grid cells x (32 + 48 x (FP32 solves - 1)) bytes"}
+    try:
+        from oracle import oracle as O
+        O.build()
+        worst = 0.0
+        for gi in range(0, len(grids), max(1, len(grids) // 8)):
+            g = grids[gi]
+            x = B.get(gi)
+            f = rhs[gi].cpu().numpy()
+            r = O.residual(g["n"], g["cbc"], g["dli"][0], g["dli"][1], 1, g["dzci"], g["dzfi"], f, x)
+            worst = max(worst, float(np.linalg.norm(r) / np.linalg.norm(f[1:-1, 1:-1, 1:-1])))
+        res["oracle_worst_relres_sample"] = worst
+    except Exception as e:  # the oracle is the checker only; its absence leaves the number out
+        res["oracle_worst_relres_sample"] = f"unavailable: {e}"
+    B.destroy()
+    return res
 
 
 def run_solve(args):
@@ -1051,6 +1149,10 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-oracle", action="store_true", help="skip the oracle step that checks the headline step")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="leave the batch (512 grids) and serving (request stream) summaries out of the headline line")
+    ap.add_argument("--serve-requests", type=int, default=4000,
+                    help="requests of the serving summary in the headline line")
     ap.add_argument("--single", action="store_true",
                     help="only the headline mode (for profiler captures): W warm-up + K steps, no extra modes, "
                          "no e2e, no CPU baseline")
@@ -1059,7 +1161,7 @@ def main():
                     help="projection: the headline two-phase step; batch: 512 uneven grids in one graph; "
                          "serve: Poisson request stream through the continuous-batching server")
     ap.add_argument("--grids", type=int, default=512)
-    ap.add_argument("--requests", type=int, default=1000)
+    ap.add_argument("--requests", type=int, default=4000)
     ap.add_argument("--slots", type=int, default=4)
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--rates", type=float, nargs="+", default=[0.5, 0.8, 1.0, 1.2])
