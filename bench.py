@@ -785,7 +785,7 @@ def run_serve(args, classes_n=32, fp64_sample=400):
             v -= v.mean()  # compatible with the singular (periodic x, y, Neumann z) problem
             f[1:-1, 1:-1, 1:-1] = v
             rhs[(c, kind)] = f
-    nout = 6
+    nout = 12  # outputs per class: two requests of a class in flight at once never share one
     outs = {c: [torch.empty_like(rhs[(c, "1p")]) for _ in range(nout)] for c in classes}
     torch.cuda.synchronize()
     dz = {c: np.full(c[2] + 2, float(c[2])) for c in classes}
@@ -873,7 +873,8 @@ def run_serve(args, classes_n=32, fp64_sample=400):
             "two_phase_frac": 0.3, "tolerances": "1e-6 / 1e-10 (50/50)", "budget_gb": args.budget_gb,
             "slots": args.slots, "fields": "device-resident (solved in place by the server)",
             "capacity_solves_per_s": round(capacity, 2), "capacity_max_device_overlap": overlap,
-            "capacity_nonzero_status": sum(1 for x in cap_stat if x[0] != 0), "sweep": sweep,
+            "capacity_nonzero_status": {str(c): sum(1 for x in cap_stat if x[0] == c)
+                                        for c in sorted({x[0] for x in cap_stat if x[0] != 0})}, "sweep": sweep,
             "fp64_served_capacity_solves_per_s": round(cap64, 2),
             "fp64_drop_in_sequential": {"solves_per_s": round(len(lat64) / (sum(lat64) / 1e3), 2),
                                         "p50_ms": round(float(np.percentile(lat64, 50)), 3),
