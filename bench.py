@@ -98,6 +98,12 @@ BYTES_PER_CELL = {
     "k_xyfwd_cluster<f64,plain>": 16,   # R S W S (FP64, in place)
     "k_xyfwd_plane<f64,plain>": 16,
     "k_stencil<f64,fillps>": 32,        # R u,v,w (24) W S FP64 (8)
+    "k_stencil<df64,fillps>": 32,       # R u,v,w (24) W S double-float (8)
+    "k_xyfwd_cluster<df64,plain>": 16,  # R S W S (double-float, in place)
+    "k_xyinv_cluster<df64,halo>": 16,   # R S W p (FP64)
+    "k_xyfwd_cluster<df64,halo>": 16,
+    "k_xyfwd_plane<df64,plain>": 16,
+    "k_xyinv_plane<df64,halo>": 16,
     "k_xyfwd_cluster<f64,halo>": 16,
     "k_xyinv_cluster<f64,halo>": 16,
     "k_xyfwd_fix<f32,f32>": 8,      # R S W S (in place)
@@ -111,7 +117,7 @@ BYTES_PER_CELL = {
 # FP64 instructions per cell of the FP64-bound kernels (the part's FP64 rate,
 # not HBM, bounds them): DF increments 3x(2 sub + 1 add), fillps 3 sub + 1 mul
 # + 2 fma, residual 2 add + 5 fma, correc 3x(sub + fma) + 1 add.
-FP64_PER_CELL = {"k_stencil<f64,fillps>": 6, "k_pres_tw_src": 9, "k_stencil<fillps>": 6, "k_stencil<residual>": 7, "k_resnorm": 7,
+FP64_PER_CELL = {"k_stencil<f64,fillps>": 6, "k_stencil<df64,fillps>": 6, "k_pres_tw_src": 9, "k_stencil<fillps>": 6, "k_stencil<residual>": 7, "k_resnorm": 7,
                  "k_correc_padd": 7, "k_resnorm_correc": 14}
 FP64_PEAK_TOPS = 0.60   # FP64 FMA instructions/s measured on this part (1.20 TFLOP/s counting an FMA as 2)
 

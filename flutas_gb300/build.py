@@ -71,9 +71,10 @@ def build_emu(verbose: bool = False) -> str:
     """Host-only build of the transform passes (CPU emulator used by the tests)."""
     src = os.path.join(CSRC, "emu.cu")
     deps = [src] + [os.path.join(CSRC, f) for f in ("fft_engine.cuh", "axis_tables.cuh", "fft_fixed.cuh", "bits.cuh",
-                                                   "ghosts.cuh", "ptrcheck.h", "fft_ext.cuh")]
+                                                   "ghosts.cuh", "ptrcheck.h", "fft_ext.cuh", "dd.cuh")]
     if _stale(EMU_LIB, deps):
-        cmd = [nvcc(), "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "--expt-relaxed-constexpr",
+        cmd = [nvcc(), "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-shared",
+               "--expt-relaxed-constexpr",
                "-o", EMU_LIB, src]
         if verbose:
             print(" ".join(cmd), flush=True)

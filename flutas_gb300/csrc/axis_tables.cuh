@@ -28,22 +28,22 @@ inline int fill_axis_tables(int n, int pair, AxisPlan *ap, std::vector<C2<T>> &W
   Q.assign(n, mk<T>(0, 0));
   for (int t = 0; t < ap->N; t++) {
     const long double a = 2.0L * PI * t / ap->N;
-    W[t] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+    W[t] = mk<T>((T)(double)cosl(a), (T)(double)(-sinl(a)));
   }
   if (pr) {
     for (int k = 0; k < n; k++) {
       const long double a = PI * k / (2.0L * n);
-      Q[k] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+      Q[k] = mk<T>((T)(double)cosl(a), (T)(double)(-sinl(a)));
     }
   } else {
     const int h = n / 2;
     for (int j = 0; j < h; j++) {
       const long double a = PI * (4.0L * j + 1.0L) / (4.0L * n);
-      Q[j] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+      Q[j] = mk<T>((T)(double)cosl(a), (T)(double)(-sinl(a)));
     }
     for (int k = 0; k < h; k++) {
       const long double a = PI * k / (long double)n;
-      Q[h + k] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+      Q[h + k] = mk<T>((T)(double)cosl(a), (T)(double)(-sinl(a)));
     }
   }
   return 0;
@@ -68,17 +68,17 @@ inline int fill_ext_tables(int n, int kf, int kb, ExtAxis *ea, std::vector<C2<T>
   W.assign(ea->L, mk<T>(0, 0));
   for (int t = 0; t < ea->L; t++) {
     const long double a = 2.0L * PI * t / ea->L;
-    W[t] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+    W[t] = mk<T>((T)(double)cosl(a), (T)(double)(-sinl(a)));
   }
   Qa.assign(n + 1, mk<T>(0, 0));
   for (int m = 0; m <= n; m++) {
     const long double a = PI * m / (2.0L * n);
-    Qa[m] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+    Qa[m] = mk<T>((T)(double)cosl(a), (T)(double)(-sinl(a)));
   }
   Qb.assign(n, mk<T>(0, 0));
   for (int k = 0; k < n; k++) {
     const long double a = PI * (2.0L * k + 1.0L) / (4.0L * n);
-    Qb[k] = mk<T>((T)cosl(a), (T)(-sinl(a)));
+    Qb[k] = mk<T>((T)(double)cosl(a), (T)(double)(-sinl(a)));
   }
   return 0;
 }

@@ -66,6 +66,7 @@ int run_lines(int pair, int n, int M, int backward, int cols, const double *in, 
 extern "C" __attribute__((visibility("default"))) int fg_emu_lines(int dbl, int pair, int n, int M, int backward,
                                                                    int cols, const double *in, double *out) {
   if (n < 1 || M < 1 || pair < 0 || pair > 4) return -1;
+  if (dbl == 2) return run_lines<dd>(pair, n, M, backward, cols, in, out);  // double-float
   return dbl ? run_lines<double>(pair, n, M, backward, cols, in, out)
              : run_lines<float>(pair, n, M, backward, cols, in, out);
 }

@@ -23,6 +23,8 @@
 #define FG_HD __host__ __device__ __forceinline__
 #endif
 
+#include "dd.cuh"
+
 namespace fg {
 
 // BC-pair codes (the x/y transform kind).
@@ -31,6 +33,10 @@ enum BcPair : int { BC_PP = 0, BC_NN = 1, BC_DD = 2, BC_ND = 3, BC_DN = 4 };
 template <typename T> struct cplx_of;
 template <> struct cplx_of<float> { using type = float2; };
 template <> struct cplx_of<double> { using type = double2; };
+struct dd2 {  // complex double-float (dd.cuh)
+  dd x, y;
+};
+template <> struct cplx_of<dd> { using type = dd2; };
 template <typename T> using C2 = typename cplx_of<T>::type;
 
 template <typename T> FG_HD C2<T> mk(T x, T y) { C2<T> r; r.x = x; r.y = y; return r; }

@@ -385,6 +385,7 @@ struct flutas_plan {
   DBuf czc;            // folded correc factors dt*dzci(k)/rho0
   DBuf zdf;            // per-level factors of the Dodd-Ferrante term
   AxisTables tx64, ty64, tx32, ty32;
+  AxisTables txd, tyd;  // double-float tables of the FP64 solver's transforms (dd.cuh)
   DBuf S64, S32, fbuf, phi, phi2, nrm;
   bool face = false;      // a face-centred axis (c_or_f = 'f')
   bool ext[2] = {false, false};  // x / y transform through the extended FFT (fft_ext.cuh)
@@ -483,7 +484,8 @@ enum KId { KID_XYFWD, KID_XFWD, KID_XYINV, KID_XINV, KID_XYFWD_CL, KID_XYINV_CL,
 template <int KID, typename T, typename F> const char *kname() {
   static const char *base[] = {"k_xyfwd_plane", "k_xfwd", "k_xyinv_plane", "k_xinv", "k_xyfwd_cluster",
                                "k_xyinv_cluster", "k_xyfwd_fix", "k_xyinv_fix"};
-  static const std::string s = std::string(base[KID]) + (sizeof(T) == 8 ? "<f64," : "<f32,") + F::tag + ">";
+  const char *tn = std::is_same<T, dd>::value ? "<df64," : (sizeof(T) == 8 ? "<f64," : "<f32,");
+  static const std::string s = std::string(base[KID]) + tn + F::tag + ">";
   return s.c_str();
 }
 
@@ -601,8 +603,10 @@ int inv_xy(flutas_plan *pl, const T *S, const Out &out, const AxisTables &tx, co
   return 0;
 }
 
-template <typename T>
-int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const double *b, const double *c, bool pin) {
+// T: the arithmetic of the sweeps; ST: the storage of the spectrum (T itself,
+// or double-float pairs for the FP64 solver, swept in FP64).
+template <typename T, typename ST = T>
+int zsolve(flutas_plan *pl, ST *S, const double *lam, const double *a, const double *b, const double *c, bool pin) {
   ZArgs za;
   za.a = a; za.b = b; za.c = c; za.lam = lam;
   // the FP64 path has no residual norm: its z kernel flags a non-finite solution
@@ -627,7 +631,7 @@ int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const doub
     const int nt = 128;
     const size_t sm = zstream_smem<T, CH>(za.nn, nt);
     if ((int)sm > max_smem_optin()) return fail(FLUTAS_EUNSUPPORTED, "nz=%d too large for the z kernel", za.nz);
-    TRY(allow_smem(k_zstream<T, CH>));
+    TRY(allow_smem(k_zstream<T, CH, ST>));
     // launch in column batches whose eliminated values (one column of T per
     // column) stay L2-resident between the two sweeps
     const long per_batch = std::max<long>(nt, (long)(80.0e6 / (sizeof(T) * (double)za.nn)) / nt * nt);
@@ -635,7 +639,7 @@ int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const doub
       const long q1 = std::min<long>(za.nq, q0 + per_batch);
       const int grid = (int)((q1 - q0 + nt - 1) / nt);
       TRY(launch(sizeof(T) == 8 ? "k_zstream<f64>" : "k_zstream<f32>", pl->stream,
-                 [&] { k_zstream<T, CH><<<grid, nt, sm, pl->stream>>>(za, S, q0, q1); }));
+                 [&] { k_zstream<T, CH, ST><<<grid, nt, sm, pl->stream>>>(za, S, q0, q1); }));
     }
     return 0;
   }
@@ -644,10 +648,10 @@ int zsolve(flutas_plan *pl, T *S, const double *lam, const double *a, const doub
   if ((int)sm > max_smem_optin()) TC = 32;
   const size_t sm2 = sizeof(T) * (size_t)3 * za.nz * TC;
   if ((int)sm2 > max_smem_optin()) return fail(FLUTAS_EUNSUPPORTED, "nz=%d too large for the z kernel", za.nz);
-  int grid = grid_for(k_zsolve<T>, TC, sm2, ((long)za.nq + TC - 1) / TC);
+  int grid = grid_for(k_zsolve<T, ST>, TC, sm2, ((long)za.nq + TC - 1) / TC);
   if (grid < 0) return grid;
   TRY(launch(sizeof(T) == 8 ? "k_zsolve<f64>" : "k_zsolve<f32>", pl->stream,
-             [&] { k_zsolve<T><<<grid, TC, sm2, pl->stream>>>(za, S); }));
+             [&] { k_zsolve<T, ST><<<grid, TC, sm2, pl->stream>>>(za, S); }));
   return 0;
 }
 
@@ -792,10 +796,11 @@ int solve_fp64_dev(flutas_plan *pl, double *p, const double *lam, const double *
     return solve_fp64_ext_spec(pl, S, p, lam, a, b, c);
   }
   TRY(pl->S64.ensure(sizeof(double) * (size_t)g.nx * g.ny * g.nz));
-  double *S = pl->S64.as<double>();
-  TRY(fwd_xy<double>(pl, InHalo{p, g}, S, pl->tx64, pl->ty64, pl->path64));
-  TRY(zsolve<double>(pl, S, lam, a, b, c, pl->pin_zero_mode));
-  TRY(inv_xy<double>(pl, S, OutHalo{p, pl->normfft, g}, pl->tx64, pl->ty64, pl->path64));
+  // transforms in double-float (dd.cuh), z sweeps in FP64 on the same 8-byte spectrum
+  dd *S = pl->S64.as<dd>();
+  TRY(fwd_xy<dd>(pl, InHalo{p, g}, S, pl->txd, pl->tyd, pl->path64));
+  TRY((zsolve<double, dd>(pl, S, lam, a, b, c, pl->pin_zero_mode)));
+  TRY(inv_xy<dd>(pl, S, OutHalo{p, pl->normfft, g}, pl->txd, pl->tyd, pl->path64));
   return 0;
 }
 
@@ -1131,14 +1136,17 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
   if ((rc = pl->ext[0] ? build_ext(nx, kx.kf, kx.kb, &pl->ex[0]) : build_axis<double>(nx, px, &pl->tx64)) ||
       (rc = pl->ext[1] ? build_ext(ny, ky.kf, ky.kb, &pl->ex[1]) : build_axis<double>(ny, py, &pl->ty64)))
     return bail(rc);
+  if (!pl->ext[0] && !pl->ext[1] &&
+      ((rc = build_axis<dd>(nx, px, &pl->txd)) || (rc = build_axis<dd>(ny, py, &pl->tyd))))
+    return bail(rc);
   if (!pl->fp64_only &&
       ((rc = build_axis<float>(nx, px, &pl->tx32)) || (rc = build_axis<float>(ny, py, &pl->ty32))))
     return bail(rc);
   const int smax = max_smem_optin();
-  pl->path64 = (nx % 2 == 0 && ny % 2 == 0 && (int)plane_smem<double>(nx, ny) <= smax) ? 1 : 0;
+  pl->path64 = (nx % 2 == 0 && ny % 2 == 0 && (int)plane_smem<dd>(nx, ny) <= smax) ? 1 : 0;
   pl->path32 = (nx % 2 == 0 && ny % 2 == 0 && (int)plane_smem<float>(nx, ny) <= smax) ? 1 : 0;
-  if (!pl->path64 && (pl->clus64 = cluster_size_for<double>(nx, ny, smax)) &&
-      cluster_capacity(k_xyinv_cluster<double, OutHalo>, cluster_plane_smem(nx, ny, pl->clus64, 8), pl->clus64) > 0)
+  if (!pl->path64 && (pl->clus64 = cluster_size_for<dd>(nx, ny, smax)) &&
+      cluster_capacity(k_xyinv_cluster<dd, OutHalo>, cluster_plane_smem(nx, ny, pl->clus64, 8), pl->clus64) > 0)
     pl->path64 = 2;
   if (!pl->path32 && (pl->clus32 = cluster_size_for<float>(nx, ny, smax)) &&
       cluster_capacity(k_xyinv_cluster<float, OutHalo>, cluster_plane_smem(nx, ny, pl->clus32, 4), pl->clus32) > 0)
@@ -1177,7 +1185,8 @@ int flutas_gb300_fftend(void **arrplan) {
   }
   DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->czc, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
                   &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W, &pl->tx32.Q, &pl->ty32.W,
-                  &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm, &pl->nf_flag};
+                  &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm, &pl->nf_flag,
+                  &pl->txd.W, &pl->txd.Q, &pl->tyd.W, &pl->tyd.Q};
   for (DBuf *d : bufs) d->release();
   pl->ex[0].release();
   pl->ex[1].release();
@@ -1203,7 +1212,8 @@ int flutas_gb300_plan_info(void *plan, size_t *device_bytes, int *xy_path_fp64, 
     size_t s = 0;
     const DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->czc, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1],
                           &pl->rhsb[2], &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W,
-                          &pl->tx32.Q, &pl->ty32.W, &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm, &pl->nf_flag};
+                          &pl->tx32.Q, &pl->ty32.W, &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm, &pl->nf_flag,
+                          &pl->txd.W, &pl->txd.Q, &pl->tyd.W, &pl->tyd.Q};
     for (const DBuf *d : bufs) s += d->bytes;
     for (const DBuf &d : pl->mir.bufs) s += d.bytes;
     *device_bytes = s;
@@ -1779,27 +1789,34 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   int rc = 0;
   if (precision == 0) {
     TRY(pl->S64.ensure(sizeof(double) * (size_t)nx * ny * nz));
-    double *S = pl->S64.as<double>();
-    // fillps at full occupancy (the FP64 pipe bounds it), then the transform in place
+    // fillps at full occupancy (the FP64 pipe bounds it) into the spectrum array, then the
+    // transforms in place: double-float (dd.cuh) for the paired / DCT-IV kinds, FP64 for
+    // the extended-FFT kinds
     const Geo gs{nx, ny, nz, 1};
     const long cells = (long)nx * ny * nz;
-    const int grid = grid_for(k_stencil_pass<InFillps, double>, 256, 0, (cells + 1023) / 1024);
-    if (grid < 0) return grid;
-    if (cells >= (1L << 31) - 4096)  // the int variant also forms indices up to 3 blocks past the end
-      TRY(launch("k_stencil<f64,fillps>", st, [&] {
-        k_stencil_pass<InFillps, double, long long><<<grid, 256, 0, st>>>(in, gs, nullptr, S, nullptr);
-      }));
-    else
-      TRY(launch("k_stencil<f64,fillps>", st,
-                 [&] { k_stencil_pass<InFillps, double><<<grid, 256, 0, st>>>(in, gs, nullptr, S, nullptr); }));
+    auto fill = [&](auto *S) -> int {
+      using TO = std::remove_pointer_t<decltype(S)>;
+      const int grid = grid_for(k_stencil_pass<InFillps, TO>, 256, 0, (cells + 1023) / 1024);
+      if (grid < 0) return grid;
+      const char *nm = std::is_same<TO, dd>::value ? "k_stencil<df64,fillps>" : "k_stencil<f64,fillps>";
+      if (cells >= (1L << 31) - 4096)  // the int variant also forms indices up to 3 blocks past the end
+        return launch(nm, st, [&] {
+          k_stencil_pass<InFillps, TO, long long><<<grid, 256, 0, st>>>(in, gs, nullptr, S, nullptr);
+        });
+      return launch(nm, st, [&] { k_stencil_pass<InFillps, TO><<<grid, 256, 0, st>>>(in, gs, nullptr, S, nullptr); });
+    };
     if (pl->ext[0] || pl->ext[1]) {  // odd-length ND/DN: extended-FFT passes
+      double *S = pl->S64.as<double>();
+      TRY(fill(S));
       TRY(solve_fp64_ext_spec(pl, S, phi, pl->lam.as<double>(), pl->a.as<double>(), pl->b.as<double>(),
                               pl->c.as<double>()));
     } else {
-      TRY(fwd_xy<double>(pl, InPlain{S, gs}, S, pl->tx64, pl->ty64, pl->path64));
-      TRY(zsolve<double>(pl, S, pl->lam.as<double>(), pl->a.as<double>(), pl->b.as<double>(), pl->c.as<double>(),
-                         pl->pin_zero_mode));
-      TRY(inv_xy<double>(pl, S, OutHalo{phi, pl->normfft, gp}, pl->tx64, pl->ty64, pl->path64));
+      dd *S = pl->S64.as<dd>();
+      TRY(fill(S));
+      TRY(fwd_xy<dd>(pl, InPlainDD{S, gs}, S, pl->txd, pl->tyd, pl->path64));
+      TRY((zsolve<double, dd>(pl, S, pl->lam.as<double>(), pl->a.as<double>(), pl->b.as<double>(),
+                              pl->c.as<double>(), pl->pin_zero_mode)));
+      TRY(inv_xy<dd>(pl, S, OutHalo{phi, pl->normfft, gp}, pl->txd, pl->tyd, pl->path64));
     }
   }
   CorrecAddArgs ca;

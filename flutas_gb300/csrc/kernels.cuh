@@ -99,8 +99,19 @@ __device__ __forceinline__ void to_pass_into(float &o, double v) { o = f32_of(v)
 __device__ __forceinline__ void to_pass_into(float &o, float v) { o = v; }
 __device__ __forceinline__ void to_pass_into(double &o, double v) { o = v; }
 __device__ __forceinline__ void to_pass_into(double &o, float v) { o = f64_of(v); }
+__device__ __forceinline__ void to_pass_into(dd &o, double v) { o = dd_of(v); }
+__device__ __forceinline__ void to_pass_into(dd &o, dd v) { o = v; }
+// Storage <-> arithmetic of the z sweeps: the FP64 solver keeps its spectrum as
+// double-float pairs (its transforms' type) and sweeps in FP64.
+__device__ __forceinline__ double z_load(const dd &v) { return double_of(v); }
+__device__ __forceinline__ double z_load(const double &v) { return v; }
+__device__ __forceinline__ float z_load(const float &v) { return v; }
+__device__ __forceinline__ void z_store(dd &o, double v) { o = dd_of(v); }
+__device__ __forceinline__ void z_store(double &o, double v) { o = v; }
+__device__ __forceinline__ void z_store(float &o, float v) { o = v; }
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(double v) { return f32_of(v); }
+__device__ __forceinline__ float to_f32(dd v) { return v.h; }
 
 // ------------------------------------------------------- forward input modes
 // All take 0-based interior coordinates (i0,j0,k0) and return the RHS value.
@@ -127,6 +138,14 @@ struct InPlain {  // contiguous (nx,ny,nz) FP64 array
   Geo g;
   __device__ double operator()(int i0, int j0, int k0) const { return f[g.sidx(i0, j0, k0)]; }
   __device__ void keep(int, int, int, double) const {}
+};
+
+struct InPlainDD {  // contiguous (nx,ny,nz) double-float array (the FP64 solver's spectrum)
+  static constexpr const char *tag = "plain";
+  const dd *f;
+  Geo g;
+  __device__ dd operator()(int i0, int j0, int k0) const { return f[g.sidx(i0, j0, k0)]; }
+  __device__ void keep(int, int, int, dd) const {}
 };
 
 // fillps (src/fillps.f90:50-57) + optional updt_rhs_b (src/bound.f90:829-944).
@@ -220,9 +239,11 @@ struct OutHalo {  // p(i,j,k) = v * scale   (scale applied in the arithmetic typ
   __device__ void operator()(int i0, int j0, int k0, float v) const {
     p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = f64_of(v * f32_of(scale));
   }
+  __device__ void operator()(int i0, int j0, int k0, dd v) const { p[g.pidx(i0 + 1, j0 + 1, k0 + 1)] = double_of(v) * scale; }
   __device__ double pre(int, int, int) const { return 0.0; }
   __device__ void put(int i0, int j0, int k0, double, double v) const { (*this)(i0, j0, k0, v); }
   __device__ void put(int i0, int j0, int k0, double, float v) const { (*this)(i0, j0, k0, v); }
+  __device__ void put(int i0, int j0, int k0, double, dd v) const { (*this)(i0, j0, k0, v); }
 };
 struct OutPlain {  // the contiguous (nx,ny,nz) spectral array itself (an in-place inverse pass)
   static constexpr const char *tag = "plain";
@@ -762,25 +783,25 @@ __device__ __forceinline__ void thomas_col(int n, const double *a, const double 
   for (int l = n - 2; l >= 0; l--) p[l * ts] = (St)((T)p[l * ts] - (T)d[l * ts] * (T)p[(l + 1) * ts]);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(128) k_zsolve(ZArgs za, T *S) {
+template <typename T, typename ST = T>
+__global__ void __launch_bounds__(128) k_zsolve(ZArgs za, ST *S) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int TC = blockDim.x, nz = za.nz, tid = threadIdx.x;
   T *col = (T *)smem_raw;        // nz x TC
-  T *dd = col + (long)nz * TC;   // nz x TC
-  T *p2 = dd + (long)nz * TC;    // nz x TC (periodic only)
+  T *dsc = col + (long)nz * TC;  // nz x TC
+  T *p2 = dsc + (long)nz * TC;   // nz x TC (periodic only)
   const long plane = za.nq;
   for (long q0 = (long)blockIdx.x * TC; q0 < za.nq; q0 += (long)gridDim.x * TC) {
     const int tcv = (int)min((long)TC, za.nq - q0);
     for (int idx = tid; idx < nz * TC; idx += TC) {
       const int k = idx / TC, t = idx % TC;
-      if (t < tcv) col[idx] = S[q0 + t + plane * k];
+      if (t < tcv) col[idx] = z_load(S[q0 + t + plane * k]);
     }
     __syncthreads();
     if (tid < tcv) {
       const long q = q0 + tid;
       const double lam = za.lam[q];
-      T *pc = col + tid, *dc = dd + tid;
+      T *pc = col + tid, *dc = dsc + tid;
       const int n = za.nn;
       if (!za.periodic) {
         const bool pin = za.pin && lam == 0.0;
@@ -805,7 +826,7 @@ __global__ void __launch_bounds__(128) k_zsolve(ZArgs za, T *S) {
     __syncthreads();
     for (int idx = tid; idx < nz * TC; idx += TC) {
       const int k = idx / TC, t = idx % TC;
-      if (t < tcv) S[q0 + t + plane * k] = col[idx];
+      if (t < tcv) z_store(S[q0 + t + plane * k], col[idx]);
     }
     __syncthreads();
   }
@@ -1261,8 +1282,8 @@ template <typename T, int CH> FG_HD size_t zstream_smem(int nn, int nt) {
 // without per-level predicates; the last one takes the general path (the last
 // level divides, and a pinned singular column ends in zero).  Level 0 needs no
 // case of its own: its pivot b + lam - a*0 is b + lam exactly (a is finite).
-template <typename T, int CH>
-__global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, long q_begin, long q_end) {
+template <typename T, int CH, typename ST = T>
+__global__ void __launch_bounds__(128) k_zstream(ZArgs za, ST *__restrict__ S, long q_begin, long q_end) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x, nt = blockDim.x;
   const int n = za.nn;
@@ -1277,20 +1298,20 @@ __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, lo
   const double lam64 = za.lam[q];
   const bool pin = za.pin && lam64 == 0.0;
   const T lam = (T)lam64;
-  T *col = S + q;
+  ST *col = S + q;
   const int nch = (n + CH - 1) / CH;
   // ---- forward elimination
   T r[CH], rn[CH];
 #pragma unroll
-  for (int i = 0; i < CH; i++) r[i] = i < n ? col[(long)i * plane] : (T)0;
+  for (int i = 0; i < CH; i++) r[i] = i < n ? z_load(col[(long)i * plane]) : (T)0;
   T dprev = (T)0, yprev = (T)0;
   for (int m = 0; m < nch; m++) {
     const int k0 = m * CH;
-    T *p = col + (long)k0 * plane;
+    ST *p = col + (long)k0 * plane;
     {
-      const T *pn = p + (long)CH * plane;
+      const ST *pn = p + (long)CH * plane;
 #pragma unroll
-      for (int i = 0; i < CH; i++) rn[i] = k0 + CH + i < n ? pn[(long)i * plane] : (T)0;
+      for (int i = 0; i < CH; i++) rn[i] = k0 + CH + i < n ? z_load(pn[(long)i * plane]) : (T)0;
     }
     chk[m * nt + tid] = dprev;
     if (k0 + CH < n) {
@@ -1300,7 +1321,7 @@ __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, lo
         const T z = zrcp(fma(-cf.a, dprev, cf.b + lam));
         const T y = fma(-cf.a, yprev, r[i]) * z;
         dprev = cf.c * z;
-        *p = y;
+        z_store(*p, y);
         p += plane;
         yprev = y;
       }
@@ -1320,7 +1341,7 @@ __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, lo
             y = (piv != (T)0 && !pin) ? fma(-cf.a, yprev, r[i]) / piv : (T)0;
             d = (T)0;
           }
-          *p = y;
+          z_store(*p, y);
           p += plane;
           dprev = d;
           yprev = y;
@@ -1335,14 +1356,14 @@ __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, lo
   {
     const int k0 = (nch - 1) * CH;
 #pragma unroll
-    for (int i = 0; i < CH; i++) r[i] = k0 + i < n ? col[(long)(k0 + i) * plane] : (T)0;
+    for (int i = 0; i < CH; i++) r[i] = k0 + i < n ? z_load(col[(long)(k0 + i) * plane]) : (T)0;
   }
   for (int m = nch - 1; m >= 0; m--) {
     const int k0 = m * CH;
     if (m > 0) {
-      const T *pp = col + (long)(k0 - CH) * plane;
+      const ST *pp = col + (long)(k0 - CH) * plane;
 #pragma unroll
-      for (int i = 0; i < CH; i++) rn[i] = pp[(long)i * plane];
+      for (int i = 0; i < CH; i++) rn[i] = z_load(pp[(long)i * plane]);
     }
     T dd[CH];
     T dp = chk[m * nt + tid];
@@ -1354,11 +1375,11 @@ __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, lo
         dd[i] = cf.c * z;
         dp = dd[i];
       }
-      T *p = col + (long)(k0 + CH - 1) * plane;
+      ST *p = col + (long)(k0 + CH - 1) * plane;
 #pragma unroll
       for (int i = CH - 1; i >= 0; i--) {
         const T x = fma(-dd[i], xnext, r[i]);
-        *p = x;
+        z_store(*p, x);
         p -= plane;
         xnext = x;
       }
@@ -1380,7 +1401,7 @@ __global__ void __launch_bounds__(128) k_zstream(ZArgs za, T *__restrict__ S, lo
         const int k = k0 + i;
         if (k < n) {
           const T x = (k == n - 1) ? r[i] : fma(-dd[i], xnext, r[i]);
-          col[(long)k * plane] = x;
+          z_store(col[(long)k * plane], x);
           xnext = x;
         }
       }
