@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #ifndef FG_HD
 #define FG_HD __host__ __device__ __forceinline__
 #endif
@@ -230,9 +232,37 @@ FG_HD void stage_pass(const C2<T> *in, C2<T> *out, int N, int B, int ldb, int Ns
   }
 }
 
+// A radix-R stage with rolled loops: each output of a butterfly summed directly
+// from the R inputs (read from the buffer, twiddled on the fly).  Few registers;
+// the double-float engine takes it for the large odd radices, whose unrolled
+// butterflies would set the register count of every kernel they are part of.
+template <typename T, bool INV>
+FG_HD void stage_pass_rolled(int R, const C2<T> *in, C2<T> *out, int N, int B, int ldb, int Ns, const C2<T> *W,
+                             int tid, int nth) {
+  const int NR = N / R, total = B * NR, tws = N / (Ns * R), step = N / R;
+  for (int bf = tid; bf < total; bf += nth) {
+    const int c = bf % B, j = bf / B, kk = j % Ns, idxD = (j - kk) * R + kk;
+    for (int q = 0; q < R; q++) {
+      C2<T> acc = in[j * ldb + c];
+      for (int r = 1; r < R; r++) {
+        C2<T> a = in[(j + r * NR) * ldb + c];
+        if (Ns > 1) a = cmul<T>(a, twid<T>(W, N, kk * r * tws, INV));
+        acc = cadd<T>(acc, cmul<T>(a, twid<T>(W, N, ((r * q) % R) * step, INV)));
+      }
+      out[(idxD + q * Ns) * ldb + c] = acc;
+    }
+  }
+}
+
 template <typename T, bool INV>
 FG_HD void stage_dispatch(int R, const C2<T> *in, C2<T> *out, int N, int B, int ldb, int Ns,
                           const C2<T> *W, int tid, int nth) {
+  if constexpr (std::is_same<T, dd>::value) {
+    if (R == 11 || R == 13) {
+      stage_pass_rolled<T, INV>(R, in, out, N, B, ldb, Ns, W, tid, nth);
+      return;
+    }
+  }
   switch (R) {
     case 2: stage_pass<T, 2, INV>(in, out, N, B, ldb, Ns, W, tid, nth); break;
     case 3: stage_pass<T, 3, INV>(in, out, N, B, ldb, Ns, W, tid, nth); break;
@@ -240,9 +270,15 @@ FG_HD void stage_dispatch(int R, const C2<T> *in, C2<T> *out, int N, int B, int 
     case 5: stage_pass<T, 5, INV>(in, out, N, B, ldb, Ns, W, tid, nth); break;
     case 7: stage_pass<T, 7, INV>(in, out, N, B, ldb, Ns, W, tid, nth); break;
     case 8: stage_pass<T, 8, INV>(in, out, N, B, ldb, Ns, W, tid, nth); break;
-    case 11: stage_pass<T, 11, INV>(in, out, N, B, ldb, Ns, W, tid, nth); break;
-    case 13: stage_pass<T, 13, INV>(in, out, N, B, ldb, Ns, W, tid, nth); break;
-    case 16: stage_pass<T, 16, INV>(in, out, N, B, ldb, Ns, W, tid, nth); break;
+    case 11:
+      if constexpr (!std::is_same<T, dd>::value) stage_pass<T, 11, INV>(in, out, N, B, ldb, Ns, W, tid, nth);
+      break;
+    case 13:
+      if constexpr (!std::is_same<T, dd>::value) stage_pass<T, 13, INV>(in, out, N, B, ldb, Ns, W, tid, nth);
+      break;
+    case 16:  // double-float plans stop at radix 8 (fill_axis_tables): no radix-16 registers
+      if constexpr (sizeof(T) == 4) stage_pass<T, 16, INV>(in, out, N, B, ldb, Ns, W, tid, nth);
+      break;
     default: break;  // plans only contain the radices above
   }
 }

@@ -422,14 +422,14 @@ template <typename T> size_t plane_smem(int nx, int ny) {
 }
 
 // Cluster plane kernels: smallest cluster (2..16 CTAs) whose per-CTA share of
-// the plane fits two CTAs per SM (FP32: 128 registers) or one (FP64: up to
-// 255 registers); 0 when the plane does not split evenly.
+// the plane fits two CTAs per SM (FP32 and double-float: 128 registers) or one
+// (FP64: up to 255 registers); 0 when the plane does not split evenly.
 constexpr int CLUSTER_THREADS = 256;
 template <typename T> int cluster_size_for(int nx, int ny, int smax) {
   for (int C = 2; C <= 16; C *= 2) {
     if (nx % C || ny % C || (nx / C) % 2 || (ny / C) % 2) continue;
     const size_t sm = cluster_plane_smem(nx, ny, C, sizeof(T));
-    if (sm <= (sizeof(T) == 4 ? (size_t)smax / 2 - 1024 : (size_t)smax)) return C;
+    if (sm <= (!std::is_same<T, double>::value ? (size_t)smax / 2 - 1024 : (size_t)smax)) return C;
   }
   return 0;
 }

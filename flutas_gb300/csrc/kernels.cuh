@@ -16,6 +16,7 @@
 //   velocities     (1-h:nx+h, 1-h:ny+h, 1-h:nz+h)   double, h = nh_u
 //   spectral S     (nx, ny, nz) no halo             T (double or float)
 #pragma once
+#include <type_traits>
 #include "fft_engine.cuh"
 #include "fft_ext.cuh"
 #include "bits.cuh"
@@ -112,6 +113,10 @@ __device__ __forceinline__ void z_store(float &o, float v) { o = v; }
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(double v) { return f32_of(v); }
 __device__ __forceinline__ float to_f32(dd v) { return v.h; }
+
+// CTAs per SM the transform kernels are compiled for: two (at most 128
+// registers a thread) for FP32 and double-float, one for FP64.
+template <typename T> constexpr int xf_minb() { return std::is_same<T, double>::value ? 1 : 2; }
 
 // ------------------------------------------------------- forward input modes
 // All take 0-based interior coordinates (i0,j0,k0) and return the RHS value.
@@ -480,7 +485,7 @@ __device__ __forceinline__ void xfwd_tile(const AxisPlan &ax, const In &in, T *S
 }
 
 template <typename T, typename In>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xfwd(AxisPlan ax, In in, T *S, Geo g, int M, double *nrm) {
+__global__ void __launch_bounds__(256, xf_minb<T>()) k_xfwd(AxisPlan ax, In in, T *S, Geo g, int M, double *nrm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const long rows = (long)g.ny * g.nz;
   float ss = 0.0f;  // sum of squares for convergence checks (FP32 per thread)
@@ -543,7 +548,7 @@ __device__ __forceinline__ void xinv_tile(const AxisPlan &ax, const T *S, const 
 }
 
 template <typename T, typename Out>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xinv(AxisPlan ax, const T *S, Out out, Geo g, int M) {
+__global__ void __launch_bounds__(256, xf_minb<T>()) k_xinv(AxisPlan ax, const T *S, Out out, Geo g, int M) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const long rows = (long)g.ny * g.nz;
   for (long row0 = (long)blockIdx.x * M; row0 < rows; row0 += (long)gridDim.x * M)
@@ -608,7 +613,7 @@ __device__ __forceinline__ void ypass_tile(const AxisPlan &ay, T *S, const Geo &
 }
 
 template <typename T, bool BACKWARD>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_ypass(AxisPlan ay, T *S, Geo g, int W) {
+__global__ void __launch_bounds__(256, xf_minb<T>()) k_ypass(AxisPlan ay, T *S, Geo g, int W) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const long ntiles = (long)((g.nx + W - 1) / W) * g.nz;
   for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) ypass_tile<T, BACKWARD>(ay, S, g, W, tile, smem_raw);
@@ -1929,7 +1934,7 @@ __device__ __forceinline__ void cluster_gather_rows(cg::cluster_group &cluster, 
 }
 
 template <typename T, typename In>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xyfwd_cluster(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
+__global__ void __launch_bounds__(256, xf_minb<T>()) k_xyfwd_cluster(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
@@ -1980,7 +1985,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xyfwd_cluster(A
 }
 
 template <typename T, typename Out>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_xyinv_cluster(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
+__global__ void __launch_bounds__(256, xf_minb<T>()) k_xyinv_cluster(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
