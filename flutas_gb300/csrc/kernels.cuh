@@ -990,15 +990,6 @@ struct PresTwArgs {
   int fp32;               // 1: increment evaluated in FP32 from FP64 differences (mixed path)
   Geo g;
 };
-__device__ __forceinline__ double rcp64_1(double x) {
-  const double y = f64_of(__frcp_rn(f32_of(x)));  // FP32 seed (integer-ALU conversions), error < 2^-22
-  return y * fma(-x, y, 2.0);                       // one Newton step: error < 2^-44
-}
-__device__ __forceinline__ double df_incr(double dp, double dq, double rs, double A, double B, double f2) {
-  const double t = dp - dq;
-  const double dg = fma(f2, t, dp);
-  return fma(A, t, -B * (rcp64_1(rs) * dg));
-}
 // FP32 increment (mixed path) from the differences of p and of pold across a
 // face (dp, dq: FP32 roundings of differences that cancel, formed without
 // rounding the operands first); the rest of the Dodd-Ferrante increment
@@ -1045,12 +1036,28 @@ __device__ __forceinline__ void df_cell32(const PresTwArgs &a, float zA, float z
   v += df_incr32(dpy, dqy, ry, a.yA32, a.yB32, a.f2_32);
   w += df_incr32(dpz, dqz, rz, zA, zB, a.f2_32);
 }
-// FP64 increments, rounded as the reference expression is.
-__device__ __forceinline__ void df_cell64(const PresTwArgs &a, int k, const DfPoint &c, const DfPoint &x,
+// FP64 path: the differences of p and pold across a face in FP64 (exact when
+// they cancel), the rest of the increment in double-float arithmetic (dd.cuh:
+// about 2^-47 of its terms), the update u += increment in FP64 (two additions:
+// the increment's two parts).  Four FP64 instructions a component instead of
+// the eleven of an FP64 evaluation (FP64 is the scarce pipe of this part).
+__device__ __forceinline__ dd dd_rcp(dd b) {  // 1/b: FP32 seed, one double-float Newton step
+  const float y = __frcp_rn(b.h);
+  const dd e = dd(1.0f, 0.0f) - b * dd(y, 0.0f);
+  return dd_fast_two_sum(y, y * e.h);
+}
+__device__ __forceinline__ double df_incr_dd(double dp, double dq, dd rs, dd A, dd B, dd f2) {
+  const dd p = dd_of(dp), t = p - dd_of(dq);
+  const dd dg = f2 * t + p;
+  const dd r = A * t - B * (dd_rcp(rs) * dg);
+  return f64_of(r.h) + f64_of(r.l);
+}
+__device__ __forceinline__ void df_cell64(const PresTwArgs &a, dd zA, dd zB, const DfPoint &c, const DfPoint &x,
                                           const DfPoint &y, const DfPoint &z, double &u, double &v, double &w) {
-  u += df_incr(x.p - c.p, x.q - c.q, x.r + c.r, a.xA, a.xB, a.f2);
-  v += df_incr(y.p - c.p, y.q - c.q, y.r + c.r, a.yA, a.yB, a.f2);
-  w += df_incr(z.p - c.p, z.q - c.q, z.r + c.r, a.zA[k], a.zB[k], a.f2);
+  const dd f2 = dd_of(a.f2), rc = dd_of(c.r);
+  u += df_incr_dd(x.p - c.p, x.q - c.q, dd_of(x.r) + rc, dd_of(a.xA), dd_of(a.xB), f2);
+  v += df_incr_dd(y.p - c.p, y.q - c.q, dd_of(y.r) + rc, dd_of(a.yA), dd_of(a.yB), f2);
+  w += df_incr_dd(z.p - c.p, z.q - c.q, dd_of(z.r) + rc, zA, zB, f2);
 }
 
 // One thread per (i, j) column and PRESTW_KZ consecutive levels: the z
@@ -1089,7 +1096,7 @@ __global__ void __launch_bounds__(PRESTW_NT) k_pres_tw_src(PresTwArgs a) {
         un = U[ui + usz]; vn = V[ui + usz]; wn = W[ui + usz];
       }
       if (a.fp32) df_cell32(a, zab[0][k - kb], zab[1][k - kb], cen, x, y, z, u, v, w);
-      else df_cell64(a, k, cen, x, y, z, u, v, w);
+      else df_cell64(a, dd_of(a.zA[k]), dd_of(a.zB[k]), cen, x, y, z, u, v, w);
       U[ui] = u; V[ui] = v; W[ui] = w;
       cen = z; x = xn; y = yn; z = zn;
       u = un; v = vn; w = wn;
