@@ -698,6 +698,7 @@ def run_batch(args, keep=False):
         iters.append(it)
         rels.append(rr)
     launches = (F.launch_count() - l0) // max(1, args.steps)
+    queue = [ln for ln in B.report().splitlines() if ln.startswith("queue:")]
     # the same grids one by one with the single-grid paths (a sample)
     sample = list(range(0, len(grids), max(1, len(grids) // 24)))
     t_seq_mixed = t_seq_fp64 = 0.0
@@ -729,6 +730,9 @@ def run_batch(args, keep=False):
             "max_relres": float(np.max(rels)), "fp32_solves_per_grid": {
                 "mean": float(np.mean(iters)), "max": int(np.max(iters))},
             "gpu_launches_per_batch": int(launches), "create_s": round(t_create, 2),
+            "queue": queue[0][7:] if queue else ("one persistent kernel"
+                                                  if os.environ.get("FLUTAS_GB300_BATCH_PERSISTENT") == "1"
+                                                  else "one work-queue kernel per pass, in one CUDA graph"),
             "sequential_single_grid": {"mixed_grids_per_s": round(len(sample) / t_seq_mixed, 2),
                                        "fp64_grids_per_s": round(len(sample) / t_seq_fp64, 2),
                                        "sample_grids": len(sample), "est_batch_equivalent_ms":

@@ -2144,9 +2144,15 @@ struct flutas_batch {
   std::vector<double *> x;    // device halo arrays handed to the caller
   DBuf d_grids, d_prefix, d_counters, d_nrm, d_active, d_relres, d_iters;
   DBuf d_act, d_ids, d_nslots;  // compacted work lists of the grids still refining
+  // the persistent kernel's queue: tile totals (z tiles of 256 columns), passes, counts, norms, error flags
+  DBuf p_prefix, p_type, p_iter, p_off, p_start, p_done, p_pdone, p_nrm, p_err;
   std::vector<BatchGrid> grids;
-  size_t smem_x = 0, smem_y = 0, smem_z = 0;
-  int grid_x = 0, grid_y = 0, grid_z = 0;
+  size_t smem_x = 0, smem_y = 0, smem_z = 0, smem_p = 0;
+  int grid_x = 0, grid_y = 0, grid_z = 0, grid_p = 0;
+  bool per_pass = true;   // false (FLUTAS_GB300_BATCH_PERSISTENT=1): the whole refinement in one persistent kernel
+  int minb = 2;           // FLUTAS_GB300_BATCH_MINB: register budget of the persistent kernel
+  int chunk = 4;          // FLUTAS_GB300_BATCH_CHUNK: items a block takes from the queue at once
+  bool stats = false;     // FLUTAS_GB300_BATCH_STATS=1: queue statistics and per-pass-type timers
   cudaStream_t stream = nullptr;
   cudaGraphExec_t exec = nullptr;
   double g_tol = -1.0;
@@ -2286,11 +2292,91 @@ void batch_free(flutas_batch *bt) {
     if (p) flutas_gb300_fftend(arr);
   }
   DBuf *bufs[] = {&bt->arena, &bt->d_grids, &bt->d_prefix, &bt->d_counters, &bt->d_nrm, &bt->d_active,
-                  &bt->d_relres, &bt->d_iters, &bt->d_act, &bt->d_ids, &bt->d_nslots};
+                  &bt->d_relres, &bt->d_iters, &bt->d_act, &bt->d_ids, &bt->d_nslots, &bt->p_prefix,
+                  &bt->p_type, &bt->p_iter, &bt->p_off, &bt->p_start, &bt->p_done, &bt->p_pdone, &bt->p_nrm,
+                  &bt->p_err};
   for (DBuf *d : bufs) d->release();
   if (bt->stream) cudaStreamDestroy(bt->stream);
   bt->magic = 0;
   delete bt;
+}
+
+// The whole refinement as one persistent kernel (kb_persist) and the read-out
+// of the per-grid residuals (kb_finalize), after the resets of the queue.
+int batch_capture_persistent(flutas_batch *bt, double tol, int max_iter) {
+  const int ng = bt->ng;
+  std::vector<int> ptype, piter;
+  auto add = [&](int t, int it) { ptype.push_back(t); piter.push_back(it); };
+  add(PB_XF0, 0); add(PB_Y, 0); add(PB_Z, 0); add(PB_YI, 0); add(PB_XI0, 0);
+  for (int it = 1; it <= max_iter; it++) {
+    add(PB_XR, it);
+    if (it < max_iter) { add(PB_Y, it); add(PB_Z, it); add(PB_YI, it); add(PB_XI1, it); }
+  }
+  const int npass = (int)ptype.size();
+  std::vector<long> pre(3 * (size_t)(ng + 1));
+  CK(cudaMemcpy(pre.data(), bt->p_prefix.p, sizeof(long) * pre.size(), cudaMemcpyDeviceToHost));
+  std::vector<long> poff(npass + 1, 0);
+  for (int p = 0; p < npass; p++) poff[p + 1] = poff[p] + pre[(size_t)pass_kind(ptype[p]) * (ng + 1) + ng];
+  if (poff[npass] >= (1L << 31) - 1) return fail(FLUTAS_EUNSUPPORTED, "batch: too many work items");
+  std::vector<int> pstart((size_t)npass * ng + 1);
+  for (int p = 0; p < npass; p++)
+    for (int g = 0; g < ng; g++) pstart[(size_t)p * ng + g] = (int)(poff[p] + pre[(size_t)pass_kind(ptype[p]) * (ng + 1) + g]);
+  pstart[(size_t)npass * ng] = (int)poff[npass];
+  TRY(bt->p_start.ensure(sizeof(int) * pstart.size()));
+  TRY(bt->p_pdone.ensure(sizeof(int) * npass));
+  CK(cudaMemcpy(bt->p_start.p, pstart.data(), sizeof(int) * pstart.size(), cudaMemcpyHostToDevice));
+  TRY(bt->p_type.ensure(sizeof(int) * npass));
+  TRY(bt->p_iter.ensure(sizeof(int) * npass));
+  TRY(bt->p_off.ensure(sizeof(long) * (npass + 1)));
+  TRY(bt->p_done.ensure(sizeof(int) * (size_t)npass * ng));
+  TRY(bt->p_nrm.ensure(sizeof(double) * (size_t)ng * (max_iter + 1)));
+  TRY(bt->p_err.ensure(sizeof(int) * 4 + sizeof(unsigned long long) * 12));  // flags, counter; queue statistics
+  CK(cudaMemcpy(bt->p_type.p, ptype.data(), sizeof(int) * npass, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(bt->p_iter.p, piter.data(), sizeof(int) * npass, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(bt->p_off.p, poff.data(), sizeof(long) * (npass + 1), cudaMemcpyHostToDevice));
+  PersistArgs a;
+  a.grids = bt->d_grids.as<BatchGrid>();
+  a.ng = ng;
+  a.prefix = bt->p_prefix.as<long>();
+  a.ptype = bt->p_type.as<int>();
+  a.piter = bt->p_iter.as<int>();
+  a.poff = bt->p_off.as<long>();
+  a.npass = npass;
+  a.chunk = bt->chunk;
+  a.pstart = bt->p_start.as<int>();
+  a.pass_done = bt->p_pdone.as<int>();
+  a.err = bt->p_err.as<int>();
+  a.counter = a.err + 2;
+  a.done = bt->p_done.as<int>();
+  a.nrm = bt->p_nrm.as<double>();
+  a.stride = max_iter + 1;
+  a.tol = tol;
+  a.max_iter = max_iter;
+  a.spin_limit = 1L << 25;  // polls of about 100 ns: a few seconds
+  a.stats = bt->stats ? (unsigned long long *)(a.err + 4) : nullptr;
+  auto kern = bt->minb == 1 ? kb_persist<1> : kb_persist<2>;
+  int per_sm = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, bt->smem_p));
+  if (per_sm < 1) return fail(FLUTAS_EUNSUPPORTED, "batch: the persistent kernel does not fit an SM");
+  bt->grid_p = (int)std::min<long>(poff[npass], (long)per_sm * num_sms());
+  cudaStream_t st = bt->stream;
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  cudaMemsetAsync(a.err, 0, sizeof(int) * 4 + sizeof(unsigned long long) * 12, st);  // flags, counter, statistics
+  cudaMemsetAsync(a.done, 0, sizeof(int) * (size_t)npass * ng, st);
+  cudaMemsetAsync(a.pass_done, 0, sizeof(int) * npass, st);
+  cudaMemsetAsync(a.nrm, 0, sizeof(double) * (size_t)ng * (max_iter + 1), st);
+  kern<<<bt->grid_p, 256, bt->smem_p, st>>>(a);
+  kb_finalize<<<(ng + 255) / 256, 256, 0, st>>>(a, bt->d_relres.as<double>(), bt->d_iters.as<int>());
+  cudaError_t e = cudaStreamEndCapture(st, &graph);
+  if (e != cudaSuccess) return fail(FLUTAS_ECUDA, "batch graph capture failed: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&bt->exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(FLUTAS_ECUDA, "batch graph instantiation failed: %s", cudaGetErrorString(e));
+  bt->g_tol = tol;
+  bt->g_maxit = max_iter;
+  bt->nodes = 2;
+  return 0;
 }
 
 int batch_capture(flutas_batch *bt, double tol, int max_iter) {
@@ -2298,6 +2384,7 @@ int batch_capture(flutas_batch *bt, double tol, int max_iter) {
     cudaGraphExecDestroy(bt->exec);
     bt->exec = nullptr;
   }
+  if (!bt->per_pass) return batch_capture_persistent(bt, tol, max_iter);
   const int ng = bt->ng;
   const int npass = 5 + 5 * max_iter;
   TRY(bt->d_counters.ensure(sizeof(int) * npass));
@@ -2468,6 +2555,27 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
     return bail(fail(FLUTAS_ECUDA, "batch_create: upload failed"));
   if ((int)std::max({bt->smem_x, bt->smem_y, bt->smem_z}) > max_smem_optin())
     return bail(fail(FLUTAS_EUNSUPPORTED, "batch_create: tiles exceed shared memory"));
+  {
+    // the persistent kernel's tiles: x and y as above, z in blocks of 256 columns
+    std::vector<long> pp(pre);
+    size_t smz = 0;
+    for (int g = 0; g < ngrids; g++) {
+      const Geo &G = bt->grids[g].g;
+      pp[2 * (ngrids + 1) + g + 1] = pp[2 * (ngrids + 1) + g] + ((long)G.nx * G.ny + 255) / 256;
+      smz = std::max(smz, sizeof(float) * (size_t)((G.nz + 15) / 16) * 256);
+    }
+    bt->smem_p = std::max({bt->smem_x, bt->smem_y, smz});
+    if ((rc = bt->p_prefix.ensure(sizeof(long) * pp.size()))) return bail(rc);
+    if (cudaMemcpy(bt->p_prefix.p, pp.data(), sizeof(long) * pp.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+      return bail(fail(FLUTAS_ECUDA, "batch_create: upload failed"));
+    if ((rc = allow_smem(kb_persist<1>)) || (rc = allow_smem(kb_persist<2>))) return bail(rc);
+    if (const char *e = getenv("FLUTAS_GB300_BATCH_PERSISTENT")) bt->per_pass = atoi(e) == 0;
+    // the persistent kernel's own tables take about 2 KB of static shared memory besides the tiles
+    if ((int)bt->smem_p + 2048 > max_smem_optin()) bt->per_pass = true;
+    if (const char *e = getenv("FLUTAS_GB300_BATCH_MINB")) bt->minb = atoi(e) == 1 ? 1 : 2;
+    if (const char *e = getenv("FLUTAS_GB300_BATCH_CHUNK")) bt->chunk = std::max(1, std::min(64, atoi(e)));
+    if (const char *e = getenv("FLUTAS_GB300_BATCH_STATS")) bt->stats = atoi(e) != 0;
+  }
   int g1, g2, g3;
   if ((g1 = grid_for(kb_xfwd, 256, bt->smem_x, pre[ngrids])) < 0) return bail(g1);
   if ((g2 = grid_for(kb_ypass<false>, 256, bt->smem_y, pre[2 * ngrids + 1])) < 0) return bail(g2);
@@ -2499,7 +2607,10 @@ int flutas_gb300_batch_solve(void *batch, double tol, int max_iter, double *relr
   std::vector<int> it(bt->ng);
   CK(cudaMemcpyAsync(rr.data(), bt->d_relres.p, sizeof(double) * bt->ng, cudaMemcpyDeviceToHost, bt->stream));
   CK(cudaMemcpyAsync(it.data(), bt->d_iters.p, sizeof(int) * bt->ng, cudaMemcpyDeviceToHost, bt->stream));
+  int perr = 0;
+  if (!bt->per_pass) CK(cudaMemcpyAsync(&perr, bt->p_err.p, sizeof(int), cudaMemcpyDeviceToHost, bt->stream));
   CK(cudaStreamSynchronize(bt->stream));
+  if (perr) return fail(FLUTAS_ECUDA, "batch_solve: a work item's wait for its grid's previous pass gave up");
   int rc = FLUTAS_OK;
   for (int g = 0; g < bt->ng; g++) {
     if (relres) relres[g] = rr[g];
@@ -2538,7 +2649,21 @@ int flutas_gb300_batch_report(void *batch, char *buf, int len) {
   flutas_batch *bt;
   TRY(check_batch(batch, &bt));
   if (!buf || len <= 0) return fail(FLUTAS_EINVAL, "batch_report: bad buffer");
-  snprintf(buf, (size_t)len, "%s", bt->report.c_str());
+  std::string r = bt->report;
+  if (bt->exec && !bt->per_pass && bt->stats && bt->p_err.p) {
+    // the last solve's queue: items worked, tiles skipped (converged grids), waits and their polls
+    unsigned long long st[12] = {};
+    CK(cudaStreamSynchronize(bt->stream));
+    CK(cudaMemcpy(st, (char *)bt->p_err.p + sizeof(int) * 4, sizeof(st), cudaMemcpyDeviceToHost));
+    char line[512];
+    const double nb = bt->grid_p > 0 ? 1e6 * bt->grid_p : 1.0;  // ms a block, averaged over the blocks
+    snprintf(line, sizeof line, "queue: %d blocks, %llu items worked, %llu tiles skipped, %llu waits, %llu polls; "
+             "ms a block x0 %.2f y %.2f z %.2f yi %.2f xi0 %.2f xr %.2f xi1 %.2f sched %.2f\n", bt->grid_p, st[0],
+             st[1], st[2], st[3], st[4] / nb, st[5] / nb, st[6] / nb, st[7] / nb, st[8] / nb, st[9] / nb, st[10] / nb,
+             st[11] / nb);
+    r += line;
+  }
+  snprintf(buf, (size_t)len, "%s", r.c_str());
   return FLUTAS_OK;
 }
 

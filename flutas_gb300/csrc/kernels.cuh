@@ -1613,7 +1613,7 @@ __global__ void __launch_bounds__(256) kb_ypass(BatchQueue q) {
 
 // mode 0: x = e * normfft; mode 1: x += e * normfft
 #ifndef FG_NO_PLAIN_KERNELS
-__global__ void __launch_bounds__(256) kb_xinv(BatchQueue q, int mode) {
+__global__ void __launch_bounds__(256, 2) kb_xinv(BatchQueue q, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ns = *q.nslots;
   const long total = q.prefix[ns];
@@ -1744,6 +1744,273 @@ __global__ void __launch_bounds__(128) kb_z(BatchQueue q) {
     if (!*G.active) continue;
     const long qcol = (item - q.prefix[slot]) * blockDim.x + threadIdx.x;
     zcol_f32<16>(G.za, G.S, G.S2, qcol, qcol < G.za.nq, chk);
+  }
+}
+#endif
+
+// ===========================================================================
+// The whole batched refinement as one persistent kernel.  One work queue runs
+// over every (pass, grid, tile) item of the solve in pass order: the first
+// solve (x, y, z, y^-1, x^-1), then per refinement iteration the residual x
+// pass and, for the grids still above tol, the next correction.  An item waits
+// for the previous pass of its own grid only (a per-(pass, grid) count of the
+// finished tiles), so the passes of different grids overlap: small grids run
+// their z sweeps while large ones still transform.  A grid that has reached
+// tol skips its later passes: the first item of such a pass moves the queue
+// past the grid's other tiles of it (atomicMax) and counts them finished, so a
+// skipped pass costs about one item, not one per tile.  Items leave the queue in
+// order and every earlier item belongs to a running block, so a wait always
+// ends; it is still bounded: past the limit the kernel records the failure,
+// raises the abort flag every block checks, and returns.
+// ===========================================================================
+enum BatchPass : int { PB_XF0 = 0, PB_Y = 1, PB_Z = 2, PB_YI = 3, PB_XI0 = 4, PB_XR = 5, PB_XI1 = 6 };
+
+struct PersistArgs {
+  const BatchGrid *grids;
+  int ng;
+  const long *prefix;  // 3 x (ng+1) running totals of the x tiles, y tiles, z tiles (blockDim columns) of the grids
+  const int *ptype;    // per pass: BatchPass
+  const int *piter;    // per pass: refinement iteration (0: the first solve)
+  const long *poff;    // npass + 1: first queue item of each pass
+  const int *pstart;   // npass * ng + 1: first queue item of (pass p, grid g) at p * ng + g
+  int *pass_done;      // npass: finished tiles of each pass over all grids
+  int npass;
+  int chunk;           // consecutive items a block takes from the queue at once
+  int *counter;        // queue position (zeroed before the launch)
+  int *done;           // npass x ng: finished tiles of (pass, grid)
+  int *err;            // [0]: a wait gave up; [1]: abort flag
+  double *nrm;         // per grid, stride entries: [0] ||f||^2, [it] ||r||^2 after it FP32 solves
+  int stride;          // max_iter + 1
+  double tol;
+  int max_iter;
+  long spin_limit;     // polls of a dependency wait before it gives up
+  unsigned long long *stats;  // items worked, tiles skipped, waits that polled, polls, ns per pass type (or null)
+};
+
+__host__ __device__ inline int pass_kind(int type) {  // 0: x tiles, 1: y tiles, 2: z tiles
+  return (type == PB_Y || type == PB_YI) ? 1 : (type == PB_Z ? 2 : 0);
+}
+
+#ifndef FG_NO_PLAIN_KERNELS
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Largest i in [0, n) with A[i] <= key, for A non-decreasing and A[0] <= key:
+// a 32-way search by one warp (every lane calls it), two dependent loads for
+// up to 1024 entries.
+__device__ __forceinline__ int warp_find32(const int *A, int n, int key) {
+  const int lane = threadIdx.x & 31;
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int step = (hi - lo + 31) >> 5;
+    const int idx = lo + lane * step;
+    const unsigned m = __ballot_sync(0xffffffffu, idx < hi && A[idx] <= key);
+    lo += (31 - __clz(m)) * step;
+    hi = min(lo + step, hi);
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int ld_acquire_gpu(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_release_gpu_add(int *p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <int MINB>  // resident blocks per SM the registers are sized for (2: 128 a thread, 1: up to 255)
+__global__ void __launch_bounds__(256, MINB) kb_persist(PersistArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int kMaxPass = 5 + 5 * 32;
+  __shared__ int s_ptype[kMaxPass], s_piter[kMaxPass];
+  __shared__ int s_p, s_g, s_go, s_count;  // s_go 1: work, 0: skip (grid converged), -1: abort or end
+  __shared__ long s_tile;
+  for (int i = threadIdx.x; i < a.npass; i += blockDim.x) {
+    s_ptype[i] = a.ptype[i];
+    s_piter[i] = a.piter[i];
+  }
+  const int total = a.pstart[(long)a.npass * a.ng];
+  const int npair = a.npass * a.ng;
+  const int lane = threadIdx.x & 31;
+  const bool w0 = threadIdx.x < 32;
+  // Warp 0 schedules.  The queue hands out chunks of `chunk` consecutive items;
+  // lane 0 takes the next chunk while the block works on the current one, so
+  // the queue's round trip hides behind the tiles.  Every item depends on
+  // lower-numbered items only, and a block finishes its items in order, so the
+  // lowest unfinished item is always some block's current one and can run.
+  const int K = a.chunk;
+  int cur = 0, cend = 0, nxt = (w0 && lane == 0) ? atomicAdd(a.counter, K) : 0;
+  bool want = false;  // the next chunk is to be taken
+  // The (pass, grid) pair of the last item, its queue range [qs, qe) and the
+  // decision for it: later items of the same pair reuse all three.
+  int q = 0, qs = 0, qe = 0, qgo = 1;
+  // Every pass <= acq_upto had finished over all grids when an acquire of this
+  // block saw it: items whose previous pass is among them need no wait and no
+  // acquire (all they read was final then; tiles of one pass read and write
+  // disjoint data).  Fewer acquires also keep the tables in L1.
+  int acq_upto = -1;
+  unsigned long long n_work = 0, n_skip = 0, n_wait = 0, n_poll = 0, t_sched = 0;
+  __syncthreads();
+  for (;;) {
+    if (w0) {
+      const unsigned long long ts = a.stats ? globaltimer_ns() : 0;
+      if (cur >= cend) {
+        cur = nxt;
+        cend = nxt + K;
+        want = true;
+      }
+      const int item = __shfl_sync(0xffffffffu, cur, 0);
+      cur++;
+      int go = -1, count = 1;
+      if (item < total) {
+        if (item >= qe) {  // a new pair: find it, wait for its grid's previous pass, decide
+          {  // one scan of the next 32 pairs, a search of the rest when it is further
+            const int idx = q + lane;
+            const int v = idx <= npair ? a.pstart[idx] : INT_MAX;
+            const unsigned m = __ballot_sync(0xffffffffu, v <= item);
+            if (m != 0xffffffffu) q += 31 - __clz(m);
+            else q += 31 + warp_find32(a.pstart + q + 31, npair - q - 31, item);
+          }
+          qs = a.pstart[q];
+          qe = a.pstart[q + 1];
+          const int p = q / a.ng, g = q - p * a.ng;
+          const int type = s_ptype[p], it = s_piter[p];
+          qgo = 1;
+          if (p > 0 && acq_upto < p - 1 && lane == 0) {  // the previous pass of this grid, every tile of it
+            const int qp = q - a.ng;
+            const int need = a.pstart[qp + 1] - a.pstart[qp];
+            const int need_all = (int)(a.poff[p] - a.poff[p - 1]);
+            const int *d = a.done + qp, *dall = a.pass_done + (p - 1);
+            long spins = 0;
+            for (;;) {  // acquire: the finished tiles' writes are visible from here on
+              const int c = ld_acquire_gpu(d), call = ld_acquire_gpu(dall);
+              if (call >= need_all) acq_upto = p - 1;
+              if (c >= need) break;
+              if (((volatile int *)a.err)[1] || ++spins > a.spin_limit) {
+                atomicExch(a.err, 1);
+                atomicExch(a.err + 1, 1);
+                qgo = -1;
+                break;
+              }
+              __nanosleep(64);
+            }
+            n_wait += spins > 0;
+            n_poll += spins;
+          }
+          qgo = __shfl_sync(0xffffffffu, qgo, 0);
+          __syncwarp();
+          // converged after iteration j <= jmax: lane j-1 looks at ||r_j||^2 / ||f||^2
+          const int jmax = type == PB_XR ? it - 1 : it;
+          if (qgo == 1 && jmax >= 1) {
+            const double *nr = a.nrm + (long)g * a.stride;
+            bool conv = false;
+            if (lane < jmax) {
+              const double f2 = __ldcg(nr), r2 = __ldcg(nr + lane + 1);
+              const double rel = f2 > 0.0 ? sqrt(r2 / f2) : sqrt(r2);
+              conv = !(rel > a.tol);  // NaN stops the grid too
+            }
+            conv = __any_sync(0xffffffffu, conv);
+            if (conv || (type != PB_XR && it >= a.max_iter)) qgo = 0;
+          }
+          if (qgo == 0 && lane == 0) {
+            // The grid is done: move the queue past the rest of its tiles of this pass
+            // and count the ones no block has taken yet as finished.
+            const int old = atomicMax(a.counter, qe);
+            if (old < qe) count += qe - old;
+          }
+        }
+        go = qgo;
+        if (lane == 0) {
+          if (go == 0) n_skip += count;
+          else if (go == 1) n_work++;
+          if (go >= 0 && want) {
+            nxt = atomicAdd(a.counter, K);
+            want = false;
+          }
+        }
+      }
+      if (lane == 0) {
+        const int p = q / a.ng;
+        s_p = p; s_g = q - p * a.ng; s_tile = item - qs; s_go = go; s_count = count;
+        if (a.stats) t_sched += globaltimer_ns() - ts;
+      }
+    }
+    __syncthreads();
+    const int go = s_go, p = s_p, g = s_g;
+    const long tile = s_tile;
+    if (go < 0) break;
+    const int type = s_ptype[p], it = s_piter[p];
+    const unsigned long long t0 = a.stats ? globaltimer_ns() : 0;
+    if (go) {
+      const BatchGrid &G = a.grids[g];
+      double *nr = a.nrm + (long)g * a.stride;
+      float ss = 0.0f;
+      switch (type) {
+        case PB_XF0: {
+          InKeep<InHalo> in{InHalo{G.x, G.g}, G.f, G.g};
+          xfwd_tile<float, InKeep<InHalo>>(G.ax, in, G.S, G.g, G.M, tile * G.M, smem_raw, ss);
+          block_sum_add((double)ss, nr);
+          break;
+        }
+        case PB_XR: {
+          InResidual in;
+          in.f = G.f; in.x = G.x; in.zc = G.zres; in.dxi2 = G.dxi2; in.dyi2 = G.dyi2;
+          for (int t = 0; t < 6; t++) in.bc[t] = G.bc[t];
+          in.g = G.g;
+          xfwd_tile<float, InResidual>(G.ax, in, G.S, G.g, G.M, tile * G.M, smem_raw, ss);
+          block_sum_add((double)ss, nr + it);
+          break;
+        }
+        case PB_Y: ypass_tile<float, false>(G.ay, G.S, G.g, G.W, tile, smem_raw); break;
+        case PB_YI: ypass_tile<float, true>(G.ay, G.S, G.g, G.W, tile, smem_raw); break;
+        case PB_Z: {
+          const long qcol = tile * blockDim.x + threadIdx.x;
+          zcol_f32<16>(G.za, G.S, G.S2, qcol, qcol < G.za.nq, (float *)smem_raw);
+          break;
+        }
+        case PB_XI0:
+          xinv_tile<float, OutHalo>(G.ax, G.S, OutHalo{G.x, G.normfft, G.g}, G.g, G.M, tile * G.M, smem_raw);
+          break;
+        default:
+          xinv_tile<float, OutHaloAdd>(G.ax, G.S, OutHaloAdd{G.x, G.normfft, G.g}, G.g, G.M, tile * G.M, smem_raw);
+          break;
+      }
+    }
+    __syncthreads();  // every thread's writes of this tile precede the count
+    if (threadIdx.x == 0) {
+      // release, cumulative over the block's writes that the barrier ordered before it
+      red_release_gpu_add(a.done + (long)p * a.ng + g, s_count);
+      red_release_gpu_add(a.pass_done + p, s_count);
+      if (a.stats && go) atomicAdd(a.stats + 4 + type, globaltimer_ns() - t0);  // ns per pass type
+    }
+  }
+  if (threadIdx.x == 0 && a.stats) {
+    atomicAdd(a.stats + 0, n_work);
+    atomicAdd(a.stats + 1, n_skip);
+    atomicAdd(a.stats + 2, n_wait);
+    atomicAdd(a.stats + 3, n_poll);
+    atomicAdd(a.stats + 11, t_sched);
+  }
+}
+
+// relres and FP32 solves of every grid from the norms the persistent kernel left.
+__global__ void kb_finalize(PersistArgs a, double *relres, int *iters) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < a.ng; g += gridDim.x * blockDim.x) {
+    const double *n = a.nrm + (long)g * a.stride;
+    const double f2 = n[0];
+    double rel = 0.0;
+    int j = 1;
+    for (; j <= a.max_iter; j++) {
+      rel = f2 > 0.0 ? sqrt(n[j] / f2) : sqrt(n[j]);
+      if (!(rel > a.tol) || j == a.max_iter) break;
+    }
+    relres[g] = rel;
+    iters[g] = j;
   }
 }
 #endif

@@ -1,8 +1,10 @@
 """Batched mixed-precision solves: many grids of uneven sizes and BCs in one
-graph-replayed sequence of persistent pass kernels.  Each grid must reach the
-requested relative residual, agree with the FP64 oracle within the error that
-residual allows, and give the same answer alone (single-grid mixed solve) as in
-the batch."""
+graph-replayed sequence of work-queue pass kernels (the default), or in one
+persistent kernel that drains a (pass, grid, tile) queue
+(FLUTAS_GB300_BATCH_PERSISTENT=1).  Each grid must reach the requested relative
+residual, agree with the FP64 oracle within the error that residual allows, and
+give the same answer alone (single-grid mixed solve) as in the batch; the two
+batch forms give the same solutions bit for bit."""
 import numpy as np
 import pytest
 
@@ -32,8 +34,14 @@ def _batch_inputs():
     return grids, rhs
 
 
+@pytest.fixture(params=["passes", "persistent"])
+def batch_form(request, monkeypatch):
+    monkeypatch.setenv("FLUTAS_GB300_BATCH_PERSISTENT", "1" if request.param == "persistent" else "0")
+    return request.param
+
+
 @pytest.mark.parametrize("tol", [1e-6, 1e-10])
-def test_batch_matches_oracle_and_single(lib, oracle, tol):
+def test_batch_matches_oracle_and_single(lib, oracle, tol, batch_form):
     grids, rhs = _batch_inputs()
     B = lib.Batch(grids, autotune=True)
     for g, r in enumerate(rhs):
@@ -60,7 +68,7 @@ def test_batch_matches_oracle_and_single(lib, oracle, tol):
     B.destroy()
 
 
-def test_batch_second_solve_reuses_graph(lib):
+def test_batch_second_solve_reuses_graph(lib, batch_form):
     grids, rhs = _batch_inputs()
     B = lib.Batch(grids[:3], autotune=False)
     for g in range(3):
@@ -97,3 +105,26 @@ def test_batch_grid_alone_equals_in_batch(lib, tol):
         d = rel_l2(mixed[g][1:-1, 1:-1, 1:-1], alone[1:-1, 1:-1, 1:-1], remove_mean=singular(gd["cbc"]))
         print(f"batch grid {g} in the mix vs alone: {d:.2e}")
         assert d <= tol, (g, d)
+
+
+@pytest.mark.parametrize("tol", [1e-6, 1e-10])
+def test_persistent_kernel_equals_pass_kernels(lib, monkeypatch, tol):
+    """The persistent kernel runs the same tiles as the pass kernels: the same
+    FP32 solves per grid and the same solutions, bit for bit."""
+    grids, rhs = _batch_inputs()
+    out = {}
+    for form in ("0", "1"):
+        monkeypatch.setenv("FLUTAS_GB300_BATCH_PERSISTENT", form)
+        monkeypatch.setenv("FLUTAS_GB300_BATCH_STATS", form)
+        B = lib.Batch(grids, autotune=False)
+        for g, r in enumerate(rhs):
+            B.set(g, r)
+        rr, it = B.solve(tol=tol, max_iter=8)
+        out[form] = (rr, it, [B.get(g) for g in range(len(grids))], B.report())
+        B.destroy()
+    assert np.array_equal(out["0"][1], out["1"][1])
+    np.testing.assert_allclose(out["0"][0], out["1"][0], rtol=1e-9)  # norms summed in another order
+    for a, b in zip(out["0"][2], out["1"][2]):
+        assert np.array_equal(a, b)
+    q = [ln for ln in out["1"][3].splitlines() if ln.startswith("queue:")]
+    assert q and "0 tiles skipped" not in q[0], out["1"][3]

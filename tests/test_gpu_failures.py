@@ -65,7 +65,9 @@ def test_projection_nonfinite_velocity(lib, precision):
     assert e.value.code == lib.FLUTAS_ENONFINITE
 
 
-def test_batch_nonfinite_rhs(lib):
+@pytest.mark.parametrize("form", ["0", "1"], ids=["passes", "persistent"])
+def test_batch_nonfinite_rhs(lib, monkeypatch, form):
+    monkeypatch.setenv("FLUTAS_GB300_BATCH_PERSISTENT", form)
     grids, rhs = [], []
     rng = np.random.default_rng(5)
     for n, cbc in (((32, 32, 16), "PPPPNN"), ((48, 32, 16), "NNDDNN")):
