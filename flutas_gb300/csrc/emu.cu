@@ -137,6 +137,50 @@ extern "C" __attribute__((visibility("default"))) int fg_emu_bounduvw(const char
     for (int c = 0; c < 3; c++) setbc_maps(a.m[c][d], sides[d][c], n[d], h);
   return emu_ghosts(a);
 }
+// bounduvw slab by slab through the segments k_ghosts_seg runs (z-slabs of K
+// interior planes, the ghost planes with the first and last slab).  Returns 1
+// when the maps do not compose, 3 when the slabs' segments do not cover every
+// written cell exactly once or hold a cell outside their planes.
+extern "C" __attribute__((visibility("default"))) int fg_emu_bounduvw_slabs(const char *cbc, const int *n,
+                                                                             const double *bc, int nh_d, int h,
+                                                                             const double *dl, const double *dzc,
+                                                                             const double *dzf, double *u, double *v,
+                                                                             double *w, int K) {
+  if (h < 1 || h > 4 || K < 1) return 2;
+  BcSide sides[3][3][2];
+  setbc_sides(cbc, bc, n[2], nh_d, h, dl, dzc, dzf, sides);
+  GhostArgs<3> a;
+  a.f[0] = u; a.f[1] = v; a.f[2] = w;
+  a.n[0] = n[0]; a.n[1] = n[1]; a.n[2] = n[2]; a.h = h;
+  for (int d = 0; d < 3; d++)
+    for (int c = 0; c < 3; c++) setbc_maps(a.m[c][d], sides[d][c], n[d], h);
+  long count = 0;
+  if (!ghosts_ready(a, &count)) return 1;
+  std::vector<int> seen(count, 0);
+  const int nz = n[2], nslab = (nz + K - 1) / K;
+  for (int sl = 0; sl < nslab; sl++) {
+    const int ka = 1 + sl * K, kb = std::min(nz, ka + K - 1);
+    const int e0 = sl == 0 ? 0 : ka + h - 1, e1 = sl == nslab - 1 ? nz + 2 * h : kb + h;
+    const GhostSegs s = ghost_segs_of_planes(a, e0, e1);
+    for (long q = 0; q < s.total; q++) {
+      const long t = ghost_seg_cell(s, q);
+      if (t < 0 || t >= count) return 3;
+      seen[t]++;
+      int ip[3];
+      ghost_cell(a, t, ip);
+      const int e = ip[2] - 1 + h;
+      if (e < e0 || e >= e1) return 3;
+      const long o = ghost_index(a, ip);
+      for (int c = 0; c < 3; c++) {
+        double val;
+        if (ghost_value(a, c, ip, &val)) a.f[c][o] = val;
+      }
+    }
+  }
+  for (long t = 0; t < count; t++)
+    if (seen[t] != 1) return 3;
+  return 0;
+}
 extern "C" __attribute__((visibility("default"))) void fg_emu_diff32(const double *a, const double *b, float *d,
                                                                       long n) {
   for (long i = 0; i < n; i++) {

@@ -166,7 +166,8 @@ struct Mirrors {
   }
 };
 
-int stage_in(Mirrors &m, const void *user, size_t bytes, bool in, bool out, cudaStream_t st, Staged *s) {
+int stage_in(Mirrors &m, const void *user, size_t bytes, bool in, bool out, cudaStream_t st, Staged *s,
+             bool copy_now = true) {  // copy_now false: the caller copies a host array in itself
   s->host = nullptr;
   s->bytes = bytes;
   s->out = out;
@@ -181,7 +182,7 @@ int stage_in(Mirrors &m, const void *user, size_t bytes, bool in, bool out, cuda
   TRY(m.get(bytes, &d));
   s->d = (double *)d;
   s->host = user;
-  if (in) CK(cudaMemcpyAsync(d, user, bytes, cudaMemcpyHostToDevice, st));
+  if (in && copy_now) CK(cudaMemcpyAsync(d, user, bytes, cudaMemcpyHostToDevice, st));
   return 0;
 }
 
@@ -397,6 +398,7 @@ struct flutas_plan {
   cudaStream_t stream = 0;
   cudaStream_t copy_stream = nullptr;  // device -> host copies that overlap the plan stream's kernels
   cudaEvent_t ev_ready = nullptr, ev_copied = nullptr;
+  std::vector<cudaEvent_t> slab_ev;  // host-to-device copy of each z-slab done (copy stream)
   bool sync = true;
   int path64 = 0, path32 = 0;  // 0 separate passes, 1 fused plane kernel, 2 cluster plane kernel
   int clus64 = 0, clus32 = 0;  // cluster size of path 2
@@ -494,8 +496,8 @@ template <int KID, typename T, typename F> const char *kname() {
 // --------------------------------------------------------------------------
 template <typename T, typename In>
 int fwd_xy(flutas_plan *pl, const In &in, T *S, const AxisTables &tx, const AxisTables &ty, int path,
-           double *nrm = nullptr) {
-  Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
+           double *nrm = nullptr, int nz_planes = 0) {  // nz_planes: the first planes only (a z-slab)
+  Geo g{pl->n[0], pl->n[1], nz_planes > 0 ? nz_planes : pl->n[2], 1};
   cudaStream_t st = pl->stream;
   if (path == 1) {
     const size_t sm = plane_smem<T>(g.nx, g.ny);
@@ -831,7 +833,9 @@ struct FinalCorrec {
 
 template <typename First>
 int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, int max_iter, double *relres,
-                    int *iters, FinalCorrec *fc = nullptr) {
+                    int *iters, FinalCorrec *fc = nullptr, bool first_done = false) {
+  // first_done: the first pass (RHS kept in fbuf, FP32 RHS transformed in S32,
+  // ||f||^2 in nrm[0], the other norms zeroed) was run by the caller (slab_first_pass)
   Geo g{pl->n[0], pl->n[1], pl->n[2], 1};
   const size_t halo_bytes = sizeof(double) * (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
   TRY(pl->S32.ensure(sizeof(float) * (size_t)g.nx * g.ny * g.nz));
@@ -861,11 +865,14 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
     TRY(stencil(R, nullptr, S, acc));
     return fwd_xy<float>(pl, InF32{S, g}, S, pl->tx32, pl->ty32, pl->path32);
   };
-  CK(cudaMemsetAsync(nrm, 0, sizeof(double) * (max_iter + 2), st));
-  if (split) {
+  if (first_done) {
+    if (!split) return fail(FLUTAS_ECUDA, "internal: a slab first pass needs the split form");
+  } else if (split) {
+    CK(cudaMemsetAsync(nrm, 0, sizeof(double) * (max_iter + 2), st));
     TRY(stencil(first, f, S, nrm + 0));
     TRY(fwd_xy<float>(pl, InF32{S, g}, S, pl->tx32, pl->ty32, pl->path32));
   } else {
+    CK(cudaMemsetAsync(nrm, 0, sizeof(double) * (max_iter + 2), st));
     TRY(fwd_xy<float>(pl, InKeep<First>{first, f, g}, S, pl->tx32, pl->ty32, pl->path32, nrm + 0));
   }
   TRY(zsolve<float>(pl, S, lam, a, b, c, true));
@@ -1183,6 +1190,7 @@ int flutas_gb300_fftend(void **arrplan) {
     cudaEventDestroy(pl->ev_ready);
     cudaEventDestroy(pl->ev_copied);
   }
+  for (cudaEvent_t e : pl->slab_ev) cudaEventDestroy(e);
   DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->czc, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
                   &pl->tx64.W, &pl->tx64.Q, &pl->ty64.W, &pl->ty64.Q, &pl->tx32.W, &pl->tx32.Q, &pl->ty32.W,
                   &pl->ty32.Q, &pl->S64, &pl->S32, &pl->fbuf, &pl->phi, &pl->phi2, &pl->nrm, &pl->nf_flag,
@@ -1615,12 +1623,24 @@ namespace {
 // src/bound.f90:649-773 when isoutflow is given.  dzc/dzf host
 // values.  One k_ghosts launch for the three set_bc passes (the pass-by-pass
 // kernel, x then y then z as the reference, where the maps do not compose).
+// bounduvw's ghost maps (one launch of k_ghosts for the three passes).
+void bounduvw_maps(const char *cbc, const double *bc, int nx, int ny, int nz, int nh_d, int h, const double dl[3],
+                   const double *dzc_h, const double *dzf_h, double *u, double *v, double *w, GhostArgs<3> *ga,
+                   BcSide sides[3][3][2]) {
+  setbc_sides(cbc, bc, nz, nh_d, h, dl, dzc_h, dzf_h, sides);
+  ga->f[0] = u; ga->f[1] = v; ga->f[2] = w;
+  ga->n[0] = nx; ga->n[1] = ny; ga->n[2] = nz; ga->h = h;
+  for (int d = 0; d < 3; d++)
+    for (int c = 0; c < 3; c++) setbc_maps(ga->m[c][d], sides[d][c], ga->n[d], h);
+}
+
 int bounduvw_dev(const char *cbc, const double *bc, int nx, int ny, int nz, int nh_d, int h, const double dl[3],
                  const double *dzc_h, const double *dzf_h, double *u, double *v, double *w, cudaStream_t st,
                  const int *isoutflow = nullptr, const double *dzf_d = nullptr) {
   if (h < 1 || h > 4) return fail(FLUTAS_EUNSUPPORTED, "bounduvw: halo %d not in 1..4", h);
   BcSide sides[3][3][2];
-  setbc_sides(cbc, bc, nz, nh_d, h, dl, dzc_h, dzf_h, sides);
+  GhostArgs<3> ga;
+  bounduvw_maps(cbc, bc, nx, ny, nz, nh_d, h, dl, dzc_h, dzf_h, u, v, w, &ga, sides);
   SetBc3Args passes[3];
   for (int d = 0; d < 3; d++) {
     SetBc3Args &a = passes[d];
@@ -1629,11 +1649,6 @@ int bounduvw_dev(const char *cbc, const double *bc, int nx, int ny, int nz, int 
     for (int c = 0; c < 3; c++)
       for (int ib = 0; ib < 2; ib++) a.side[c][ib] = sides[d][c][ib];
   }
-  GhostArgs<3> ga;
-  ga.f[0] = u; ga.f[1] = v; ga.f[2] = w;
-  ga.n[0] = nx; ga.n[1] = ny; ga.n[2] = nz; ga.h = h;
-  for (int d = 0; d < 3; d++)
-    for (int c = 0; c < 3; c++) setbc_maps(ga.m[c][d], sides[d][c], ga.n[d], h);
   bool done;
   TRY(ghosts_launch(ga, st, &done));
   for (int d = 0; d < 3 && !done; d++) {  // grids too small for the maps to compose: pass by pass
@@ -1715,13 +1730,181 @@ int flutas_gb300_bounduvw(const char cbcvel[18], const int n[3], const double bc
 
 namespace {
 
+int ensure_copy_stream(flutas_plan *pl) {
+  if (pl->copy_stream) return 0;
+  CK(cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&pl->ev_ready, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&pl->ev_copied, cudaEventDisableTiming));
+  return 0;
+}
+
+// The mixed solve's first pass runs as a stencil pass plus the compile-time
+// plane kernels (solve_mixed_dev's split form).
+bool mixed_split(const flutas_plan *pl) {
+  return pl->path32 == 2 && fixed_supported(pl->n[0], pl->n[1], pl->clus32, pl->tx32.ap.pair, pl->ty32.ap.pair);
+}
+
+// Host fields of the fused mixed projection copied in on the plan's copy
+// stream, the last one (w) in z-slabs, with the step's first pass
+// (Dodd-Ferrante terms, ghost cells of u*, v*, w*, fillps into the FP64 RHS
+// and the FP32 spectrum, the forward plane transforms) running slab by slab
+// behind the copies on the plan stream.  None of them reads w above the planes
+// it writes, so slab s runs once w's slab s is in; the other fields arrive
+// whole, first (one copy each: the link loses ~5 us a copy, and while kernels
+// run beside it the copies also slow down, so only the last field is cut).
+// Fields: halo h, device mirror, host array (page-locked), cut in slabs or not.
+struct SlabIn {
+  int nslab = 0, K = 0;  // slabs of K interior planes (the last one may be shorter)
+  struct Field {
+    const void *host;
+    double *dev;
+    int h;
+    bool sliced;
+  } f[6];
+  int nf = 0;
+  GhostArgs<3> ga;  // bounduvw's maps (cbcvel given)
+  bool ghosts = false;
+};
+
+// Slab s's extended planes [e0, e1) of a field with halo h: its interior
+// planes, and the ghost planes below the first slab / above the last one.
+void slab_planes(int s, int nslab, int K, int nz, int h, int *e0, int *e1) {
+  const int ka = 1 + s * K, kb = std::min(nz, ka + K - 1);
+  *e0 = s == 0 ? 0 : ka + h - 1;
+  *e1 = s == nslab - 1 ? nz + 2 * h : kb + h;
+}
+
+// The slab form of the fused mixed projection, when it applies: every field
+// a page-locked host array, the split first pass, no boundary RHS (fillps adds
+// no plane-dependent terms), and bounduvw's z ghost cells below the first slab
+// computed from planes of the first slab (not z-periodic velocities).
+bool slab_plan(flutas_plan *pl, int nh_u, double dxi, double dyi, const char *cbcvel, const double *bcvel,
+               const void *const hosts[6], SlabIn *sl) {
+  const char *e = getenv("FLUTAS_GB300_SLABS");
+  if (e && atoi(e) == 0) return false;
+  if (!mixed_split(pl) || !pl->rhsb_zero) return false;
+  for (int q = 0; q < 6; q++)
+    if (hosts[q] && (ptr_kind(hosts[q]) != PTR_HOST || !is_pinned_host(hosts[q]))) return false;
+  const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2], nh_d = pl->nh_d;
+  sl->K = std::max(16, ((nz + 7) / 8 + 15) / 16 * 16);  // about eight slabs of a multiple of 16 planes
+  sl->nslab = (nz + sl->K - 1) / sl->K;
+  if (sl->nslab < 2 || sl->K < nh_u + 2) return false;
+  if (cbcvel) {
+    std::vector<double> dzc_h(nz + 2 * nh_d), dzf_h(nz + 2 * nh_d);
+    for (int k = 0; k < nz + 2 * nh_d; k++) {
+      dzc_h[k] = 1.0 / pl->dzci_h[k];
+      dzf_h[k] = 1.0 / pl->dzfi_h[k];
+    }
+    const double dl[3] = {1.0 / dxi, 1.0 / dyi, 0.0};
+    BcSide sides[3][3][2];
+    bounduvw_maps(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dl, dzc_h.data(), dzf_h.data(), nullptr, nullptr,
+                  nullptr, &sl->ga, sides);
+    long tot = 0;
+    if (!ghosts_ready(sl->ga, &tot)) return false;
+    for (int c = 0; c < 3; c++)
+      for (int t = 1 - nh_u; t <= 0; t++) {
+        const GMap &m = sl->ga.m[c][2][-t];
+        if ((m.kind == GM_COPY || m.kind == GM_AFF) && m.src > sl->K) return false;
+      }
+    sl->ghosts = true;
+  }
+  return true;
+}
+
+// The copies in on the copy stream (the sliced field slab by slab, after the
+// whole ones), and the first pass of the step behind them on the plan stream
+// (slab s once the sliced field's slab s is in):
+// pres_tw_src (a non-null), bounduvw's ghost cells of the slab's planes,
+// fillps into the FP64 RHS (fbuf) and the FP32 spectrum with ||f||^2, and the
+// forward plane transforms.  The kernels take the slab as a grid of nzs
+// planes whose arrays start ka - 1 planes in (every access is relative to the
+// cell); the results equal one pass over the grid bit for bit.
+int slab_first_pass(flutas_plan *pl, SlabIn &sl, const PresTwArgs *a, const InFillps &in, int max_iter,
+                    cudaStream_t st) {
+  const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2];
+  TRY(ensure_copy_stream(pl));
+  while ((int)pl->slab_ev.size() < sl.nslab) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    pl->slab_ev.push_back(e);
+  }
+  cudaStream_t cs = pl->copy_stream;
+  CK(cudaEventRecord(pl->ev_ready, st));  // the mirrors are free once the plan stream's earlier work is done
+  CK(cudaStreamWaitEvent(cs, pl->ev_ready, 0));
+  for (int q = 0; q < sl.nf; q++) {
+    const SlabIn::Field &F = sl.f[q];
+    if (!F.sliced)
+      CK(cudaMemcpyAsync(F.dev, F.host, sizeof(double) * (size_t)(nx + 2 * F.h) * (ny + 2 * F.h) * (nz + 2 * F.h),
+                         cudaMemcpyHostToDevice, cs));
+  }
+  for (int s = 0; s < sl.nslab; s++) {
+    for (int q = 0; q < sl.nf; q++) {
+      const SlabIn::Field &F = sl.f[q];
+      if (!F.sliced) continue;
+      const size_t plane = sizeof(double) * (size_t)(nx + 2 * F.h) * (ny + 2 * F.h);
+      int e0, e1;
+      slab_planes(s, sl.nslab, sl.K, nz, F.h, &e0, &e1);
+      CK(cudaMemcpyAsync((char *)F.dev + plane * e0, (const char *)F.host + plane * e0, plane * (e1 - e0),
+                         cudaMemcpyHostToDevice, cs));
+    }
+    CK(cudaEventRecord(pl->slab_ev[s], cs));
+  }
+  const int nrm_len = std::max(max_iter, 1) + 2;
+  TRY(pl->S32.ensure(sizeof(float) * (size_t)nx * ny * nz));
+  TRY(pl->fbuf.ensure(sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2)));
+  TRY(pl->nrm.ensure(sizeof(double) * nrm_len));
+  float *S = pl->S32.as<float>();
+  double *f = pl->fbuf.as<double>(), *nrm = pl->nrm.as<double>();
+  CK(cudaMemsetAsync(nrm, 0, sizeof(double) * nrm_len, st));
+  const long psz = (long)(nx + 2) * (ny + 2), usz = (long)(nx + 2 * in.g.h) * (ny + 2 * in.g.h);
+  const long ssz = (long)nx * ny;
+  for (int s = 0; s < sl.nslab; s++) {
+    const int ka = 1 + s * sl.K, kb = std::min(nz, ka + sl.K - 1), nzs = kb - ka + 1;
+    const long sh = ka - 1;
+    CK(cudaStreamWaitEvent(st, pl->slab_ev[s], 0));
+    if (a) {
+      PresTwArgs as = *a;
+      as.p += sh * psz; as.pold += sh * psz; as.rho += sh * psz;
+      as.u += sh * usz; as.v += sh * usz; as.w += sh * usz;
+      as.zA += sh; as.zB += sh;
+      as.g.nz = nzs;
+      TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<presw_grid(as.g), PRESTW_NT, 0, st>>>(as); }));
+    }
+    if (sl.ghosts) {
+      int e0, e1;
+      slab_planes(s, sl.nslab, sl.K, nz, sl.ga.h, &e0, &e1);
+      const GhostSegs gs = ghost_segs_of_planes(sl.ga, e0, e1);
+      if (gs.total > 0)
+        TRY(launch("k_ghosts<3>", st, [&] { k_ghosts_seg<3><<<stream_grid(gs.total), 256, 0, st>>>(sl.ga, gs); }));
+    }
+    InFillps is = in;
+    is.u += sh * usz; is.v += sh * usz; is.w += sh * usz;
+    is.cz += sh;
+    is.g.nz = nzs;
+    const Geo gs{nx, ny, nzs, 1};
+    const long cells = (long)nx * ny * nzs;
+    const int grid = grid_for(k_stencil_pass<InFillps, float>, 256, 0, (cells + 1023) / 1024);
+    if (grid < 0) return grid;
+    if (cells >= (1L << 31) - 4096)
+      TRY(launch("k_stencil<fillps>", st, [&] {
+        k_stencil_pass<InFillps, float, long long><<<grid, 256, 0, st>>>(is, gs, f + sh * psz, S + sh * ssz, nrm);
+      }));
+    else
+      TRY(launch("k_stencil<fillps>", st, [&] {
+        k_stencil_pass<InFillps, float><<<grid, 256, 0, st>>>(is, gs, f + sh * psz, S + sh * ssz, nrm);
+      }));
+    TRY(fwd_xy<float>(pl, InF32{S + sh * ssz, gs}, S + sh * ssz, pl->tx32, pl->ty32, pl->path32, nullptr, nzs));
+  }
+  return 0;
+}
+
 // Body of the fused projection on staged device pointers (plan stream).
 // rho/pold non-null: the Dodd-Ferrante explicit terms of pres_tw_src
 // (src/source.f90:247-309) are added to u*,v*,w* first.
 int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const double *dzci_d, const double *dzfi_d,
                    double dt, double rho0, double *u, double *v, double *w, double *p, int precision, double tol,
                    int max_iter, const double *rho, double *pold, double f_t12_o, const char *cbcvel,
-                   const double *bcvel, Staged *pold_host = nullptr) {
+                   const double *bcvel, Staged *pold_host = nullptr, SlabIn *slabs = nullptr) {
   const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2], nh_d = pl->nh_d;
   Geo g{nx, ny, nz, nh_u};
   std::vector<double> dzc_h(nz + 2 * nh_d), dzf_h(nz + 2 * nh_d);
@@ -1748,23 +1931,31 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   jobs.add(dzfi_d, dti * rho0, pl->czf.as<double>(), nz + 2 * nh_d);
   jobs.add(dzci_d, dt * rho0i, pl->czc.as<double>(), nz + 2 * nh_d);
   TRY(scale_jobs(jobs, st));
+  InFillps in;
+  in.u = u; in.v = v; in.w = w;
+  in.cz = pl->czf.as<double>() + (nh_d - 1);
+  in.cx = dti * dxi * rho0; in.cy = dti * dyi * rho0;
+  in.rhsbx = pl->rhsb[0].as<double>(); in.rhsby = pl->rhsb[1].as<double>(); in.rhsbz = pl->rhsb[2].as<double>();
+  if (pl->rhsb_zero) in.rhsbx = in.rhsby = in.rhsbz = nullptr;  // adding zeros changes nothing
+  in.q1 = in.q2 = in.q3 = 0;
+  in.g = g;
   if (rho) {
     a.p = p; a.pold = pold; a.rho = rho;
     a.u = u; a.v = v; a.w = w;
     a.fp32 = precision == 1 ? 1 : 0;  // FP32 increment in the mixed path, FP64 in the FP64 path
     a.g = g;
-    TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<presw_grid(a.g), PRESTW_NT, 0, st>>>(a); }));
+  }
+  if (slabs) TRY(slab_first_pass(pl, *slabs, rho ? &a : nullptr, in, max_iter, st));
+  if (rho) {
+    if (!slabs)
+      TRY(launch("k_pres_tw_src", st, [&] { k_pres_tw_src<<<presw_grid(a.g), PRESTW_NT, 0, st>>>(a); }));
     if (pold_host && pold_host->host && pold_host->out && is_pinned_host(pold_host->host)) {
       // pres_tw_src has read pold: pold = p now (whole array, then boundp: the same values as the
       // correction pass would write), and its copy to the page-locked host array runs on the
       // plan's copy stream while the solve runs on this one
       CK(cudaMemcpyAsync(pold, p, pb, cudaMemcpyDeviceToDevice, st));
       TRY(boundp_dev(pold, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
-      if (!pl->copy_stream) {
-        CK(cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking));
-        CK(cudaEventCreateWithFlags(&pl->ev_ready, cudaEventDisableTiming));
-        CK(cudaEventCreateWithFlags(&pl->ev_copied, cudaEventDisableTiming));
-      }
+      TRY(ensure_copy_stream(pl));
       CK(cudaEventRecord(pl->ev_ready, st));
       CK(cudaStreamWaitEvent(pl->copy_stream, pl->ev_ready, 0));
       CK(cudaMemcpyAsync((void *)pold_host->host, pold, pb, cudaMemcpyDeviceToHost, pl->copy_stream));
@@ -1774,17 +1965,10 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     }
   }
   // ghosts of u*,v*,w* as the app leaves them before fillps (bounduvw)
-  if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
+  if (cbcvel && !slabs)
+    TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
   TRY(pl->phi.ensure(pb));
   double *phi = pl->phi.as<double>();
-  InFillps in;
-  in.u = u; in.v = v; in.w = w;
-  in.cz = pl->czf.as<double>() + (nh_d - 1);
-  in.cx = dti * dxi * rho0; in.cy = dti * dyi * rho0;
-  in.rhsbx = pl->rhsb[0].as<double>(); in.rhsby = pl->rhsb[1].as<double>(); in.rhsbz = pl->rhsb[2].as<double>();
-  if (pl->rhsb_zero) in.rhsbx = in.rhsby = in.rhsbz = nullptr;  // adding zeros changes nothing
-  in.q1 = in.q2 = in.q3 = 0;
-  in.g = g;
   const Geo gp{nx, ny, nz, 1};
   int rc = 0;
   if (precision == 0) {
@@ -1829,7 +2013,7 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   if (precision != 0) {
     fc.ca = ca;
     fc.boundp_phi = [&] { return boundp_dev(phi, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st); };
-    rc = solve_mixed_dev(pl, in, phi, tol, max_iter, &pl->last_relres, &pl->last_iters, &fc);
+    rc = solve_mixed_dev(pl, in, phi, tol, max_iter, &pl->last_relres, &pl->last_iters, &fc, slabs != nullptr);
     if (rc != 0 && rc != FLUTAS_EITER) return rc;
   }
   if (!fc.applied) {
@@ -1876,19 +2060,33 @@ int projection_entry(void *plan, int nh_u, double dxi, double dyi, const double 
   const size_t ub = sizeof(double) * (size_t)(nx + 2 * nh_u) * (ny + 2 * nh_u) * (nz + 2 * nh_u);
   const size_t pb = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (nz + 2);
   Staged su, sv, sw, sp, sci, sfi, sr, so;
-  TRY(stage_in(pl->mir, u, ub, true, true, st, &su));
-  TRY(stage_in(pl->mir, v, ub, true, true, st, &sv));
-  TRY(stage_in(pl->mir, w, ub, true, true, st, &sw));
-  TRY(stage_in(pl->mir, p, pb, true, true, st, &sp));
+  // host arrays: copied in z-slabs behind which the first pass runs, when the form allows it
+  SlabIn sl;
+  const void *hosts[6] = {u, v, w, p, rho, pold};
+  const bool slab = precision == 1 && slab_plan(pl, nh_u, dxi, dyi, cbcvel, bcvel, hosts, &sl);
+  TRY(stage_in(pl->mir, u, ub, true, true, st, &su, !slab));
+  TRY(stage_in(pl->mir, v, ub, true, true, st, &sv, !slab));
+  TRY(stage_in(pl->mir, w, ub, true, true, st, &sw, !slab));
+  TRY(stage_in(pl->mir, p, pb, true, true, st, &sp, !slab));
   TRY(stage_in(pl->mir, dzci, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sci));
   TRY(stage_in(pl->mir, dzfi, sizeof(double) * (nz + 2 * nh_d), true, false, st, &sfi));
   if (rho) {
-    TRY(stage_in(pl->mir, rho, pb, true, false, st, &sr));
-    TRY(stage_in(pl->mir, pold, pb, true, true, st, &so));  // in: p^(n-1); out: p^n
+    TRY(stage_in(pl->mir, rho, pb, true, false, st, &sr, !slab));
+    TRY(stage_in(pl->mir, pold, pb, true, true, st, &so, !slab));  // in: p^(n-1); out: p^n
+  }
+  if (slab) {
+    const Staged *fs[6] = {&su, &sv, &sw, &sp, &sr, &so};
+    const int order[6] = {3, 4, 5, 0, 1, 2};  // p, rho, pold, u, v whole; w last, in slabs
+    for (int i = 0; i < 6; i++) {
+      const int q = order[i];
+      if (q >= 4 && !rho) continue;
+      sl.f[sl.nf++] = SlabIn::Field{fs[q]->host, fs[q]->d, q < 3 ? nh_u : 1, q == 2};
+    }
+    sl.ga.f[0] = su.d; sl.ga.f[1] = sv.d; sl.ga.f[2] = sw.d;
   }
   int rc = projection_dev(pl, nh_u, dxi, dyi, sci.d, sfi.d, dt, rho0, su.d, sv.d, sw.d, sp.d, precision, tol,
                           max_iter, rho ? sr.d : nullptr, rho ? so.d : nullptr, f_t12_o, cbcvel, bcvel,
-                          rho ? &so : nullptr);
+                          rho ? &so : nullptr, slab ? &sl : nullptr);
   if (rc != 0 && rc != FLUTAS_EITER) {
     if (pl->copy_stream) cudaStreamSynchronize(pl->copy_stream);  // no copy into the caller's array after return
     return rc;

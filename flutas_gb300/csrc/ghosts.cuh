@@ -193,6 +193,46 @@ template <int NC> FG_HD void ghost_cell(const GhostArgs<NC> &a, long t, int ip[3
   }
 }
 
+// Up to four ranges of the enumeration above: the written cells whose z
+// position lies in a range of planes (x faces, y faces, low and high z faces
+// of those planes), for the ghost cells of a z-slab of the field.
+struct GhostSegs {
+  long begin[4], count[4];
+  int n;
+  long total;
+};
+FG_HD long ghost_seg_cell(const GhostSegs &s, long q) {
+  int r = 0;
+  while (r < s.n - 1 && q >= s.count[r]) q -= s.count[r++];
+  return s.begin[r] + q;
+}
+// The segments of extended z planes [e0, e1) (plane e = z position - 1 + h);
+// a.hi must be set (ghosts_ready).
+template <int NC> inline GhostSegs ghost_segs_of_planes(const GhostArgs<NC> &a, int e0, int e1) {
+  const int h = a.h;
+  const long E0 = a.n[0] + 2 * h, E1 = a.n[1] + 2 * h, E2 = a.n[2] + 2 * h;
+  const long w0 = E0 - a.hi[0], w1 = E1 - a.hi[1], w2 = E2 - a.hi[2];
+  const long c0 = a.hi[0], c1 = a.hi[1];
+  const long T0 = w0 * E1 * E2, T1 = c0 * w1 * E2;
+  GhostSegs s{};
+  auto add = [&](long b, long c) {
+    if (c <= 0) return;
+    s.begin[s.n] = b;
+    s.count[s.n] = c;
+    s.n++;
+    s.total += c;
+  };
+  add(w0 * E1 * e0, w0 * E1 * (e1 - e0));             // x faces of the planes
+  add(T0 + c0 * w1 * e0, c0 * w1 * (e1 - e0));        // y faces
+  long lo = e0 > 0 ? e0 : 0, hi = e1 < h ? e1 : h;    // low z faces: slot s at plane s
+  add(T0 + T1 + c0 * c1 * lo, c0 * c1 * (hi - lo));
+  lo = e0 - a.hi[2] > h ? e0 - a.hi[2] : h;           // high z faces: slot s at plane hi[2] + s
+  hi = e1 - a.hi[2] < w2 ? e1 - a.hi[2] : w2;
+  add(T0 + T1 + c0 * c1 * lo, c0 * c1 * (hi - lo));
+  if (s.n == 0) s.n = 1;  // empty: one segment of no cells
+  return s;
+}
+
 // The final value of field c at the written cell ip; false when the cell is
 // unchanged for that field (nothing to write).  The x map applies first.
 template <int NC> FG_HD bool ghost_value(const GhostArgs<NC> &a, int c, const int ip[3], double *out) {

@@ -1482,6 +1482,20 @@ namespace fg {
 // Ghost cells of boundp / bounduvw in one launch: one thread per written cell,
 // each field's value from the composition of set_bc's maps (ghosts.cuh).
 #ifndef FG_NO_PLAIN_KERNELS
+// k_ghosts over the written cells of a range of z planes (GhostSegs).
+template <int NC> __global__ void k_ghosts_seg(const __grid_constant__ GhostArgs<NC> a, GhostSegs s) {
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < s.total; q += (long)gridDim.x * blockDim.x) {
+    const long t = ghost_seg_cell(s, q);
+    int ip[3];
+    ghost_cell(a, t, ip);
+    const long o = ghost_index(a, ip);
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+      double v;
+      if (ghost_value(a, c, ip, &v)) a.f[c][o] = v;
+    }
+  }
+}
 template <int NC> __global__ void k_ghosts(const __grid_constant__ GhostArgs<NC> a, long count) {  // maps read in place
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (long)gridDim.x * blockDim.x) {
     int ip[3];

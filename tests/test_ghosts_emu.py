@@ -22,6 +22,8 @@ def emu():
     L.fg_emu_boundp.restype = C.c_int
     L.fg_emu_bounduvw.argtypes = [C.c_char_p, ip, dp, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp]
     L.fg_emu_bounduvw.restype = C.c_int
+    L.fg_emu_bounduvw_slabs.argtypes = [C.c_char_p, ip, dp, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp, C.c_int]
+    L.fg_emu_bounduvw_slabs.restype = C.c_int
     return L
 
 
@@ -81,3 +83,28 @@ def test_small_grids_do_not_compose(emu, oracle):
     rc = emu.fg_emu_bounduvw(("DD" * 9).encode(), np.array(n, np.int32), np.zeros(18), h, h,
                              np.array([0.25, 1 / 6, 0.0]), dzc, dzf, u, v, w)
     assert rc == 1
+
+
+@pytest.mark.parametrize("h", [1, 2, 3])
+@pytest.mark.parametrize("seed", range(6))
+def test_bounduvw_by_slabs_equals_one_pass(emu, oracle, h, seed):
+    """The slab form of the e2e projection fills the ghost cells of each z-slab
+    after its planes arrive (k_ghosts_seg): the slabs' segments cover every
+    written cell once, each within its slab's planes, and the values equal
+    bounduvw's."""
+    rng = np.random.default_rng(1000 * h + seed)
+    n = [int(x) for x in rng.integers(2 * h + 1, 2 * h + 6, 2)] + [int(rng.integers(2 * h + 3, 40))]
+    K = int(rng.integers(h + 2, max(h + 3, n[2] // 2 + 1)))
+    cbc = _pairs(rng, 9)
+    bc = rng.uniform(-1, 1, 18)
+    dzc, dzf, _, _ = oracle.initgrid(n[2], float(rng.uniform(0, 2)), 1.0, h)
+    dl = np.array([1.0 / n[0], 1.0 / n[1], 0.0])
+    shp = (n[2] + 2 * h, n[1] + 2 * h, n[0] + 2 * h)
+    u, v, w = (rng.standard_normal(shp) for _ in range(3))
+    ref = [a.copy() for a in (u, v, w)]
+    oracle.bounduvw(cbc, n, list(bc), h, h, list(dl), dzc, dzf, *ref)
+    got = [a.copy() for a in (u, v, w)]
+    rc = emu.fg_emu_bounduvw_slabs(cbc.encode(), np.array(n, np.int32), bc, h, h, dl, dzc, dzf, *got, K)
+    assert rc == 0, (rc, n, K, cbc)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b), cbc
