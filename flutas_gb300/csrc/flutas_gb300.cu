@@ -398,6 +398,7 @@ struct flutas_plan {
   cudaStream_t stream = 0;
   cudaStream_t copy_stream = nullptr;  // device -> host copies that overlap the plan stream's kernels
   cudaEvent_t ev_ready = nullptr, ev_copied = nullptr;
+  cudaEvent_t ev_u_ready = nullptr, ev_u_copied = nullptr;  // u's early copy to the host
   std::vector<cudaEvent_t> slab_ev;  // host-to-device copy of each z-slab done (copy stream)
   bool sync = true;
   int path64 = 0, path32 = 0;  // 0 separate passes, 1 fused plane kernel, 2 cluster plane kernel
@@ -827,8 +828,11 @@ int solve_fp64_dev(flutas_plan *pl, double *p, const double *lam, const double *
 struct FinalCorrec {
   CorrecAddArgs ca;
   std::function<int()> boundp_phi;  // ghosts of phi, read by the correction
+  // set: u's correction runs first (k_correc_u), then this (its ghost cells and
+  // its copy to the host on the copy stream), then the check with the rest
+  std::function<int()> u_first;
   double *snapshot = nullptr;       // x as applied, when the solve went on
-  bool applied = false, continued = false;
+  bool applied = false, continued = false, u_early = false;
 };
 
 template <typename First>
@@ -897,10 +901,17 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
       const long cells = (long)g.nx * g.ny * g.nz;
       const int grid = grid_for(k_resnorm_correc<int>, 256, 0, (cells + 511) / 512);
       if (grid < 0) return grid;
+      CorrecAddArgs ca = fc->ca;
+      if (fc->u_first) {
+        TRY(launch("k_correc_u", st, [&] { k_correc_u<<<grid_cells(ca.g), 256, 0, st>>>(ca); }));
+        TRY(fc->u_first());
+        fc->u_early = true;
+        ca.u = nullptr;
+      }
       if (cells >= (1L << 31) - 4096)
-        TRY(launch("k_resnorm_correc", st, [&] { k_resnorm_correc<long long><<<grid, 256, 0, st>>>(R, fc->ca, acc); }));
+        TRY(launch("k_resnorm_correc", st, [&] { k_resnorm_correc<long long><<<grid, 256, 0, st>>>(R, ca, acc); }));
       else
-        TRY(launch("k_resnorm_correc", st, [&] { k_resnorm_correc<int><<<grid, 256, 0, st>>>(R, fc->ca, acc); }));
+        TRY(launch("k_resnorm_correc", st, [&] { k_resnorm_correc<int><<<grid, 256, 0, st>>>(R, ca, acc); }));
       fc->applied = true;
     } else if (norm_only) {
       TRY(stencil(R, nullptr, nullptr, acc));
@@ -1189,6 +1200,8 @@ int flutas_gb300_fftend(void **arrplan) {
     cudaStreamDestroy(pl->copy_stream);
     cudaEventDestroy(pl->ev_ready);
     cudaEventDestroy(pl->ev_copied);
+    cudaEventDestroy(pl->ev_u_ready);
+    cudaEventDestroy(pl->ev_u_copied);
   }
   for (cudaEvent_t e : pl->slab_ev) cudaEventDestroy(e);
   DBuf *bufs[] = {&pl->zdf, &pl->zres, &pl->czf, &pl->czc, &pl->a32, &pl->b32, &pl->c32, &pl->lam, &pl->a, &pl->b, &pl->c, &pl->dzci, &pl->dzfi, &pl->rhsb[0], &pl->rhsb[1], &pl->rhsb[2],
@@ -1735,6 +1748,8 @@ int ensure_copy_stream(flutas_plan *pl) {
   CK(cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&pl->ev_ready, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&pl->ev_copied, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&pl->ev_u_ready, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&pl->ev_u_copied, cudaEventDisableTiming));
   return 0;
 }
 
@@ -1904,7 +1919,8 @@ int slab_first_pass(flutas_plan *pl, SlabIn &sl, const PresTwArgs *a, const InFi
 int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const double *dzci_d, const double *dzfi_d,
                    double dt, double rho0, double *u, double *v, double *w, double *p, int precision, double tol,
                    int max_iter, const double *rho, double *pold, double f_t12_o, const char *cbcvel,
-                   const double *bcvel, Staged *pold_host = nullptr, SlabIn *slabs = nullptr) {
+                   const double *bcvel, Staged *pold_host = nullptr, SlabIn *slabs = nullptr,
+                   Staged *u_host = nullptr) {
   const int nx = pl->n[0], ny = pl->n[1], nz = pl->n[2], nh_d = pl->nh_d;
   Geo g{nx, ny, nz, nh_u};
   std::vector<double> dzc_h(nz + 2 * nh_d), dzf_h(nz + 2 * nh_d);
@@ -2010,12 +2026,53 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
   ca.cx = (dt * dxi) * rho0i; ca.cy = (dt * dyi) * rho0i;
   ca.g = g;
   FinalCorrec fc;
+  // u's copy to a page-locked host array starts while v, w and p are corrected:
+  // its ghost cells (bounduvw's maps of u alone; v's and w's after the solve)
+  GhostArgs<1> gu;
+  GhostArgs<2> gvw;
+  bool u_split = false;
+  if (precision != 0 && u_host && u_host->host && u_host->out && is_pinned_host(u_host->host)) {
+    u_split = true;
+    if (cbcvel) {
+      GhostArgs<3> g3;
+      BcSide sides[3][3][2];
+      bounduvw_maps(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, &g3, sides);
+      gu.f[0] = u;
+      gvw.f[0] = v; gvw.f[1] = w;
+      for (int d = 0; d < 3; d++) {
+        gu.n[d] = gvw.n[d] = g3.n[d];
+        for (int sl = 0; sl < GM_SLOTS; sl++) {
+          gu.m[0][d][sl] = g3.m[0][d][sl];
+          gvw.m[0][d][sl] = g3.m[1][d][sl];
+          gvw.m[1][d][sl] = g3.m[2][d][sl];
+        }
+      }
+      gu.h = gvw.h = g3.h;
+      long t1 = 0, t2 = 0;
+      u_split = ghosts_ready(gu, &t1) && ghosts_ready(gvw, &t2);
+    }
+  }
   if (precision != 0) {
     fc.ca = ca;
     fc.boundp_phi = [&] { return boundp_dev(phi, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st); };
+    if (u_split)
+      fc.u_first = [&]() -> int {
+        if (cbcvel) {
+          bool done = false;
+          TRY(ghosts_launch(gu, st, &done));
+        }
+        TRY(ensure_copy_stream(pl));
+        CK(cudaEventRecord(pl->ev_u_ready, st));
+        CK(cudaStreamWaitEvent(pl->copy_stream, pl->ev_u_ready, 0));
+        CK(cudaMemcpyAsync((void *)u_host->host, u, u_host->bytes, cudaMemcpyDeviceToHost, pl->copy_stream));
+        CK(cudaEventRecord(pl->ev_u_copied, pl->copy_stream));
+        return 0;
+      };
     rc = solve_mixed_dev(pl, in, phi, tol, max_iter, &pl->last_relres, &pl->last_iters, &fc, slabs != nullptr);
     if (rc != 0 && rc != FLUTAS_EITER) return rc;
   }
+  // u changes again below (the solve went on after its fused check): after its early copy
+  if (fc.u_early && fc.continued) CK(cudaStreamWaitEvent(st, pl->ev_u_copied, 0));
   if (!fc.applied) {
     TRY(boundp_dev(phi, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st));
     TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<grid_cells(ca.g), 256, 0, st>>>(ca); }));
@@ -2029,9 +2086,21 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     cd.pold = nullptr;  // written by the first application
     TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<grid_cells(cd.g), 256, 0, st>>>(cd); }));
   }
-  if (cbcvel) TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
+  const bool u_final = fc.u_early && !fc.continued;  // u's early copy holds its final values
+  if (cbcvel) {
+    if (u_final) {
+      bool done = false;
+      TRY(ghosts_launch(gvw, st, &done));
+    } else {
+      TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
+    }
+  }
   TRY(boundp_dev(p, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st, pold_early ? nullptr : pold));  // and pold
   if (pold_early) CK(cudaStreamWaitEvent(st, pl->ev_copied, 0));  // the stream's end covers the copy
+  if (fc.u_early) {
+    if (u_final) u_host->out = false;  // copied; the caller's stage_out skips it
+    CK(cudaStreamWaitEvent(st, pl->ev_u_copied, 0));
+  }
   return rc;
 }
 
@@ -2086,7 +2155,7 @@ int projection_entry(void *plan, int nh_u, double dxi, double dyi, const double 
   }
   int rc = projection_dev(pl, nh_u, dxi, dyi, sci.d, sfi.d, dt, rho0, su.d, sv.d, sw.d, sp.d, precision, tol,
                           max_iter, rho ? sr.d : nullptr, rho ? so.d : nullptr, f_t12_o, cbcvel, bcvel,
-                          rho ? &so : nullptr, slab ? &sl : nullptr);
+                          rho ? &so : nullptr, slab ? &sl : nullptr, &su);
   if (rc != 0 && rc != FLUTAS_EITER) {
     if (pl->copy_stream) cudaStreamSynchronize(pl->copy_stream);  // no copy into the caller's array after return
     return rc;

@@ -1235,7 +1235,7 @@ __global__ void __launch_bounds__(256) k_resnorm_correc(InResidual R, CorrecAddA
         const int i = xs[u] + 1, j = ys[u] + 1, k = ks[u] + 1;
         const long pc = g.pidx(i, j, k), ui = g.uidx(i, j, k);
         const double ph = a.phi[pc];
-        a.u[ui] = fma(-a.cx, a.phi[pc + 1] - ph, a.u[ui]);
+        if (a.u) a.u[ui] = fma(-a.cx, a.phi[pc + 1] - ph, a.u[ui]);  // null: applied before (k_correc_u)
         a.v[ui] = fma(-a.cy, a.phi[pc + (g.nx + 2)] - ph, a.v[ui]);
         a.w[ui] = fma(-a.cz[k], a.phi[pc + plane] - ph, a.w[ui]);
         const double p0 = a.p[pc];
@@ -1246,6 +1246,20 @@ __global__ void __launch_bounds__(256) k_resnorm_correc(InResidual R, CorrecAddA
   }
   block_sum_add((double)ss, nrm);
 }
+
+// The u part of correc alone (the same expression as k_resnorm_correc's), so
+// that u's ghost cells and its copy to the host can start while the rest of
+// the correction runs.
+#ifndef FG_NO_PLAIN_KERNELS
+__global__ void k_correc_u(CorrecAddArgs a) {
+  const Geo &g = a.g;
+  for_cells(g, [&](int i0, int j0, int k0) {
+    const int i = i0 + 1, j = j0 + 1, k = k0 + 1;
+    const long pc = g.pidx(i, j, k), ui = g.uidx(i, j, k);
+    a.u[ui] = fma(-a.cx, a.phi[pc + 1] - a.phi[pc], a.u[ui]);
+  });
+}
+#endif
 
 // d = x - s on a whole halo-1 array (the correction still to apply after a
 // fused check that did not end the solve).
