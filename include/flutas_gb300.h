@@ -176,7 +176,10 @@ FLUTAS_API int flutas_gb300_solve_mixed(void *plan, double *p, double tol, int m
  * on exit u,v,w are projected and p holds pold + phi.  precision: 0 = FP64,
  * 1 = mixed to tol.  dzci/dzfi: (1-nh_d:nz+nh_d).  bcpre = bc(0:1,1:3).
  * cbcvel/bcvel (nullable): velocity BCs; when given, bounduvw is applied
- * after correc. */
+ * after correc.  With page-locked host arrays the mixed form overlaps its
+ * copies with its kernels (w copied in z-slabs with the first pass behind
+ * it, u copied back while v, w and p are corrected; FLUTAS_GB300_SLABS=0
+ * turns the slabs off); the results equal the device-array call bit for bit. */
 FLUTAS_API int flutas_gb300_projection(void *plan, int nh_u, double dxi, double dyi, const double *dzci,
                             const double *dzfi, const double bcpre[6], const char *cbcvel,
                             const double *bcvel, double dt, double rho0,
