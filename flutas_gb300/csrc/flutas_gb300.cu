@@ -831,8 +831,11 @@ struct FinalCorrec {
   // set: u's correction runs first (k_correc_u), then this (its ghost cells and
   // its copy to the host on the copy stream), then the check with the rest
   std::function<int()> u_first;
+  // set: the ghost cells of the corrected fields, queued right behind the
+  // fused check (before the host reads its norm); redone if the solve goes on
+  std::function<int()> ghosts_after;
   double *snapshot = nullptr;       // x as applied, when the solve went on
-  bool applied = false, continued = false, u_early = false;
+  bool applied = false, continued = false, u_early = false, ghosts_queued = false;
 };
 
 template <typename First>
@@ -913,6 +916,10 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
       else
         TRY(launch("k_resnorm_correc", st, [&] { k_resnorm_correc<int><<<grid, 256, 0, st>>>(R, ca, acc); }));
       fc->applied = true;
+      if (fc->ghosts_after) {
+        TRY(fc->ghosts_after());
+        fc->ghosts_queued = true;
+      }
     } else if (norm_only) {
       TRY(stencil(R, nullptr, nullptr, acc));
     } else {
@@ -2052,9 +2059,23 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
       u_split = ghosts_ready(gu, &t1) && ghosts_ready(gvw, &t2);
     }
   }
+  // ghost cells of the corrected u, v, w (bounduvw; v and w only when u went back early
+  // with its own) and of p and pold (boundp)
+  auto final_ghosts = [&](bool skip_u) -> int {
+    if (cbcvel) {
+      if (skip_u) {
+        bool done = false;
+        TRY(ghosts_launch(gvw, st, &done));
+      } else {
+        TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
+      }
+    }
+    return boundp_dev(p, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st, pold_early ? nullptr : pold);  // and pold
+  };
   if (precision != 0) {
     fc.ca = ca;
     fc.boundp_phi = [&] { return boundp_dev(phi, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st); };
+    fc.ghosts_after = [&] { return final_ghosts(u_split); };
     if (u_split)
       fc.u_first = [&]() -> int {
         if (cbcvel) {
@@ -2087,15 +2108,7 @@ int projection_dev(flutas_plan *pl, int nh_u, double dxi, double dyi, const doub
     TRY(launch("k_correc_padd", st, [&] { k_correc_padd<<<grid_cells(cd.g), 256, 0, st>>>(cd); }));
   }
   const bool u_final = fc.u_early && !fc.continued;  // u's early copy holds its final values
-  if (cbcvel) {
-    if (u_final) {
-      bool done = false;
-      TRY(ghosts_launch(gvw, st, &done));
-    } else {
-      TRY(bounduvw_dev(cbcvel, bcvel, nx, ny, nz, nh_d, nh_u, dlv, dzc_h.data(), dzf_h.data(), u, v, w, st));
-    }
-  }
-  TRY(boundp_dev(p, pl->n, pl->cbc, pl->bc, dl, dzc0, dzcn, st, pold_early ? nullptr : pold));  // and pold
+  if (!fc.ghosts_queued || fc.continued) TRY(final_ghosts(u_final));
   if (pold_early) CK(cudaStreamWaitEvent(st, pl->ev_copied, 0));  // the stream's end covers the copy
   if (fc.u_early) {
     if (u_final) u_host->out = false;  // copied; the caller's stage_out skips it
