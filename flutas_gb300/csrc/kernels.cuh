@@ -1789,7 +1789,11 @@ __global__ void __launch_bounds__(128) kb_z(BatchQueue q) {
 // skipped pass costs about one item, not one per tile.  Items leave the queue in
 // order and every earlier item belongs to a running block, so a wait always
 // ends; it is still bounded: past the limit the kernel records the failure,
-// raises the abort flag every block checks, and returns.
+// raises the abort flag every block checks, and returns.  Selected with
+// FLUTAS_GB300_BATCH_PERSISTENT=1: the default form (one work-queue kernel per
+// pass, kb_xfwd ... kb_xinv) measured faster from 8 to 512 grids, because here
+// the compute warps wait at each item's barrier while warp 0 resolves the next
+// item through dependent L2 round trips.
 // ===========================================================================
 enum BatchPass : int { PB_XF0 = 0, PB_Y = 1, PB_Z = 2, PB_YI = 3, PB_XI0 = 4, PB_XR = 5, PB_XI1 = 6 };
 
