@@ -99,12 +99,18 @@ def test_iteration_limit_returns_eiter(lib):
                      max_iter=1)
     assert e.value.code == lib.FLUTAS_EITER
     grids = [dict(n=n, dli=[48.0, 40.0, 24.0], dzci=dzci, dzfi=dzfi, cbc=cbc)]
-    B = lib.Batch(grids, autotune=False)
-    B.set(0, f)
-    with pytest.raises(lib.FlutasError) as e:
-        B.solve(tol=1e-15, max_iter=1)
-    assert e.value.code == lib.FLUTAS_EITER
-    B.destroy()
+    import os
+    for form in ("0", "1"):  # pass kernels, persistent kernel
+        os.environ["FLUTAS_GB300_BATCH_PERSISTENT"] = form
+        try:
+            B = lib.Batch(grids, autotune=False)
+        finally:
+            del os.environ["FLUTAS_GB300_BATCH_PERSISTENT"]
+        B.set(0, f)
+        with pytest.raises(lib.FlutasError) as e:
+            B.solve(tol=1e-15, max_iter=1)
+        assert e.value.code == lib.FLUTAS_EITER
+        B.destroy()
 
 
 def test_server_rejects_corrupted_requests_before_admission(lib):
