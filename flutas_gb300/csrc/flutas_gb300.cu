@@ -402,7 +402,7 @@ struct flutas_plan {
   std::vector<cudaEvent_t> slab_ev;  // host-to-device copy of each z-slab done (copy stream)
   bool sync = true;
   int path64 = 0, path32 = 0;  // 0 separate passes, 1 fused plane kernel, 2 cluster plane kernel
-  int clus64 = 0, clus32 = 0;  // cluster size of path 2
+  int clus32 = 0;              // cluster size of path 2 (FP32 transforms)
   bool pin_zero_mode = false;  // singular (lam == 0, z in N/N or P/P) column
   bool rhsb_zero = false;      // every boundary-RHS value is 0 (homogeneous BCs): updt_rhs_b adds nothing
   double last_relres = 0.0;    // relative residual / FP32 solves of the last mixed solve
@@ -424,9 +424,9 @@ template <typename T> size_t plane_smem(int nx, int ny) {
   return align_up<T>(sizeof(T) * (size_t)ny * xpitch(nx)) + sizeof(T) * (size_t)nx * ny;
 }
 
-// Cluster plane kernels: smallest cluster (2..16 CTAs) whose per-CTA share of
-// the plane fits two CTAs per SM (FP32 and double-float: 128 registers) or one
-// (FP64: up to 255 registers); 0 when the plane does not split evenly.
+// Cluster plane kernels (FP32 transforms): smallest cluster (2..16 CTAs) whose
+// per-CTA share of the plane fits two CTAs per SM (128 registers); 0 when the
+// plane does not split evenly.
 constexpr int CLUSTER_THREADS = 256;
 template <typename T> int cluster_size_for(int nx, int ny, int smax) {
   for (int C = 2; C <= 16; C *= 2) {
@@ -507,9 +507,9 @@ int fwd_xy(flutas_plan *pl, const In &in, T *S, const AxisTables &tx, const Axis
     TRY(launch(kname<KID_XYFWD, T, In>(), st, [&] { k_xyfwd_plane<T, In><<<grid, 512, sm, st>>>(tx.ap, ty.ap, in, S, g, nrm); }));
     return 0;
   }
-  if (path == 2) {
-    const int C = sizeof(T) == 8 ? pl->clus64 : pl->clus32;
-    if (sizeof(T) == 4 && fixed_supported(g.nx, g.ny, C, tx.ap.pair, ty.ap.pair)) {
+  if constexpr (sizeof(T) == 4) if (path == 2) {  // cluster planes: FP32 only
+    const int C = pl->clus32;
+    if (fixed_supported(g.nx, g.ny, C, tx.ap.pair, ty.ap.pair)) {
       cudaError_t e = cudaSuccess;
       bool handled = false;
       TRY(launch(kname<KID_XYFWD_FIX, T, In>(), st,
@@ -563,9 +563,9 @@ int inv_xy(flutas_plan *pl, const T *S, const Out &out, const AxisTables &tx, co
     TRY(launch(kname<KID_XYINV, T, Out>(), st, [&] { k_xyinv_plane<T, Out><<<grid, 512, sm, st>>>(tx.ap, ty.ap, S, out, g); }));
     return 0;
   }
-  if (path == 2) {
-    const int C = sizeof(T) == 8 ? pl->clus64 : pl->clus32;
-    if (sizeof(T) == 4 && fixed_supported(g.nx, g.ny, C, tx.ap.pair, ty.ap.pair)) {
+  if constexpr (sizeof(T) == 4) if (path == 2) {  // cluster planes: FP32 only
+    const int C = pl->clus32;
+    if (fixed_supported(g.nx, g.ny, C, tx.ap.pair, ty.ap.pair)) {
       cudaError_t e = cudaSuccess;
       bool handled = false;
       TRY(launch(kname<KID_XYINV_FIX, T, Out>(), st,
@@ -1170,9 +1170,9 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
   const int smax = max_smem_optin();
   pl->path64 = (nx % 2 == 0 && ny % 2 == 0 && (int)plane_smem<dd>(nx, ny) <= smax) ? 1 : 0;
   pl->path32 = (nx % 2 == 0 && ny % 2 == 0 && (int)plane_smem<float>(nx, ny) <= smax) ? 1 : 0;
-  if (!pl->path64 && (pl->clus64 = cluster_size_for<dd>(nx, ny, smax)) &&
-      cluster_capacity(k_xyinv_cluster<dd, OutHalo>, cluster_plane_smem(nx, ny, pl->clus64, 8), pl->clus64) > 0)
-    pl->path64 = 2;
+  // The FP64 solver's double-float transforms take no cluster path: its separate x and y
+  // passes measured faster than the cluster plane kernels at 192^2 to 256^2 planes (2.39
+  // against 2.56 ms a 256^3 solve) and even at 128^2.
   if (!pl->path32 && (pl->clus32 = cluster_size_for<float>(nx, ny, smax)) &&
       cluster_capacity(k_xyinv_cluster<float, OutHalo>, cluster_plane_smem(nx, ny, pl->clus32, 4), pl->clus32) > 0)
     pl->path32 = 2;
@@ -1185,6 +1185,9 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
   }
   if (const char *e = getenv("FLUTAS_GB300_XY_PATH")) {  // 0 forces separate passes (A/B timing)
     if (atoi(e) == 0) pl->path64 = pl->path32 = 0;
+  }
+  if (const char *e = getenv("FLUTAS_GB300_XY_PATH64")) {  // the FP64 solver's transforms alone (A/B timing)
+    if (atoi(e) == 0) pl->path64 = 0;
   }
   if (pl->ext[0] || pl->ext[1]) pl->path64 = pl->path32 = 0;  // one pass per axis (k_r2r_ext or k_xfwd/k_ypass)
   if (const char *e = getenv("FLUTAS_GB300_CONTRACTION")) {  // initial predicted contraction (tests)
