@@ -965,6 +965,63 @@ int solve_mixed_dev(flutas_plan *pl, const First &first, double *x, double tol, 
 
 }  // namespace
 
+// FP32 plane transforms: the whole-plane form (one CTA, or a cluster) against
+// separate x and y passes, the forward and inverse transforms of the grid's
+// planes timed once per process and grid signature on scratch data (the faster wins; the
+// plane forms lose on some sizes, e.g. 160^2 planes with radix-5 stages).  The choice is cached, so every plan
+// of one signature in a process runs the same kernels.
+std::mutex g_path_mu;
+std::map<std::tuple<int, int, int, int, int, int>, int> g_path32;
+
+int choose_path32(flutas_plan *pl) {
+  const int nx = pl->n[0], ny = pl->n[1];
+  const auto key = std::make_tuple(nx, ny, pl->n[2], pl->tx32.ap.pair, pl->ty32.ap.pair, pl->path32);
+  {
+    std::lock_guard<std::mutex> lk(g_path_mu);
+    auto it = g_path32.find(key);
+    if (it != g_path32.end()) {
+      pl->path32 = it->second;
+      return 0;
+    }
+  }
+  const int planes = pl->n[2];  // every plane: the whole-plane forms run one CTA (or cluster) a plane
+  DBuf scratch, xout;
+  TRY(scratch.ensure(sizeof(float) * (size_t)nx * ny * planes));
+  const size_t xbytes = sizeof(double) * (size_t)(nx + 2) * (ny + 2) * (planes + 2);
+  TRY(xout.ensure(xbytes));
+  float *S = scratch.as<float>();
+  CK(cudaMemsetAsync(S, 0, sizeof(float) * (size_t)nx * ny * planes, pl->stream));
+  CK(cudaMemsetAsync(xout.p, 0, xbytes, pl->stream));
+  const Geo g{nx, ny, planes, 1};
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  float best[2] = {1e30f, 1e30f};
+  const int cand[2] = {pl->path32, 0};
+  int rc = 0;
+  for (int rep = 0; rep < 4 && !rc; rep++)
+    for (int c = 0; c < 2 && !rc; c++) {
+      cudaEventRecord(a, pl->stream);
+      rc = fwd_xy<float>(pl, InF32{S, g}, S, pl->tx32, pl->ty32, cand[c], nullptr, planes);
+      if (!rc) rc = inv_xy<float>(pl, S, OutHalo{xout.as<double>(), 1.0, g}, pl->tx32, pl->ty32, cand[c]);
+      cudaEventRecord(b, pl->stream);
+      if (cudaEventSynchronize(b) != cudaSuccess) rc = fail(FLUTAS_ECUDA, "initsolver: transform timing failed");
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (rep > 0) best[c] = std::min(best[c], ms);  // the first round warms up
+    }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  scratch.release();
+  xout.release();
+  if (rc) return rc;
+  const int chosen = best[1] < best[0] ? 0 : cand[0];
+  std::lock_guard<std::mutex> lk(g_path_mu);
+  g_path32[key] = chosen;
+  pl->path32 = chosen;
+  return 0;
+}
+
 // ===========================================================================
 // C ABI
 // ===========================================================================
@@ -1183,7 +1240,10 @@ int flutas_gb300_initsolver(const int n[3], const double dli[3], int nh_d, const
       pl->clus32 = cf;
     }
   }
-  if (const char *e = getenv("FLUTAS_GB300_XY_PATH")) {  // 0 forces separate passes (A/B timing)
+  if (pl->path32 && !getenv("FLUTAS_GB300_XY_PATH") && (rc = choose_path32(pl))) return bail(rc);
+  // FLUTAS_GB300_XY_PATH: unset, the FP32 form is timed (choose_path32); 0 forces separate
+  // passes; any other value keeps the whole-plane form where one exists (A/B timing, tests)
+  if (const char *e = getenv("FLUTAS_GB300_XY_PATH")) {
     if (atoi(e) == 0) pl->path64 = pl->path32 = 0;
   }
   if (const char *e = getenv("FLUTAS_GB300_XY_PATH64")) {  // the FP64 solver's transforms alone (A/B timing)

@@ -218,6 +218,7 @@ LARGE_PLANES = [((256, 256, 4), "PPPPNN", 0.0), ((320, 192, 6), "NNPPDD", 1.0),
 @pytest.mark.parametrize("n,cbc,gr", LARGE_PLANES, ids=[f"{c}-{n[0]}x{n[1]}x{n[2]}" for n, c, _ in LARGE_PLANES])
 def test_gpu_cluster_plane_path(lib, oracle, n, cbc, gr, monkeypatch):
     rng = np.random.default_rng(7 + sum(n))
+    monkeypatch.setenv("FLUTAS_GB300_XY_PATH", "2")  # the cluster form, not the timed choice
     P, dzci, dzfi, dzc, dzf, dli = plan_for(lib, n, cbc, gr)
     info = P.info()
     assert info["xy_path_fp64"] == 0 and info["xy_path_fp32"] == 2, info
