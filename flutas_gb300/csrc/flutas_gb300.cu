@@ -2490,8 +2490,9 @@ struct flutas_batch {
   // the persistent kernel's queue: tile totals (z tiles of 256 columns), passes, counts, norms, error flags
   DBuf p_prefix, p_type, p_iter, p_off, p_start, p_done, p_pdone, p_nrm, p_err;
   std::vector<BatchGrid> grids;
-  size_t smem_x = 0, smem_y = 0, smem_z = 0, smem_p = 0;
-  int grid_x = 0, grid_y = 0, grid_z = 0, grid_p = 0;
+  size_t smem_x = 0, smem_y = 0, smem_z = 0, smem_p = 0, smem_pl = 0, smem_xr = 0, smem_yr = 0;
+  int grid_x = 0, grid_y = 0, grid_z = 0, grid_p = 0, grid_pl = 0;
+  bool planes = false;    // some grids take the whole-plane kernels (pass-kernel form)
   bool per_pass = true;   // false (FLUTAS_GB300_BATCH_PERSISTENT=1): the whole refinement in one persistent kernel
   int minb = 2;           // FLUTAS_GB300_BATCH_MINB: register budget of the persistent kernel
   int chunk = 4;          // FLUTAS_GB300_BATCH_CHUNK: items a block takes from the queue at once
@@ -2729,12 +2730,12 @@ int batch_capture(flutas_batch *bt, double tol, int max_iter) {
   }
   if (!bt->per_pass) return batch_capture_persistent(bt, tol, max_iter);
   const int ng = bt->ng;
-  const int npass = 5 + 5 * max_iter;
+  const int npass = 7 + 7 * max_iter;  // queue counters: up to 7 work-queue launches per iteration
   TRY(bt->d_counters.ensure(sizeof(int) * npass));
   BatchGrid *dg = bt->d_grids.as<BatchGrid>();
   const long *full = bt->d_prefix.as<long>();
   long *act = bt->d_act.as<long>();
-  const long *px = act, *py = px + (ng + 1), *pz = py + (ng + 1);
+  const long *px = act, *py = px + (ng + 1), *pz = py + (ng + 1), *pq = pz + (ng + 1);
   int *ids = bt->d_ids.as<int>(), *nslots = bt->d_nslots.as<int>();
   int *cnt = bt->d_counters.as<int>();
   double *relres = bt->d_relres.as<double>();
@@ -2751,6 +2752,10 @@ int batch_capture(flutas_batch *bt, double tol, int max_iter) {
   auto fwd_chain = [&](int xmode, int outmode) {
     kb_xfwd<<<bt->grid_x, 256, bt->smem_x, st>>>(Q(px), xmode);
     nodes++;
+    if (bt->planes) {  // both transforms of the planes that fit one CTA
+      kb_xyfwd_plane<<<bt->grid_pl, 512, bt->smem_pl, st>>>(Q(pq), xmode);
+      nodes++;
+    }
     (void)outmode;
   };
   auto rest_chain = [&](int outmode) {
@@ -2759,6 +2764,10 @@ int batch_capture(flutas_batch *bt, double tol, int max_iter) {
     kb_ypass<true><<<bt->grid_y, 256, bt->smem_y, st>>>(Q(py));
     kb_xinv<<<bt->grid_x, 256, bt->smem_x, st>>>(Q(px), outmode);
     nodes += 4;
+    if (bt->planes) {
+      kb_xyinv_plane<<<bt->grid_pl, 512, bt->smem_pl, st>>>(Q(pq), outmode);
+      nodes++;
+    }
   };
   cudaMemsetAsync(cnt, 0, sizeof(int) * npass, st);
   kb_reset<<<(ng + 255) / 256, 256, 0, st>>>(dg, ng);
@@ -2799,12 +2808,21 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
     return bail(fail(FLUTAS_ECUDA, "batch_create: stream creation failed"));
   bt->plans.assign(ngrids, nullptr);
   bt->grids.resize(ngrids);
+  if (const char *e = getenv("FLUTAS_GB300_BATCH_PERSISTENT")) bt->per_pass = atoi(e) == 0;
+  // pass-kernel form: grids whose planes fit one CTA transform a whole plane per item
+  // (FLUTAS_GB300_BATCH_PLANES=0: row and column tiles for every grid)
+  bool use_planes = true;
+  if (const char *e = getenv("FLUTAS_GB300_BATCH_PLANES")) use_planes = atoi(e) != 0;
+  // largest plane (nx*ny) taken whole: every plane that fits one CTA's shared memory (512 grids
+  // of 32..192: 65.2 ms a batch against 66.8 ms with 144^2 as the limit and 85.5 ms without)
+  long plane_max = 1L << 30;
+  if (const char *e = getenv("FLUTAS_GB300_BATCH_PLANE_MAX")) plane_max = atol(e);
   const size_t budget = 96 * 1024;
   // plans and tile choices
   std::vector<size_t> sx(ngrids), sf(ngrids), sS(ngrids), sS2(ngrids);
   size_t total = 0;
   auto take = [&](size_t bytes) { size_t o = total; total += (bytes + 255) & ~(size_t)255; return o; };
-  std::vector<long> tx(ngrids), ty(ngrids), tz(ngrids);
+  std::vector<long> tx(ngrids), ty(ngrids), tz(ngrids), tp(ngrids), txr(ngrids), tyr(ngrids);
   std::ostringstream rep;
   for (int g = 0; g < ngrids; g++) {
     const int *ng3 = n + 3 * g;
@@ -2858,12 +2876,26 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
     sf[g] = take(halo);
     sS[g] = take(sizeof(float) * (size_t)nx * ny * nz);
     sS2[g] = za.periodic ? take(sizeof(float) * (size_t)nx * ny * nz) : (size_t)-1;
-    tx[g] = ((long)ny * nz + G.M - 1) / G.M;
-    ty[g] = (long)((nx + G.W - 1) / G.W) * nz;
+    txr[g] = ((long)ny * nz + G.M - 1) / G.M;  // row tiles (the persistent form: every grid)
+    tyr[g] = (long)((nx + G.W - 1) / G.W) * nz;
+    // whole planes where one fits a CTA
+    const size_t psm = plane_smem<float>(nx, ny);
+    G.plane = (use_planes && bt->per_pass && nx % 2 == 0 && ny % 2 == 0 && (long)nx * ny <= plane_max &&
+               (int)psm <= max_smem_optin()) ? 1 : 0;
+    tx[g] = G.plane ? 0 : txr[g];
+    ty[g] = G.plane ? 0 : tyr[g];
+    tp[g] = G.plane ? nz : 0;
     tz[g] = ((long)nx * ny + 127) / 128;
-    bt->smem_x = std::max(bt->smem_x, smem_xpass(nx, G.M));
-    bt->smem_y = std::max(bt->smem_y, smem_ypass(ny, G.W));
+    if (G.plane) {
+      bt->smem_pl = std::max(bt->smem_pl, psm);
+    } else {
+      bt->smem_x = std::max(bt->smem_x, smem_xpass(nx, G.M));
+      bt->smem_y = std::max(bt->smem_y, smem_ypass(ny, G.W));
+    }
+    bt->smem_xr = std::max(bt->smem_xr, smem_xpass(nx, G.M));
+    bt->smem_yr = std::max(bt->smem_yr, smem_ypass(ny, G.W));
     bt->smem_z = std::max(bt->smem_z, sizeof(float) * (size_t)((nz + 15) / 16) * 128);
+    if (G.plane) rep << "grid " << g << ": whole planes\n";
   }
   bt->report = rep.str();
   if ((rc = bt->arena.ensure(total))) return bail(rc);
@@ -2883,11 +2915,11 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
     G.active = bt->d_active.as<int>() + g;
     bt->x[g] = G.x;
   }
-  std::vector<long> pre(3 * (size_t)(ngrids + 1), 0);
+  std::vector<long> pre(BATCH_KINDS * (size_t)(ngrids + 1), 0);
   for (int g = 0; g < ngrids; g++) {
-    pre[g + 1] = pre[g] + tx[g];
-    pre[(ngrids + 1) + g + 1] = pre[(ngrids + 1) + g] + ty[g];
-    pre[2 * (ngrids + 1) + g + 1] = pre[2 * (ngrids + 1) + g] + tz[g];
+    const long *t[BATCH_KINDS] = {tx.data(), ty.data(), tz.data(), tp.data()};
+    for (int k = 0; k < BATCH_KINDS; k++)
+      pre[k * (size_t)(ngrids + 1) + g + 1] = pre[k * (size_t)(ngrids + 1) + g] + t[k][g];
   }
   if ((rc = bt->d_prefix.ensure(sizeof(long) * pre.size())) || (rc = bt->d_grids.ensure(sizeof(BatchGrid) * ngrids)) ||
       (rc = bt->d_act.ensure(sizeof(long) * pre.size())) || (rc = bt->d_ids.ensure(sizeof(int) * ngrids)) ||
@@ -2896,37 +2928,46 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
   if (cudaMemcpy(bt->d_prefix.p, pre.data(), sizeof(long) * pre.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(bt->d_grids.p, bt->grids.data(), sizeof(BatchGrid) * ngrids, cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(fail(FLUTAS_ECUDA, "batch_create: upload failed"));
-  if ((int)std::max({bt->smem_x, bt->smem_y, bt->smem_z}) > max_smem_optin())
+  if ((int)std::max({bt->smem_x, bt->smem_y, bt->smem_z, bt->smem_pl}) > max_smem_optin())
     return bail(fail(FLUTAS_EUNSUPPORTED, "batch_create: tiles exceed shared memory"));
   {
-    // the persistent kernel's tiles: x and y as above, z in blocks of 256 columns
-    std::vector<long> pp(pre);
+    // the persistent kernel's tiles: row and column tiles for every grid, z in blocks of 256 columns
+    std::vector<long> pp(3 * (size_t)(ngrids + 1), 0);
     size_t smz = 0;
     for (int g = 0; g < ngrids; g++) {
       const Geo &G = bt->grids[g].g;
+      pp[g + 1] = pp[g] + txr[g];
+      pp[(ngrids + 1) + g + 1] = pp[(ngrids + 1) + g] + tyr[g];
       pp[2 * (ngrids + 1) + g + 1] = pp[2 * (ngrids + 1) + g] + ((long)G.nx * G.ny + 255) / 256;
       smz = std::max(smz, sizeof(float) * (size_t)((G.nz + 15) / 16) * 256);
     }
-    bt->smem_p = std::max({bt->smem_x, bt->smem_y, smz});
+    bt->smem_p = std::max({bt->smem_xr, bt->smem_yr, smz});
     if ((rc = bt->p_prefix.ensure(sizeof(long) * pp.size()))) return bail(rc);
     if (cudaMemcpy(bt->p_prefix.p, pp.data(), sizeof(long) * pp.size(), cudaMemcpyHostToDevice) != cudaSuccess)
       return bail(fail(FLUTAS_ECUDA, "batch_create: upload failed"));
     if ((rc = allow_smem(kb_persist<1>)) || (rc = allow_smem(kb_persist<2>))) return bail(rc);
-    if (const char *e = getenv("FLUTAS_GB300_BATCH_PERSISTENT")) bt->per_pass = atoi(e) == 0;
     // the persistent kernel's own tables take about 2 KB of static shared memory besides the tiles
-    if ((int)bt->smem_p + 2048 > max_smem_optin()) bt->per_pass = true;
+    if (!bt->per_pass && (int)bt->smem_p + 2048 > max_smem_optin())
+      return bail(fail(FLUTAS_EUNSUPPORTED, "batch_create: tiles too large for the persistent kernel"));
     if (const char *e = getenv("FLUTAS_GB300_BATCH_MINB")) bt->minb = atoi(e) == 1 ? 1 : 2;
     if (const char *e = getenv("FLUTAS_GB300_BATCH_CHUNK")) bt->chunk = std::max(1, std::min(64, atoi(e)));
     if (const char *e = getenv("FLUTAS_GB300_BATCH_STATS")) bt->stats = atoi(e) != 0;
   }
-  int g1, g2, g3;
-  if ((g1 = grid_for(kb_xfwd, 256, bt->smem_x, pre[ngrids])) < 0) return bail(g1);
-  if ((g2 = grid_for(kb_ypass<false>, 256, bt->smem_y, pre[2 * ngrids + 1])) < 0) return bail(g2);
-  if ((g3 = grid_for(kb_z, 128, bt->smem_z, pre[3 * ngrids + 2])) < 0) return bail(g3);
+  auto total_of = [&](int k) { return std::max<long>(1, pre[k * (size_t)(ngrids + 1) + ngrids]); };
+  int g1, g2, g3, g4 = 0;
+  if ((g1 = grid_for(kb_xfwd, 256, bt->smem_x, total_of(0))) < 0) return bail(g1);
+  if ((g2 = grid_for(kb_ypass<false>, 256, bt->smem_y, total_of(1))) < 0) return bail(g2);
+  if ((g3 = grid_for(kb_z, 128, bt->smem_z, total_of(2))) < 0) return bail(g3);
   if ((rc = allow_smem(kb_xinv)) || (rc = allow_smem(kb_ypass<true>))) return bail(rc);
+  bt->planes = pre[3 * (size_t)(ngrids + 1) + ngrids] > 0;
+  if (bt->planes) {
+    if ((g4 = grid_for(kb_xyfwd_plane, 512, bt->smem_pl, total_of(3))) < 0) return bail(g4);
+    if ((rc = allow_smem(kb_xyinv_plane))) return bail(rc);
+  }
   bt->grid_x = g1;
   bt->grid_y = g2;
   bt->grid_z = g3;
+  bt->grid_pl = g4;
   *batch = bt;
   return FLUTAS_OK;
 }

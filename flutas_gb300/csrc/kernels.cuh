@@ -648,100 +648,111 @@ __device__ __forceinline__ C2<T> *run_stages(const AxisPlan &ap, C2<T> *cur, C2<
   return cur;
 }
 
+// Both transforms of one z-plane k in one CTA's shared memory (ny x P + nx*ny
+// reals); accumulates the squares of the inputs in ss.
+template <typename T, typename In>
+__device__ __forceinline__ void xyfwd_plane_tile(const AxisPlan &ax, const AxisPlan &ay, const In &in, T *S,
+                                                 const Geo &g, int k, unsigned char *smem, float &ss) {
+  const int nx = g.nx, ny = g.ny, P = xpitch(nx);
+  T *A = (T *)smem;  // ny x P
+  T *Bu = (T *)(smem + align_up<T>(sizeof(T) * (size_t)ny * P));  // nx*ny reals
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const FastDiv fnx(nx);
+  load_cells<T>(
+      in, nx * ny,
+      [&](int idx, int &x, int &y, int &kk) -> bool {
+        y = fnx.div(idx);
+        x = idx - y * nx;
+        kk = k;
+        return true;
+      },
+      [&](int idx, T t) { A[idx + fnx.div(idx)] = t; }, ss);
+  __syncthreads();
+  // ---- x transform: lines = rows of A
+  const int Bx = cbatch(ax.pair, ny);
+  pre_fwd<T>(ax, A, P, 1, ny, (C2<T> *)Bu, Bx, tid, nth);
+  __syncthreads();
+  C2<T> *fin = run_stages<T, false>(ax, (C2<T> *)Bu, (C2<T> *)A, Bx, tid, nth);
+  T *G = (fin == (C2<T> *)Bu) ? A : Bu;   // free buffer for the real x-spectrum
+  const int gp = (G == A) ? P : nx;
+  StorePlaneReal<T> sx{G, gp, 0};
+  post_fwd<T>(ax, fin, Bx, ny, sx, tid, nth);
+  __syncthreads();
+  // ---- y transform: lines = columns of G
+  const int By = cbatch(ay.pair, nx);
+  C2<T> *F = (C2<T> *)(G == A ? Bu : A);
+  pre_fwd<T>(ay, G, 1, gp, nx, F, By, tid, nth);
+  __syncthreads();
+  C2<T> *fy = run_stages<T, false>(ay, F, (C2<T> *)G, By, tid, nth);
+  StoreColsS<T> st{S, (long)k * nx * ny, nx, 0, nx};
+  post_fwd<T>(ay, fy, By, nx, st, tid, nth);
+  __syncthreads();
+}
+
 template <typename T, typename In>
 __global__ void __launch_bounds__(512) k_xyfwd_plane(AxisPlan ax, AxisPlan ay, In in, T *S, Geo g, double *nrm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int nx = g.nx, ny = g.ny, P = xpitch(nx);
-  T *A = (T *)smem_raw;  // ny x P
-  T *Bu = (T *)(smem_raw + align_up<T>(sizeof(T) * (size_t)ny * P));  // nx*ny reals
-  const int tid = threadIdx.x, nth = blockDim.x;
   float ss = 0.0f;  // sum of squares for convergence checks (FP32 per thread)
-  const FastDiv fnx(nx);
-  for (int k = blockIdx.x; k < g.nz; k += gridDim.x) {
-    load_cells<T>(
-        in, nx * ny,
-        [&](int idx, int &x, int &y, int &kk) -> bool {
-          y = fnx.div(idx);
-          x = idx - y * nx;
-          kk = k;
-          return true;
-        },
-        [&](int idx, T t) { A[idx + fnx.div(idx)] = t; }, ss);
-    __syncthreads();
-    // ---- x transform: lines = rows of A
-    const int Bx = cbatch(ax.pair, ny);
-    pre_fwd<T>(ax, A, P, 1, ny, (C2<T> *)Bu, Bx, tid, nth);
-    __syncthreads();
-    C2<T> *fin = run_stages<T, false>(ax, (C2<T> *)Bu, (C2<T> *)A, Bx, tid, nth);
-    T *G = (fin == (C2<T> *)Bu) ? A : Bu;   // free buffer for the real x-spectrum
-    const int gp = (G == A) ? P : nx;
-    StorePlaneReal<T> sx{G, gp, 0};
-    post_fwd<T>(ax, fin, Bx, ny, sx, tid, nth);
-    __syncthreads();
-    // ---- y transform: lines = columns of G
-    const int By = cbatch(ay.pair, nx);
-    C2<T> *F = (C2<T> *)(G == A ? Bu : A);
-    pre_fwd<T>(ay, G, 1, gp, nx, F, By, tid, nth);
-    __syncthreads();
-    C2<T> *fy = run_stages<T, false>(ay, F, (C2<T> *)G, By, tid, nth);
-    StoreColsS<T> st{S, (long)k * nx * ny, nx, 0, nx};
-    post_fwd<T>(ay, fy, By, nx, st, tid, nth);
-    __syncthreads();
-  }
+  for (int k = blockIdx.x; k < g.nz; k += gridDim.x) xyfwd_plane_tile<T, In>(ax, ay, in, S, g, k, smem_raw, ss);
   if (nrm) block_sum_add((double)ss, nrm);
+}
+
+// Both inverse transforms of one z-plane k in one CTA's shared memory.
+template <typename T, typename Out>
+__device__ __forceinline__ void xyinv_plane_tile(const AxisPlan &ax, const AxisPlan &ay, const T *S, const Out &out,
+                                                 const Geo &g, int k, unsigned char *smem) {
+  const int nx = g.nx, ny = g.ny, P = xpitch(nx);
+  T *A = (T *)smem;
+  T *Bu = (T *)(smem + align_up<T>(sizeof(T) * (size_t)ny * P));
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const bool invx = fft_inverse(ax.pair, true), invy = fft_inverse(ay.pair, true);
+  const T *Sp = S + (long)k * nx * ny;
+  for (int idx = tid; idx < nx * ny; idx += nth) {
+    const int y = idx / nx, x = idx % nx;
+    A[y * P + x] = Sp[idx];
+  }
+  __syncthreads();
+  // ---- y^-1: lines = columns of A
+  const int By = cbatch(ay.pair, nx);
+  pre_bwd<T>(ay, A, 1, P, nx, (C2<T> *)Bu, By, tid, nth);
+  __syncthreads();
+  C2<T> *fy = invy ? run_stages<T, true>(ay, (C2<T> *)Bu, (C2<T> *)A, By, tid, nth)
+                   : run_stages<T, false>(ay, (C2<T> *)Bu, (C2<T> *)A, By, tid, nth);
+  T *G = (fy == (C2<T> *)Bu) ? A : Bu;
+  const int gp = (G == A) ? P : nx;
+  StorePlaneRealCols<T> sy{G, gp};
+  post_bwd<T>(ay, fy, By, nx, sy, tid, nth);
+  __syncthreads();
+  // ---- x^-1: lines = rows of G
+  const int Bx = cbatch(ax.pair, ny);
+  C2<T> *F = (C2<T> *)(G == A ? Bu : A);
+  pre_bwd<T>(ax, G, gp, 1, ny, F, Bx, tid, nth);
+  __syncthreads();
+  C2<T> *fx = invx ? run_stages<T, true>(ax, F, (C2<T> *)G, Bx, tid, nth)
+                   : run_stages<T, false>(ax, F, (C2<T> *)G, Bx, tid, nth);
+  // real plane into the free buffer, then the batched epilogue
+  T *R = (fx == F) ? G : (T *)F;
+  const int PR = (R == A) ? P : nx;
+  StorePlaneReal<T> sr{R, PR, 0};
+  post_bwd<T>(ax, fx, Bx, ny, sr, tid, nth);
+  __syncthreads();
+  const FastDiv fnx(nx);
+  store_cells<T>(
+      out, nx * ny,
+      [&](int idx, int &x, int &y, int &kk) -> bool {
+        y = fnx.div(idx);
+        x = idx - y * nx;
+        kk = k;
+        return true;
+      },
+      [&](int idx) { const int y = fnx.div(idx); return R[y * PR + (idx - y * nx)]; });
+  __syncthreads();
 }
 
 template <typename T, typename Out>
 __global__ void __launch_bounds__(512) k_xyinv_plane(AxisPlan ax, AxisPlan ay, const T *S, Out out, Geo g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int nx = g.nx, ny = g.ny, P = xpitch(nx);
-  T *A = (T *)smem_raw;
-  T *Bu = (T *)(smem_raw + align_up<T>(sizeof(T) * (size_t)ny * P));
-  const int tid = threadIdx.x, nth = blockDim.x;
-  const bool invx = fft_inverse(ax.pair, true), invy = fft_inverse(ay.pair, true);
-  for (int k = blockIdx.x; k < g.nz; k += gridDim.x) {
-    const T *Sp = S + (long)k * nx * ny;
-    for (int idx = tid; idx < nx * ny; idx += nth) {
-      const int y = idx / nx, x = idx % nx;
-      A[y * P + x] = Sp[idx];
-    }
-    __syncthreads();
-    // ---- y^-1: lines = columns of A
-    const int By = cbatch(ay.pair, nx);
-    pre_bwd<T>(ay, A, 1, P, nx, (C2<T> *)Bu, By, tid, nth);
-    __syncthreads();
-    C2<T> *fy = invy ? run_stages<T, true>(ay, (C2<T> *)Bu, (C2<T> *)A, By, tid, nth)
-                     : run_stages<T, false>(ay, (C2<T> *)Bu, (C2<T> *)A, By, tid, nth);
-    T *G = (fy == (C2<T> *)Bu) ? A : Bu;
-    const int gp = (G == A) ? P : nx;
-    StorePlaneRealCols<T> sy{G, gp};
-    post_bwd<T>(ay, fy, By, nx, sy, tid, nth);
-    __syncthreads();
-    // ---- x^-1: lines = rows of G
-    const int Bx = cbatch(ax.pair, ny);
-    C2<T> *F = (C2<T> *)(G == A ? Bu : A);
-    pre_bwd<T>(ax, G, gp, 1, ny, F, Bx, tid, nth);
-    __syncthreads();
-    C2<T> *fx = invx ? run_stages<T, true>(ax, F, (C2<T> *)G, Bx, tid, nth)
-                     : run_stages<T, false>(ax, F, (C2<T> *)G, Bx, tid, nth);
-    // real plane into the free buffer, then the batched epilogue
-    T *R = (fx == F) ? G : (T *)F;
-    const int PR = (R == A) ? P : nx;
-    StorePlaneReal<T> sr{R, PR, 0};
-    post_bwd<T>(ax, fx, Bx, ny, sr, tid, nth);
-    __syncthreads();
-    const FastDiv fnx(nx);
-    store_cells<T>(
-        out, nx * ny,
-        [&](int idx, int &x, int &y, int &kk) -> bool {
-          y = fnx.div(idx);
-          x = idx - y * nx;
-          kk = k;
-          return true;
-        },
-        [&](int idx) { const int y = fnx.div(idx); return R[y * PR + (idx - y * nx)]; });
-    __syncthreads();
-  }
+  for (int k = blockIdx.x; k < g.nz; k += gridDim.x) xyinv_plane_tile<T, Out>(ax, ay, S, out, g, k, smem_raw);
 }
 
 // ===========================================================================
@@ -1565,6 +1576,7 @@ struct BatchGrid {
   double dxi2, dyi2, normfft;
   char bc[6];
   int M, W;              // x-pass rows per tile, y-pass columns per tile
+  int plane;             // 1: both transforms of a z-plane in one CTA (kb_xyfwd_plane / kb_xyinv_plane)
   double *nrm;           // [0] ||f||^2, [1] ||r||^2 of the current check
   int *active;           // 1 while the grid still refines
 };
@@ -1573,6 +1585,8 @@ struct BatchGrid {
 // compacted list is grid ids[s]; prefix[s] is the running total of tiles of
 // slots < s (nslots + 1 entries).  kb_compact rebuilds the list after every
 // convergence update, so a pass over converged grids has no items at all.
+// Tile kinds of the batched passes: x tiles, y tiles, z tiles, plane items.
+constexpr int BATCH_KINDS = 4;
 struct BatchQueue {
   const BatchGrid *grids;
   const long *prefix;
@@ -1622,6 +1636,49 @@ __global__ void __launch_bounds__(256) kb_xfwd(BatchQueue q, int mode) {
       xfwd_tile<float, InResidual>(G.ax, in, G.S, G.g, G.M, row0, smem_raw, ss);
     }
     block_sum_add((double)ss, G.nrm + (mode == 0 ? 0 : 1));
+  }
+}
+#endif
+
+// Grids whose planes fit one CTA: both transforms of a plane per item (the
+// x and y pass kernels carry no items for them).  mode 0: first pass (RHS =
+// x, keep f), mode 1: residual pass.
+#ifndef FG_NO_PLAIN_KERNELS
+__global__ void __launch_bounds__(512) kb_xyfwd_plane(BatchQueue q, int mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ns = *q.nslots;
+  const long total = q.prefix[ns];
+  for (long item = batch_next(q.counter); item < total; item = batch_next(q.counter)) {
+    const int slot = batch_find(q.prefix, ns, item);
+    const BatchGrid &G = q.grids[q.ids[slot]];
+    if (!*G.active) continue;
+    const int k = (int)(item - q.prefix[slot]);
+    float ss = 0.0f;
+    if (mode == 0) {
+      InKeep<InHalo> in{InHalo{G.x, G.g}, G.f, G.g};
+      xyfwd_plane_tile<float, InKeep<InHalo>>(G.ax, G.ay, in, G.S, G.g, k, smem_raw, ss);
+    } else {
+      InResidual in;
+      in.f = G.f; in.x = G.x; in.zc = G.zres; in.dxi2 = G.dxi2; in.dyi2 = G.dyi2;
+      for (int t = 0; t < 6; t++) in.bc[t] = G.bc[t];
+      in.g = G.g;
+      xyfwd_plane_tile<float, InResidual>(G.ax, G.ay, in, G.S, G.g, k, smem_raw, ss);
+    }
+    block_sum_add((double)ss, G.nrm + (mode == 0 ? 0 : 1));
+  }
+}
+// mode 0: x = e * normfft; mode 1: x += e * normfft
+__global__ void __launch_bounds__(512) kb_xyinv_plane(BatchQueue q, int mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ns = *q.nslots;
+  const long total = q.prefix[ns];
+  for (long item = batch_next(q.counter); item < total; item = batch_next(q.counter)) {
+    const int slot = batch_find(q.prefix, ns, item);
+    const BatchGrid &G = q.grids[q.ids[slot]];
+    if (!*G.active) continue;
+    const int k = (int)(item - q.prefix[slot]);
+    if (mode == 0) xyinv_plane_tile<float, OutHalo>(G.ax, G.ay, G.S, OutHalo{G.x, G.normfft, G.g}, G.g, k, smem_raw);
+    else xyinv_plane_tile<float, OutHaloAdd>(G.ax, G.ay, G.S, OutHaloAdd{G.x, G.normfft, G.g}, G.g, k, smem_raw);
   }
 }
 #endif
@@ -2073,24 +2130,26 @@ __global__ void kb_reset(BatchGrid *grids, int ng) {
 }
 
 // Compacted work lists (one block): the grids still active, in grid order,
-// and for each of the three passes the running totals of their tiles.  full
-// holds the per-grid running totals of the passes (3 x (ng+1)), act receives
-// the compacted ones (3 x (ng+1)), ids the slot -> grid map, nslots the count.
+// and for each of the BATCH_KINDS tile kinds (x tiles, y tiles, z tiles, plane
+// items) the running totals of their tiles.  full holds the per-grid running
+// totals (BATCH_KINDS x (ng+1)), act receives the compacted ones, ids the
+// slot -> grid map, nslots the count.
 __global__ void __launch_bounds__(1024) kb_compact(const BatchGrid *grids, int ng, const long *full, long *act,
                                                    int *ids, int *nslots) {
-  __shared__ long wsum[4][32];
+  constexpr int NK = BATCH_KINDS + 1;
+  __shared__ long wsum[NK][32];
   const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, wid = t >> 5;
   const int chunk = (ng + nt - 1) / nt, g0 = t * chunk, g1 = min(ng, g0 + chunk);
   const long L = ng + 1;
-  long c[4] = {0, 0, 0, 0};  // active grids, x tiles, y tiles, z tiles of this thread's range
+  long c[NK] = {};  // active grids, then the tiles of each kind in this thread's range
   for (int g = g0; g < g1; g++)
     if (*grids[g].active) {
       c[0]++;
-      for (int p = 0; p < 3; p++) c[p + 1] += full[p * L + g + 1] - full[p * L + g];
+      for (int p = 0; p < BATCH_KINDS; p++) c[p + 1] += full[p * L + g + 1] - full[p * L + g];
     }
-  long incl[4];
+  long incl[NK];
 #pragma unroll
-  for (int k = 0; k < 4; k++) {  // exclusive scan over the block: warp scan, then over the warp totals
+  for (int k = 0; k < NK; k++) {  // exclusive scan over the block: warp scan, then over the warp totals
     long v = c[k];
     for (int o = 1; o < 32; o <<= 1) {
       const long u = __shfl_up_sync(0xffffffffu, v, o);
@@ -2102,7 +2161,7 @@ __global__ void __launch_bounds__(1024) kb_compact(const BatchGrid *grids, int n
   __syncthreads();
   if (wid == 0) {
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < NK; k++) {
       long v = lane < (nt >> 5) ? wsum[k][lane] : 0;
       for (int o = 1; o < 32; o <<= 1) {
         const long u = __shfl_up_sync(0xffffffffu, v, o);
@@ -2112,15 +2171,16 @@ __global__ void __launch_bounds__(1024) kb_compact(const BatchGrid *grids, int n
     }
   }
   __syncthreads();
-  long base[4];
+  long base[NK];
 #pragma unroll
-  for (int k = 0; k < 4; k++) base[k] = (wid ? wsum[k][wid - 1] : 0) + incl[k] - c[k];
+  for (int k = 0; k < NK; k++) base[k] = (wid ? wsum[k][wid - 1] : 0) + incl[k] - c[k];
   int slot = (int)base[0];
-  long pos[3] = {base[1], base[2], base[3]};
+  long pos[BATCH_KINDS];
+  for (int p = 0; p < BATCH_KINDS; p++) pos[p] = base[p + 1];
   for (int g = g0; g < g1; g++)
     if (*grids[g].active) {
       ids[slot] = g;
-      for (int p = 0; p < 3; p++) {
+      for (int p = 0; p < BATCH_KINDS; p++) {
         act[p * L + slot] = pos[p];
         pos[p] += full[p * L + g + 1] - full[p * L + g];
       }
@@ -2128,7 +2188,7 @@ __global__ void __launch_bounds__(1024) kb_compact(const BatchGrid *grids, int n
     }
   if (t == nt - 1) {  // the last thread ends the lists
     *nslots = slot;
-    for (int p = 0; p < 3; p++) act[p * L + slot] = pos[p];
+    for (int p = 0; p < BATCH_KINDS; p++) act[p * L + slot] = pos[p];
   }
 }
 #endif

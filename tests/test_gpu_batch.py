@@ -113,6 +113,7 @@ def test_persistent_kernel_equals_pass_kernels(lib, monkeypatch, tol):
     FP32 solves per grid and the same solutions, bit for bit."""
     grids, rhs = _batch_inputs()
     out = {}
+    monkeypatch.setenv("FLUTAS_GB300_BATCH_PLANES", "0")  # row and column tiles in both forms
     for form in ("0", "1"):
         monkeypatch.setenv("FLUTAS_GB300_BATCH_PERSISTENT", form)
         monkeypatch.setenv("FLUTAS_GB300_BATCH_STATS", form)
@@ -128,3 +129,31 @@ def test_persistent_kernel_equals_pass_kernels(lib, monkeypatch, tol):
         assert np.array_equal(a, b)
     q = [ln for ln in out["1"][3].splitlines() if ln.startswith("queue:")]
     assert q and "0 tiles skipped" not in q[0], out["1"][3]
+
+
+@pytest.mark.parametrize("tol", [1e-6, 1e-10])
+def test_whole_plane_items_equal_row_and_column_tiles(lib, oracle, monkeypatch, tol):
+    """Grids whose planes fit one CTA take both transforms of a plane per item
+    (kb_xyfwd_plane / kb_xyinv_plane); the same batch with row and column tiles
+    (FLUTAS_GB300_BATCH_PLANES=0) reaches tol as well, and the two solutions
+    agree within it.  A 192x160 grid stays on rows and columns in both."""
+    grids, rhs = _batch_inputs()
+    rng = np.random.default_rng(9)
+    dzci, dzfi, dzc, dzf = zgrid(12, 0.0)
+    grids.append(dict(n=(192, 160, 12), dli=[192.0, 176.0, 1.0], dzci=dzci, dzfi=dzfi, cbc="PPNNDD"))
+    rhs.append(compatible_rhs(rng, (192, 160, 12), "PPNNDD", dzf))
+    sols = {}
+    for planes in ("1", "0"):
+        monkeypatch.setenv("FLUTAS_GB300_BATCH_PLANES", planes)
+        B = lib.Batch(grids, autotune=False)
+        for g, r in enumerate(rhs):
+            B.set(g, r)
+        rr, it = B.solve(tol=tol, max_iter=8)
+        assert np.all(rr <= tol), (planes, rr)
+        if planes == "1":
+            assert "whole planes" in B.report()
+        sols[planes] = [B.get(g) for g in range(len(grids))]
+        B.destroy()
+    for g, gd in enumerate(grids):
+        d = rel_l2(sols["1"][g][1:-1, 1:-1, 1:-1], sols["0"][g][1:-1, 1:-1, 1:-1], remove_mean=singular(gd["cbc"]))
+        assert d <= max(10 * tol, 1e-12), (g, d)
