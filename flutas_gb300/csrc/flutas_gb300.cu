@@ -2490,9 +2490,9 @@ struct flutas_batch {
   // the persistent kernel's queue: tile totals (z tiles of 256 columns), passes, counts, norms, error flags
   DBuf p_prefix, p_type, p_iter, p_off, p_start, p_done, p_pdone, p_nrm, p_err;
   std::vector<BatchGrid> grids;
-  size_t smem_x = 0, smem_y = 0, smem_z = 0, smem_p = 0, smem_pl = 0, smem_xr = 0, smem_yr = 0;
-  int grid_x = 0, grid_y = 0, grid_z = 0, grid_p = 0, grid_pl = 0;
-  bool planes = false;    // some grids take the whole-plane kernels (pass-kernel form)
+  size_t smem_x = 0, smem_y = 0, smem_z = 0, smem_p = 0, smem_pl0 = 0, smem_pl1 = 0, smem_xr = 0, smem_yr = 0;
+  int grid_x = 0, grid_y = 0, grid_z = 0, grid_p = 0, grid_pl0 = 0, grid_pl1 = 0;
+  bool planes0 = false, planes1 = false;  // some grids take the whole-plane kernels (small / large planes)
   bool per_pass = true;   // false (FLUTAS_GB300_BATCH_PERSISTENT=1): the whole refinement in one persistent kernel
   int minb = 2;           // FLUTAS_GB300_BATCH_MINB: register budget of the persistent kernel
   int chunk = 4;          // FLUTAS_GB300_BATCH_CHUNK: items a block takes from the queue at once
@@ -2730,12 +2730,12 @@ int batch_capture(flutas_batch *bt, double tol, int max_iter) {
   }
   if (!bt->per_pass) return batch_capture_persistent(bt, tol, max_iter);
   const int ng = bt->ng;
-  const int npass = 7 + 7 * max_iter;  // queue counters: up to 7 work-queue launches per iteration
+  const int npass = 9 + 9 * max_iter;  // queue counters: up to 9 work-queue launches per iteration
   TRY(bt->d_counters.ensure(sizeof(int) * npass));
   BatchGrid *dg = bt->d_grids.as<BatchGrid>();
   const long *full = bt->d_prefix.as<long>();
   long *act = bt->d_act.as<long>();
-  const long *px = act, *py = px + (ng + 1), *pz = py + (ng + 1), *pq = pz + (ng + 1);
+  const long *px = act, *py = px + (ng + 1), *pz = py + (ng + 1), *pq0 = pz + (ng + 1), *pq1 = pq0 + (ng + 1);
   int *ids = bt->d_ids.as<int>(), *nslots = bt->d_nslots.as<int>();
   int *cnt = bt->d_counters.as<int>();
   double *relres = bt->d_relres.as<double>();
@@ -2752,8 +2752,12 @@ int batch_capture(flutas_batch *bt, double tol, int max_iter) {
   auto fwd_chain = [&](int xmode, int outmode) {
     kb_xfwd<<<bt->grid_x, 256, bt->smem_x, st>>>(Q(px), xmode);
     nodes++;
-    if (bt->planes) {  // both transforms of the planes that fit one CTA
-      kb_xyfwd_plane<<<bt->grid_pl, 512, bt->smem_pl, st>>>(Q(pq), xmode);
+    if (bt->planes0) {  // both transforms of the planes that fit one CTA
+      kb_xyfwd_plane<256><<<bt->grid_pl0, 256, bt->smem_pl0, st>>>(Q(pq0), xmode);
+      nodes++;
+    }
+    if (bt->planes1) {
+      kb_xyfwd_plane<512><<<bt->grid_pl1, 512, bt->smem_pl1, st>>>(Q(pq1), xmode);
       nodes++;
     }
     (void)outmode;
@@ -2764,8 +2768,12 @@ int batch_capture(flutas_batch *bt, double tol, int max_iter) {
     kb_ypass<true><<<bt->grid_y, 256, bt->smem_y, st>>>(Q(py));
     kb_xinv<<<bt->grid_x, 256, bt->smem_x, st>>>(Q(px), outmode);
     nodes += 4;
-    if (bt->planes) {
-      kb_xyinv_plane<<<bt->grid_pl, 512, bt->smem_pl, st>>>(Q(pq), outmode);
+    if (bt->planes0) {
+      kb_xyinv_plane<256><<<bt->grid_pl0, 256, bt->smem_pl0, st>>>(Q(pq0), outmode);
+      nodes++;
+    }
+    if (bt->planes1) {
+      kb_xyinv_plane<512><<<bt->grid_pl1, 512, bt->smem_pl1, st>>>(Q(pq1), outmode);
       nodes++;
     }
   };
@@ -2816,13 +2824,15 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
   // largest plane (nx*ny) taken whole: every plane that fits one CTA's shared memory (512 grids
   // of 32..192: 65.2 ms a batch against 66.8 ms with 144^2 as the limit and 85.5 ms without)
   long plane_max = 1L << 30;
+  size_t kSmallPlane = 60 * 1024;  // planes up to this shared memory: 256 threads, two CTAs a SM
+  if (const char *e = getenv("FLUTAS_GB300_BATCH_SMALL_PLANE")) kSmallPlane = (size_t)atol(e);
   if (const char *e = getenv("FLUTAS_GB300_BATCH_PLANE_MAX")) plane_max = atol(e);
   const size_t budget = 96 * 1024;
   // plans and tile choices
   std::vector<size_t> sx(ngrids), sf(ngrids), sS(ngrids), sS2(ngrids);
   size_t total = 0;
   auto take = [&](size_t bytes) { size_t o = total; total += (bytes + 255) & ~(size_t)255; return o; };
-  std::vector<long> tx(ngrids), ty(ngrids), tz(ngrids), tp(ngrids), txr(ngrids), tyr(ngrids);
+  std::vector<long> tx(ngrids), ty(ngrids), tz(ngrids), tp0(ngrids), tp1(ngrids), txr(ngrids), tyr(ngrids);
   std::ostringstream rep;
   for (int g = 0; g < ngrids; g++) {
     const int *ng3 = n + 3 * g;
@@ -2882,12 +2892,17 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
     const size_t psm = plane_smem<float>(nx, ny);
     G.plane = (use_planes && bt->per_pass && nx % 2 == 0 && ny % 2 == 0 && (long)nx * ny <= plane_max &&
                (int)psm <= max_smem_optin()) ? 1 : 0;
+    // two classes of planes, each launched with its own shared memory: the small ones run
+    // several CTAs a SM, the large ones one
+    const bool small = psm <= kSmallPlane;
     tx[g] = G.plane ? 0 : txr[g];
     ty[g] = G.plane ? 0 : tyr[g];
-    tp[g] = G.plane ? nz : 0;
+    tp0[g] = G.plane && small ? nz : 0;
+    tp1[g] = G.plane && !small ? nz : 0;
     tz[g] = ((long)nx * ny + 127) / 128;
     if (G.plane) {
-      bt->smem_pl = std::max(bt->smem_pl, psm);
+      size_t &sm = small ? bt->smem_pl0 : bt->smem_pl1;
+      sm = std::max(sm, psm);
     } else {
       bt->smem_x = std::max(bt->smem_x, smem_xpass(nx, G.M));
       bt->smem_y = std::max(bt->smem_y, smem_ypass(ny, G.W));
@@ -2917,7 +2932,7 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
   }
   std::vector<long> pre(BATCH_KINDS * (size_t)(ngrids + 1), 0);
   for (int g = 0; g < ngrids; g++) {
-    const long *t[BATCH_KINDS] = {tx.data(), ty.data(), tz.data(), tp.data()};
+    const long *t[BATCH_KINDS] = {tx.data(), ty.data(), tz.data(), tp0.data(), tp1.data()};
     for (int k = 0; k < BATCH_KINDS; k++)
       pre[k * (size_t)(ngrids + 1) + g + 1] = pre[k * (size_t)(ngrids + 1) + g] + t[k][g];
   }
@@ -2928,7 +2943,7 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
   if (cudaMemcpy(bt->d_prefix.p, pre.data(), sizeof(long) * pre.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(bt->d_grids.p, bt->grids.data(), sizeof(BatchGrid) * ngrids, cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(fail(FLUTAS_ECUDA, "batch_create: upload failed"));
-  if ((int)std::max({bt->smem_x, bt->smem_y, bt->smem_z, bt->smem_pl}) > max_smem_optin())
+  if ((int)std::max({bt->smem_x, bt->smem_y, bt->smem_z, bt->smem_pl0, bt->smem_pl1}) > max_smem_optin())
     return bail(fail(FLUTAS_EUNSUPPORTED, "batch_create: tiles exceed shared memory"));
   {
     // the persistent kernel's tiles: row and column tiles for every grid, z in blocks of 256 columns
@@ -2954,20 +2969,21 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
     if (const char *e = getenv("FLUTAS_GB300_BATCH_STATS")) bt->stats = atoi(e) != 0;
   }
   auto total_of = [&](int k) { return std::max<long>(1, pre[k * (size_t)(ngrids + 1) + ngrids]); };
-  int g1, g2, g3, g4 = 0;
+  int g1, g2, g3, g4 = 0, g5 = 0;
   if ((g1 = grid_for(kb_xfwd, 256, bt->smem_x, total_of(0))) < 0) return bail(g1);
   if ((g2 = grid_for(kb_ypass<false>, 256, bt->smem_y, total_of(1))) < 0) return bail(g2);
   if ((g3 = grid_for(kb_z, 128, bt->smem_z, total_of(2))) < 0) return bail(g3);
   if ((rc = allow_smem(kb_xinv)) || (rc = allow_smem(kb_ypass<true>))) return bail(rc);
-  bt->planes = pre[3 * (size_t)(ngrids + 1) + ngrids] > 0;
-  if (bt->planes) {
-    if ((g4 = grid_for(kb_xyfwd_plane, 512, bt->smem_pl, total_of(3))) < 0) return bail(g4);
-    if ((rc = allow_smem(kb_xyinv_plane))) return bail(rc);
-  }
+  bt->planes0 = pre[3 * (size_t)(ngrids + 1) + ngrids] > 0;
+  bt->planes1 = pre[4 * (size_t)(ngrids + 1) + ngrids] > 0;
+  if (bt->planes0 && (g4 = grid_for(kb_xyfwd_plane<256>, 256, bt->smem_pl0, total_of(3))) < 0) return bail(g4);
+  if (bt->planes1 && (g5 = grid_for(kb_xyfwd_plane<512>, 512, bt->smem_pl1, total_of(4))) < 0) return bail(g5);
+  if ((rc = allow_smem(kb_xyinv_plane<256>)) || (rc = allow_smem(kb_xyinv_plane<512>))) return bail(rc);
   bt->grid_x = g1;
   bt->grid_y = g2;
   bt->grid_z = g3;
-  bt->grid_pl = g4;
+  bt->grid_pl0 = g4;
+  bt->grid_pl1 = g5;
   *batch = bt;
   return FLUTAS_OK;
 }

@@ -1585,8 +1585,9 @@ struct BatchGrid {
 // compacted list is grid ids[s]; prefix[s] is the running total of tiles of
 // slots < s (nslots + 1 entries).  kb_compact rebuilds the list after every
 // convergence update, so a pass over converged grids has no items at all.
-// Tile kinds of the batched passes: x tiles, y tiles, z tiles, plane items.
-constexpr int BATCH_KINDS = 4;
+// Tile kinds of the batched passes: x tiles, y tiles, z tiles, plane items of
+// small planes (several CTAs a SM), plane items of large planes.
+constexpr int BATCH_KINDS = 5;
 struct BatchQueue {
   const BatchGrid *grids;
   const long *prefix;
@@ -1644,7 +1645,8 @@ __global__ void __launch_bounds__(256) kb_xfwd(BatchQueue q, int mode) {
 // x and y pass kernels carry no items for them).  mode 0: first pass (RHS =
 // x, keep f), mode 1: residual pass.
 #ifndef FG_NO_PLAIN_KERNELS
-__global__ void __launch_bounds__(512) kb_xyfwd_plane(BatchQueue q, int mode) {
+template <int NT>  // threads a CTA: 256 for small planes (two CTAs a SM), 512 for large ones (one)
+__global__ void __launch_bounds__(NT) kb_xyfwd_plane(BatchQueue q, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ns = *q.nslots;
   const long total = q.prefix[ns];
@@ -1668,7 +1670,8 @@ __global__ void __launch_bounds__(512) kb_xyfwd_plane(BatchQueue q, int mode) {
   }
 }
 // mode 0: x = e * normfft; mode 1: x += e * normfft
-__global__ void __launch_bounds__(512) kb_xyinv_plane(BatchQueue q, int mode) {
+template <int NT>
+__global__ void __launch_bounds__(NT) kb_xyinv_plane(BatchQueue q, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ns = *q.nslots;
   const long total = q.prefix[ns];
@@ -2131,7 +2134,7 @@ __global__ void kb_reset(BatchGrid *grids, int ng) {
 
 // Compacted work lists (one block): the grids still active, in grid order,
 // and for each of the BATCH_KINDS tile kinds (x tiles, y tiles, z tiles, plane
-// items) the running totals of their tiles.  full holds the per-grid running
+// items of two size classes) the running totals of their tiles.  full holds the per-grid running
 // totals (BATCH_KINDS x (ng+1)), act receives the compacted ones, ids the
 // slot -> grid map, nslots the count.
 __global__ void __launch_bounds__(1024) kb_compact(const BatchGrid *grids, int ng, const long *full, long *act,
