@@ -2824,8 +2824,8 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
   // largest plane (nx*ny) taken whole: every plane that fits one CTA's shared memory (512 grids
   // of 32..192: 65.2 ms a batch against 66.8 ms with 144^2 as the limit and 85.5 ms without)
   long plane_max = 1L << 30;
-  size_t kSmallPlane = 60 * 1024;  // planes up to this shared memory: 256 threads, two CTAs a SM
-  if (const char *e = getenv("FLUTAS_GB300_BATCH_SMALL_PLANE")) kSmallPlane = (size_t)atol(e);
+  size_t small_plane = 60 * 1024;  // planes up to this shared memory: 256 threads, two CTAs a SM
+  if (const char *e = getenv("FLUTAS_GB300_BATCH_SMALL_PLANE")) small_plane = (size_t)atol(e);
   if (const char *e = getenv("FLUTAS_GB300_BATCH_PLANE_MAX")) plane_max = atol(e);
   const size_t budget = 96 * 1024;
   // plans and tile choices
@@ -2894,7 +2894,7 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
                (int)psm <= max_smem_optin()) ? 1 : 0;
     // two classes of planes, each launched with its own shared memory: the small ones run
     // several CTAs a SM, the large ones one
-    const bool small = psm <= kSmallPlane;
+    const bool small = psm <= small_plane;
     tx[g] = G.plane ? 0 : txr[g];
     ty[g] = G.plane ? 0 : tyr[g];
     tp0[g] = G.plane && small ? nz : 0;
