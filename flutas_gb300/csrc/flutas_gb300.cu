@@ -2494,7 +2494,6 @@ struct flutas_batch {
   int grid_x = 0, grid_y = 0, grid_z = 0, grid_p = 0, grid_pl0 = 0, grid_pl1 = 0;
   bool planes0 = false, planes1 = false;  // some grids take the whole-plane kernels (small / large planes)
   bool per_pass = true;   // false (FLUTAS_GB300_BATCH_PERSISTENT=1): the whole refinement in one persistent kernel
-  int minb = 2;           // FLUTAS_GB300_BATCH_MINB: register budget of the persistent kernel
   int chunk = 4;          // FLUTAS_GB300_BATCH_CHUNK: items a block takes from the queue at once
   bool stats = false;     // FLUTAS_GB300_BATCH_STATS=1: queue statistics and per-pass-type timers
   cudaStream_t stream = nullptr;
@@ -2698,7 +2697,7 @@ int batch_capture_persistent(flutas_batch *bt, double tol, int max_iter) {
   a.max_iter = max_iter;
   a.spin_limit = 1L << 25;  // polls of about 100 ns: a few seconds
   a.stats = bt->stats ? (unsigned long long *)(a.err + 4) : nullptr;
-  auto kern = bt->minb == 1 ? kb_persist<1> : kb_persist<2>;
+  auto kern = kb_persist;
   int per_sm = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, bt->smem_p));
   if (per_sm < 1) return fail(FLUTAS_EUNSUPPORTED, "batch: the persistent kernel does not fit an SM");
@@ -2960,11 +2959,10 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
     if ((rc = bt->p_prefix.ensure(sizeof(long) * pp.size()))) return bail(rc);
     if (cudaMemcpy(bt->p_prefix.p, pp.data(), sizeof(long) * pp.size(), cudaMemcpyHostToDevice) != cudaSuccess)
       return bail(fail(FLUTAS_ECUDA, "batch_create: upload failed"));
-    if ((rc = allow_smem(kb_persist<1>)) || (rc = allow_smem(kb_persist<2>))) return bail(rc);
+    if ((rc = allow_smem(kb_persist))) return bail(rc);
     // the persistent kernel's own tables take about 2 KB of static shared memory besides the tiles
     if (!bt->per_pass && (int)bt->smem_p + 2048 > max_smem_optin())
       return bail(fail(FLUTAS_EUNSUPPORTED, "batch_create: tiles too large for the persistent kernel"));
-    if (const char *e = getenv("FLUTAS_GB300_BATCH_MINB")) bt->minb = atoi(e) == 1 ? 1 : 2;
     if (const char *e = getenv("FLUTAS_GB300_BATCH_CHUNK")) bt->chunk = std::max(1, std::min(64, atoi(e)));
     if (const char *e = getenv("FLUTAS_GB300_BATCH_STATS")) bt->stats = atoi(e) != 0;
   }
