@@ -935,7 +935,7 @@ def batch_summary(args):
             r = O.residual(g["n"], g["cbc"], g["dli"][0], g["dli"][1], 1, g["dzci"], g["dzfi"], f, x)
             worst = max(worst, float(np.linalg.norm(r) / np.linalg.norm(f[1:-1, 1:-1, 1:-1])))
         res["oracle_worst_relres_sample"] = worst
-    except Exception as e:  # the oracle is the checker only; its absence leaves the number out
+    except Exception as e:  # the oracle only checks this number; without it the number is left out
         res["oracle_worst_relres_sample"] = f"unavailable: {e}"
     B.destroy()
     return res

@@ -1,6 +1,6 @@
 /*
  * flutas_oracle.c -- CPU FP64 restatement of the FluTAS pressure-projection
- * path.  TEST INFRASTRUCTURE ONLY: the checker for the CUDA path (tests,
+ * path.  TEST INFRASTRUCTURE ONLY: the CUDA path is checked against it (tests,
  * smoke(), bench.py's CPU-baseline leg).  The product library never links it.
  *
  * "parity unpinned" against the reference binary: the reference solver_cpu

@@ -1,7 +1,7 @@
 /*
  * flutas_oracle.h -- CPU FP64 restatement of the FluTAS pressure-projection
- * path (fillps -> updt_rhs_b -> solver_cpu -> boundp -> correc), used ONLY as
- * the checker for the CUDA path (tests, smoke(), the CPU-baseline leg of
+ * path (fillps -> updt_rhs_b -> solver_cpu -> boundp -> correc), used ONLY to
+ * check the CUDA path against (tests, smoke(), the CPU-baseline leg of
  * bench.py).  Nothing in the product library links or calls this code.
  *
  * Parity status: the reference's own solver_cpu needs gfortran + FFTW 3.3.10

@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  The CUDA product path never imports this module;
 only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` use it, as the checker.
+``bench.py`` use it, to check the CUDA path against.
 
 Parity status: "parity unpinned" against a run of the reference itself.  The
 reference's ``solver_cpu`` (src/solver_cpu.f90) needs gfortran and FFTW 3.3.10,

@@ -1,4 +1,4 @@
-"""CPU tests of the FP64 oracle (the checker of the CUDA path).
+"""CPU tests of the FP64 oracle (the CUDA path is checked against it).
 
 The oracle is pinned three ways: (1) every r2r kind against FFTW's published
 O(n^2) definitions; (2) the whole solver against the closed-form discrete
