@@ -2961,8 +2961,9 @@ int flutas_gb300_batch_create(int ngrids, const int *n, const double *dli, int n
       return bail(fail(FLUTAS_ECUDA, "batch_create: upload failed"));
     if ((rc = allow_smem(kb_persist))) return bail(rc);
     // the persistent kernel's own tables take about 2 KB of static shared memory besides the tiles
-    if (!bt->per_pass && (int)bt->smem_p + 2048 > max_smem_optin())
-      return bail(fail(FLUTAS_EUNSUPPORTED, "batch_create: tiles too large for the persistent kernel"));
+    // (tiles too large for it: the pass kernels run the batch, with the row and column tiles
+    // chosen for the persistent form)
+    if (!bt->per_pass && (int)bt->smem_p + 2048 > max_smem_optin()) bt->per_pass = true;
     if (const char *e = getenv("FLUTAS_GB300_BATCH_CHUNK")) bt->chunk = std::max(1, std::min(64, atoi(e)));
     if (const char *e = getenv("FLUTAS_GB300_BATCH_STATS")) bt->stats = atoi(e) != 0;
   }
